@@ -1,0 +1,176 @@
+// Plugin-level entry points: the reference's BoxIteration contract on the GPU, and the FP64
+// verification reduction on caller-owned device arrays.
+//
+// bqp_box_* mirror sovereign::make_cuda_box / CudaBox (02-software/solver/src/cuda_box.cu:22-37):
+// the CSR and vectors are uploaded once, step(beta) runs one FISTA iteration on the device and
+// primal() copies x back.  One fused kernel replaces the reference's csr_product + fista_step
+// pair; w is double-buffered instead of keeping a separate gradient array.  The arithmetic is
+// the CPU loop's (division by L, separately rounded products and sums), so a host loop driving
+// this plugin reproduces the CPU engine's iterates.
+#include "boxqp.h"
+#include "engine.cuh"
+#include "kernels.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+struct bqp_box {
+    int device = 0;
+    int64_t n = 0, nnz = 0;
+    double L = 0;
+    int32_t* rowptr = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+    double* c = nullptr;
+    double* l = nullptr;
+    double* u = nullptr;
+    double* x = nullptr;
+    double* w[2] = {nullptr, nullptr};
+    int cur = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+};
+
+namespace {
+thread_local std::string g_box_error;
+
+void box_free(bqp_box* b) {
+    if (!b) return;
+    cudaFree(b->rowptr); cudaFree(b->col); cudaFree(b->val); cudaFree(b->c); cudaFree(b->l); cudaFree(b->u);
+    cudaFree(b->x); cudaFree(b->w[0]); cudaFree(b->w[1]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+bool ok(cudaError_t e, std::string& why) {
+    if (e == cudaSuccess) return true;
+    why = std::string("CUDA: ") + cudaGetErrorString(e);
+    return false;
+}
+}  // namespace
+
+extern "C" {
+
+bqp_box* bqp_box_create(int device, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,
+                        const double* val, const double* c, const double* lower, const double* upper,
+                        double lipschitz) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        g_box_error = "No CUDA device available";
+        return nullptr;
+    }
+    if (device < 0 || device >= count || n <= 0 || nnz < 0 || !rowptr || !c || !lower || !upper || (nnz && (!col || !val)) ||
+        !(lipschitz > 0) || !std::isfinite(lipschitz) || n > 2000000000LL) {
+        g_box_error = "invalid argument";
+        return nullptr;
+    }
+    bqp_box* b = new bqp_box;
+    b->device = device;
+    b->n = n;
+    b->nnz = nnz;
+    b->L = lipschitz;
+    std::string why;
+    const size_t N = static_cast<size_t>(n), Z = static_cast<size_t>(nnz);
+    // x0 = w0 = clip(0, l, u) (CudaBox::initial, src/cuda_box.cu:25)
+    std::vector<double> x0(N);
+    for (size_t j = 0; j < N; ++j) {
+        double v = (0.0 < upper[j]) ? 0.0 : upper[j];
+        x0[j] = (lower[j] < v) ? v : lower[j];
+    }
+    bool good = ok(cudaSetDevice(device), why) && ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), why) &&
+                ok(cudaMalloc(&b->rowptr, (N + 1) * 4), why) && ok(cudaMalloc(&b->col, Z * 4 + 16), why) &&
+                ok(cudaMalloc(&b->val, Z * 8 + 16), why) && ok(cudaMalloc(&b->c, N * 8), why) &&
+                ok(cudaMalloc(&b->l, N * 8), why) && ok(cudaMalloc(&b->u, N * 8), why) &&
+                ok(cudaMalloc(&b->x, N * 8), why) && ok(cudaMalloc(&b->w[0], N * 8), why) &&
+                ok(cudaMalloc(&b->w[1], N * 8), why) &&
+                ok(cudaMemcpy(b->rowptr, rowptr, (N + 1) * 4, cudaMemcpyHostToDevice), why) &&
+                (Z == 0 || ok(cudaMemcpy(b->col, col, Z * 4, cudaMemcpyHostToDevice), why)) &&
+                (Z == 0 || ok(cudaMemcpy(b->val, val, Z * 8, cudaMemcpyHostToDevice), why)) &&
+                ok(cudaMemcpy(b->c, c, N * 8, cudaMemcpyHostToDevice), why) &&
+                ok(cudaMemcpy(b->l, lower, N * 8, cudaMemcpyHostToDevice), why) &&
+                ok(cudaMemcpy(b->u, upper, N * 8, cudaMemcpyHostToDevice), why) &&
+                ok(cudaMemcpy(b->x, x0.data(), N * 8, cudaMemcpyHostToDevice), why) &&
+                ok(cudaMemcpy(b->w[0], x0.data(), N * 8, cudaMemcpyHostToDevice), why);
+    if (!good) {
+        g_box_error = why;
+        box_free(b);
+        return nullptr;
+    }
+    return b;
+}
+
+int bqp_box_step(bqp_box* b, double momentum) {
+    if (!b) return BQP_ERR_INVALID;
+    cudaSetDevice(b->device);
+    bqp::launch_box_step(b->n, b->rowptr, b->col, b->val, b->c, b->l, b->u, b->L, momentum, b->x, b->w[b->cur],
+                         b->w[b->cur ^ 1], b->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        b->error = std::string("CUDA: ") + cudaGetErrorString(e);
+        return BQP_ERR_CUDA;
+    }
+    b->cur ^= 1;
+    return BQP_OK;
+}
+
+int bqp_box_primal(bqp_box* b, double* x) {
+    if (!b || !x) return BQP_ERR_INVALID;
+    cudaSetDevice(b->device);
+    cudaError_t e = cudaMemcpyAsync(x, b->x, static_cast<size_t>(b->n) * 8, cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        b->error = std::string("CUDA: ") + cudaGetErrorString(e);
+        return BQP_ERR_CUDA;
+    }
+    return BQP_OK;
+}
+
+void bqp_box_destroy(bqp_box* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    box_free(b);
+}
+
+const char* bqp_box_last_error(const bqp_box* b) { return b ? b->error.c_str() : g_box_error.c_str(); }
+
+int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val, const double* d_x,
+                     const double* d_c, const double* d_lower, const double* d_upper, double tolerance, double offset,
+                     int32_t diagonal_gate, bqp_stats* stats) {
+    if (n <= 0 || n > 2000000000LL || !d_rowptr || !d_x || !d_c || !d_lower || !d_upper || !stats ||
+        !(tolerance > 0) || !std::isfinite(offset))
+        return BQP_ERR_INVALID;
+    const size_t bytes = bqp::check_scratch_bytes(n) + 8 * sizeof(double);
+    void* scratch = nullptr;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return BQP_ERR_CUDA;
+    if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return BQP_ERR_NO_MEMORY;
+    }
+    double* result = reinterpret_cast<double*>(static_cast<char*>(scratch) + bqp::check_scratch_bytes(n));
+    double host[8];
+    cudaMemsetAsync(scratch, 0, bytes, s);
+    bqp::launch_check_standalone(n, d_rowptr, d_col, d_val, d_x, d_c, d_lower, d_upper, tolerance, offset,
+                                 diagonal_gate > 0 ? 1 : 0, scratch, result, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, result, sizeof(host), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(scratch);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) return BQP_ERR_CUDA;
+    std::memset(stats, 0, sizeof(*stats));
+    stats->objective = host[0];
+    stats->primal_residual = host[1];
+    stats->stationarity_residual = host[2];
+    stats->complementarity_residual = host[3];
+    stats->dual_bound = host[4];
+    stats->relative_gap = host[5];
+    stats->verified = host[6] != 0 ? 1 : 0;
+    stats->status = stats->verified ? BQP_STATUS_OPTIMAL : BQP_STATUS_RUNNING;
+    return BQP_OK;
+}
+
+}  // extern "C"

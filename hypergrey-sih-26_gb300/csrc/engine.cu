@@ -1,0 +1,1281 @@
+// Host side of the box-QP engine: resident solves, admission under a device-memory cap,
+// the tile table, the captured conditional CUDA graph and the engine thread.
+//
+// The graph is one WHILE loop whose body is
+//     check -> gate -> IF(fp64) 25 x step -> IF(mixed) 25 x step -> IF(exact) 25 x step
+//           -> IF(polish) [polish_init, polish_residual, 25 x (cg_matvec, cg_update, cg_direction)]
+//           -> control
+// The check kernel's per-instance finalizers decide each instance's next phase, the gate kernel
+// arms the IF nodes for the phases present, and the control kernel ends the loop when no
+// instance is running or after `body_cap` bodies (so the engine thread can admit new solves
+// between launches).  All state the kernels read lives in device tables, so the graph is
+// captured once and replayed for any mix of resident solves.
+#include "boxqp.h"
+#include "engine.cuh"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace bqp {
+namespace {
+
+thread_local std::string g_thread_error;
+
+double host_seconds() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+constexpr int kCgPerBody = 25;  // CG iterations per polish body
+constexpr size_t kNone = std::numeric_limits<size_t>::max();
+
+struct Layout {
+    size_t rowptr = kNone, col = kNone, val64 = kNone, vhi = kNone, vlo = kNone;
+    size_t c = kNone, l = kNone, u = kNone, diag = kNone;
+    size_t c32 = kNone, l32 = kNone, u32 = kNone, x32 = kNone, w32a = kNone, w32b = kNone;
+    size_t x64 = kNone, w64a = kNone, w64b = kNone;
+    size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
+    size_t total = 0;
+};
+
+Layout make_layout(int64_t n, int64_t nnz, int precision) {
+    Layout L;
+    size_t o = 0;
+    // 64 bytes of slack behind every array keep 16-byte vector loads of a tail in bounds.
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = align_up(o + bytes + 64);
+        return at;
+    };
+    const size_t N = static_cast<size_t>(n), Z = static_cast<size_t>(nnz);
+    L.rowptr = take((N + 1) * 4);
+    L.col = take(Z * 4);
+    if (precision == PREC_MIXED) {
+        L.vhi = take(Z * 4);
+        L.vlo = take(Z * 4);
+    } else {
+        L.val64 = take(Z * 8);
+    }
+    L.c = take(N * 8);
+    L.l = take(N * 8);
+    L.u = take(N * 8);
+    L.diag = take(N * 8);
+    if (precision == PREC_MIXED) {
+        L.c32 = take(N * 4);
+        L.l32 = take(N * 4);
+        L.u32 = take(N * 4);
+        L.x32 = take(N * 4);
+        L.w32a = take(N * 4);
+        L.w32b = take(N * 4);
+        L.xp = take(N * 8);
+        L.r = take(N * 8);
+        L.p = take(N * 8);
+        L.q = take(N * 8);
+        L.z = take(N * 8);
+        L.fixed = take(N);
+    } else {
+        L.x64 = take(N * 8);
+        L.w64a = take(N * 8);
+        L.w64b = take(N * 8);
+    }
+    L.total = o;
+    return L;
+}
+
+template <class T>
+T* at(void* base, size_t off) {
+    return off == kNone ? nullptr : reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+enum JobState { JOB_QUEUED = 0, JOB_ADMITTING = 1, JOB_RUNNING = 2, JOB_DONE = 3 };
+
+struct Job {
+    uint64_t id = 0;
+    int64_t n = 0, nnz = 0;
+    bqp_options opt{};
+    // owned copies (asynchronous submit) or borrowed pointers (synchronous solve)
+    std::vector<int32_t> own_rowptr, own_col;
+    std::vector<double> own_val, own_c, own_l, own_u;
+    const int32_t* rowptr = nullptr;
+    const int32_t* col = nullptr;
+    const double* val = nullptr;
+    const double* c = nullptr;
+    const double* l = nullptr;
+    const double* u = nullptr;
+    double lipschitz = 0;
+    int diag_gate = 0;
+    int lanes = 4;
+    std::vector<Tile> tiles;  // local tiles (inst field filled at admission)
+    int state = JOB_QUEUED;
+    bool resolve = false;     // re-run of a resident solve
+    bool resident = false;
+    int slot = -1;
+    void* slab = nullptr;
+    Layout layout;
+    InstDev rec{};            // host image of the device record
+    int error = BQP_OK;
+    std::string error_text;
+    bqp_stats stats{};
+    std::vector<double> x;
+    std::vector<float> x32_tmp;
+    double t_submit = 0, t_done = 0;
+};
+
+void free_inputs(Job& j) {
+    std::vector<int32_t>().swap(j.own_rowptr);
+    std::vector<int32_t>().swap(j.own_col);
+    std::vector<double>().swap(j.own_val);
+    std::vector<double>().swap(j.own_c);
+    std::vector<double>().swap(j.own_l);
+    std::vector<double>().swap(j.own_u);
+    j.rowptr = nullptr; j.col = nullptr; j.val = nullptr; j.c = nullptr; j.l = nullptr; j.u = nullptr;
+}
+
+int lanes_for(int64_t n, int64_t nnz, int precision) {
+    if (precision == PREC_FP64_EXACT) return 1;
+    const double avg = n > 0 ? static_cast<double>(nnz) / static_cast<double>(n) : 1.0;
+    if (avg < 3) return 1;
+    if (avg < 6) return 2;
+    if (avg < 12) return 4;
+    if (avg < 24) return 8;
+    if (avg < 48) return 16;
+    return 32;
+}
+
+// Row tiles of one instance: contiguous rows with about kTileNnz nonzeros and at most
+// kTileRows rows.  Depends on the instance alone, so its reductions are the same whether it
+// runs alone or inside any batch.
+std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int lanes) {
+    std::vector<Tile> t;
+    int64_t r = 0;
+    while (r < n) {
+        int64_t e = r + 1;
+        while (e < n && e - r < kTileRows && static_cast<int64_t>(rowptr[e + 1]) - rowptr[r] <= kTileNnz) ++e;
+        t.push_back(Tile{0, static_cast<int32_t>(r), static_cast<int32_t>(e), lanes});
+        r = e;
+    }
+    return t;
+}
+
+// Algorithmic bytes, fixed accounting: per FISTA iteration nnz (s_v + 4) + 4 (n + 1) + 7 n s_x;
+// per check nnz 12 + 4 (n + 1) + 32 n; per CG iteration nnz 12 + 4 (n + 1) + 112 n.
+double algorithmic_bytes(int64_t n, int64_t nnz, int precision, int64_t iters, int64_t checks, int64_t cg) {
+    const double N = static_cast<double>(n), Z = static_cast<double>(nnz);
+    const double sv = precision == PREC_MIXED ? 4.0 : 8.0;
+    const double b_iter = Z * (sv + 4) + 4 * (N + 1) + 7 * N * sv;
+    const double b_check = Z * 12 + 4 * (N + 1) + 32 * N;
+    const double b_cg = Z * 12 + 4 * (N + 1) + 112 * N;
+    return static_cast<double>(iters) * b_iter + static_cast<double>(checks) * b_check + static_cast<double>(cg) * b_cg;
+}
+
+int status_code(int32_t st) {
+    switch (st) {
+    case ST_OPTIMAL: return BQP_STATUS_OPTIMAL;
+    case ST_ITERATION_LIMIT: return BQP_STATUS_ITERATION_LIMIT;
+    case ST_TIME_LIMIT: return BQP_STATUS_TIME_LIMIT;
+    case ST_NUMERICAL_ERROR: return BQP_STATUS_NUMERICAL_ERROR;
+    default: return BQP_STATUS_RUNNING;
+    }
+}
+
+}  // namespace
+
+class Engine {
+public:
+    Engine(int device, size_t cap) : device_(device), cap_(cap) {}
+    ~Engine() { shutdown(); }
+
+    bool init(std::string& why);
+    void shutdown();
+
+    int submit(Job* job, uint64_t* id);
+    int poll(uint64_t id, int32_t* status);
+    int wait(uint64_t id, double timeout);
+    int fetch(uint64_t id, double* x, bqp_stats* stats);
+    int release(uint64_t id);
+    int resolve(const uint64_t* ids, int64_t count);
+    int load(int64_t* queued, int64_t* running, int64_t* peak, int64_t* resident_bytes);
+    int timer(int reset, double* ms, int64_t* kernels, int64_t* launches) {
+        std::lock_guard<std::mutex> g(mu_);
+        if (ms) *ms = timer_ms_;
+        if (kernels) *kernels = timer_kernels_;
+        if (launches) *launches = timer_launches_;
+        if (reset) {
+            timer_ms_ = 0;
+            timer_kernels_ = 0;
+            timer_launches_ = 0;
+        }
+        return BQP_OK;
+    }
+    int profile_step(uint64_t id, int launches, double* ms, double* bytes);
+    void set_latency_target(double ms) {
+        std::lock_guard<std::mutex> g(mu_);
+        latency_ms_ = ms;
+    }
+    void set_error(const std::string& e) {
+        std::lock_guard<std::mutex> g(err_mu_);
+        error_ = e;
+    }
+    const char* error() const {
+        std::lock_guard<std::mutex> g(err_mu_);
+        err_copy_ = error_;
+        return err_copy_.c_str();
+    }
+
+private:
+    void loop();
+    bool admit(Job& j, std::string& why);
+    bool run_once(std::string& why);
+    void collect(std::unique_lock<std::mutex>& lk);
+    void process_frees();
+    bool ensure_tables(int need_inst, int need_tiles, std::string& why);
+    bool build_graph(std::string& why);
+    View view() const {
+        View v;
+        v.inst = d_inst_;
+        v.tiles = d_tiles_;
+        v.partial = d_partial_;
+        v.tile_done = d_tile_done_;
+        v.ctrl = d_ctrl_;
+        v.status_mirror = d_status_;
+        v.ranges = d_ranges_;
+        return v;
+    }
+    bool cuda_ok(cudaError_t e, std::string& why, const char* what) {
+        if (e == cudaSuccess) return true;
+        why = std::string("CUDA: ") + what + ": " + cudaGetErrorString(e);
+        return false;
+    }
+
+    int device_;
+    size_t cap_;
+    int sms_ = 152;
+    cudaStream_t stream_ = nullptr;
+    cudaStream_t capture_ = nullptr;
+    cudaMemPool_t pool_ = nullptr;
+
+    // device tables
+    InstDev* d_inst_ = nullptr;
+    int2* d_ranges_ = nullptr;
+    int32_t* d_tile_done_ = nullptr;
+    int32_t* d_status_ = nullptr;
+    Tile* d_tiles_ = nullptr;
+    Partial* d_partial_ = nullptr;
+    Ctrl* d_ctrl_ = nullptr;
+    Ctrl* h_ctrl_ = nullptr;       // pinned
+    int32_t* h_status_ = nullptr;  // pinned
+    int inst_cap_ = 0, tile_cap_ = 0;
+
+    // host mirrors
+    std::vector<Tile> h_tiles_;
+    std::vector<int2> h_ranges_;
+    std::vector<Job*> slot_job_;
+    std::vector<int> free_slots_;
+    int n_inst_ = 0;
+    bool tables_dirty_ = false;
+
+    // graph
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int graph_grid_ = 0;
+    int graph_interval_ = 25;
+    bool graph_valid_ = false;
+
+    // jobs
+    mutable std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::map<uint64_t, std::unique_ptr<Job>> jobs_;
+    std::deque<Job*> queue_;
+    std::vector<std::pair<int, void*>> pending_free_;
+    uint64_t next_id_ = 1;
+    int64_t n_running_ = 0, peak_resident_ = 0;
+    size_t resident_bytes_ = 0;
+    double latency_ms_ = 0;
+    double body_ms_ = 0.5;
+    double timer_ms_ = 0;
+    int64_t timer_kernels_ = 0, timer_launches_ = 0;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    bool stop_ = false;
+    std::thread thread_;
+
+    mutable std::mutex err_mu_;
+    std::string error_;
+    mutable std::string err_copy_;
+};
+
+bool Engine::init(std::string& why) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        why = "No CUDA device available";
+        return false;
+    }
+    if (device_ < 0 || device_ >= count) {
+        why = "Invalid CUDA device index";
+        return false;
+    }
+    if (!cuda_ok(cudaSetDevice(device_), why, "set device")) return false;
+    cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_);
+    if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device_;
+    if (!cuda_ok(cudaMemPoolCreate(&pool_, &props), why, "memory pool")) return false;
+    uint64_t threshold = std::numeric_limits<uint64_t>::max();
+    cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &threshold);
+    if (cap_ == 0) {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        cap_ = static_cast<size_t>(0.9 * static_cast<double>(free_b));
+    }
+    if (!cuda_ok(cudaEventCreate(&ev0_), why, "event")) return false;
+    if (!cuda_ok(cudaEventCreate(&ev1_), why, "event")) return false;
+    if (!cuda_ok(cudaMalloc(&d_ctrl_, sizeof(Ctrl)), why, "control block")) return false;
+    if (!cuda_ok(cudaMemset(d_ctrl_, 0, sizeof(Ctrl)), why, "control block")) return false;
+    if (!cuda_ok(cudaMallocHost(&h_ctrl_, sizeof(Ctrl)), why, "pinned control")) return false;
+    std::memset(h_ctrl_, 0, sizeof(Ctrl));
+    if (!ensure_tables(256, 1024, why)) return false;
+    cudaSetDevice(prev);
+    thread_ = std::thread([this] { loop(); });
+    return true;
+}
+
+void Engine::shutdown() {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        if (stop_ && !thread_.joinable()) return;
+        stop_ = true;
+    }
+    cv_work_.notify_all();
+    if (thread_.joinable()) thread_.join();
+    if (stream_) {
+        cudaSetDevice(device_);
+        cudaStreamSynchronize(stream_);
+        for (auto& kv : jobs_) if (kv.second->slab) cudaFreeAsync(kv.second->slab, stream_);
+        for (auto& pf : pending_free_) if (pf.second) cudaFreeAsync(pf.second, stream_);
+        cudaStreamSynchronize(stream_);
+    }
+    jobs_.clear();
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+    cudaFree(d_inst_); cudaFree(d_ranges_); cudaFree(d_tile_done_); cudaFree(d_status_);
+    cudaFree(d_tiles_); cudaFree(d_partial_); cudaFree(d_ctrl_);
+    d_inst_ = nullptr; d_ranges_ = nullptr; d_tile_done_ = nullptr; d_status_ = nullptr;
+    d_tiles_ = nullptr; d_partial_ = nullptr; d_ctrl_ = nullptr;
+    if (h_ctrl_) cudaFreeHost(h_ctrl_);
+    if (h_status_) cudaFreeHost(h_status_);
+    h_ctrl_ = nullptr;
+    h_status_ = nullptr;
+    if (pool_) cudaMemPoolDestroy(pool_);
+    pool_ = nullptr;
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    ev0_ = nullptr;
+    ev1_ = nullptr;
+    if (stream_) cudaStreamDestroy(stream_);
+    if (capture_) cudaStreamDestroy(capture_);
+    stream_ = nullptr;
+    capture_ = nullptr;
+}
+
+// Grows the device tables (instance records, tile table, partials); invalidates the graph.
+bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
+    if (need_inst > inst_cap_) {
+        int cap = std::max(need_inst, std::max(256, inst_cap_ * 2));
+        InstDev* inst = nullptr;
+        int2* ranges = nullptr;
+        int32_t *done = nullptr, *status = nullptr, *h_status = nullptr;
+        if (!cuda_ok(cudaMalloc(&inst, sizeof(InstDev) * cap), why, "instance table")) return false;
+        if (!cuda_ok(cudaMalloc(&ranges, sizeof(int2) * cap), why, "range table")) return false;
+        if (!cuda_ok(cudaMalloc(&done, sizeof(int32_t) * cap), why, "tile counters")) return false;
+        if (!cuda_ok(cudaMalloc(&status, sizeof(int32_t) * cap), why, "status mirror")) return false;
+        if (!cuda_ok(cudaMallocHost(&h_status, sizeof(int32_t) * cap), why, "pinned status")) return false;
+        cudaMemsetAsync(inst, 0, sizeof(InstDev) * cap, stream_);
+        cudaMemsetAsync(ranges, 0, sizeof(int2) * cap, stream_);
+        cudaMemsetAsync(done, 0, sizeof(int32_t) * cap, stream_);
+        cudaMemsetAsync(status, 0xff, sizeof(int32_t) * cap, stream_);
+        if (d_inst_) {
+            cudaMemcpyAsync(inst, d_inst_, sizeof(InstDev) * inst_cap_, cudaMemcpyDeviceToDevice, stream_);
+            cudaMemcpyAsync(done, d_tile_done_, sizeof(int32_t) * inst_cap_, cudaMemcpyDeviceToDevice, stream_);
+        }
+        cudaStreamSynchronize(stream_);
+        cudaFree(d_inst_); cudaFree(d_ranges_); cudaFree(d_tile_done_); cudaFree(d_status_);
+        if (h_status_) cudaFreeHost(h_status_);
+        d_inst_ = inst; d_ranges_ = ranges; d_tile_done_ = done; d_status_ = status; h_status_ = h_status;
+        inst_cap_ = cap;
+        h_ranges_.resize(cap, int2{0, 0});
+        slot_job_.resize(cap, nullptr);
+        tables_dirty_ = true;
+        graph_valid_ = false;
+    }
+    if (need_tiles > tile_cap_) {
+        int cap = std::max(need_tiles, std::max(1024, tile_cap_ * 2));
+        Tile* tiles = nullptr;
+        Partial* partial = nullptr;
+        if (!cuda_ok(cudaMalloc(&tiles, sizeof(Tile) * cap), why, "tile table")) return false;
+        if (!cuda_ok(cudaMalloc(&partial, sizeof(Partial) * cap), why, "partials")) return false;
+        cudaFree(d_tiles_);
+        cudaFree(d_partial_);
+        d_tiles_ = tiles;
+        d_partial_ = partial;
+        tile_cap_ = cap;
+        tables_dirty_ = true;
+        graph_valid_ = false;
+    }
+    return true;
+}
+
+bool Engine::build_graph(std::string& why) {
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+    const int grid_max = sms_ * 8;
+    int want = static_cast<int>(std::min<size_t>(static_cast<size_t>(grid_max), align_up(std::max<size_t>(h_tiles_.size(), 1), 32)));
+    graph_grid_ = std::max(want, graph_grid_);
+    if (graph_grid_ > grid_max) graph_grid_ = grid_max;
+    const int grid = graph_grid_;
+    const int K = graph_interval_;
+    const View v = view();
+
+    if (!cuda_ok(cudaGraphCreate(&graph_, 0), why, "graph create")) return false;
+    cudaGraphConditionalHandle h_loop, h_f[3], h_pol;
+    if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_loop, graph_, 1, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
+    for (int k = 0; k < 3; ++k)
+        if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_f[k], graph_, 0, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
+    if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_pol, graph_, 0, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
+
+    cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    if (!cuda_ok(cudaGraphAddNode(&wnode, graph_, nullptr, nullptr, 0, &wp), why, "while node")) return false;
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+
+    auto capture = [&](cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps, auto&& launches,
+                       cudaGraphNode_t* last) -> bool {
+        if (!cuda_ok(cudaStreamBeginCaptureToGraph(capture_, g, deps, nullptr, ndeps, cudaStreamCaptureModeThreadLocal), why, "begin capture")) return false;
+        launches();
+        if (last) {
+            cudaStreamCaptureStatus st;
+            const cudaGraphNode_t* tail = nullptr;
+            size_t ntail = 0;
+            if (!cuda_ok(cudaStreamGetCaptureInfo(capture_, &st, nullptr, nullptr, &tail, nullptr, &ntail), why, "capture info")) return false;
+            *last = ntail ? tail[0] : nullptr;
+        }
+        cudaGraph_t out = nullptr;
+        if (!cuda_ok(cudaStreamEndCapture(capture_, &out), why, "end capture")) return false;
+        return cuda_ok(cudaGetLastError(), why, "captured launch");
+    };
+    auto add_if = [&](cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraphNode_t* node, cudaGraph_t* inner) -> bool {
+        cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeIf;
+        p.conditional.size = 1;
+        if (!cuda_ok(cudaGraphAddNode(node, body, &dep, nullptr, 1, &p), why, "if node")) return false;
+        *inner = p.conditional.phGraph_out[0];
+        return true;
+    };
+
+    cudaGraphNode_t last = nullptr;
+    if (!capture(body, nullptr, 0, [&] {
+            launch_check(v, grid, capture_);
+            launch_gate(v, h_f, h_pol, K, 2 + 3 * kCgPerBody, capture_);
+        }, &last)) return false;
+    const int precisions[3] = {PREC_FP64, PREC_MIXED, PREC_FP64_EXACT};
+    for (int k = 0; k < 3; ++k) {
+        cudaGraphNode_t node;
+        cudaGraph_t inner;
+        if (!add_if(last, h_f[k], &node, &inner)) return false;
+        if (!capture(inner, nullptr, 0, [&] {
+                for (int j = 0; j < K; ++j) launch_step(v, precisions[k], j, grid, capture_);
+            }, nullptr)) return false;
+        last = node;
+    }
+    {
+        cudaGraphNode_t node;
+        cudaGraph_t inner;
+        if (!add_if(last, h_pol, &node, &inner)) return false;
+        if (!capture(inner, nullptr, 0, [&] {
+                launch_polish_init(v, grid, capture_);
+                launch_polish_residual(v, grid, capture_);
+                for (int j = 0; j < kCgPerBody; ++j) {
+                    launch_cg_matvec(v, grid, capture_);
+                    launch_cg_update(v, grid, capture_);
+                    launch_cg_direction(v, grid, capture_);
+                }
+            }, nullptr)) return false;
+        last = node;
+    }
+    if (!capture(body, &last, 1, [&] { launch_control(v, h_loop, capture_); }, nullptr)) return false;
+    if (!cuda_ok(cudaGraphInstantiate(&exec_, graph_, 0), why, "graph instantiate")) return false;
+    graph_valid_ = true;
+    return true;
+}
+
+int Engine::submit(Job* raw, uint64_t* id) {
+    std::unique_ptr<Job> job(raw);
+    std::lock_guard<std::mutex> g(mu_);
+    if (stop_) return BQP_ERR_INVALID;
+    job->id = next_id_++;
+    job->t_submit = host_seconds();
+    Job* j = job.get();
+    if (id) *id = j->id;
+    const bool done = j->state == JOB_DONE;
+    jobs_[j->id] = std::move(job);
+    if (!done) {
+        queue_.push_back(j);
+        cv_work_.notify_all();
+    }
+    return BQP_OK;
+}
+
+int Engine::poll(uint64_t id, int32_t* status) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    const Job& j = *it->second;
+    if (status) {
+        if (j.state == JOB_DONE) *status = j.stats.status;
+        else if (j.state == JOB_RUNNING) *status = BQP_STATUS_RUNNING;
+        else *status = BQP_STATUS_QUEUED;
+    }
+    return BQP_OK;
+}
+
+int Engine::wait(uint64_t id, double timeout) {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto pred = [&] {
+        auto it = jobs_.find(id);
+        return it == jobs_.end() || it->second->state == JOB_DONE;
+    };
+    if (timeout < 0) cv_done_.wait(lk, pred);
+    else if (!cv_done_.wait_for(lk, std::chrono::duration<double>(timeout), pred)) return BQP_ERR_NOT_READY;
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    return it->second->error;
+}
+
+int Engine::fetch(uint64_t id, double* x, bqp_stats* stats) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    const Job& j = *it->second;
+    if (j.state != JOB_DONE) return BQP_ERR_NOT_READY;
+    if (stats) *stats = j.stats;
+    if (x && !j.x.empty()) std::memcpy(x, j.x.data(), sizeof(double) * j.x.size());
+    if (j.error != BQP_OK) set_error(j.error_text);
+    return j.error;
+}
+
+int Engine::release(uint64_t id) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    Job& j = *it->second;
+    if (j.state == JOB_QUEUED) {
+        queue_.erase(std::remove(queue_.begin(), queue_.end(), &j), queue_.end());
+    } else if (j.state != JOB_DONE) {
+        return BQP_ERR_NOT_READY;
+    }
+    if (j.resident) {
+        pending_free_.emplace_back(j.slot, j.slab);
+        resident_bytes_ -= j.layout.total;
+        j.slab = nullptr;
+        cv_work_.notify_all();
+    }
+    jobs_.erase(it);
+    return BQP_OK;
+}
+
+int Engine::resolve(const uint64_t* ids, int64_t count) {
+    std::lock_guard<std::mutex> g(mu_);
+    for (int64_t k = 0; k < count; ++k) {
+        auto it = jobs_.find(ids[k]);
+        if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+        if (it->second->state != JOB_DONE || !it->second->resident) return BQP_ERR_NOT_READY;
+    }
+    for (int64_t k = 0; k < count; ++k) {
+        Job& j = *jobs_[ids[k]];
+        j.state = JOB_QUEUED;
+        j.resolve = true;
+        j.error = BQP_OK;
+        j.t_submit = host_seconds();
+        queue_.push_back(&j);
+    }
+    cv_work_.notify_all();
+    return BQP_OK;
+}
+
+int Engine::load(int64_t* queued, int64_t* running, int64_t* peak, int64_t* resident_bytes) {
+    std::lock_guard<std::mutex> g(mu_);
+    if (queued) *queued = static_cast<int64_t>(queue_.size());
+    if (running) *running = n_running_;
+    if (peak) *peak = peak_resident_;
+    if (resident_bytes) *resident_bytes = static_cast<int64_t>(resident_bytes_);
+    return BQP_OK;
+}
+
+// Uploads (or re-arms) one solve and appends its tiles.  Engine thread only.
+bool Engine::admit(Job& j, std::string& why) {
+    const int prec = j.opt.precision;
+    if (!j.resolve) {
+        j.layout = make_layout(j.n, j.nnz, prec);
+        void* slab = nullptr;
+        if (!cuda_ok(cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, stream_), why, "allocate solve")) return false;
+        j.slab = slab;
+        const Layout& L = j.layout;
+        const size_t N = static_cast<size_t>(j.n), Z = static_cast<size_t>(j.nnz);
+        cudaMemcpyAsync(at<int32_t>(slab, L.rowptr), j.rowptr, (N + 1) * 4, cudaMemcpyHostToDevice, stream_);
+        if (Z) cudaMemcpyAsync(at<int32_t>(slab, L.col), j.col, Z * 4, cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(at<double>(slab, L.c), j.c, N * 8, cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(at<double>(slab, L.l), j.l, N * 8, cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(at<double>(slab, L.u), j.u, N * 8, cudaMemcpyHostToDevice, stream_);
+        // slot
+        int slot;
+        if (!free_slots_.empty()) {
+            slot = free_slots_.back();
+            free_slots_.pop_back();
+        } else {
+            if (!ensure_tables(n_inst_ + 1, 0, why)) return false;
+            slot = n_inst_++;
+        }
+        j.slot = slot;
+        j.resident = true;
+        InstDev& R = j.rec;
+        std::memset(&R, 0, sizeof(R));
+        R.rowptr = at<int32_t>(slab, L.rowptr);
+        R.col = at<int32_t>(slab, L.col);
+        R.val64 = at<double>(slab, L.val64);
+        R.vhi = at<float>(slab, L.vhi);
+        R.vlo = at<float>(slab, L.vlo);
+        R.c = at<double>(slab, L.c);
+        R.l = at<double>(slab, L.l);
+        R.u = at<double>(slab, L.u);
+        R.c32 = at<float>(slab, L.c32);
+        R.l32 = at<float>(slab, L.l32);
+        R.u32 = at<float>(slab, L.u32);
+        R.diag = at<double>(slab, L.diag);
+        R.x64 = at<double>(slab, L.x64);
+        R.w64[0] = at<double>(slab, L.w64a);
+        R.w64[1] = at<double>(slab, L.w64b);
+        R.x32 = at<float>(slab, L.x32);
+        R.w32[0] = at<float>(slab, L.w32a);
+        R.w32[1] = at<float>(slab, L.w32b);
+        R.xp = at<double>(slab, L.xp);
+        R.r = at<double>(slab, L.r);
+        R.p = at<double>(slab, L.p);
+        R.q = at<double>(slab, L.q);
+        R.z = at<double>(slab, L.z);
+        R.fixed = at<uint8_t>(slab, L.fixed);
+        R.n = static_cast<int32_t>(j.n);
+        R.diag_gate = j.diag_gate;
+        R.precision = prec;
+        R.L = j.lipschitz;
+        R.invL = 1.0 / j.lipschitz;
+        R.invLf = static_cast<float>(1.0 / j.lipschitz);
+        R.tol = j.opt.tolerance;
+        R.offset = j.opt.offset;
+        R.interval = j.opt.check_interval;
+        R.max_iter = j.opt.iteration_limit;
+        R.polish = prec == PREC_MIXED ? 1 : 0;
+        R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
+        R.cg_tol = 0.1 * j.opt.tolerance;
+        // tiles
+        for (Tile& t : j.tiles) t.inst = slot;
+        const int begin = static_cast<int>(h_tiles_.size());
+        if (!ensure_tables(0, begin + static_cast<int>(j.tiles.size()), why)) return false;
+        h_tiles_.insert(h_tiles_.end(), j.tiles.begin(), j.tiles.end());
+        h_ranges_[slot] = int2{begin, static_cast<int>(h_tiles_.size())};
+        tables_dirty_ = true;
+    }
+    InstDev& R = j.rec;
+    R.status = ST_RUNNING;
+    R.phase = PH_FISTA;
+    R.polish_rounds = 0;
+    R.it0 = 0;
+    R.it_next = 0;
+    R.t = 1.0;
+    R.deadline_ns = static_cast<int64_t>(std::min(j.opt.time_limit, 1e9) * 1e9);  // budget; made absolute on device
+    R.verified = 0;
+    R.stable_checks = 0;
+    R.active_hash = 0;
+    R.n_active = -1;
+    R.result_src = 0;
+    R.cg_it = 0;
+    R.cg_total = 0;
+    R.fista_iters = 0;
+    R.checks = 0;
+    R.iterations = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_), why, "instance record")) return false;
+    if (tables_dirty_) {
+        if (!h_tiles_.empty())
+            cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * n_inst_, cudaMemcpyHostToDevice, stream_);
+        tables_dirty_ = false;
+    }
+    const View v = view();
+    if (!j.resolve) {
+        const Layout& L = j.layout;
+        const size_t Z = static_cast<size_t>(j.nnz);
+        if (prec == PREC_MIXED) {
+            void* tmp = nullptr;
+            if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, stream_), why, "allocate upload buffer")) return false;
+            if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, stream_);
+            launch_prepare_instance(v, j.slot, j.n, j.nnz, static_cast<const double*>(tmp), stream_);
+            cudaFreeAsync(tmp, stream_);
+        } else {
+            double* val = at<double>(j.slab, L.val64);
+            if (Z) cudaMemcpyAsync(val, j.val, Z * 8, cudaMemcpyHostToDevice, stream_);
+            launch_prepare_instance(v, j.slot, j.n, j.nnz, val, stream_);
+        }
+    }
+    if (j.resolve) cudaEventRecord(ev0_, stream_);
+    launch_init_instance(v, j.slot, static_cast<int>(j.n), prec, stream_);
+    if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
+    if (j.resolve) {
+        // re-arming a resident solve is part of its device time: count it in the timer
+        cudaEventRecord(ev1_, stream_);
+        cudaEventSynchronize(ev1_);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0_, ev1_);
+        std::lock_guard<std::mutex> g(mu_);
+        timer_ms_ += ms;
+        timer_kernels_ += 1;
+    }
+    if (j.opt.check_interval > graph_interval_) {
+        graph_interval_ = std::min(j.opt.check_interval, kMaxInterval);
+        graph_valid_ = false;
+    }
+    const int grid_max = sms_ * 8;
+    if (graph_grid_ < grid_max && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
+    return true;
+}
+
+void Engine::process_frees() {
+    if (pending_free_.empty()) return;
+    std::vector<char> dead(static_cast<size_t>(std::max(n_inst_, 1)), 0);
+    for (auto& pf : pending_free_) {
+        if (pf.second) cudaFreeAsync(pf.second, stream_);
+        if (pf.first >= 0) {
+            dead[pf.first] = 1;
+            slot_job_[pf.first] = nullptr;
+            free_slots_.push_back(pf.first);
+            h_ranges_[pf.first] = int2{0, 0};
+        }
+    }
+    pending_free_.clear();
+    std::vector<Tile> kept;
+    kept.reserve(h_tiles_.size());
+    for (const Tile& t : h_tiles_) if (!dead[t.inst]) kept.push_back(t);
+    h_tiles_.swap(kept);
+    for (int s = 0; s < n_inst_; ++s) h_ranges_[s] = int2{0, 0};
+    for (int k = 0; k < static_cast<int>(h_tiles_.size()); ++k) {
+        int2& r = h_ranges_[h_tiles_[k].inst];
+        if (r.y == 0) r.x = k;
+        r.y = k + 1;
+    }
+    tables_dirty_ = true;
+}
+
+bool Engine::run_once(std::string& why) {
+    if (tables_dirty_) {
+        if (!h_tiles_.empty())
+            cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
+        tables_dirty_ = false;
+    }
+    if (!graph_valid_ && !build_graph(why)) return false;
+    int cap = std::numeric_limits<int>::max() / 2;
+    double latency;
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        latency = latency_ms_;
+    }
+    if (latency > 0) cap = std::max(1, static_cast<int>(latency / std::max(body_ms_, 1e-3)));
+    h_ctrl_->n_inst = n_inst_;
+    h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    h_ctrl_->bodies = 0;
+    h_ctrl_->body_cap = cap;
+    h_ctrl_->error = 0;
+    h_ctrl_->kernels = 0;
+    const double t0 = host_seconds();
+    if (!cuda_ok(cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_), why, "control upload")) return false;
+    cudaEventRecord(ev0_, stream_);
+    if (!cuda_ok(cudaGraphLaunch(exec_, stream_), why, "graph launch")) return false;
+    cudaEventRecord(ev1_, stream_);
+    cudaMemcpyAsync(h_status_, d_status_, sizeof(int32_t) * std::max(n_inst_, 1), cudaMemcpyDeviceToHost, stream_);
+    cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
+    if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine launch")) return false;
+    const double dt = host_seconds() - t0;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        timer_ms_ += ms;
+        timer_kernels_ += h_ctrl_->kernels;
+        timer_launches_ += 1;
+    }
+    if (h_ctrl_->bodies > 0) body_ms_ = 0.7 * body_ms_ + 0.3 * (1e3 * dt / h_ctrl_->bodies);
+    return true;
+}
+
+// Moves finished solves to the done state: copies their records and primals back.
+void Engine::collect(std::unique_lock<std::mutex>& lk) {
+    std::vector<Job*> finished;
+    for (int s = 0; s < n_inst_; ++s) {
+        Job* j = slot_job_[s];
+        if (j && j->state == JOB_RUNNING && h_status_[s] != ST_RUNNING) finished.push_back(j);
+    }
+    if (finished.empty()) return;
+    lk.unlock();
+    std::vector<InstDev> recs(finished.size());
+    for (size_t k = 0; k < finished.size(); ++k)
+        cudaMemcpyAsync(&recs[k], &d_inst_[finished[k]->slot], sizeof(InstDev), cudaMemcpyDeviceToHost, stream_);
+    cudaStreamSynchronize(stream_);
+    for (size_t k = 0; k < finished.size(); ++k) {
+        Job& j = *finished[k];
+        const InstDev& R = recs[k];
+        j.x.resize(static_cast<size_t>(j.n));
+        if (R.result_src == 1) {
+            j.x32_tmp.resize(static_cast<size_t>(j.n));
+            cudaMemcpyAsync(j.x32_tmp.data(), R.x32, sizeof(float) * j.n, cudaMemcpyDeviceToHost, stream_);
+        } else {
+            const double* src = R.result_src == 2 ? R.xp : R.x64;
+            cudaMemcpyAsync(j.x.data(), src, sizeof(double) * j.n, cudaMemcpyDeviceToHost, stream_);
+        }
+    }
+    cudaStreamSynchronize(stream_);
+    const double now = host_seconds();
+    for (size_t k = 0; k < finished.size(); ++k) {
+        Job& j = *finished[k];
+        const InstDev& R = recs[k];
+        if (R.result_src == 1) {
+            for (int64_t i = 0; i < j.n; ++i) j.x[i] = static_cast<double>(j.x32_tmp[i]);
+            std::vector<float>().swap(j.x32_tmp);
+        }
+        bqp_stats& s = j.stats;
+        s.status = status_code(R.status);
+        s.verified = R.verified;
+        s.iterations = R.iterations;
+        s.polish_iterations = R.cg_total;
+        s.polish_rounds = R.polish_rounds + (R.result_src == 2 ? 1 : 0);
+        s.objective = R.objective;
+        s.primal_residual = R.primal_res;
+        s.stationarity_residual = R.stationarity;
+        s.complementarity_residual = 0.0;
+        s.dual_bound = R.dual_bound;
+        s.relative_gap = R.rel_gap;
+        s.lipschitz = R.L;
+        s.device_start_ns = R.start_ns;
+        s.device_end_ns = R.end_ns;
+        s.device_seconds = 1e-9 * static_cast<double>(R.end_ns - R.start_ns);
+        s.checks = R.checks;
+        s.bytes = algorithmic_bytes(j.n, j.nnz, j.opt.precision, R.fista_iters, R.checks, R.cg_total);
+        j.t_done = now;
+    }
+    lk.lock();
+    for (Job* j : finished) {
+        j->state = JOB_DONE;
+        j->resolve = false;
+        n_running_--;
+    }
+    cv_done_.notify_all();
+}
+
+// Times the FISTA step kernel alone on one finished resident solve: `launches` back-to-back
+// launches of the same kernel and grid the graph uses, bracketed by CUDA events on the engine
+// stream.  Runs while the engine is idle (holds the engine lock); the solve's iterate is left
+// scrambled, so it must be re-solved (bqp_resolve) before its result is used again.
+int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* bytes_out) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    Job& j = *it->second;
+    if (j.state != JOB_DONE || !j.resident || n_running_ != 0 || !queue_.empty() || launches < 1) return BQP_ERR_NOT_READY;
+    cudaSetDevice(device_);
+    std::string why;
+    if (!graph_valid_ && !build_graph(why)) {
+        set_error(why);
+        return BQP_ERR_CUDA;
+    }
+    InstDev saved;
+    cudaMemcpy(&saved, &d_inst_[j.slot], sizeof(InstDev), cudaMemcpyDeviceToHost);
+    InstDev R = saved;
+    R.status = ST_RUNNING;
+    R.phase = PH_FISTA;
+    R.it0 = 0;
+    R.it_next = 1LL << 40;
+    for (int k = 0; k < kMaxInterval; ++k) R.beta[k] = 0.5;
+    cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
+    h_ctrl_->n_inst = n_inst_;
+    h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
+    const View v = view();
+    launch_step(v, j.opt.precision, 0, graph_grid_, stream_);  // warm-up
+    cudaEventRecord(ev0_, stream_);
+    for (int k = 0; k < launches; ++k) launch_step(v, j.opt.precision, 0, graph_grid_, stream_);
+    cudaEventRecord(ev1_, stream_);
+    cudaMemcpyAsync(&d_inst_[j.slot], &saved, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e != cudaSuccess) {
+        set_error(std::string("CUDA: ") + cudaGetErrorString(e));
+        return BQP_ERR_CUDA;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    if (ms_out) *ms_out = ms / launches;
+    if (bytes_out) *bytes_out = algorithmic_bytes(j.n, j.nnz, j.opt.precision, 1, 0, 0);
+    return BQP_OK;
+}
+
+void Engine::loop() {
+    cudaSetDevice(device_);
+    std::unique_lock<std::mutex> lk(mu_);
+    while (!stop_) {
+        if (!pending_free_.empty()) process_frees();
+        // admission: FIFO while the head fits under the cap
+        while (!queue_.empty()) {
+            Job* j = queue_.front();
+            const size_t need = j->resolve ? 0 : make_layout(j->n, j->nnz, j->opt.precision).total;
+            if (!j->resolve && resident_bytes_ + need > cap_) {
+                if (n_running_ == 0) {
+                    queue_.pop_front();
+                    j->error = BQP_ERR_ADMISSION;
+                    j->error_text = "solve does not fit under the device-memory cap";
+                    j->state = JOB_DONE;
+                    cv_done_.notify_all();
+                    continue;
+                }
+                break;
+            }
+            queue_.pop_front();
+            j->state = JOB_ADMITTING;
+            resident_bytes_ += need;
+            lk.unlock();
+            std::string why;
+            bool ok = admit(*j, why);
+            if (!j->resolve) free_inputs(*j);
+            lk.lock();
+            if (ok) {
+                j->state = JOB_RUNNING;
+                slot_job_[j->slot] = j;
+                n_running_++;
+                int64_t resident = 0;
+                for (Job* s : slot_job_) if (s && s->state == JOB_RUNNING) resident++;
+                peak_resident_ = std::max(peak_resident_, resident);
+            } else {
+                resident_bytes_ -= need;
+                j->error = BQP_ERR_CUDA;
+                j->error_text = why;
+                j->state = JOB_DONE;
+                set_error(why);
+                cv_done_.notify_all();
+            }
+        }
+        if (n_running_ == 0) {
+            if (queue_.empty() && pending_free_.empty()) cv_work_.wait(lk);
+            continue;
+        }
+        lk.unlock();
+        std::string why;
+        bool ok = run_once(why);
+        lk.lock();
+        if (!ok) {
+            // A CUDA error on the engine stream: fail every running solve.
+            set_error(why);
+            for (Job* j : slot_job_) {
+                if (j && j->state == JOB_RUNNING) {
+                    j->state = JOB_DONE;
+                    j->error = BQP_ERR_CUDA;
+                    j->error_text = why;
+                    n_running_--;
+                }
+            }
+            cv_done_.notify_all();
+            continue;
+        }
+        collect(lk);
+    }
+}
+
+}  // namespace bqp
+
+// =============================================================================================
+// C-ABI
+// =============================================================================================
+using bqp::Engine;
+using bqp::Job;
+
+struct bqp_ctx {
+    Engine* engine;
+};
+
+namespace {
+thread_local std::string g_error;
+
+int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+                     const double* c, const double* l, const double* u, const bqp_options* o, std::string& why) {
+    if (n <= 0 || n > 2000000000LL || nnz < 0 || nnz > 2000000000LL || !rowptr || !c || !l || !u || (nnz && (!col || !val))) {
+        why = "Invalid linear problem dimensions or offset";
+        return BQP_ERR_INVALID;
+    }
+    if (!o || !(o->tolerance > 0) || !std::isfinite(o->tolerance) || o->time_limit < 0 || !std::isfinite(o->time_limit) ||
+        o->iteration_limit < 0 || o->check_interval < 1 || o->check_interval > bqp::kMaxInterval ||
+        (o->precision != BQP_PRECISION_FP64 && o->precision != BQP_PRECISION_MIXED && o->precision != BQP_PRECISION_FP64_EXACT) ||
+        !std::isfinite(o->offset)) {
+        why = "Invalid box QP options";
+        return BQP_ERR_INVALID;
+    }
+    if (rowptr[0] != 0 || rowptr[n] != nnz) {
+        why = "Invalid CSR row pointers";
+        return BQP_ERR_INVALID;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (rowptr[i + 1] < rowptr[i]) { why = "Invalid CSR row pointers"; return BQP_ERR_INVALID; }
+        if (!std::isfinite(c[i]) || std::isnan(l[i]) || std::isnan(u[i]) || l[i] == HUGE_VAL || u[i] == -HUGE_VAL) {
+            why = "Invalid variable coefficient or bound";
+            return BQP_ERR_INVALID;
+        }
+    }
+    for (int64_t k = 0; k < nnz; ++k) {
+        if (col[k] < 0 || col[k] >= n || !std::isfinite(val[k])) { why = "Invalid Hessian"; return BQP_ERR_INVALID; }
+    }
+    return BQP_OK;
+}
+
+// Builds a job: validation, Gershgorin L, diagonal gate, tiles; infeasible bounds finish at once.
+int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+             const double* c, const double* l, const double* u, const bqp_options* options, bool copy,
+             Job** out, std::string& why) {
+    bqp_options o;
+    if (options) o = *options;
+    else bqp_options_default(&o);
+    int rc = validate_problem(n, nnz, rowptr, col, val, c, l, u, &o, why);
+    if (rc != BQP_OK) return rc;
+    double lipschitz = bqp_gershgorin(n, rowptr, val);
+    if (lipschitz == 0) {
+        why = "Zero-Hessian models use the CPU LP path";
+        return BQP_ERR_UNSUPPORTED;
+    }
+    std::unique_ptr<Job> j(new Job);
+    j->n = n;
+    j->nnz = nnz;
+    j->opt = o;
+    j->lipschitz = lipschitz;
+    if (o.diagonal_gate >= 0) {
+        j->diag_gate = o.diagonal_gate ? 1 : 0;
+    } else {
+        bool diagonal = true;
+        for (int64_t i = 0; i < n && diagonal; ++i)
+            for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+                if (col[k] != i) { diagonal = false; break; }
+        bool positive = diagonal;
+        for (int64_t i = 0; i < n && positive; ++i) {
+            double d = 0;
+            for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) d += val[k];
+            if (!(d > 0)) positive = false;
+        }
+        j->diag_gate = positive ? 1 : 0;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (l[i] > u[i]) {
+            j->state = bqp::JOB_DONE;
+            j->stats.status = BQP_STATUS_INFEASIBLE_BOUNDS;
+            j->stats.objective = std::numeric_limits<double>::quiet_NaN();
+            j->stats.primal_residual = j->stats.stationarity_residual = HUGE_VAL;
+            j->stats.complementarity_residual = j->stats.relative_gap = HUGE_VAL;
+            j->stats.dual_bound = -HUGE_VAL;
+            *out = j.release();
+            return BQP_OK;
+        }
+    }
+    j->lanes = bqp::lanes_for(n, nnz, o.precision);
+    j->tiles = bqp::make_tiles(n, rowptr, j->lanes);
+    if (copy) {
+        j->own_rowptr.assign(rowptr, rowptr + n + 1);
+        j->own_col.assign(col, col + nnz);
+        j->own_val.assign(val, val + nnz);
+        j->own_c.assign(c, c + n);
+        j->own_l.assign(l, l + n);
+        j->own_u.assign(u, u + n);
+        j->rowptr = j->own_rowptr.data();
+        j->col = j->own_col.data();
+        j->val = j->own_val.data();
+        j->c = j->own_c.data();
+        j->l = j->own_l.data();
+        j->u = j->own_u.data();
+    } else {
+        j->rowptr = rowptr; j->col = col; j->val = val; j->c = c; j->l = l; j->u = u;
+    }
+    *out = j.release();
+    return BQP_OK;
+}
+
+int fail(bqp_ctx* ctx, int rc, const std::string& why) {
+    if (ctx) ctx->engine->set_error(why);
+    g_error = why;
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+void bqp_options_default(bqp_options* o) {
+    if (!o) return;
+    o->tolerance = 1e-7;
+    o->time_limit = 30;
+    o->iteration_limit = 200000;
+    o->precision = BQP_PRECISION_FP64;
+    o->lipschitz = BQP_LIPSCHITZ_GERSHGORIN;
+    o->check_interval = 25;
+    o->diagonal_gate = -1;
+    o->offset = 0;
+}
+
+bqp_ctx* bqp_create(int device, size_t mem_cap_bytes) {
+    std::unique_ptr<Engine> e(new (std::nothrow) Engine(device, mem_cap_bytes));
+    if (!e) {
+        g_error = "out of host memory";
+        return nullptr;
+    }
+    std::string why;
+    if (!e->init(why)) {
+        g_error = why;
+        return nullptr;
+    }
+    bqp_ctx* ctx = new (std::nothrow) bqp_ctx;
+    if (!ctx) {
+        g_error = "out of host memory";
+        return nullptr;
+    }
+    ctx->engine = e.release();
+    return ctx;
+}
+
+void bqp_destroy(bqp_ctx* ctx) {
+    if (!ctx) return;
+    delete ctx->engine;
+    delete ctx;
+}
+
+const char* bqp_last_error(const bqp_ctx* ctx) {
+    if (!ctx) return g_error.c_str();
+    return ctx->engine->error();
+}
+
+int bqp_device_name(int device, char* out, size_t cap) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        const char* msg = "No CUDA device available";
+        if (out && cap) { std::strncpy(out, msg, cap - 1); out[cap - 1] = 0; }
+        g_error = msg;
+        return BQP_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp p;
+    if (device < 0 || device >= count || cudaGetDeviceProperties(&p, device) != cudaSuccess) {
+        g_error = "Invalid CUDA device index";
+        return BQP_ERR_INVALID;
+    }
+    if (out && cap) {
+        std::strncpy(out, p.name, cap - 1);
+        out[cap - 1] = 0;
+    }
+    return BQP_OK;
+}
+
+int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+               const double* c, const double* lower, const double* upper, const bqp_options* options, uint64_t* id) {
+    if (!ctx) return fail(nullptr, BQP_ERR_INVALID, "null context");
+    Job* j = nullptr;
+    std::string why;
+    int rc = make_job(n, nnz, rowptr, col, val, c, lower, upper, options, true, &j, why);
+    if (rc != BQP_OK) return fail(ctx, rc, why);
+    return ctx->engine->submit(j, id);
+}
+
+int bqp_poll(bqp_ctx* ctx, uint64_t id, int32_t* status) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->poll(id, status);
+}
+
+int bqp_wait(bqp_ctx* ctx, uint64_t id, double timeout_seconds) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->wait(id, timeout_seconds);
+}
+
+int bqp_fetch(bqp_ctx* ctx, uint64_t id, double* x, bqp_stats* stats) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->fetch(id, x, stats);
+}
+
+int bqp_release(bqp_ctx* ctx, uint64_t id) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->release(id);
+}
+
+int bqp_resolve(bqp_ctx* ctx, const uint64_t* ids, int64_t count) {
+    if (!ctx || (count > 0 && !ids) || count < 0) return BQP_ERR_INVALID;
+    return ctx->engine->resolve(ids, count);
+}
+
+int bqp_set_latency_target(bqp_ctx* ctx, double ms) {
+    if (!ctx || !(ms >= 0) || !std::isfinite(ms)) return BQP_ERR_INVALID;
+    ctx->engine->set_latency_target(ms);
+    return BQP_OK;
+}
+
+int bqp_timer(bqp_ctx* ctx, int32_t reset, double* device_ms, int64_t* kernels, int64_t* graph_launches) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->timer(reset, device_ms, kernels, graph_launches);
+}
+
+int bqp_profile_step(bqp_ctx* ctx, uint64_t id, int32_t launches, double* ms_per_launch, double* bytes_per_launch) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->profile_step(id, launches, ms_per_launch, bytes_per_launch);
+}
+
+int bqp_load(bqp_ctx* ctx, int64_t* queued, int64_t* running, int64_t* peak_resident, int64_t* resident_bytes) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->load(queued, running, peak_resident, resident_bytes);
+}
+
+int bqp_solve_sync(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+                   const double* c, const double* lower, const double* upper, const bqp_options* options, double* x,
+                   bqp_stats* stats) {
+    if (!ctx) return fail(nullptr, BQP_ERR_INVALID, "null context");
+    Job* j = nullptr;
+    std::string why;
+    int rc = make_job(n, nnz, rowptr, col, val, c, lower, upper, options, false, &j, why);
+    if (rc != BQP_OK) return fail(ctx, rc, why);
+    uint64_t id = 0;
+    rc = ctx->engine->submit(j, &id);
+    if (rc != BQP_OK) return rc;
+    rc = ctx->engine->wait(id, -1);
+    int frc = ctx->engine->fetch(id, x, stats);
+    ctx->engine->release(id);
+    return rc != BQP_OK ? rc : frc;
+}
+
+}  // extern "C"

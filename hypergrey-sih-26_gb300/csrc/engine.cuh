@@ -1,0 +1,156 @@
+// Device-side data layout of the box-QP engine (shared by the kernels and the host engine).
+//
+// One resident solve ("instance") owns a device slab holding its CSR and vectors; a
+// batch is an array of instance records plus a table of row tiles.  Every kernel is a
+// grid-stride loop over the tile table, reads the tile's instance record, and skips
+// instances that are not in the phase the kernel serves, so one captured graph serves
+// any mix of instances that are admitted, iterating, polishing or retired.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bqp {
+
+constexpr int kBlock = 256;          // threads per CTA of every tile kernel
+constexpr int kMaxInterval = 32;     // maximum check interval (iterations per chunk)
+constexpr int kTileNnz = 4096;       // target nonzeros per tile
+constexpr int kTileRows = 512;       // maximum rows per tile
+
+enum Phase : int32_t {
+    PH_FISTA = 0,        // FISTA iterations (FP64 or FP32 per precision)
+    PH_POLISH_INIT = 1,  // FP64 free-set polish: snap the active set, start CG
+    PH_POLISH_CG = 2,    // FP64 conjugate gradient on Q_FF
+    PH_POLISH_FINISH = 3,  // CG done, xp clipped: the next check verifies the polished point
+    PH_DONE = 4
+};
+
+enum Status : int32_t {
+    ST_OPTIMAL = 0,
+    ST_ITERATION_LIMIT = 1,
+    ST_TIME_LIMIT = 2,
+    ST_NUMERICAL_ERROR = 3,
+    ST_RUNNING = 101
+};
+
+enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1, PREC_FP64_EXACT = 2 };
+
+struct Tile {
+    int32_t inst;
+    int32_t row_begin;
+    int32_t row_end;
+    int32_t lanes;  // lanes per row: 1, 2, 4, 8, 16 or 32
+};
+
+// Per-tile partial results of one check (or of one CG reduction).
+struct __align__(16) Partial {
+    double stat;          // max stationarity
+    double prim;          // max scaled bound violation (starts at 0)
+    double obj_hi, obj_lo;  // double-double objective sum
+    double bnd_hi, bnd_lo;  // double-double tangent dual bound terms
+    double sep_hi, sep_lo;  // double-double separable dual bound terms
+    double a, a_lo, b;    // CG: dot product (double-double) / max scaled residual
+    uint64_t hash;        // active-set signature
+    int64_t n_active;     // variables at a bound
+    int32_t flags;        // bit0: non-finite x, bit1: infinite bound target
+    int32_t pad;
+};
+
+struct __align__(16) InstDev {
+    // problem
+    const int32_t* rowptr;
+    const int32_t* col;
+    const double* val64;   // FP64 values (PREC_FP64, PREC_FP64_EXACT)
+    const float* vhi;      // FP32 high part (PREC_MIXED)
+    const float* vlo;      // FP32 low part, val ~= hi + lo (PREC_MIXED)
+    const double* c;
+    const double* l;
+    const double* u;
+    const float* c32;
+    const float* l32;      // smallest float >= l
+    const float* u32;      // largest float <= u
+    const double* diag;    // FP64 diagonal of Q
+    // iterates
+    double* x64;
+    double* w64[2];
+    float* x32;
+    float* w32[2];
+    double* xp;            // polished point (FP64)
+    double* r;
+    double* p;
+    double* q;
+    double* z;
+    uint8_t* fixed;        // polish: 1 = held at a bound
+    // geometry (the instance's tile range lives in View::ranges)
+    int32_t n;
+    int32_t diag_gate;
+    // control
+    int32_t status;
+    int32_t phase;
+    int32_t interval;
+    int32_t polish_rounds;
+    int32_t precision;
+    int32_t polish;        // mixed: free-set polish enabled
+    int64_t it0;          // iteration of the step j = 0 of the current chunk
+    int64_t it_next;       // iteration of the next check
+    int64_t max_iter;
+    int64_t deadline_ns;   // %globaltimer deadline
+    int64_t start_ns;
+    int64_t end_ns;
+    double L;
+    double invL;
+    float invLf;
+    int32_t result_src;    // where the answer lives: 0 x64, 1 x32, 2 xp
+    double tol;
+    double offset;
+    double t;              // FISTA t_k
+    double beta[kMaxInterval];
+    // last check
+    double objective;
+    double primal_res;
+    double stationarity;
+    double dual_bound;
+    double rel_gap;
+    int32_t verified;
+    int32_t stable_checks;
+    int64_t iterations;
+    uint64_t active_hash;
+    int64_t n_active;
+    double best_stat;
+    // polish (CG on the free set)
+    double rz;
+    double alpha;
+    double beta_cg;
+    double cg_res;
+    double cg_tol;
+    int64_t cg_it;
+    int64_t cg_total;
+    int64_t cg_max;
+    // accounting
+    int64_t fista_iters;
+    int64_t checks;
+};
+
+struct Ctrl {
+    int32_t n_inst;        // instance records in use
+    int32_t n_tiles;       // tiles in use
+    int32_t bodies;        // loop bodies run in the current launch
+    int32_t body_cap;      // stop the device loop after this many bodies
+    int32_t running;       // instances still running (written by the control kernel)
+    int32_t n_fista[3];    // instances in the FISTA phase, per precision
+    int32_t n_polish;
+    int32_t error;         // non-zero: a kernel detected an inconsistency
+    long long kernels;     // engine kernels executed by this launch (counted by gate/control)
+};
+
+// Everything a tile kernel needs, passed by value.
+struct View {
+    InstDev* inst;
+    const Tile* tiles;
+    Partial* partial;
+    int32_t* tile_done;    // per-instance count of finished tiles (check / CG reductions)
+    Ctrl* ctrl;
+    int32_t* status_mirror;  // per-instance status, rewritten by the control kernel every body
+    const int2* ranges;      // per-instance tile range [x, y) in the tile table
+};
+
+}  // namespace bqp

@@ -1,0 +1,999 @@
+// sm_103a kernels of the box-QP engine.
+//
+// Hot path (one launch per FISTA iteration, graph-replayed):
+//   step_kernel   fused CSR SpMV g = Q w, gradient step, clamp to [l,u], momentum update
+//                 w+ = x+ + beta (x+ - x): reads w from one ping-pong buffer and writes the
+//                 other, so no separate gradient array or second launch is needed
+//                 (the reference uses csr_product + fista_step, src/cuda_box.cu:16-21,29).
+//   check_kernel  FP64 verification of check_qp_solution (src/qp_admm.cpp:63-117) as block
+//                 reductions: objective, primal residual, projected stationarity, dual bound,
+//                 active-set signature; the last tile of each instance reduces that instance's
+//                 tile partials in a fixed order (deterministic, independent of co-scheduled
+//                 instances) and advances the instance's state machine.
+//   polish_*/cg_* FP64 conjugate gradient on the free set Q_FF x_F = -c_F - Q_FA x_A (mixed).
+//
+// Memory-bound design: SpMV streams values/columns once per iteration with read-only loads;
+// rows are processed by sub-warps of LANES lanes (chosen per instance from its row lengths);
+// FP64 arithmetic is kept out of the FP32 iterations (GB300's FP64 rate is ~1/64 of FP32).
+#include "kernels.cuh"
+
+#include <cmath>
+#include <cstdio>
+
+namespace bqp {
+namespace {
+
+#define kInf (__longlong_as_double(0x7ff0000000000000LL))
+
+__device__ __forceinline__ int64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return static_cast<int64_t>(t);
+}
+
+// std::max / std::min semantics of the reference.
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float smaxf(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float sminf(float a, float b) { return (b < a) ? b : a; }
+
+// ---- double-double accumulation (Knuth TwoSum; FMA TwoProduct) -----------------------------
+struct DD {
+    double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+    double s = __dadd_rn(a.hi, b.hi);
+    double bb = __dsub_rn(s, a.hi);
+    double e = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bb)), __dsub_rn(b.hi, bb));
+    e = __dadd_rn(e, __dadd_rn(a.lo, b.lo));
+    double h = __dadd_rn(s, e);
+    return {h, __dsub_rn(e, __dsub_rn(h, s))};
+}
+__device__ __forceinline__ double dd_value(DD a) { return __dadd_rn(a.hi, a.lo); }
+
+template <class T>
+__device__ __forceinline__ T shfl_xor(T v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+
+template <int LANES, class T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) v += shfl_xor(v, o);
+    return v;
+}
+
+// ---- check accumulator ----------------------------------------------------------------------
+struct Acc {
+    double stat, prim, obj, bnd, sep, a, b;
+    uint64_t hash;
+    long long nact;
+    int flags;
+};
+__device__ __forceinline__ Acc acc_identity() {
+    Acc a;
+    a.stat = 0; a.prim = 0; a.obj = 0; a.bnd = 0; a.sep = 0; a.a = 0; a.b = 0;
+    a.hash = 0; a.nact = 0; a.flags = 0;
+    return a;
+}
+struct AccDD {
+    double stat, prim, b;
+    DD obj, bnd, sep, a;
+    uint64_t hash;
+    long long nact;
+    int flags;
+};
+__device__ __forceinline__ AccDD to_dd(const Acc& x) {
+    AccDD r;
+    r.stat = x.stat; r.prim = x.prim; r.b = x.b;
+    r.obj = {x.obj, 0}; r.bnd = {x.bnd, 0}; r.sep = {x.sep, 0}; r.a = {x.a, 0};
+    r.hash = x.hash; r.nact = x.nact; r.flags = x.flags;
+    return r;
+}
+__device__ __forceinline__ AccDD combine(const AccDD& x, const AccDD& y) {
+    AccDD r;
+    r.stat = smax(x.stat, y.stat);
+    r.prim = smax(x.prim, y.prim);
+    r.b = smax(x.b, y.b);
+    r.obj = dd_add(x.obj, y.obj);
+    r.bnd = dd_add(x.bnd, y.bnd);
+    r.sep = dd_add(x.sep, y.sep);
+    r.a = dd_add(x.a, y.a);
+    r.hash = x.hash ^ y.hash;
+    r.nact = x.nact + y.nact;
+    r.flags = x.flags | y.flags;
+    return r;
+}
+__device__ __forceinline__ AccDD shfl_acc(const AccDD& x, int o) {
+    AccDD r;
+    r.stat = shfl_xor(x.stat, o); r.prim = shfl_xor(x.prim, o); r.b = shfl_xor(x.b, o);
+    r.obj.hi = shfl_xor(x.obj.hi, o); r.obj.lo = shfl_xor(x.obj.lo, o);
+    r.bnd.hi = shfl_xor(x.bnd.hi, o); r.bnd.lo = shfl_xor(x.bnd.lo, o);
+    r.sep.hi = shfl_xor(x.sep.hi, o); r.sep.lo = shfl_xor(x.sep.lo, o);
+    r.a.hi = shfl_xor(x.a.hi, o); r.a.lo = shfl_xor(x.a.lo, o);
+    r.hash = shfl_xor(static_cast<unsigned long long>(x.hash), o);
+    r.nact = shfl_xor(x.nact, o);
+    r.flags = shfl_xor(x.flags, o);
+    return r;
+}
+
+// Fixed-order block reduction; the result is valid in thread 0.
+__device__ AccDD block_reduce(AccDD v) {
+    __shared__ AccDD warp_part[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = combine(v, shfl_acc(v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        AccDD w = warp_part[lane < kBlock / 32 ? lane : 0];
+        if (lane >= kBlock / 32) {
+            w = to_dd(acc_identity());
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w = combine(w, shfl_acc(w, o));
+        v = w;
+    }
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ void store_partial(Partial* p, const AccDD& v) {
+    p->stat = v.stat; p->prim = v.prim;
+    p->obj_hi = v.obj.hi; p->obj_lo = v.obj.lo;
+    p->bnd_hi = v.bnd.hi; p->bnd_lo = v.bnd.lo;
+    p->sep_hi = v.sep.hi; p->sep_lo = v.sep.lo;
+    p->a = v.a.hi; p->a_lo = v.a.lo; p->b = v.b;
+    p->hash = v.hash; p->n_active = v.nact; p->flags = v.flags;
+    p->pad = 0;
+}
+__device__ __forceinline__ AccDD load_partial(const Partial* p) {
+    AccDD r;
+    r.stat = __ldcg(&p->stat); r.prim = __ldcg(&p->prim);
+    r.obj = {__ldcg(&p->obj_hi), __ldcg(&p->obj_lo)};
+    r.bnd = {__ldcg(&p->bnd_hi), __ldcg(&p->bnd_lo)};
+    r.sep = {__ldcg(&p->sep_hi), __ldcg(&p->sep_lo)};
+    r.a = {__ldcg(&p->a), __ldcg(&p->a_lo)};
+    r.b = __ldcg(&p->b);
+    r.hash = __ldcg(reinterpret_cast<const unsigned long long*>(&p->hash));
+    r.nact = __ldcg(reinterpret_cast<const long long*>(&p->n_active));
+    r.flags = __ldcg(&p->flags);
+    return r;
+}
+
+// Publishes the block's partial for tile t and returns true in every thread of the block
+// that finished the instance's last outstanding tile.
+__device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles_inst, const AccDD& total) {
+    __shared__ int is_last;
+    if (threadIdx.x == 0) {
+        store_partial(&v.partial[t], total);
+        __threadfence();
+        int prev = atomicAdd(&v.tile_done[inst], 1);
+        is_last = (prev == ntiles_inst - 1);
+        if (is_last) v.tile_done[inst] = 0;
+    }
+    __syncthreads();
+    bool last = is_last != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+// Reduces the partials of tiles [tb, te) in a fixed order; valid in thread 0.
+__device__ AccDD reduce_instance(const View& v, int tb, int te) {
+    AccDD acc = to_dd(acc_identity());
+    for (int k = tb + threadIdx.x; k < te; k += kBlock) acc = combine(acc, load_partial(&v.partial[k]));
+    return block_reduce(acc);
+}
+
+// ---- one row of check_qp_solution ------------------------------------------------------------
+__device__ __forceinline__ uint64_t mix_index(uint64_t k) {
+    k = (k + 1) * 0x9E3779B97F4A7C15ULL;
+    k ^= k >> 31;
+    k *= 0xBF58476D1CE4E5B9ULL;
+    return k ^ (k >> 29);
+}
+
+__device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double ci, double li, double ui, double di,
+                                          int gate, int row, bool at_lower, bool at_upper) {
+    if (!isfinite(xi)) {
+        a.flags |= 1;
+        return;
+    }
+    a.obj = fma(0.5 * xi, gq, a.obj);
+    a.obj = fma(ci, xi, a.obj);
+    const double g = gq + ci;
+    double res = fabs(xi - smax(li, smin(ui, xi - g))) / (1.0 + fabs(xi));
+    if (!isfinite(g) || !isfinite(res)) res = kInf;
+    a.stat = smax(a.stat, res);
+    const double ax = fabs(xi);
+    if (isfinite(li)) a.prim = smax(a.prim, (li - xi) / (1.0 + fabs(li) + ax));
+    if (isfinite(ui)) a.prim = smax(a.prim, (xi - ui) / (1.0 + fabs(ui) + ax));
+    if (g != 0) {
+        double target = g > 0 ? li : ui;
+        if (isfinite(target)) a.bnd += g * (target - xi);
+        else a.flags |= 2;
+    }
+    if (gate) {
+        double m = smax(li, smin(ui, -ci / di));
+        a.sep += 0.5 * di * m * m + ci * m;
+    }
+    if (at_lower) {
+        a.hash ^= mix_index(2ull * static_cast<uint64_t>(row));
+        a.nact++;
+    } else if (at_upper) {
+        a.hash ^= mix_index(2ull * static_cast<uint64_t>(row) + 1);
+        a.nact++;
+    }
+}
+
+// Sources of one check: MODE 0 FP64 values + x64; 1 hi/lo values + x32; 2 hi/lo values + xp.
+struct CheckSrc {
+    const int32_t* rowptr;
+    const int32_t* col;
+    const double* val64;
+    const float* vhi;
+    const float* vlo;
+    const double* x64;
+    const float* x32;
+    const double* xp;
+    const double* c;
+    const double* l;
+    const double* u;
+    const float* l32;
+    const float* u32;
+    const double* diag;
+    int gate;
+};
+
+template <int MODE>
+__device__ __forceinline__ double check_value(const CheckSrc& s, int k) {
+    if constexpr (MODE == 0) return __ldg(s.val64 + k);
+    else return static_cast<double>(__ldg(s.vhi + k)) + static_cast<double>(__ldg(s.vlo + k));
+}
+template <int MODE>
+__device__ __forceinline__ double check_x(const CheckSrc& s, int k) {
+    if constexpr (MODE == 0) return s.x64[k];
+    else if constexpr (MODE == 1) return static_cast<double>(s.x32[k]);
+    else return s.xp[k];
+}
+
+template <int LANES, int MODE>
+__device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
+    constexpr int RPW = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
+        const int r = base + sub;
+        double acc = 0;
+        if (r < re) {
+            const int ks = __ldg(s.rowptr + r), ke = __ldg(s.rowptr + r + 1);
+            for (int k = ks + sl; k < ke; k += LANES) acc = fma(check_value<MODE>(s, k), check_x<MODE>(s, __ldg(s.col + k)), acc);
+        }
+        acc = group_sum<LANES>(acc);
+        if (r < re && sl == 0) {
+            const double xi = check_x<MODE>(s, r);
+            bool atl, atu;
+            if constexpr (MODE == 1) {
+                const float xf = s.x32[r];
+                atl = xf <= s.l32[r];
+                atu = xf >= s.u32[r];
+            } else {
+                atl = xi <= s.l[r];
+                atu = xi >= s.u[r];
+            }
+            double di = 1.0;
+            if (s.gate) {
+                if (s.diag) {
+                    di = s.diag[r];
+                } else {
+                    // a diagonal Hessian has exactly its diagonal entry in each non-empty row
+                    const int ks = __ldg(s.rowptr + r), ke = __ldg(s.rowptr + r + 1);
+                    di = ks < ke ? check_value<MODE>(s, ks) : 0.0;
+                }
+            }
+            check_row(a, xi, acc, s.c[r], s.l[r], s.u[r], di, s.gate, r, atl, atu);
+        }
+    }
+}
+
+template <int MODE>
+__device__ void check_rows_dispatch(const CheckSrc& s, int lanes, int rb, int re, Acc& a) {
+    switch (lanes) {
+    case 1: check_rows<1, MODE>(s, rb, re, a); break;
+    case 2: check_rows<2, MODE>(s, rb, re, a); break;
+    case 4: check_rows<4, MODE>(s, rb, re, a); break;
+    case 8: check_rows<8, MODE>(s, rb, re, a); break;
+    case 16: check_rows<16, MODE>(s, rb, re, a); break;
+    default: check_rows<32, MODE>(s, rb, re, a); break;
+    }
+}
+
+__device__ __forceinline__ CheckSrc source_of(const InstDev& I) {
+    CheckSrc s;
+    s.rowptr = I.rowptr; s.col = I.col; s.val64 = I.val64; s.vhi = I.vhi; s.vlo = I.vlo;
+    s.x64 = I.x64; s.x32 = I.x32; s.xp = I.xp; s.c = I.c; s.l = I.l; s.u = I.u;
+    s.l32 = I.l32; s.u32 = I.u32; s.diag = I.diag; s.gate = I.diag_gate;
+    return s;
+}
+
+// ---- the state machine after a check (thread 0 of the finalizing block) -------------------
+__device__ void fista_betas(InstDev& I, int64_t count) {
+    // t_{k+1} = (1 + sqrt(1 + 4 t_k^2)) / 2, beta_k = (t_k - 1) / t_{k+1}
+    // (src/accelerated_qp.cpp:47), each operation rounded as the reference's CPU loop rounds it.
+    double t = I.t;
+    for (int64_t j = 0; j < count; ++j) {
+        double nt = __ddiv_rn(__dadd_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(4.0, t), t)))), 2.0);
+        I.beta[j] = __ddiv_rn(__dsub_rn(t, 1.0), nt);
+        t = nt;
+    }
+    I.t = t;
+}
+
+__device__ void finish(InstDev& I, int status, int src) {
+    I.status = status;
+    I.phase = PH_DONE;
+    I.result_src = src;
+    I.end_ns = now_ns();
+}
+
+__device__ void after_check(InstDev& I, const AccDD& tot) {
+    const int64_t it_check = I.it_next;
+    const int ph = I.phase;
+    I.checks++;
+    double obj, stat, prim, bound, gap;
+    if (tot.flags & 1) {
+        obj = __longlong_as_double(0x7ff8000000000000LL);
+        stat = kInf; prim = kInf; bound = -kInf; gap = kInf;
+    } else {
+        DD value = dd_add(tot.obj, DD{I.offset, 0.0});
+        obj = dd_value(value);
+        stat = tot.stat;
+        prim = tot.prim;
+        if (I.diag_gate) bound = dd_value(dd_add(tot.sep, DD{I.offset, 0.0}));
+        else bound = (tot.flags & 2) ? -kInf : dd_value(dd_add(value, tot.bnd));
+        gap = isfinite(bound) ? fabs(obj - bound) / (1.0 + fabs(obj)) : kInf;
+    }
+    const double worst = smax(prim, smax(stat, 0.0));
+    bool verified = isfinite(obj) && worst <= I.tol;
+    if (I.diag_gate) verified = verified && gap <= I.tol;
+    I.objective = obj;
+    I.primal_res = prim;
+    I.stationarity = stat;
+    I.dual_bound = bound;
+    I.rel_gap = gap;
+    I.verified = verified ? 1 : 0;
+    I.iterations = it_check;
+    const int src = (ph == PH_POLISH_FINISH) ? 2 : (I.precision == PREC_MIXED ? 1 : 0);
+    if (verified) { finish(I, ST_OPTIMAL, src); return; }
+    if (!isfinite(obj) || !isfinite(stat)) { finish(I, ST_NUMERICAL_ERROR, src); return; }
+    if (now_ns() >= I.deadline_ns) { finish(I, ST_TIME_LIMIT, src); return; }
+    if (it_check >= I.max_iter) { finish(I, ST_ITERATION_LIMIT, src); return; }
+    if (ph == PH_POLISH_FINISH) {
+        // The polished point failed verification: the active-set guess was wrong.  FISTA
+        // resumes from its own untouched state at it_check.
+        I.polish_rounds++;
+        I.stable_checks = 0;
+    } else if (I.precision == PREC_MIXED && I.polish && I.polish_rounds < 3) {
+        const bool stable = tot.hash == I.active_hash && tot.nact == I.n_active;
+        I.stable_checks = stable ? I.stable_checks + 1 : 0;
+        I.active_hash = tot.hash;
+        I.n_active = tot.nact;
+        double sw = 1e-3;
+        for (int k = 0; k < I.polish_rounds; ++k) sw *= 0.1;
+        if (I.stable_checks >= 1 && stat <= sw) {
+            I.phase = PH_POLISH_INIT;
+            I.cg_it = 0;
+            return;
+        }
+    }
+    I.phase = PH_FISTA;
+    I.it0 = it_check;
+    I.it_next = it_check + I.interval < I.max_iter ? it_check + I.interval : I.max_iter;
+    const int64_t count = I.it_next - I.it0;
+    fista_betas(I, count);
+    I.fista_iters += count;
+}
+
+// ---- step kernel ------------------------------------------------------------------------------
+template <int LANES, int PREC>
+__device__ void step_rows(const InstDev& I, int rb, int re, int j) {
+    const int64_t it = I.it0 + j;
+    const int in = static_cast<int>(it & 1), out = in ^ 1;
+    constexpr int RPW = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    const int32_t* __restrict__ rowptr = I.rowptr;
+    const int32_t* __restrict__ col = I.col;
+    if constexpr (PREC == PREC_MIXED) {
+        const float* __restrict__ val = I.vhi;
+        const float* __restrict__ win = I.w32[in];
+        float* __restrict__ wout = I.w32[out];
+        float* __restrict__ x = I.x32;
+        const float* __restrict__ c = I.c32;
+        const float* __restrict__ l = I.l32;
+        const float* __restrict__ u = I.u32;
+        const float beta = static_cast<float>(I.beta[j]);
+        const float invL = I.invLf;
+        for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
+            const int r = base + sub;
+            float acc = 0.f;
+            if (r < re) {
+                const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+                for (int k = ks + sl; k < ke; k += LANES) acc = fmaf(__ldg(val + k), __ldg(win + __ldg(col + k)), acc);
+            }
+            acc = group_sum<LANES>(acc);
+            if (r < re && sl == 0) {
+                const float v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+                const float nx = smaxf(__ldg(l + r), sminf(__ldg(u + r), v));
+                wout[r] = nx + beta * (nx - x[r]);
+                x[r] = nx;
+            }
+        }
+    } else if constexpr (PREC == PREC_FP64) {
+        const double* __restrict__ val = I.val64;
+        const double* __restrict__ win = I.w64[in];
+        double* __restrict__ wout = I.w64[out];
+        double* __restrict__ x = I.x64;
+        const double* __restrict__ c = I.c;
+        const double* __restrict__ l = I.l;
+        const double* __restrict__ u = I.u;
+        const double beta = I.beta[j];
+        const double invL = I.invL;
+        for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
+            const int r = base + sub;
+            double acc = 0.0;
+            if (r < re) {
+                const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+                for (int k = ks + sl; k < ke; k += LANES) acc = fma(__ldg(val + k), __ldg(win + __ldg(col + k)), acc);
+            }
+            acc = group_sum<LANES>(acc);
+            if (r < re && sl == 0) {
+                const double v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+                const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
+                wout[r] = nx + beta * (nx - x[r]);
+                x[r] = nx;
+            }
+        }
+    } else {
+        // PREC_FP64_EXACT: one thread per row, products and sums rounded separately in column
+        // order from 0.0 and division by L -- the reference CPU loop's arithmetic exactly.
+        const double* __restrict__ val = I.val64;
+        const double* __restrict__ win = I.w64[in];
+        double* __restrict__ wout = I.w64[out];
+        double* __restrict__ x = I.x64;
+        const double* __restrict__ c = I.c;
+        const double* __restrict__ l = I.l;
+        const double* __restrict__ u = I.u;
+        const double beta = I.beta[j];
+        const double L = I.L;
+        for (int r = rb + static_cast<int>(threadIdx.x); r < re; r += kBlock) {
+            double acc = 0.0;
+            const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+            for (int k = ks; k < ke; ++k) acc = __dadd_rn(acc, __dmul_rn(__ldg(val + k), __ldg(win + __ldg(col + k))));
+            const double v = __dsub_rn(__ldg(win + r), __ddiv_rn(__dadd_rn(acc, __ldg(c + r)), L));
+            const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
+            wout[r] = __dadd_rn(nx, __dmul_rn(beta, __dsub_rn(nx, x[r])));
+            x[r] = nx;
+        }
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kBlock) step_kernel(View v, int j) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        const InstDev& I = v.inst[T.inst];
+        if (I.status != ST_RUNNING || I.phase != PH_FISTA || I.precision != PREC) continue;
+        if (I.it0 + j >= I.it_next) continue;
+        if constexpr (PREC == PREC_FP64_EXACT) {
+            step_rows<1, PREC>(I, T.row_begin, T.row_end, j);
+        } else {
+            switch (T.lanes) {
+            case 1: step_rows<1, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 2: step_rows<2, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 4: step_rows<4, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 8: step_rows<8, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 16: step_rows<16, PREC>(I, T.row_begin, T.row_end, j); break;
+            default: step_rows<32, PREC>(I, T.row_begin, T.row_end, j); break;
+            }
+        }
+    }
+}
+
+// ---- check kernel -----------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) check_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        InstDev& I = v.inst[T.inst];
+        if (I.status != ST_RUNNING) continue;
+        const int ph = I.phase;
+        if (ph != PH_FISTA && ph != PH_POLISH_FINISH) continue;
+        const CheckSrc s = source_of(I);
+        Acc a = acc_identity();
+        if (I.precision == PREC_MIXED) {
+            if (ph == PH_POLISH_FINISH) check_rows_dispatch<2>(s, T.lanes, T.row_begin, T.row_end, a);
+            else check_rows_dispatch<1>(s, T.lanes, T.row_begin, T.row_end, a);
+        } else {
+            check_rows_dispatch<0>(s, T.lanes, T.row_begin, T.row_end, a);
+        }
+        AccDD total = block_reduce(to_dd(a));
+        const int2 R = v.ranges[T.inst];
+        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
+            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            if (threadIdx.x == 0) after_check(I, inst_total);
+            __syncthreads();
+        }
+    }
+}
+
+// ---- FP64 free-set polish ---------------------------------------------------------------------
+__device__ __forceinline__ bool polish_phase(const InstDev& I, int phase) {
+    return I.status == ST_RUNNING && I.phase == phase;
+}
+
+__global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        const InstDev& I = v.inst[T.inst];
+        if (!polish_phase(I, PH_POLISH_INIT)) continue;
+        for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
+            const float xf = I.x32[r];
+            uint8_t fixed = 1;
+            double xv;
+            if (xf <= I.l32[r]) xv = I.l[r];
+            else if (xf >= I.u32[r]) xv = I.u[r];
+            else { xv = static_cast<double>(xf); fixed = 0; }
+            I.xp[r] = xv;
+            I.fixed[r] = fixed;
+        }
+    }
+}
+
+template <int LANES>
+__device__ void hilo_matvec_rows(const InstDev& I, int rb, int re, const double* __restrict__ src,
+                                 bool residual, Acc& a) {
+    constexpr int RPW = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
+        const int r = base + sub;
+        double acc = 0;
+        const bool live = r < re && !I.fixed[r];
+        if (live) {
+            const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+            for (int k = ks + sl; k < ke; k += LANES) {
+                const double vk = static_cast<double>(__ldg(I.vhi + k)) + static_cast<double>(__ldg(I.vlo + k));
+                acc = fma(vk, src[__ldg(I.col + k)], acc);
+            }
+        }
+        acc = group_sum<LANES>(acc);
+        if (r < re && sl == 0) {
+            if (residual) {
+                // r = -(Q xp + c) on the free set, z = D^-1 r, p = z
+                double rr = 0, zz = 0;
+                if (live) {
+                    rr = -(acc + I.c[r]);
+                    const double d = I.diag[r];
+                    zz = d > 0 ? rr / d : rr;
+                    a.a = fma(rr, zz, a.a);
+                    a.b = smax(a.b, fabs(rr) / (1.0 + fabs(I.xp[r])));
+                }
+                I.r[r] = rr;
+                I.z[r] = zz;
+                I.p[r] = zz;
+            } else {
+                const double qq = live ? acc : 0.0;
+                I.q[r] = qq;
+                if (live) a.a = fma(I.p[r], qq, a.a);
+            }
+        }
+    }
+}
+
+__device__ void hilo_matvec_dispatch(const InstDev& I, int lanes, int rb, int re, const double* src, bool residual, Acc& a) {
+    switch (lanes) {
+    case 1: hilo_matvec_rows<1>(I, rb, re, src, residual, a); break;
+    case 2: hilo_matvec_rows<2>(I, rb, re, src, residual, a); break;
+    case 4: hilo_matvec_rows<4>(I, rb, re, src, residual, a); break;
+    case 8: hilo_matvec_rows<8>(I, rb, re, src, residual, a); break;
+    case 16: hilo_matvec_rows<16>(I, rb, re, src, residual, a); break;
+    default: hilo_matvec_rows<32>(I, rb, re, src, residual, a); break;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) polish_residual_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        InstDev& I = v.inst[T.inst];
+        if (!polish_phase(I, PH_POLISH_INIT)) continue;
+        Acc a = acc_identity();
+        hilo_matvec_dispatch(I, T.lanes, T.row_begin, T.row_end, I.xp, true, a);
+        AccDD total = block_reduce(to_dd(a));
+        const int2 R = v.ranges[T.inst];
+        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
+            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            if (threadIdx.x == 0) {
+                I.rz = dd_value(inst_total.a);
+                I.cg_res = inst_total.b;
+                I.cg_it = 0;
+                I.phase = (inst_total.b <= I.cg_tol || !(I.rz > 0)) ? PH_POLISH_FINISH : PH_POLISH_CG;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) cg_matvec_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        InstDev& I = v.inst[T.inst];
+        if (!polish_phase(I, PH_POLISH_CG)) continue;
+        Acc a = acc_identity();
+        hilo_matvec_dispatch(I, T.lanes, T.row_begin, T.row_end, I.p, false, a);
+        AccDD total = block_reduce(to_dd(a));
+        const int2 R = v.ranges[T.inst];
+        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
+            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            if (threadIdx.x == 0) {
+                const double pq = dd_value(inst_total.a);
+                if (pq > 0 && isfinite(pq)) {
+                    I.alpha = I.rz / pq;
+                } else {
+                    I.alpha = 0;
+                    I.cg_it = I.cg_max;  // breakdown: stop after this update
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        InstDev& I = v.inst[T.inst];
+        if (!polish_phase(I, PH_POLISH_CG)) continue;
+        const double alpha = I.alpha;
+        Acc a = acc_identity();
+        for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
+            if (I.fixed[r]) continue;
+            const double xv = fma(alpha, I.p[r], I.xp[r]);
+            const double rr = fma(-alpha, I.q[r], I.r[r]);
+            const double d = I.diag[r];
+            const double zz = d > 0 ? rr / d : rr;
+            I.xp[r] = xv;
+            I.r[r] = rr;
+            I.z[r] = zz;
+            a.a = fma(rr, zz, a.a);
+            a.b = smax(a.b, fabs(rr) / (1.0 + fabs(xv)));
+        }
+        AccDD total = block_reduce(to_dd(a));
+        const int2 R = v.ranges[T.inst];
+        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
+            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            if (threadIdx.x == 0) {
+                const double rz_new = dd_value(inst_total.a);
+                I.beta_cg = I.rz > 0 ? rz_new / I.rz : 0.0;
+                I.rz = rz_new;
+                I.cg_res = inst_total.b;
+                I.cg_it++;
+                I.cg_total++;
+                if (inst_total.b <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) I.phase = PH_POLISH_FINISH;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Tile T = v.tiles[t];
+        const InstDev& I = v.inst[T.inst];
+        if (I.status != ST_RUNNING) continue;
+        if (I.phase == PH_POLISH_CG) {
+            const double beta = I.beta_cg;
+            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock)
+                if (!I.fixed[r]) I.p[r] = fma(beta, I.p[r], I.z[r]);
+        } else if (I.phase == PH_POLISH_FINISH) {
+            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock)
+                I.xp[r] = smax(I.l[r], smin(I.u[r], I.xp[r]));
+        }
+    }
+}
+
+// ---- control kernels (one block) ---------------------------------------------------------------
+struct Counts {
+    int running, fista[3], polish;
+};
+
+__device__ Counts count_phases(const View& v, bool mirror) {
+    __shared__ int s[5];
+    if (threadIdx.x < 5) s[threadIdx.x] = 0;
+    __syncthreads();
+    int nr = 0, nf0 = 0, nf1 = 0, nf2 = 0, np = 0;
+    const int n = v.ctrl->n_inst;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const InstDev& I = v.inst[i];
+        const int st = I.status;
+        if (mirror) v.status_mirror[i] = st;
+        if (st != ST_RUNNING) continue;
+        nr++;
+        if (I.phase == PH_FISTA) {
+            if (I.precision == PREC_MIXED) nf1++;
+            else if (I.precision == PREC_FP64_EXACT) nf2++;
+            else nf0++;
+        } else if (I.phase == PH_POLISH_INIT || I.phase == PH_POLISH_CG) {
+            np++;
+        }
+    }
+    if (nr) atomicAdd(&s[0], nr);
+    if (nf0) atomicAdd(&s[1], nf0);
+    if (nf1) atomicAdd(&s[2], nf1);
+    if (nf2) atomicAdd(&s[3], nf2);
+    if (np) atomicAdd(&s[4], np);
+    __syncthreads();
+    Counts c;
+    c.running = s[0];
+    c.fista[0] = s[1];
+    c.fista[1] = s[2];
+    c.fista[2] = s[3];
+    c.polish = s[4];
+    return c;
+}
+
+__global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraphConditionalHandle h_mixed,
+                            cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish, int steps,
+                            int polish_kernels) {
+    const Counts c = count_phases(v, false);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
+        v.ctrl->n_polish = c.polish;
+        long long launched = 2;  // check + gate
+        for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps : 0;
+        launched += c.polish > 0 ? polish_kernels : 0;
+        v.ctrl->kernels += launched;
+        cudaGraphSetConditional(h_fp64, c.fista[0] > 0 ? 1u : 0u);
+        cudaGraphSetConditional(h_mixed, c.fista[1] > 0 ? 1u : 0u);
+        cudaGraphSetConditional(h_exact, c.fista[2] > 0 ? 1u : 0u);
+        cudaGraphSetConditional(h_polish, c.polish > 0 ? 1u : 0u);
+    }
+}
+
+__global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h) {
+    const Counts c = count_phases(v, true);
+    if (threadIdx.x == 0) {
+        Ctrl* ctrl = v.ctrl;
+        ctrl->bodies++;
+        ctrl->kernels += 1;
+        ctrl->running = c.running;
+        cudaGraphSetConditional(loop_h, (c.running > 0 && ctrl->bodies < ctrl->body_cap) ? 1u : 0u);
+    }
+}
+
+__global__ void gate_plain_kernel(View v) {
+    const Counts c = count_phases(v, false);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
+        v.ctrl->n_polish = c.polish;
+    }
+}
+
+__global__ void control_plain_kernel(View v) {
+    const Counts c = count_phases(v, true);
+    if (threadIdx.x == 0) {
+        v.ctrl->bodies++;
+        v.ctrl->running = c.running;
+    }
+}
+
+__global__ void init_instance_kernel(View v, int slot, int n, int precision) {
+    InstDev& I = v.inst[slot];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        if (precision == PREC_MIXED) {
+            const float x0 = smaxf(I.l32[r], sminf(I.u32[r], 0.0f));
+            I.x32[r] = x0;
+            I.w32[0][r] = x0;
+        } else {
+            const double x0 = smax(I.l[r], smin(I.u[r], 0.0));
+            I.x64[r] = x0;
+            I.w64[0][r] = x0;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int64_t start = now_ns();
+        I.start_ns = start;
+        I.deadline_ns = start + I.deadline_ns;  // host stores the budget in nanoseconds
+        I.end_ns = 0;
+    }
+}
+
+// Derives the device-side forms of an uploaded instance: FP64 diagonal (Jacobi preconditioner and
+// the diagonal dual-gap gate) and, for mixed precision, hi/lo FP32 values (val ~= hi + lo), the
+// FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
+// so FP32 iterates never leave the FP64 box).
+__global__ void prepare_kernel(View v, int slot, int n, const double* __restrict__ val) {
+    InstDev& I = v.inst[slot];
+    const int stride = gridDim.x * blockDim.x;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x;
+    double* diag = const_cast<double*>(I.diag);
+    for (int r = first; r < n; r += stride) {
+        const int ks = I.rowptr[r], ke = I.rowptr[r + 1];
+        double d = 0;
+        for (int k = ks; k < ke; ++k) if (I.col[k] == r) d += val[k];
+        diag[r] = d;
+        if (I.precision == PREC_MIXED) {
+            const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
+            const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
+            const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+        }
+    }
+    if (I.precision == PREC_MIXED) {
+        const int nnz = I.rowptr[n];
+        for (int k = first; k < nnz; k += stride) {
+            const double x = val[k];
+            const float hi = __double2float_rn(x);
+            const_cast<float*>(I.vhi)[k] = hi;
+            const_cast<float*>(I.vlo)[k] = __double2float_rn(x - static_cast<double>(hi));
+        }
+    }
+}
+
+// ---- standalone check on caller arrays ---------------------------------------------------------
+struct StandaloneScratch {
+    int done;
+    int pad[3];
+};
+
+__global__ void __launch_bounds__(kBlock) check_standalone_kernel(CheckSrc s, int n, double tol, double offset,
+                                                                 Partial* partial, StandaloneScratch* scr,
+                                                                 double* result) {
+    const int rows_per_block = (n + gridDim.x - 1) / gridDim.x;
+    const int rb = blockIdx.x * rows_per_block;
+    const int re = min(n, rb + rows_per_block);
+    Acc a = acc_identity();
+    if (rb < re) check_rows<4, 0>(s, rb, re, a);
+    AccDD total = block_reduce(to_dd(a));
+    __shared__ int is_last;
+    if (threadIdx.x == 0) {
+        store_partial(&partial[blockIdx.x], total);
+        __threadfence();
+        is_last = atomicAdd(&scr->done, 1) == static_cast<int>(gridDim.x) - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    AccDD acc = to_dd(acc_identity());
+    for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += kBlock) acc = combine(acc, load_partial(&partial[k]));
+    AccDD tot = block_reduce(acc);
+    if (threadIdx.x == 0) {
+        scr->done = 0;
+        double obj, stat, prim, bound, gap;
+        if (tot.flags & 1) {
+            obj = __longlong_as_double(0x7ff8000000000000LL);
+            stat = kInf; prim = kInf; bound = -kInf; gap = kInf;
+        } else {
+            DD value = dd_add(tot.obj, DD{offset, 0.0});
+            obj = dd_value(value);
+            stat = tot.stat;
+            prim = tot.prim;
+            if (s.gate) bound = dd_value(dd_add(tot.sep, DD{offset, 0.0}));
+            else bound = (tot.flags & 2) ? -kInf : dd_value(dd_add(value, tot.bnd));
+            gap = isfinite(bound) ? fabs(obj - bound) / (1.0 + fabs(obj)) : kInf;
+        }
+        bool verified = isfinite(obj) && smax(prim, smax(stat, 0.0)) <= tol;
+        if (s.gate) verified = verified && gap <= tol;
+        result[0] = obj;
+        result[1] = prim;
+        result[2] = stat;
+        result[3] = 0.0;
+        result[4] = bound;
+        result[5] = gap;
+        result[6] = verified ? 1.0 : 0.0;
+        result[7] = static_cast<double>(tot.nact);
+    }
+}
+
+// ---- plugin-level FISTA step --------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) box_step_kernel(int n, const int32_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const double* __restrict__ val,
+                                                          const double* __restrict__ c,
+                                                          const double* __restrict__ l,
+                                                          const double* __restrict__ u, double L, double beta,
+                                                          double* __restrict__ x, const double* __restrict__ w_in,
+                                                          double* __restrict__ w_out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+        for (int k = ks; k < ke; ++k) acc = __dadd_rn(acc, __dmul_rn(__ldg(val + k), __ldg(w_in + __ldg(col + k))));
+        const double v = __dsub_rn(__ldg(w_in + r), __ddiv_rn(__dadd_rn(acc, __ldg(c + r)), L));
+        const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
+        w_out[r] = __dadd_rn(nx, __dmul_rn(beta, __dsub_rn(nx, x[r])));
+        x[r] = nx;
+    }
+}
+
+}  // namespace
+
+// ---- launch wrappers -----------------------------------------------------------------------------
+void launch_check(const View& v, int grid, cudaStream_t s) { check_kernel<<<grid, kBlock, 0, s>>>(v); }
+
+void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s) {
+    switch (precision) {
+    case PREC_MIXED: step_kernel<PREC_MIXED><<<grid, kBlock, 0, s>>>(v, j); break;
+    case PREC_FP64_EXACT: step_kernel<PREC_FP64_EXACT><<<grid, kBlock, 0, s>>>(v, j); break;
+    default: step_kernel<PREC_FP64><<<grid, kBlock, 0, s>>>(v, j); break;
+    }
+}
+
+void launch_polish_init(const View& v, int grid, cudaStream_t s) { polish_init_kernel<<<grid, kBlock, 0, s>>>(v); }
+void launch_polish_residual(const View& v, int grid, cudaStream_t s) { polish_residual_kernel<<<grid, kBlock, 0, s>>>(v); }
+void launch_cg_matvec(const View& v, int grid, cudaStream_t s) { cg_matvec_kernel<<<grid, kBlock, 0, s>>>(v); }
+void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<grid, kBlock, 0, s>>>(v); }
+void launch_cg_direction(const View& v, int grid, cudaStream_t s) { cg_direction_kernel<<<grid, kBlock, 0, s>>>(v); }
+
+void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish, int steps,
+                 int polish_kernels, cudaStream_t s) {
+    gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, steps, polish_kernels);
+}
+void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s) {
+    control_kernel<<<1, 1024, 0, s>>>(v, loop);
+}
+void launch_gate_plain(const View& v, cudaStream_t s) { gate_plain_kernel<<<1, 1024, 0, s>>>(v); }
+void launch_control_plain(const View& v, cudaStream_t s) { control_plain_kernel<<<1, 1024, 0, s>>>(v); }
+
+void launch_init_instance(const View& v, int slot, int n, int precision, cudaStream_t s) {
+    int grid = (n + kBlock - 1) / kBlock;
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    init_instance_kernel<<<grid, kBlock, 0, s>>>(v, slot, n, precision);
+}
+
+void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
+    int64_t work = n > nnz ? n : nnz;
+    int64_t grid = (work + kBlock - 1) / kBlock;
+    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid < 1) grid = 1;
+    prepare_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(v, slot, static_cast<int>(n), val);
+}
+
+int check_grid(int64_t n) {
+    int64_t g = (n + 4095) / 4096;
+    if (g > 2048) g = 2048;
+    if (g < 1) g = 1;
+    return static_cast<int>(g);
+}
+
+size_t check_scratch_bytes(int64_t n) {
+    return sizeof(Partial) * static_cast<size_t>(check_grid(n)) + 256;
+}
+
+void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                             const double* x, const double* c, const double* l, const double* u,
+                             double tol, double offset, int gate, void* scratch, double* result,
+                             cudaStream_t s) {
+    CheckSrc src{};
+    src.rowptr = rowptr; src.col = col; src.val64 = val; src.x64 = x; src.c = c; src.l = l; src.u = u;
+    src.diag = nullptr;  // a diagonal Hessian's only entry per row is its diagonal
+    src.gate = gate;
+    const int grid = check_grid(n);
+    auto* scr = static_cast<StandaloneScratch*>(scratch);
+    auto* partial = reinterpret_cast<Partial*>(static_cast<char*>(scratch) + 256);
+    check_standalone_kernel<<<grid, kBlock, 0, s>>>(src, static_cast<int>(n), tol, offset, partial, scr, result);
+}
+
+void launch_box_step(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                     const double* c, const double* l, const double* u, double L, double beta,
+                     double* x, const double* w_in, double* w_out, cudaStream_t s) {
+    int grid = static_cast<int>((n + kBlock - 1) / kBlock);
+    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid < 1) grid = 1;
+    box_step_kernel<<<grid, kBlock, 0, s>>>(static_cast<int>(n), rowptr, col, val, c, l, u, L, beta, x, w_in, w_out);
+}
+
+}  // namespace bqp

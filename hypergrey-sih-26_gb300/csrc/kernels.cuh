@@ -1,0 +1,43 @@
+// Launch wrappers of the box-QP kernels (definitions in kernels.cu).
+#pragma once
+#include "engine.cuh"
+
+namespace bqp {
+
+// Tile kernels: grid-stride over the tile table (the grid size is fixed at capture).
+void launch_check(const View& v, int grid, cudaStream_t s);
+void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s);
+void launch_polish_init(const View& v, int grid, cudaStream_t s);
+void launch_polish_residual(const View& v, int grid, cudaStream_t s);
+void launch_cg_matvec(const View& v, int grid, cudaStream_t s);
+void launch_cg_update(const View& v, int grid, cudaStream_t s);
+void launch_cg_direction(const View& v, int grid, cudaStream_t s);
+// Single-block control kernels that steer the conditional graph nodes.
+// fista[k]: handle of the IF node of the precision-k step launches.
+// `steps` / `polish_kernels`: kernels inside each FISTA / the polish IF body (for the count).
+void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish, int steps,
+                 int polish_kernels, cudaStream_t s);
+void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s);
+// Host-driven variants of the control kernels (no conditional handles).
+void launch_gate_plain(const View& v, cudaStream_t s);
+void launch_control_plain(const View& v, cudaStream_t s);
+// Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
+void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
+// Admission: x0 = clip(0, l, u), w = x0, start clock; one instance.
+void launch_init_instance(const View& v, int slot, int n, int precision, cudaStream_t s);
+
+// Standalone FP64 check on caller device arrays (one instance, block partials in scratch).
+// scratch must hold check_scratch_bytes(n) bytes.
+size_t check_scratch_bytes(int64_t n);
+int check_grid(int64_t n);
+void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                             const double* x, const double* c, const double* l, const double* u,
+                             double tol, double offset, int gate, void* scratch, double* result,
+                             cudaStream_t s);
+
+// Plugin-level FISTA step (reference numerics: FP64, division by L, no FMA), ping-pong w.
+void launch_box_step(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                     const double* c, const double* l, const double* u, double L, double beta,
+                     double* x, const double* w_in, double* w_out, cudaStream_t s);
+
+}  // namespace bqp

@@ -1,0 +1,291 @@
+"""ctypes access to the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries:
+  oracle/_build/liboracle.so     the plain-C restatement in oracle/boxqp_oracle.c (always
+                                 buildable: gcc + OpenMP on any host)
+  oracle/_ref/libsovereign_ref.so  the reference's own solver sources compiled by
+                                 oracle/ref.mk plus oracle/ref_shim.cpp (only where the
+                                 reference checkout exists)
+Only the tests, the smoke check and the benchmark's CPU-baseline leg use this module; the
+engine never does.
+"""
+import ctypes
+import subprocess
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SRC = HERE / 'boxqp_oracle.c'
+ORACLE_LIB = HERE / '_build' / 'liboracle.so'
+REF_LIB = HERE / '_ref' / 'libsovereign_ref.so'
+
+STATUS = {0: 'optimal', 1: 'iteration_limit', 2: 'time_limit', 3: 'numerical_error',
+          4: 'unsupported_curvature', 5: 'infeasible_bounds', 6: 'zero_hessian'}
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [('objective', c_double), ('primal_residual', c_double), ('stationarity_residual', c_double),
+                ('complementarity_residual', c_double), ('dual_bound', c_double), ('relative_gap', c_double),
+                ('verified', c_double), ('iterations', c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_I32P, _I64P, _F64P = POINTER(c_int32), POINTER(c_int64), POINTER(c_double)
+
+
+def build_oracle(force=False):
+    """Compiles the C restatement (no FMA contraction, OpenMP)."""
+    if force or not ORACLE_LIB.exists() or ORACLE_SRC.stat().st_mtime > ORACLE_LIB.stat().st_mtime:
+        ORACLE_LIB.parent.mkdir(exist_ok=True)
+        tmp = ORACLE_LIB.with_suffix('.tmp.so')
+        subprocess.run(['gcc', '-O2', '-std=gnu11', '-fopenmp', '-fPIC', '-shared', '-ffp-contract=off',
+                        str(ORACLE_SRC), '-o', str(tmp), '-lm'], check=True, capture_output=True)
+        tmp.replace(ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_reference(ref_dir='/root/reference/02-software/solver'):
+    """Builds oracle/_ref from the reference's sources when they are present; True on success."""
+    if not Path(ref_dir).is_dir():
+        return REF_LIB.exists()
+    proc = subprocess.run(['make', '-s', '-j8', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}'],
+                          cwd=str(HERE.parent), capture_output=True, text=True)
+    return proc.returncode == 0 and REF_LIB.exists()
+
+
+_orc = None
+_ref = None
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        build_oracle()
+        L = ctypes.CDLL(str(ORACLE_LIB))
+        L.orc_solve_box.restype = c_int
+        L.orc_solve_box.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double,
+                                    c_double, c_int64, c_double, c_int, _F64P, POINTER(OrcStats), POINTER(c_int)]
+        L.orc_solve_box_csr.restype = c_int
+        L.orc_solve_box_csr.argtypes = [c_int64, _I32P, _I32P, _F64P, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P,
+                                        _F64P, c_double, c_int64, c_double, c_int, _F64P, POINTER(OrcStats),
+                                        POINTER(c_int)]
+        L.orc_check.restype = None
+        L.orc_check.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double, _F64P,
+                                c_double, POINTER(OrcStats)]
+        L.orc_check_convex.restype = c_int
+        L.orc_check_convex.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, c_int]
+        L.orc_build_csr.restype = c_int64
+        L.orc_build_csr.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, c_double, _I32P, _I32P, _F64P]
+        L.orc_fista_steps.restype = None
+        L.orc_fista_steps.argtypes = [c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P, c_double, _F64P, _F64P,
+                                      _F64P, c_int64, c_int]
+        L.orc_max_abs_row_sum.restype = c_double
+        L.orc_max_abs_row_sum.argtypes = [c_int64, _I32P, _F64P]
+        L.orc_max_threads.restype = c_int
+        _orc = L
+    return _orc
+
+
+def ref_available():
+    return REF_LIB.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            raise RuntimeError('oracle/_ref is not built (the reference checkout is needed to build it)')
+        L = ctypes.CDLL(str(REF_LIB))
+        L.ref_solve_box.restype = c_int
+        L.ref_solve_box.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double,
+                                    c_double, c_int64, c_double, c_int, _F64P, _F64P, c_char_p, c_int]
+        L.ref_check.restype = c_int
+        L.ref_check.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double, _F64P,
+                                c_double, _F64P]
+        L.ref_check_convex.restype = c_int
+        L.ref_check_convex.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, c_int]
+        L.ref_qplib_open.restype = c_void_p
+        L.ref_qplib_open.argtypes = [c_char_p, c_char_p, c_int]
+        L.ref_qplib_sizes.restype = None
+        L.ref_qplib_sizes.argtypes = [c_void_p, _I64P, _I64P, _I64P, POINTER(c_int), _F64P]
+        L.ref_qplib_copy.restype = None
+        L.ref_qplib_copy.argtypes = [c_void_p, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P]
+        L.ref_qplib_close.restype = None
+        L.ref_qplib_close.argtypes = [c_void_p]
+        _ref = L
+    return _ref
+
+
+def _p(a, t):
+    return a.ctypes.data_as(POINTER(t))
+
+
+def _arrays(hrow, hcol, hval, cost, lower, upper):
+    return (np.ascontiguousarray(hrow, np.int64), np.ascontiguousarray(hcol, np.int64),
+            np.ascontiguousarray(hval, np.float64), np.ascontiguousarray(cost, np.float64),
+            np.ascontiguousarray(lower, np.float64), np.ascontiguousarray(upper, np.float64))
+
+
+def solve_box(hrow, hcol, hval, cost, lower, upper, tol=1e-7, iteration_limit=200000, time_limit=30.0,
+              threads=1, maximize=False, offset=0.0):
+    """Oracle solve_accelerated_box(cuda=false); returns (status, x, stats dict)."""
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    n = cost.shape[0]
+    x = np.zeros(n)
+    st = OrcStats()
+    status = c_int(-1)
+    rc = orc().orc_solve_box(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                             _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), int(maximize),
+                             float(offset), float(tol), int(iteration_limit), float(time_limit), int(threads),
+                             _p(x, c_double), st, ctypes.byref(status))
+    if rc == 1:
+        raise ValueError('invalid argument')
+    if rc != 0:
+        raise MemoryError('oracle allocation failed')
+    return STATUS[status.value], x, st.as_dict()
+
+
+def solve_box_csr(rowptr, col, val, hrow, hcol, hval, cost, lower, upper, tol=1e-7, iteration_limit=200000,
+                  time_limit=30.0, threads=1):
+    """Oracle FISTA on an assembled full CSR (minimisation, no offset)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    n = cost.shape[0]
+    x = np.zeros(n)
+    st = OrcStats()
+    status = c_int(-1)
+    rc = orc().orc_solve_box_csr(n, _p(rowptr, c_int32), _p(col, c_int32), _p(val, c_double), hrow.shape[0],
+                                 _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double), _p(cost, c_double),
+                                 _p(lower, c_double), _p(upper, c_double), float(tol), int(iteration_limit),
+                                 float(time_limit), int(threads), _p(x, c_double), st, ctypes.byref(status))
+    if rc != 0:
+        raise RuntimeError('oracle failure')
+    return STATUS[status.value], x, st.as_dict()
+
+
+def check(hrow, hcol, hval, cost, lower, upper, x, tol=1e-7, maximize=False, offset=0.0):
+    """Oracle check_qp_solution; returns the stats dict."""
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    x = np.ascontiguousarray(x, np.float64)
+    st = OrcStats()
+    orc().orc_check(cost.shape[0], hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                    _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), int(maximize), float(offset),
+                    _p(x, c_double), float(tol), st)
+    return st.as_dict()
+
+
+def check_convex(n, hrow, hcol, hval, maximize=False):
+    hrow = np.ascontiguousarray(hrow, np.int64)
+    hcol = np.ascontiguousarray(hcol, np.int64)
+    hval = np.ascontiguousarray(hval, np.float64)
+    return orc().orc_check_convex(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                                  int(maximize))
+
+
+def build_csr(n, hrow, hcol, hval, sign=1.0):
+    hrow = np.ascontiguousarray(hrow, np.int64)
+    hcol = np.ascontiguousarray(hcol, np.int64)
+    hval = np.ascontiguousarray(hval, np.float64)
+    nh = hrow.shape[0]
+    rowptr = np.zeros(n + 1, np.int32)
+    col = np.zeros(max(2 * nh, 1), np.int32)
+    val = np.zeros(max(2 * nh, 1))
+    nnz = orc().orc_build_csr(n, nh, _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double), float(sign),
+                              _p(rowptr, c_int32), _p(col, c_int32), _p(val, c_double))
+    if nnz < 0:
+        raise ValueError('invalid Hessian')
+    return rowptr, col[:nnz].copy(), val[:nnz].copy()
+
+
+def fista_steps(rowptr, col, val, c, lower, upper, lipschitz, x, w, t, steps, threads=1):
+    """Runs `steps` CPU FISTA iterations in place on (x, w); returns the new t."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    c = np.ascontiguousarray(c, np.float64)
+    lower = np.ascontiguousarray(lower, np.float64)
+    upper = np.ascontiguousarray(upper, np.float64)
+    tt = np.array([t], np.float64)
+    orc().orc_fista_steps(c.shape[0], _p(rowptr, c_int32), _p(col, c_int32), _p(val, c_double), _p(c, c_double),
+                          _p(lower, c_double), _p(upper, c_double), float(lipschitz), _p(x, c_double),
+                          _p(w, c_double), _p(tt, c_double), int(steps), int(threads))
+    return float(tt[0])
+
+
+def max_abs_row_sum(rowptr, val):
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    return orc().orc_max_abs_row_sum(rowptr.shape[0] - 1, _p(rowptr, c_int32), _p(val, c_double))
+
+
+def max_threads():
+    return orc().orc_max_threads()
+
+
+# ---- the reference itself (oracle/_ref) ---------------------------------------------------
+def ref_solve_box(hrow, hcol, hval, cost, lower, upper, tol=1e-7, iteration_limit=200000, time_limit=30.0,
+                  threads=1, maximize=False, offset=0.0):
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    n = cost.shape[0]
+    x = np.zeros(n)
+    stats = np.zeros(8)
+    msg = ctypes.create_string_buffer(256)
+    rc = ref().ref_solve_box(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                             _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), int(maximize),
+                             float(offset), float(tol), int(iteration_limit), float(time_limit), int(threads),
+                             _p(x, c_double), _p(stats, c_double), msg, 256)
+    if rc == 1:
+        raise ValueError(msg.value.decode())
+    if rc != 0:
+        raise RuntimeError(msg.value.decode())
+    keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+            'relative_gap', 'verified', 'iterations']
+    return msg.value.decode(), x, dict(zip(keys, stats.tolist()))
+
+
+def ref_check(hrow, hcol, hval, cost, lower, upper, x, tol=1e-7, maximize=False, offset=0.0):
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    x = np.ascontiguousarray(x, np.float64)
+    stats = np.zeros(8)
+    ref().ref_check(cost.shape[0], hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                    _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), int(maximize), float(offset),
+                    _p(x, c_double), float(tol), _p(stats, c_double))
+    keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+            'relative_gap', 'verified', 'iterations']
+    return dict(zip(keys, stats.tolist()))
+
+
+def ref_check_convex(n, hrow, hcol, hval, maximize=False):
+    hrow = np.ascontiguousarray(hrow, np.int64)
+    hcol = np.ascontiguousarray(hcol, np.int64)
+    hval = np.ascontiguousarray(hval, np.float64)
+    return ref().ref_check_convex(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                                  int(maximize))
+
+
+def ref_read_qplib(path):
+    """Parses a QPLIB file with the reference's reader; returns a dict of arrays."""
+    msg = ctypes.create_string_buffer(256)
+    h = ref().ref_qplib_open(str(path).encode(), msg, 256)
+    if not h:
+        raise ValueError(msg.value.decode())
+    try:
+        n, nh, m = c_int64(0), c_int64(0), c_int64(0)
+        mx = c_int(0)
+        off = c_double(0)
+        ref().ref_qplib_sizes(h, ctypes.byref(n), ctypes.byref(nh), ctypes.byref(m), ctypes.byref(mx),
+                              ctypes.byref(off))
+        hr, hc, hv = np.zeros(nh.value, np.int64), np.zeros(nh.value, np.int64), np.zeros(nh.value)
+        cost, lo, up = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        ref().ref_qplib_copy(h, _p(hr, c_int64), _p(hc, c_int64), _p(hv, c_double), _p(cost, c_double),
+                             _p(lo, c_double), _p(up, c_double))
+        return {'n': n.value, 'rows': m.value, 'maximize': bool(mx.value), 'offset': off.value, 'hrow': hr,
+                'hcol': hc, 'hval': hv, 'cost': cost, 'lower': lo, 'upper': up}
+    finally:
+        ref().ref_qplib_close(h)

@@ -1,0 +1,161 @@
+// C shim over the reference's own C++ box-QP API (TEST INFRASTRUCTURE ONLY).
+//
+// Compiled by oracle/ref.mk together with the reference's unmodified solver sources
+// into oracle/_ref/libsovereign_ref.so, so that Python tests and the golden-vector
+// script can call the real reference engine through ctypes:
+//   - sovereign::solve_accelerated_box(q, opt, false)   src/accelerated_qp.cpp:13-61
+//   - sovereign::check_qp_solution(q, r, tol)           src/qp_admm.cpp:63-117
+//   - sovereign::check_convex_hessian(q)                src/qp_admm.cpp:30-62
+//   - sovereign::read_qplib(stream)                     src/qp.cpp:67-117
+// No C++ exception crosses this boundary: errors come back as codes plus a message.
+#include "accelerated_qp.hpp"
+#include "qp.hpp"
+
+#include <cstdint>
+#include <cstring>
+#include <fstream>
+#include <stdexcept>
+#include <string>
+
+namespace {
+void put_message(char* out, std::size_t cap, const std::string& text) {
+    if (!out || !cap) return;
+    std::size_t n = text.size() < cap - 1 ? text.size() : cap - 1;
+    std::memcpy(out, text.data(), n);
+    out[n] = 0;
+}
+
+sovereign::QuadraticProblem make_problem(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol,
+                                         const double* hval, const double* cost, const double* lower,
+                                         const double* upper, int maximize, double offset) {
+    sovereign::QuadraticProblem q;
+    auto& p = q.linear;
+    p.name = "shim";
+    p.names.resize(static_cast<std::size_t>(n));
+    for (int64_t j = 0; j < n; ++j) p.names[j] = "x" + std::to_string(j);
+    p.cost.assign(cost, cost + n);
+    p.lower.assign(lower, lower + n);
+    p.upper.assign(upper, upper + n);
+    p.integer.assign(static_cast<std::size_t>(n), false);
+    p.offset = offset;
+    p.maximize = maximize != 0;
+    q.hessian.reserve(static_cast<std::size_t>(nh));
+    for (int64_t k = 0; k < nh; ++k)
+        q.hessian.push_back({static_cast<std::size_t>(hrow[k]), static_cast<std::size_t>(hcol[k]), hval[k]});
+    return q;
+}
+
+void fill_stats(const sovereign::QpResult& r, double* stats) {
+    stats[0] = r.objective;
+    stats[1] = r.primal_residual;
+    stats[2] = r.stationarity_residual;
+    stats[3] = r.complementarity_residual;
+    stats[4] = r.dual_bound;
+    stats[5] = r.relative_gap;
+    stats[6] = r.optimality_verified ? 1.0 : 0.0;
+    stats[7] = static_cast<double>(r.iterations);
+}
+
+struct QplibHandle {
+    sovereign::QuadraticProblem q;
+};
+}  // namespace
+
+extern "C" {
+
+// Runs the reference CPU engine.  status_out receives the reference's status string.
+// Returns 0 on success, 1 if the reference threw std::invalid_argument, 2 for any
+// other exception (message in status_out).
+int ref_solve_box(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol, const double* hval,
+                  const double* cost, const double* lower, const double* upper, int maximize, double offset,
+                  double tol, int64_t iteration_limit, double time_limit, int threads,
+                  double* x_out, double* stats, char* status_out, int status_cap) {
+    try {
+        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, maximize, offset);
+        sovereign::QpOptions o;
+        o.tolerance = tol;
+        o.iteration_limit = static_cast<std::size_t>(iteration_limit);
+        o.time_limit = time_limit;
+        o.threads = threads;
+        auto r = sovereign::solve_accelerated_box(q, o, false);
+        fill_stats(r, stats);
+        for (std::size_t j = 0; j < r.primal.size() && j < static_cast<std::size_t>(n); ++j) x_out[j] = r.primal[j];
+        put_message(status_out, static_cast<std::size_t>(status_cap), r.status);
+        return 0;
+    } catch (const std::invalid_argument& e) {
+        put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
+        return 1;
+    } catch (const std::exception& e) {
+        put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
+        return 2;
+    }
+}
+
+// Runs the reference checker on a caller-supplied primal.
+int ref_check(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol, const double* hval,
+              const double* cost, const double* lower, const double* upper, int maximize, double offset,
+              const double* x, double tol, double* stats) {
+    try {
+        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, maximize, offset);
+        sovereign::QpResult r;
+        r.primal.assign(x, x + n);
+        sovereign::check_qp_solution(q, r, tol);
+        fill_stats(r, stats);
+        return 0;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// 1 convex, 0 not convex, -2 invalid Hessian (the reference throws invalid_argument).
+int ref_check_convex(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol, const double* hval, int maximize) {
+    try {
+        std::vector<double> zero(static_cast<std::size_t>(n), 0.0);
+        auto q = make_problem(n, nh, hrow, hcol, hval, zero.data(), zero.data(), zero.data(), maximize, 0.0);
+        return sovereign::check_convex_hessian(q) ? 1 : 0;
+    } catch (...) {
+        return -2;
+    }
+}
+
+// QPLIB reading through the reference parser: open, query sizes, copy, close.
+void* ref_qplib_open(const char* path, char* message, int cap) {
+    try {
+        std::ifstream in(path);
+        if (!in) throw std::runtime_error("Cannot open model");
+        auto* h = new QplibHandle;
+        h->q = sovereign::read_qplib(in);
+        return h;
+    } catch (const std::exception& e) {
+        put_message(message, static_cast<std::size_t>(cap), e.what());
+        return nullptr;
+    }
+}
+
+void ref_qplib_sizes(void* handle, int64_t* n, int64_t* nh, int64_t* m, int* maximize, double* offset) {
+    auto* h = static_cast<QplibHandle*>(handle);
+    *n = static_cast<int64_t>(h->q.linear.cost.size());
+    *nh = static_cast<int64_t>(h->q.hessian.size());
+    *m = static_cast<int64_t>(h->q.linear.rows.size());
+    *maximize = h->q.linear.maximize ? 1 : 0;
+    *offset = h->q.linear.offset;
+}
+
+void ref_qplib_copy(void* handle, int64_t* hrow, int64_t* hcol, double* hval, double* cost, double* lower, double* upper) {
+    auto* h = static_cast<QplibHandle*>(handle);
+    for (std::size_t k = 0; k < h->q.hessian.size(); ++k) {
+        hrow[k] = static_cast<int64_t>(h->q.hessian[k].row);
+        hcol[k] = static_cast<int64_t>(h->q.hessian[k].col);
+        hval[k] = h->q.hessian[k].value;
+    }
+    const auto& p = h->q.linear;
+    for (std::size_t j = 0; j < p.cost.size(); ++j) {
+        cost[j] = p.cost[j];
+        lower[j] = p.lower[j];
+        upper[j] = p.upper[j];
+    }
+}
+
+void ref_qplib_close(void* handle) { delete static_cast<QplibHandle*>(handle); }
+
+}  // extern "C"

@@ -1,0 +1,145 @@
+"""Generates the golden fixtures of the box-QP path from the reference itself.
+
+Run from the repository root where the reference checkout exists:
+    python tests/golden/make_golden.py [--reference /root/reference/02-software/solver]
+
+It builds oracle/_ref (the reference's unmodified solver sources + oracle/ref_shim.cpp, see
+oracle/ref.mk), runs the reference's own CPU engine solve_accelerated_box(q, opt, false) and
+checker on each case below, and writes
+    tests/golden/reference_cases.json   statuses, iterations, objectives, residuals, x digests
+    tests/golden/reference_x.npz        primal vectors of the cases with n <= 2000
+The cases are the reference's known answers for this path (its tests and published harness)
+plus planted instances of the synthetic families.  QPLIB instances are read from the
+reference's datasets folder by the reference's own reader; only scalar results and the input
+file's SHA-256 are stored.
+"""
+import argparse
+import hashlib
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / 'hypergrey-sih-26_gb300'))
+
+import boxqp  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def digest(x):
+    return hashlib.sha256(np.ascontiguousarray(x, np.float64).tobytes()).hexdigest()
+
+
+def v2_psd_case():
+    """src/tests/test_v2.cpp:18-25: n=300, PSD, not diagonally dominant."""
+    n = 300
+    hr, hc, hv = [], [], []
+    for j in range(n):
+        hr.append(j); hc.append(j); hv.append(5.0 if j % 2 else 1.0)
+        if j % 2:
+            hr.append(j); hc.append(j - 1); hv.append(2.0)
+    return dict(hrow=np.array(hr), hcol=np.array(hc), hval=np.array(hv), cost=-np.ones(n), lower=np.zeros(n),
+                upper=np.full(n, 10.0))
+
+
+def two_var_case():
+    """src/tests/test_solver.cpp:85-90: objective -5."""
+    return dict(hrow=np.array([0, 1]), hcol=np.array([0, 1]), hval=np.array([2.0, 2.0]), cost=np.array([-2.0, -4.0]),
+                lower=np.array([-10.0, -10.0]), upper=np.array([10.0, 10.0]))
+
+
+def cases():
+    out = []
+    for seed in range(4):
+        inst = boxqp.planted('graph10k', seed=seed, lower_triplets=True)
+        out.append((f'graph10k_s{seed}', inst, dict(tol=1e-6), {'preset': 'graph10k', 'seed': seed}))
+    for seed in range(6):
+        inst = boxqp.planted('graph10k', seed=100 + seed, n=2000, lower_triplets=True)
+        out.append((f'graph2k_s{100 + seed}', inst, dict(tol=1e-6), {'preset': 'graph10k', 'seed': 100 + seed, 'n': 2000}))
+    inst = boxqp.planted('graph10k', seed=7, n=2000, lower_triplets=True)
+    out.append(('graph2k_tol1e-8', inst, dict(tol=1e-8), {'preset': 'graph10k', 'seed': 7, 'n': 2000}))
+    out.append(('graph2k_limit60', inst, dict(tol=1e-9, iteration_limit=60), {'preset': 'graph10k', 'seed': 7, 'n': 2000}))
+    out.append(('graph2k_limit0', inst, dict(tol=1e-9, iteration_limit=0), {'preset': 'graph10k', 'seed': 7, 'n': 2000}))
+    for n in (1000, 10000):
+        inst = boxqp.planted('tridiagonal', n=n, lower_triplets=True)
+        # solver_scale's options: iteration_limit 20000, tolerance 1e-7 (src/scale_benchmark.cpp:19)
+        out.append((f'tridiagonal_{n}', inst, dict(tol=1e-7, iteration_limit=20000), {'preset': 'tridiagonal', 'n': n}))
+    for tol in (1e-6, 1e-8):
+        inst = boxqp.planted('grid', seed=2, n=32 * 32, lower_triplets=True)
+        out.append((f'grid32_tol{tol:g}', inst, dict(tol=tol), {'preset': 'grid', 'seed': 2, 'n': 1024}))
+    for seed in range(3):
+        inst = boxqp.planted('batch', seed=3, index=seed, lower_triplets=True)
+        out.append((f'batch_i{seed}', inst, dict(tol=1e-6), {'preset': 'batch', 'seed': 3, 'index': seed}))
+    return out
+
+
+def run_case(name, p, opts, maximize=False, offset=0.0):
+    args = (p['hrow'], p['hcol'], p['hval'], p['cost'] if 'cost' in p else p['c'], p['lower'], p['upper'])
+    status, x, st = O.ref_solve_box(*args, tol=opts.get('tol', 1e-7), iteration_limit=opts.get('iteration_limit', 200000),
+                                    time_limit=600.0, threads=1, maximize=maximize, offset=offset)
+    rec = {'name': name, 'status': status, 'iterations': int(st['iterations']), 'objective': st['objective'],
+           'stationarity_residual': st['stationarity_residual'], 'primal_residual': st['primal_residual'],
+           'relative_gap': st['relative_gap'], 'dual_bound': st['dual_bound'], 'verified': bool(st['verified']),
+           'x_sha256': digest(x), 'n': int(len(x)), 'tol': opts.get('tol', 1e-7),
+           'iteration_limit': opts.get('iteration_limit', 200000), 'maximize': maximize, 'offset': offset}
+    return rec, x
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--reference', default='/root/reference/02-software/solver')
+    a = ap.parse_args()
+    if not O.build_reference(a.reference):
+        raise SystemExit('cannot build oracle/_ref from ' + a.reference)
+    records, vectors = [], {}
+    for name, inst, opts, gen in cases():
+        rec, x = run_case(name, inst, opts)
+        rec['generator'] = gen
+        rec['fstar'] = inst['fstar']
+        records.append(rec)
+        if len(x) <= 2000:
+            vectors[name] = x
+        print(name, rec['status'], rec['iterations'], rec['objective'], flush=True)
+    explicit = [('v2_psd_300', v2_psd_case(), dict(tol=1e-7), False, 0.0),
+                ('two_var', two_var_case(), dict(tol=1e-7), False, 0.0),
+                ('two_var_maximize', {**two_var_case(), 'hval': -two_var_case()['hval'],
+                                      'cost': -two_var_case()['cost']}, dict(tol=1e-7), True, 3.0)]
+    for name, p, opts, mx, off in explicit:
+        rec, x = run_case(name, p, opts, mx, off)
+        rec['problem'] = {k: np.asarray(v).tolist() for k, v in p.items()}
+        records.append(rec)
+        vectors[name] = x
+        print(name, rec['status'], rec['iterations'], rec['objective'], flush=True)
+    # convexity verdicts of the reference (src/qp_admm.cpp:30-62)
+    p = v2_psd_case()
+    bad = p['hval'].copy(); bad[0] = -1.0
+    convex = {'v2_psd_300': O.ref_check_convex(300, p['hrow'], p['hcol'], p['hval']),
+              'v2_indefinite_300': O.ref_check_convex(300, p['hrow'], p['hcol'], bad)}
+    # public QPLIB box instances (scalar results only)
+    qplib = []
+    data = Path(a.reference) / 'datasets' / 'qplib'
+    for name in ('8792', '8991'):
+        path = data / f'{name}.qplib'
+        if not path.exists():
+            continue
+        q = O.ref_read_qplib(path)
+        status, x, st = O.ref_solve_box(q['hrow'], q['hcol'], q['hval'], q['cost'], q['lower'], q['upper'], tol=1e-7,
+                                        time_limit=600.0, threads=1, maximize=q['maximize'], offset=q['offset'])
+        qplib.append({'name': name, 'sha256': hashlib.sha256(path.read_bytes()).hexdigest(), 'n': q['n'],
+                      'hessian_entries': int(len(q['hrow'])), 'status': status, 'iterations': int(st['iterations']),
+                      'objective': st['objective'], 'stationarity_residual': st['stationarity_residual']})
+        print('qplib', name, status, st['iterations'], st['objective'], flush=True)
+    meta = {'generated_by': 'tests/golden/make_golden.py', 'engine': 'reference solve_accelerated_box(cuda=false), 1 thread',
+            'build': 'oracle/ref.mk (g++ -O3 -fopenmp -ffp-contract=off)'}
+    (OUT / 'reference_cases.json').write_text(json.dumps({'meta': meta, 'cases': records, 'convex': convex,
+                                                           'qplib': qplib}, indent=1) + '\n')
+    np.savez_compressed(OUT / 'reference_x.npz', **vectors)
+
+
+if __name__ == '__main__':
+    main()

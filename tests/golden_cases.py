@@ -1,0 +1,23 @@
+"""Rebuilds the inputs of the golden fixtures (tests/golden/reference_cases.json)."""
+import numpy as np
+
+import boxqp
+
+
+def inputs(rec):
+    """Returns (problem dict with hrow/hcol/hval/cost/lower/upper, planted instance or None)."""
+    if 'problem' in rec:
+        p = {k: np.asarray(v) for k, v in rec['problem'].items()}
+        p['hrow'] = p['hrow'].astype(np.int64)
+        p['hcol'] = p['hcol'].astype(np.int64)
+        return p, None
+    g = rec['generator']
+    inst = boxqp.planted(g['preset'], seed=g.get('seed', 1), index=g.get('index', 0), n=g.get('n', 0),
+                         lower_triplets=True)
+    p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
+         'lower': inst['lower'], 'upper': inst['upper']}
+    return p, inst
+
+
+def args(p):
+    return p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper']

@@ -1,0 +1,192 @@
+"""GPU engine parity against the CPU oracle and the reference's golden results (needs a GPU).
+
+Tolerances (the bar for floating point):
+  * BQP_PRECISION_FP64_EXACT: bit-identical iterates, statuses and iteration counts.
+  * BQP_PRECISION_FP64 (FMA, multiply by 1/L): same status, iterations within one check
+    interval, objective relative difference <= 1e-10, primal max difference <= 1e-6.
+  * BQP_PRECISION_MIXED: verified at the requested KKT tolerance by the FP64 oracle checker on
+    the host, objective relative error vs the planted optimum <= 1e-7, active set identical to
+    the planted one wherever the planted dual margin exceeds 1e-6.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import boxqp
+from oracle import oracle as O
+from golden_cases import args, inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def digest(x):
+    return hashlib.sha256(np.ascontiguousarray(x, np.float64).tobytes()).hexdigest()
+
+
+def solve(engine, inst, precision, tol, iteration_limit=200000, time_limit=60.0):
+    o = boxqp.options_struct(tol, time_limit, iteration_limit, precision)
+    return engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+
+
+def planted_args(inst):
+    return inst['hrow'], inst['hcol'], inst['hval'], inst['c'], inst['lower'], inst['upper']
+
+
+def active_set_ok(inst, x, margin=1e-6):
+    z = inst['z']
+    at_lo = z > margin
+    at_up = z < -margin
+    return (np.all(x[at_lo] == inst['lower'][at_lo]) and np.all(x[at_up] == inst['upper'][at_up]) and
+            np.all((x[~(at_lo | at_up)] > inst['lower'][~(at_lo | at_up)]) &
+                   (x[~(at_lo | at_up)] < inst['upper'][~(at_lo | at_up)])))
+
+
+@pytest.mark.parametrize('name', ['graph2k_s100', 'graph2k_s103', 'graph2k_tol1e-8', 'graph2k_limit60',
+                                  'graph2k_limit0', 'tridiagonal_1000', 'grid32_tol1e-08', 'batch_i0',
+                                  'graph10k_s0'])
+def test_exact_mode_reproduces_reference_bits(engine, golden, name):
+    d, xs = golden
+    rec = next(c for c in d['cases'] if c['name'] == name)
+    _, inst = inputs(rec)
+    x, st = solve(engine, inst, 'fp64_exact', rec['tol'], rec['iteration_limit'], 600.0)
+    assert boxqp.STATUS_NAMES[st.status] == rec['status']
+    assert st.iterations == rec['iterations']
+    assert digest(x) == rec['x_sha256']
+    if name in xs:
+        assert np.array_equal(x, xs[name])
+    assert st.objective == pytest.approx(rec['objective'], rel=1e-13, abs=1e-13)
+
+
+@pytest.mark.parametrize('name', ['v2_psd_300', 'two_var', 'two_var_maximize'])
+def test_reference_api_known_answers(engine, golden, name):
+    """The reference's own test problems through the mirrored solve_accelerated_box."""
+    d, xs = golden
+    rec = next(c for c in d['cases'] if c['name'] == name)
+    p, _ = inputs(rec)
+    q = boxqp.QuadraticProblem(cost=p['cost'], lower=p['lower'], upper=p['upper'], hessian_row=p['hrow'],
+                               hessian_col=p['hcol'], hessian_val=p['hval'], maximize=rec['maximize'],
+                               offset=rec['offset'])
+    r = boxqp.solve_accelerated_box(q, boxqp.QpOptions(tolerance=rec['tol'], precision='fp64_exact'), engine=engine)
+    assert r.status == rec['status'] and r.optimality_verified
+    assert r.iterations == rec['iterations']
+    assert r.objective == pytest.approx(rec['objective'], rel=1e-12, abs=1e-12)
+    assert np.array_equal(r.primal, xs[name])
+
+
+@pytest.mark.parametrize('seed', [0, 1])
+def test_fp64_mode_matches_oracle(engine, seed):
+    inst = boxqp.planted('graph10k', seed=seed, lower_triplets=True)
+    status, xo, so = O.solve_box(*planted_args(inst), tol=1e-6, threads=8)
+    x, st = solve(engine, inst, 'fp64', 1e-6)
+    assert boxqp.STATUS_NAMES[st.status] == status == 'optimal'
+    assert abs(st.iterations - so['iterations']) <= 25
+    assert st.objective == pytest.approx(so['objective'], rel=1e-10)
+    assert np.max(np.abs(x - xo)) <= 1e-6
+    chk = O.check(*planted_args(inst), x, tol=1e-6)
+    assert chk['verified'] == 1.0
+
+
+@pytest.mark.parametrize('preset,n,seed,tol', [('graph10k', 0, 3, 1e-6), ('graph10k', 0, 4, 1e-8),
+                                               ('grid', 64 * 64, 2, 1e-6), ('grid', 64 * 64, 2, 1e-8),
+                                               ('graph1m', 50000, 1, 1e-6), ('batch', 0, 3, 1e-6)])
+def test_mixed_mode_meets_tolerance_against_fp64_oracle(engine, preset, n, seed, tol):
+    inst = boxqp.planted(preset, seed=seed, n=n, lower_triplets=True)
+    x, st = solve(engine, inst, 'mixed', tol)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+    chk = O.check(*planted_args(inst), x, tol=tol)
+    assert chk['verified'] == 1.0, chk
+    assert chk['stationarity_residual'] <= tol
+    assert abs(chk['objective'] - inst['fstar']) / (1 + abs(inst['fstar'])) <= 1e-7
+    assert st.objective == pytest.approx(chk['objective'], rel=1e-12)
+    assert active_set_ok(inst, x)
+
+
+def test_plugin_box_iteration_reproduces_cpu_loop(golden):
+    """make_cuda_box + the reference's host loop == the CPU branch, iterate for iterate."""
+    inst = boxqp.planted('graph10k', seed=21, n=3000, lower_triplets=True)
+    L = boxqp.gershgorin(inst['rowptr'], inst['val'])
+    box = boxqp.make_cuda_box(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], L)
+    x = np.maximum(inst['lower'], np.minimum(inst['upper'], 0.0))
+    w = x.copy()
+    t = 1.0
+    for k in range(4):
+        # 25 iterations on each side, then compare the primal as the reference's check would
+        tt = t
+        for _ in range(25):
+            nt = (1 + np.sqrt(1 + 4 * tt * tt)) / 2
+            beta = (tt - 1) / nt
+            tt = nt
+            box.step(beta)
+        t = O.fista_steps(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], L, x,
+                          w, t, 25)
+        assert t == tt
+        assert np.array_equal(box.primal(), x)
+    box.close()
+
+
+def test_batch_results_equal_solo_results(engine):
+    """Each solve is bit-identical alone and inside a batch of unequal solves."""
+    insts = [boxqp.planted('batch', seed=3, index=i) for i in range(12)]
+    solo = []
+    for inst in insts:
+        x, st = solve(engine, inst, 'mixed', 1e-6)
+        solo.append((x, st.iterations, st.objective))
+    ids = []
+    for inst in insts:
+        o = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+        ids.append(engine.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o))
+    for inst, ident, (xs, its, obj) in zip(insts, ids, solo):
+        assert engine.wait(ident, 120.0)
+        x, st = engine.fetch(ident, inst['n'])
+        engine.release(ident)
+        assert boxqp.STATUS_NAMES[st.status] == 'optimal'
+        assert np.array_equal(x, xs) and st.iterations == its and st.objective == obj
+
+
+def test_resolve_resident_is_reproducible(engine):
+    inst = boxqp.planted('graph10k', seed=8, n=20000)
+    o = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+    ident = engine.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+    assert engine.wait(ident, 120.0)
+    x1, s1 = engine.fetch(ident, inst['n'])
+    engine.resolve([ident])
+    assert engine.wait(ident, 120.0)
+    x2, s2 = engine.fetch(ident, inst['n'])
+    engine.release(ident)
+    assert np.array_equal(x1, x2) and s1.iterations == s2.iterations
+    assert s2.device_end_ns > s2.device_start_ns > 0
+
+
+def test_iteration_and_time_limits(engine):
+    inst = boxqp.planted('grid', seed=2, n=128 * 128)
+    x, st = solve(engine, inst, 'fp64', 1e-12, iteration_limit=37)
+    assert boxqp.STATUS_NAMES[st.status] == 'iteration_limit' and st.iterations == 37
+    x, st = solve(engine, inst, 'fp64', 1e-14, iteration_limit=10 ** 9, time_limit=0.05)
+    assert boxqp.STATUS_NAMES[st.status] == 'time_limit'
+    assert np.all(np.isfinite(x))
+
+
+def test_check_device_matches_oracle_checker():
+    torch = pytest.importorskip('torch')
+    inst = boxqp.planted('graph10k', seed=9, n=5000, lower_triplets=True)
+    rng = np.random.default_rng(2)
+    x = np.clip(inst['xstar'] + 1e-5 * rng.standard_normal(inst['n']), inst['lower'], inst['upper'])
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in
+           [('rowptr', inst['rowptr']), ('col', inst['col']), ('val', inst['val']), ('x', x), ('c', inst['c']),
+            ('l', inst['lower']), ('u', inst['upper'])]}
+    st = boxqp.Stats()
+    rc = boxqp.lib().bqp_check_device(inst['n'], dev['rowptr'].data_ptr(), dev['col'].data_ptr(),
+                                      dev['val'].data_ptr(), dev['x'].data_ptr(), dev['c'].data_ptr(),
+                                      dev['l'].data_ptr(), dev['u'].data_ptr(), 1e-6, 0.0, 0, st)
+    assert rc == 0
+    ref = O.check(*planted_args(inst), x, tol=1e-6)
+    assert st.objective == pytest.approx(ref['objective'], rel=1e-13)
+    assert st.stationarity_residual == pytest.approx(ref['stationarity_residual'], rel=1e-9)
+    assert st.primal_residual == pytest.approx(ref['primal_residual'], abs=1e-15)
+    assert st.dual_bound == pytest.approx(ref['dual_bound'], rel=1e-12)
+    assert bool(st.verified) == bool(ref['verified'])
+
+
+def test_device_name():
+    assert 'GB300' in boxqp.cuda_device_name() or len(boxqp.cuda_device_name()) > 0

@@ -1,0 +1,141 @@
+"""The CPU oracle (oracle/boxqp_oracle.c) against the reference's own results.
+
+The golden fixtures were produced by the reference engine itself (tests/golden/make_golden.py);
+the oracle must reproduce its statuses and iteration counts exactly and its primal vectors bit
+for bit (both round every product and sum separately, in the same order).
+"""
+import hashlib
+import math
+import os
+import platform
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import boxqp
+from oracle import oracle as O
+from golden_cases import args, inputs
+
+EXACT_HOST = platform.machine() in ('x86_64', 'AMD64')
+
+
+def digest(x):
+    return hashlib.sha256(np.ascontiguousarray(x, np.float64).tobytes()).hexdigest()
+
+
+def test_fixture_covers_reference_known_answers(golden):
+    d, _ = golden
+    names = {c['name'] for c in d['cases']}
+    assert {'tridiagonal_1000', 'tridiagonal_10000', 'v2_psd_300', 'two_var', 'graph2k_limit60'} <= names
+    by = {c['name']: c for c in d['cases']}
+    # solver_scale's published known objective for n = 10,000 (-947.124889445...) and 1700 iterations
+    assert abs(by['tridiagonal_10000']['objective'] - (-947.124889445)) < 1e-8
+    assert by['tridiagonal_10000']['iterations'] == 1700
+    # test_solver.cpp:85-90 objective -5; test_v2.cpp:18-25 verified optimal
+    assert abs(by['two_var']['objective'] + 5) < 1e-7
+    assert by['v2_psd_300']['status'] == 'optimal' and by['v2_psd_300']['verified']
+    # QPLIB box instances, objectives published with the reference's CPU benchmark record
+    q = {r['name']: r for r in d['qplib']}
+    assert q['8792']['objective'] == pytest.approx(3593.5162939294105, rel=1e-12)
+    assert q['8991']['objective'] == pytest.approx(-0.0016678673619609664, rel=1e-9)
+    assert d['convex'] == {'v2_psd_300': 1, 'v2_indefinite_300': 0}
+
+
+@pytest.mark.parametrize('idx', range(24))
+def test_oracle_matches_reference(golden, idx):
+    d, xs = golden
+    if idx >= len(d['cases']):
+        pytest.skip('fewer cases')
+    rec = d['cases'][idx]
+    p, inst = inputs(rec)
+    status, x, st = O.solve_box(*args(p), tol=rec['tol'], iteration_limit=rec['iteration_limit'], time_limit=600,
+                                threads=1, maximize=rec['maximize'], offset=rec['offset'])
+    assert status == rec['status']
+    assert int(st['iterations']) == rec['iterations']
+    if EXACT_HOST:
+        assert digest(x) == rec['x_sha256']
+        assert st['objective'] == rec['objective']
+    else:
+        assert st['objective'] == pytest.approx(rec['objective'], rel=1e-13, abs=1e-13)
+    if rec['name'] in xs:
+        ref_x = xs[rec['name']]
+        assert np.max(np.abs(x - ref_x)) <= (0 if EXACT_HOST else 1e-12)
+
+
+def test_oracle_multithreaded_equals_single(golden):
+    """OpenMP row partitioning changes no rounding: threads give the same bits."""
+    d, _ = golden
+    rec = next(c for c in d['cases'] if c['name'] == 'graph10k_s0')
+    p, _ = inputs(rec)
+    s1, x1, _ = O.solve_box(*args(p), tol=1e-6, threads=1)
+    s4, x4, _ = O.solve_box(*args(p), tol=1e-6, threads=4)
+    assert s1 == s4 and np.array_equal(x1, x4)
+
+
+def test_planted_optimum_is_verified_by_oracle():
+    inst = boxqp.planted('graph10k', seed=5, n=3000, lower_triplets=True)
+    p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
+         'lower': inst['lower'], 'upper': inst['upper']}
+    st = O.check(*args(p), inst['xstar'], tol=1e-12)
+    assert st['verified'] == 1.0
+    assert st['objective'] == pytest.approx(inst['fstar'], rel=1e-13)
+
+
+def test_checker_adversarial_cases():
+    """The checker trusts nothing: NaN, out-of-box and non-stationary candidates fail."""
+    inst = boxqp.planted('graph10k', seed=6, n=500, lower_triplets=True)
+    p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
+         'lower': inst['lower'], 'upper': inst['upper']}
+    x = inst['xstar'].copy()
+    x[3] = np.nan
+    st = O.check(*args(p), x)
+    assert st['verified'] == 0 and math.isnan(st['objective'])
+    x = inst['xstar'].copy()
+    x[0] = inst['upper'][0] + 0.5
+    st = O.check(*args(p), x)
+    assert st['primal_residual'] > 0.1 and st['verified'] == 0
+    x = inst['xstar'].copy()
+    free = np.flatnonzero((x > inst['lower']) & (x < inst['upper']))
+    x[free[0]] += 1e-3
+    st = O.check(*args(p), x, tol=1e-6)
+    assert st['stationarity_residual'] > 1e-6 and st['verified'] == 0
+
+
+def test_oracle_checker_agrees_with_reference_checker():
+    if not O.ref_available():
+        pytest.skip('oracle/_ref not built on this host')
+    inst = boxqp.planted('grid', seed=9, n=400, lower_triplets=True)
+    p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
+         'lower': inst['lower'], 'upper': inst['upper']}
+    rng = np.random.default_rng(0)
+    for scale in (0.0, 1e-8, 1e-4, 1e-1):
+        x = np.clip(inst['xstar'] + scale * rng.standard_normal(inst['n']), inst['lower'] - scale, inst['upper'])
+        a = O.check(*args(p), x, tol=1e-6)
+        b = O.ref_check(*args(p), x, tol=1e-6)
+        for k in ('objective', 'primal_residual', 'stationarity_residual', 'dual_bound', 'relative_gap', 'verified'):
+            assert a[k] == pytest.approx(b[k], rel=1e-15, abs=1e-300), k
+
+
+def test_oracle_convexity_matches_reference(golden):
+    d, _ = golden
+    p, _ = inputs(next(c for c in d['cases'] if c['name'] == 'v2_psd_300'))
+    assert O.check_convex(300, p['hrow'], p['hcol'], p['hval']) == d['convex']['v2_psd_300']
+    bad = p['hval'].copy()
+    bad[0] = -1.0
+    assert O.check_convex(300, p['hrow'], p['hcol'], bad) == d['convex']['v2_indefinite_300']
+
+
+@pytest.mark.skipif(not os.environ.get('BOXQP_REFERENCE_DIR'), reason='set BOXQP_REFERENCE_DIR to the reference solver')
+def test_oracle_on_qplib_box_instances(golden):
+    """QPLIB 8792 / 8991 read by the reference's reader, solved by the oracle."""
+    d, _ = golden
+    if not O.ref_available():
+        pytest.skip('oracle/_ref not built')
+    data = Path(os.environ['BOXQP_REFERENCE_DIR']) / 'datasets' / 'qplib'
+    for rec in d['qplib']:
+        q = O.ref_read_qplib(data / f"{rec['name']}.qplib")
+        status, x, st = O.solve_box(q['hrow'], q['hcol'], q['hval'], q['cost'], q['lower'], q['upper'], tol=1e-7,
+                                    time_limit=600, maximize=q['maximize'], offset=q['offset'])
+        assert status == rec['status'] and int(st['iterations']) == rec['iterations']
+        assert st['objective'] == pytest.approx(rec['objective'], rel=1e-12)
