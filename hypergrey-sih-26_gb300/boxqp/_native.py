@@ -20,7 +20,8 @@ PRECISIONS = {'fp64': 0, 'mixed': 1, 'fp64_exact': 2}
 class Options(ctypes.Structure):
     _fields_ = [('tolerance', c_double), ('time_limit', c_double), ('iteration_limit', c_int64),
                 ('precision', c_int32), ('lipschitz', c_int32), ('check_interval', c_int32),
-                ('diagonal_gate', c_int32), ('offset', c_double)]
+                ('diagonal_gate', c_int32), ('offset', c_double), ('kernel_variant', c_int32),
+                ('reserved', c_int32)]
 
 
 class Stats(ctypes.Structure):

@@ -94,7 +94,7 @@ def _i64(a):
 
 
 def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, precision='fp64',
-                   check_interval=25, diagonal_gate=-1, offset=0.0):
+                   check_interval=25, diagonal_gate=-1, offset=0.0, kernel_variant=-1):
     o = Options()
     lib().bqp_options_default(o)
     o.tolerance = float(tolerance)
@@ -104,6 +104,7 @@ def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, prec
     o.check_interval = int(check_interval)
     o.diagonal_gate = int(diagonal_gate)
     o.offset = float(offset)
+    o.kernel_variant = int(kernel_variant)
     return o
 
 
@@ -181,6 +182,7 @@ class Engine:
     def submit(self, rowptr, col, val, c, lower, upper, options: Options):
         rowptr, col, val = _i32(rowptr), _i32(col), _f64(val)
         c, lower, upper = _f64(c), _f64(lower), _f64(upper)
+        options = _tuned(options, c.shape[0], col.shape[0])
         ident = N.c_uint64(0)
         rc = lib().bqp_submit(self._ctx, c.shape[0], col.shape[0], ptr(rowptr, N.c_int32), ptr(col, N.c_int32),
                               ptr(val, N.c_double), ptr(c, N.c_double), ptr(lower, N.c_double),
@@ -239,6 +241,7 @@ class Engine:
         """Synchronous solve through bqp_solve_sync; returns (x, Stats)."""
         rowptr, col, val = _i32(rowptr), _i32(col), _f64(val)
         c, lower, upper = _f64(c), _f64(lower), _f64(upper)
+        options = _tuned(options, c.shape[0], col.shape[0])
         x = np.empty(c.shape[0], dtype=np.float64)
         st = Stats()
         rc = lib().bqp_solve_sync(self._ctx, c.shape[0], col.shape[0], ptr(rowptr, N.c_int32), ptr(col, N.c_int32),
@@ -246,6 +249,23 @@ class Engine:
                                   ptr(upper, N.c_double), options, ptr(x, N.c_double), st)
         self._check(rc)
         return x, st
+
+
+_PRECISION_NAMES = {v: k for k, v in N.PRECISIONS.items()}
+
+
+def _tuned(options, n, nnz):
+    """Fills kernel_variant from the autotuning table when the caller left it automatic."""
+    if options.kernel_variant >= 0:
+        return options
+    from .autotune import tuned_variant
+    v = tuned_variant(_PRECISION_NAMES.get(options.precision, 'fp64'), n, nnz)
+    if v < 0:
+        return options
+    o = Options()
+    N.ctypes.pointer(o)[0] = options
+    o.kernel_variant = v
+    return o
 
 
 _default = {}

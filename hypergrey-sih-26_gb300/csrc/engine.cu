@@ -19,6 +19,8 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <limits>
@@ -49,6 +51,7 @@ struct Layout {
     size_t c32 = kNone, l32 = kNone, u32 = kNone, x32 = kNone, w32a = kNone, w32b = kNone;
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
+    size_t xp2 = kNone, p2 = kNone, dinv = kNone;
     size_t total = 0;
 };
 
@@ -86,6 +89,9 @@ Layout make_layout(int64_t n, int64_t nnz, int precision) {
         L.p = take(N * 8);
         L.q = take(N * 8);
         L.z = take(N * 8);
+        L.xp2 = take(N * 8);
+        L.p2 = take(N * 8);
+        L.dinv = take(N * 8);
         L.fixed = take(N);
     } else {
         L.x64 = take(N * 8);
@@ -118,7 +124,7 @@ struct Job {
     const double* u = nullptr;
     double lipschitz = 0;
     int diag_gate = 0;
-    int lanes = 4;
+    int variant = 0;
     std::vector<Tile> tiles;  // local tiles (inst field filled at admission)
     int state = JOB_QUEUED;
     bool resolve = false;     // re-run of a resident solve
@@ -145,40 +151,38 @@ void free_inputs(Job& j) {
     j.rowptr = nullptr; j.col = nullptr; j.val = nullptr; j.c = nullptr; j.l = nullptr; j.u = nullptr;
 }
 
-int lanes_for(int64_t n, int64_t nnz, int precision) {
+// Default SpMV structure of the step kernel when the caller's options do not name one
+// (kernel_variant < 0): rows longer than a warp use sub-warps, the rest the block-staged tile.
+int default_variant(int64_t n, int64_t nnz, int precision) {
     if (precision == PREC_FP64_EXACT) return 1;
     const double avg = n > 0 ? static_cast<double>(nnz) / static_cast<double>(n) : 1.0;
-    if (avg < 3) return 1;
-    if (avg < 6) return 2;
-    if (avg < 12) return 4;
-    if (avg < 24) return 8;
-    if (avg < 48) return 16;
-    return 32;
+    if (avg >= 48) return 32;
+    return VAR_TILE;
 }
 
 // Row tiles of one instance: contiguous rows with about kTileNnz nonzeros and at most
 // kTileRows rows.  Depends on the instance alone, so its reductions are the same whether it
 // runs alone or inside any batch.
-std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int lanes) {
+std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int variant) {
     std::vector<Tile> t;
     int64_t r = 0;
     while (r < n) {
         int64_t e = r + 1;
         while (e < n && e - r < kTileRows && static_cast<int64_t>(rowptr[e + 1]) - rowptr[r] <= kTileNnz) ++e;
-        t.push_back(Tile{0, static_cast<int32_t>(r), static_cast<int32_t>(e), lanes});
+        t.push_back(Tile{0, static_cast<int32_t>(r), static_cast<int32_t>(e), variant});
         r = e;
     }
     return t;
 }
 
 // Algorithmic bytes, fixed accounting: per FISTA iteration nnz (s_v + 4) + 4 (n + 1) + 7 n s_x;
-// per check nnz 12 + 4 (n + 1) + 32 n; per CG iteration nnz 12 + 4 (n + 1) + 112 n.
+// per check nnz 12 + 4 (n + 1) + 32 n; per CG iteration nnz 12 + 4 (n + 1) + 128 n.
 double algorithmic_bytes(int64_t n, int64_t nnz, int precision, int64_t iters, int64_t checks, int64_t cg) {
     const double N = static_cast<double>(n), Z = static_cast<double>(nnz);
     const double sv = precision == PREC_MIXED ? 4.0 : 8.0;
     const double b_iter = Z * (sv + 4) + 4 * (N + 1) + 7 * N * sv;
     const double b_check = Z * 12 + 4 * (N + 1) + 32 * N;
-    const double b_cg = Z * 12 + 4 * (N + 1) + 112 * N;
+    const double b_cg = Z * 12 + 4 * (N + 1) + 128 * N;
     return static_cast<double>(iters) * b_iter + static_cast<double>(checks) * b_check + static_cast<double>(cg) * b_cg;
 }
 
@@ -240,6 +244,8 @@ private:
     void loop();
     bool admit(Job& j, std::string& why);
     bool run_once(std::string& why);
+    bool run_stream(int cap, std::string& why);
+    void update_grid();
     void collect(std::unique_lock<std::mutex>& lk);
     void process_frees();
     bool ensure_tables(int need_inst, int need_tiles, std::string& why);
@@ -264,6 +270,7 @@ private:
     int device_;
     size_t cap_;
     int sms_ = 152;
+    int grid_max_ = 152 * 8;
     cudaStream_t stream_ = nullptr;
     cudaStream_t capture_ = nullptr;
     cudaMemPool_t pool_ = nullptr;
@@ -309,6 +316,13 @@ private:
     double timer_ms_ = 0;
     int64_t timer_kernels_ = 0, timer_launches_ = 0;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    // launch mode: conditional graph (default) or host-driven stream launches (BOXQP_LAUNCH=stream;
+    // per-kernel profilers cannot see kernels inside conditional graphs)
+    bool stream_mode_ = false;
+    bool profile_phases_ = false;  // BOXQP_PROFILE=1: per-phase CUDA-event times, printed at exit
+    cudaEvent_t pev_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    double phase_ms_[4] = {0, 0, 0, 0};  // check+gate, steps, polish, control
+    int64_t phase_bodies_ = 0;
     bool stop_ = false;
     std::thread thread_;
 
@@ -331,6 +345,7 @@ bool Engine::init(std::string& why) {
     }
     if (!cuda_ok(cudaSetDevice(device_), why, "set device")) return false;
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_);
+    grid_max_ = tile_grid(sms_);
     if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
     cudaMemPoolProps props;
@@ -346,6 +361,10 @@ bool Engine::init(std::string& why) {
         cudaMemGetInfo(&free_b, &total_b);
         cap_ = static_cast<size_t>(0.9 * static_cast<double>(free_b));
     }
+    if (const char* m = std::getenv("BOXQP_LAUNCH")) stream_mode_ = std::string(m) == "stream";
+    if (const char* m = std::getenv("BOXQP_PROFILE")) profile_phases_ = std::string(m) == "1";
+    if (profile_phases_)
+        for (auto& e : pev_) cudaEventCreate(&e);
     if (!cuda_ok(cudaEventCreate(&ev0_), why, "event")) return false;
     if (!cuda_ok(cudaEventCreate(&ev1_), why, "event")) return false;
     if (!cuda_ok(cudaMalloc(&d_ctrl_, sizeof(Ctrl)), why, "control block")) return false;
@@ -388,6 +407,11 @@ void Engine::shutdown() {
     h_status_ = nullptr;
     if (pool_) cudaMemPoolDestroy(pool_);
     pool_ = nullptr;
+    if (profile_phases_) {
+        std::fprintf(stderr, "[boxqp] phase ms over %lld bodies: check+gate %.3f steps %.3f polish %.3f control %.3f\n",
+                     static_cast<long long>(phase_bodies_), phase_ms_[0], phase_ms_[1], phase_ms_[2], phase_ms_[3]);
+        for (auto& e : pev_) if (e) cudaEventDestroy(e);
+    }
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     ev0_ = nullptr;
@@ -445,15 +469,77 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
     return true;
 }
 
+void Engine::update_grid() {
+    const int grid_max = grid_max_;
+    int want = static_cast<int>(std::min<size_t>(static_cast<size_t>(grid_max), align_up(std::max<size_t>(h_tiles_.size(), 1), 32)));
+    graph_grid_ = std::max(want, graph_grid_);
+    if (graph_grid_ > grid_max) graph_grid_ = grid_max;
+}
+
+// Host-driven launches of the same loop body: the host reads the gate's phase counts after
+// each check and launches only the kernels those phases need.
+bool Engine::run_stream(int cap, std::string& why) {
+    update_grid();
+    const int grid = graph_grid_;
+    const int K = graph_interval_;
+    const View v = view();
+    const int precisions[3] = {PREC_FP64, PREC_MIXED, PREC_FP64_EXACT};
+    long long kernels = 0;
+    int bodies = 0;
+    for (; bodies < cap; ++bodies) {
+        if (profile_phases_) cudaEventRecord(pev_[0], stream_);
+        launch_check(v, grid, stream_);
+        launch_gate_plain(v, stream_);
+        kernels += 2;
+        cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
+        if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine check")) return false;
+        if (profile_phases_) cudaEventRecord(pev_[1], stream_);
+        for (int k = 0; k < 3; ++k) {
+            if (h_ctrl_->n_fista[k] <= 0) continue;
+            for (int j = 0; j < K; ++j) launch_step(v, precisions[k], j, grid, stream_);
+            kernels += K;
+        }
+        if (profile_phases_) cudaEventRecord(pev_[2], stream_);
+        if (h_ctrl_->n_polish > 0) {
+            launch_polish_init(v, grid, stream_);
+            launch_polish_residual(v, grid, stream_);
+            for (int j = 0; j < kCgPerBody; ++j) {
+                launch_cg_matvec(v, grid, stream_);
+                launch_cg_update(v, grid, stream_);
+                launch_cg_direction(v, grid, stream_);
+            }
+            kernels += 2 + 3 * kCgPerBody;
+        }
+        if (profile_phases_) cudaEventRecord(pev_[3], stream_);
+        launch_control_plain(v, stream_);
+        kernels += 1;
+        if (profile_phases_) cudaEventRecord(pev_[4], stream_);
+        cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
+        if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine body")) return false;
+        if (profile_phases_) {
+            float a = 0;
+            for (int k = 0; k < 4; ++k) {
+                cudaEventElapsedTime(&a, pev_[k], pev_[k + 1]);
+                phase_ms_[k] += a;
+            }
+            phase_bodies_++;
+        }
+        if (h_ctrl_->running == 0) {
+            ++bodies;
+            break;
+        }
+    }
+    h_ctrl_->kernels = kernels;
+    h_ctrl_->bodies = bodies;
+    return cuda_ok(cudaGetLastError(), why, "stream launches");
+}
+
 bool Engine::build_graph(std::string& why) {
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     exec_ = nullptr;
     graph_ = nullptr;
-    const int grid_max = sms_ * 8;
-    int want = static_cast<int>(std::min<size_t>(static_cast<size_t>(grid_max), align_up(std::max<size_t>(h_tiles_.size(), 1), 32)));
-    graph_grid_ = std::max(want, graph_grid_);
-    if (graph_grid_ > grid_max) graph_grid_ = grid_max;
+    update_grid();
     const int grid = graph_grid_;
     const int K = graph_interval_;
     const View v = view();
@@ -689,6 +775,9 @@ bool Engine::admit(Job& j, std::string& why) {
         R.q = at<double>(slab, L.q);
         R.z = at<double>(slab, L.z);
         R.fixed = at<uint8_t>(slab, L.fixed);
+        R.xp2 = at<float2>(slab, L.xp2);
+        R.p2 = at<float2>(slab, L.p2);
+        R.dinv = at<double>(slab, L.dinv);
         R.n = static_cast<int32_t>(j.n);
         R.diag_gate = j.diag_gate;
         R.precision = prec;
@@ -768,7 +857,7 @@ bool Engine::admit(Job& j, std::string& why) {
         graph_interval_ = std::min(j.opt.check_interval, kMaxInterval);
         graph_valid_ = false;
     }
-    const int grid_max = sms_ * 8;
+    const int grid_max = grid_max_;
     if (graph_grid_ < grid_max && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
     return true;
 }
@@ -806,7 +895,7 @@ bool Engine::run_once(std::string& why) {
         cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
         tables_dirty_ = false;
     }
-    if (!graph_valid_ && !build_graph(why)) return false;
+    if (!stream_mode_ && !graph_valid_ && !build_graph(why)) return false;
     int cap = std::numeric_limits<int>::max() / 2;
     double latency;
     {
@@ -823,7 +912,12 @@ bool Engine::run_once(std::string& why) {
     const double t0 = host_seconds();
     if (!cuda_ok(cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_), why, "control upload")) return false;
     cudaEventRecord(ev0_, stream_);
-    if (!cuda_ok(cudaGraphLaunch(exec_, stream_), why, "graph launch")) return false;
+    if (stream_mode_) {
+        if (!run_stream(cap, why)) return false;
+        cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
+    } else if (!cuda_ok(cudaGraphLaunch(exec_, stream_), why, "graph launch")) {
+        return false;
+    }
     cudaEventRecord(ev1_, stream_);
     cudaMemcpyAsync(h_status_, d_status_, sizeof(int32_t) * std::max(n_inst_, 1), cudaMemcpyDeviceToHost, stream_);
     cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
@@ -916,10 +1010,7 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     if (j.state != JOB_DONE || !j.resident || n_running_ != 0 || !queue_.empty() || launches < 1) return BQP_ERR_NOT_READY;
     cudaSetDevice(device_);
     std::string why;
-    if (!graph_valid_ && !build_graph(why)) {
-        set_error(why);
-        return BQP_ERR_CUDA;
-    }
+    update_grid();
     InstDev saved;
     cudaMemcpy(&saved, &d_inst_[j.slot], sizeof(InstDev), cudaMemcpyDeviceToHost);
     InstDev R = saved;
@@ -1044,7 +1135,10 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
     if (!o || !(o->tolerance > 0) || !std::isfinite(o->tolerance) || o->time_limit < 0 || !std::isfinite(o->time_limit) ||
         o->iteration_limit < 0 || o->check_interval < 1 || o->check_interval > bqp::kMaxInterval ||
         (o->precision != BQP_PRECISION_FP64 && o->precision != BQP_PRECISION_MIXED && o->precision != BQP_PRECISION_FP64_EXACT) ||
-        !std::isfinite(o->offset)) {
+        !std::isfinite(o->offset) ||
+        (o->kernel_variant >= 0 && o->kernel_variant != 0 && o->kernel_variant != 64 && o->kernel_variant != 1 &&
+         o->kernel_variant != 2 && o->kernel_variant != 4 && o->kernel_variant != 8 && o->kernel_variant != 16 &&
+         o->kernel_variant != 32)) {
         why = "Invalid box QP options";
         return BQP_ERR_INVALID;
     }
@@ -1111,8 +1205,10 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
             return BQP_OK;
         }
     }
-    j->lanes = bqp::lanes_for(n, nnz, o.precision);
-    j->tiles = bqp::make_tiles(n, rowptr, j->lanes);
+    if (o.precision == BQP_PRECISION_FP64_EXACT) j->variant = 1;
+    else if (o.kernel_variant >= 0) j->variant = o.kernel_variant;
+    else j->variant = bqp::default_variant(n, nnz, o.precision);
+    j->tiles = bqp::make_tiles(n, rowptr, j->variant);
     if (copy) {
         j->own_rowptr.assign(rowptr, rowptr + n + 1);
         j->own_col.assign(col, col + nnz);
@@ -1152,6 +1248,8 @@ void bqp_options_default(bqp_options* o) {
     o->check_interval = 25;
     o->diagonal_gate = -1;
     o->offset = 0;
+    o->kernel_variant = -1;
+    o->reserved = 0;
 }
 
 bqp_ctx* bqp_create(int device, size_t mem_cap_bytes) {

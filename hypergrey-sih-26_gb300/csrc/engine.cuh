@@ -34,21 +34,31 @@ enum Status : int32_t {
 
 enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1, PREC_FP64_EXACT = 2 };
 
+// SpMV structure of a tile's step kernel (chosen per instance by the autotuning table).
+enum Variant : int32_t {
+    VAR_TILE = 0,    // block-staged: products of the whole tile, then one thread per row
+    VAR_WARP = 64,   // warp-staged: 32 rows per warp, products then one lane per row
+    // 1, 2, 4, 8, 16, 32: sub-warp rows, that many lanes per row
+};
+
 struct Tile {
     int32_t inst;
     int32_t row_begin;
     int32_t row_end;
-    int32_t lanes;  // lanes per row: 1, 2, 4, 8, 16 or 32
+    int32_t variant;  // Variant, or lanes per row (1..32)
 };
 
-// Per-tile partial results of one check (or of one CG reduction).
+// Per-tile partial results of one check (or of one CG reduction).  Sums are plain FP64 reduced in
+// a fixed tree; maxima of non-negative doubles travel as their IEEE bit patterns, whose unsigned
+// integer order is the numeric order, so they reduce on the integer pipes.
 struct __align__(16) Partial {
-    double stat;          // max stationarity
-    double prim;          // max scaled bound violation (starts at 0)
-    double obj_hi, obj_lo;  // double-double objective sum
-    double bnd_hi, bnd_lo;  // double-double tangent dual bound terms
-    double sep_hi, sep_lo;  // double-double separable dual bound terms
-    double a, a_lo, b;    // CG: dot product (double-double) / max scaled residual
+    double obj;           // objective terms
+    double bnd;           // tangent dual-bound terms
+    double sep;           // separable dual-bound terms
+    double a;             // CG: dot product
+    uint64_t stat;        // max stationarity (bits)
+    uint64_t prim;        // max scaled bound violation (bits, >= +0)
+    uint64_t b;           // CG: max scaled residual (bits)
     uint64_t hash;        // active-set signature
     int64_t n_active;     // variables at a bound
     int32_t flags;        // bit0: non-finite x, bit1: infinite bound target
@@ -69,12 +79,15 @@ struct __align__(16) InstDev {
     const float* l32;      // smallest float >= l
     const float* u32;      // largest float <= u
     const double* diag;    // FP64 diagonal of Q
+    const double* dinv;    // 1 / diagonal (mixed: Jacobi preconditioner of the polish)
     // iterates
     double* x64;
     double* w64[2];
     float* x32;
     float* w32[2];
     double* xp;            // polished point (FP64)
+    float2* xp2;           // xp as an FP32 pair (hi, lo) for FP32-only gathers
+    float2* p2;            // CG direction p as an FP32 pair
     double* r;
     double* p;
     double* q;

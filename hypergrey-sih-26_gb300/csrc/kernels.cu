@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 namespace bqp {
 namespace {
@@ -37,20 +38,6 @@ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b 
 __device__ __forceinline__ float smaxf(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float sminf(float a, float b) { return (b < a) ? b : a; }
 
-// ---- double-double accumulation (Knuth TwoSum; FMA TwoProduct) -----------------------------
-struct DD {
-    double hi, lo;
-};
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-    double s = __dadd_rn(a.hi, b.hi);
-    double bb = __dsub_rn(s, a.hi);
-    double e = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bb)), __dsub_rn(b.hi, bb));
-    e = __dadd_rn(e, __dadd_rn(a.lo, b.lo));
-    double h = __dadd_rn(s, e);
-    return {h, __dsub_rn(e, __dsub_rn(h, s))};
-}
-__device__ __forceinline__ double dd_value(DD a) { return __dadd_rn(a.hi, a.lo); }
-
 template <class T>
 __device__ __forceinline__ T shfl_xor(T v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 
@@ -61,98 +48,80 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
-// ---- check accumulator ----------------------------------------------------------------------
+// ---- check / CG accumulators ---------------------------------------------------------------------
+// Sums in plain FP64, maxima of non-negative doubles as unsigned bit patterns.
+__device__ __forceinline__ unsigned long long dbits(double v) {
+    return static_cast<unsigned long long>(__double_as_longlong(v));
+}
+__device__ __forceinline__ double bdouble(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a < b ? b : a; }
+
 struct Acc {
-    double stat, prim, obj, bnd, sep, a, b;
-    uint64_t hash;
+    double obj, bnd, sep, a;
+    unsigned long long stat, prim, b, hash;
     long long nact;
     int flags;
 };
 __device__ __forceinline__ Acc acc_identity() {
     Acc a;
-    a.stat = 0; a.prim = 0; a.obj = 0; a.bnd = 0; a.sep = 0; a.a = 0; a.b = 0;
-    a.hash = 0; a.nact = 0; a.flags = 0;
+    a.obj = 0; a.bnd = 0; a.sep = 0; a.a = 0;
+    a.stat = 0; a.prim = 0; a.b = 0; a.hash = 0;
+    a.nact = 0; a.flags = 0;
     return a;
 }
-struct AccDD {
-    double stat, prim, b;
-    DD obj, bnd, sep, a;
-    uint64_t hash;
-    long long nact;
-    int flags;
-};
-__device__ __forceinline__ AccDD to_dd(const Acc& x) {
-    AccDD r;
-    r.stat = x.stat; r.prim = x.prim; r.b = x.b;
-    r.obj = {x.obj, 0}; r.bnd = {x.bnd, 0}; r.sep = {x.sep, 0}; r.a = {x.a, 0};
-    r.hash = x.hash; r.nact = x.nact; r.flags = x.flags;
-    return r;
-}
-__device__ __forceinline__ AccDD combine(const AccDD& x, const AccDD& y) {
-    AccDD r;
-    r.stat = smax(x.stat, y.stat);
-    r.prim = smax(x.prim, y.prim);
-    r.b = smax(x.b, y.b);
-    r.obj = dd_add(x.obj, y.obj);
-    r.bnd = dd_add(x.bnd, y.bnd);
-    r.sep = dd_add(x.sep, y.sep);
-    r.a = dd_add(x.a, y.a);
+__device__ __forceinline__ Acc combine(const Acc& x, const Acc& y) {
+    Acc r;
+    r.obj = x.obj + y.obj;
+    r.bnd = x.bnd + y.bnd;
+    r.sep = x.sep + y.sep;
+    r.a = x.a + y.a;
+    r.stat = umax64(x.stat, y.stat);
+    r.prim = umax64(x.prim, y.prim);
+    r.b = umax64(x.b, y.b);
     r.hash = x.hash ^ y.hash;
     r.nact = x.nact + y.nact;
     r.flags = x.flags | y.flags;
     return r;
 }
-__device__ __forceinline__ AccDD shfl_acc(const AccDD& x, int o) {
-    AccDD r;
+__device__ __forceinline__ Acc shfl_acc(const Acc& x, int o) {
+    Acc r;
+    r.obj = shfl_xor(x.obj, o); r.bnd = shfl_xor(x.bnd, o); r.sep = shfl_xor(x.sep, o); r.a = shfl_xor(x.a, o);
     r.stat = shfl_xor(x.stat, o); r.prim = shfl_xor(x.prim, o); r.b = shfl_xor(x.b, o);
-    r.obj.hi = shfl_xor(x.obj.hi, o); r.obj.lo = shfl_xor(x.obj.lo, o);
-    r.bnd.hi = shfl_xor(x.bnd.hi, o); r.bnd.lo = shfl_xor(x.bnd.lo, o);
-    r.sep.hi = shfl_xor(x.sep.hi, o); r.sep.lo = shfl_xor(x.sep.lo, o);
-    r.a.hi = shfl_xor(x.a.hi, o); r.a.lo = shfl_xor(x.a.lo, o);
-    r.hash = shfl_xor(static_cast<unsigned long long>(x.hash), o);
+    r.hash = shfl_xor(x.hash, o);
     r.nact = shfl_xor(x.nact, o);
     r.flags = shfl_xor(x.flags, o);
     return r;
 }
 
 // Fixed-order block reduction; the result is valid in thread 0.
-__device__ AccDD block_reduce(AccDD v) {
-    __shared__ AccDD warp_part[kBlock / 32];
+__device__ Acc block_reduce(Acc v) {
+    __shared__ Acc warp_part[kBlock / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = combine(v, shfl_acc(v, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) warp_part[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        AccDD w = warp_part[lane < kBlock / 32 ? lane : 0];
-        if (lane >= kBlock / 32) {
-            w = to_dd(acc_identity());
-        }
+        Acc w = lane < kBlock / 32 ? warp_part[lane] : acc_identity();
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) w = combine(w, shfl_acc(w, o));
+        for (int o = (kBlock / 64); o > 0; o >>= 1) w = combine(w, shfl_acc(w, o));
         v = w;
     }
     __syncthreads();
     return v;
 }
 
-__device__ __forceinline__ void store_partial(Partial* p, const AccDD& v) {
-    p->stat = v.stat; p->prim = v.prim;
-    p->obj_hi = v.obj.hi; p->obj_lo = v.obj.lo;
-    p->bnd_hi = v.bnd.hi; p->bnd_lo = v.bnd.lo;
-    p->sep_hi = v.sep.hi; p->sep_lo = v.sep.lo;
-    p->a = v.a.hi; p->a_lo = v.a.lo; p->b = v.b;
-    p->hash = v.hash; p->n_active = v.nact; p->flags = v.flags;
-    p->pad = 0;
+__device__ __forceinline__ void store_partial(Partial* p, const Acc& v) {
+    p->obj = v.obj; p->bnd = v.bnd; p->sep = v.sep; p->a = v.a;
+    p->stat = v.stat; p->prim = v.prim; p->b = v.b; p->hash = v.hash;
+    p->n_active = v.nact; p->flags = v.flags; p->pad = 0;
 }
-__device__ __forceinline__ AccDD load_partial(const Partial* p) {
-    AccDD r;
-    r.stat = __ldcg(&p->stat); r.prim = __ldcg(&p->prim);
-    r.obj = {__ldcg(&p->obj_hi), __ldcg(&p->obj_lo)};
-    r.bnd = {__ldcg(&p->bnd_hi), __ldcg(&p->bnd_lo)};
-    r.sep = {__ldcg(&p->sep_hi), __ldcg(&p->sep_lo)};
-    r.a = {__ldcg(&p->a), __ldcg(&p->a_lo)};
-    r.b = __ldcg(&p->b);
+__device__ __forceinline__ Acc load_partial(const Partial* p) {
+    Acc r;
+    r.obj = __ldcg(&p->obj); r.bnd = __ldcg(&p->bnd); r.sep = __ldcg(&p->sep); r.a = __ldcg(&p->a);
+    r.stat = __ldcg(reinterpret_cast<const unsigned long long*>(&p->stat));
+    r.prim = __ldcg(reinterpret_cast<const unsigned long long*>(&p->prim));
+    r.b = __ldcg(reinterpret_cast<const unsigned long long*>(&p->b));
     r.hash = __ldcg(reinterpret_cast<const unsigned long long*>(&p->hash));
     r.nact = __ldcg(reinterpret_cast<const long long*>(&p->n_active));
     r.flags = __ldcg(&p->flags);
@@ -161,7 +130,7 @@ __device__ __forceinline__ AccDD load_partial(const Partial* p) {
 
 // Publishes the block's partial for tile t and returns true in every thread of the block
 // that finished the instance's last outstanding tile.
-__device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles_inst, const AccDD& total) {
+__device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles_inst, const Acc& total) {
     __shared__ int is_last;
     if (threadIdx.x == 0) {
         store_partial(&v.partial[t], total);
@@ -177,8 +146,8 @@ __device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles
 }
 
 // Reduces the partials of tiles [tb, te) in a fixed order; valid in thread 0.
-__device__ AccDD reduce_instance(const View& v, int tb, int te) {
-    AccDD acc = to_dd(acc_identity());
+__device__ Acc reduce_instance(const View& v, int tb, int te) {
+    Acc acc = acc_identity();
     for (int k = tb + threadIdx.x; k < te; k += kBlock) acc = combine(acc, load_partial(&v.partial[k]));
     return block_reduce(acc);
 }
@@ -202,10 +171,10 @@ __device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double c
     const double g = gq + ci;
     double res = fabs(xi - smax(li, smin(ui, xi - g))) / (1.0 + fabs(xi));
     if (!isfinite(g) || !isfinite(res)) res = kInf;
-    a.stat = smax(a.stat, res);
-    const double ax = fabs(xi);
-    if (isfinite(li)) a.prim = smax(a.prim, (li - xi) / (1.0 + fabs(li) + ax));
-    if (isfinite(ui)) a.prim = smax(a.prim, (xi - ui) / (1.0 + fabs(ui) + ax));
+    a.stat = umax64(a.stat, dbits(res));
+    // scaled bound violation, only where the bound is violated (iterates are clamped)
+    if (li - xi > 0) a.prim = umax64(a.prim, dbits((li - xi) / (1.0 + fabs(li) + fabs(xi))));
+    if (xi - ui > 0) a.prim = umax64(a.prim, dbits((xi - ui) / (1.0 + fabs(ui) + fabs(xi))));
     if (g != 0) {
         double target = g > 0 ? li : ui;
         if (isfinite(target)) a.bnd += g * (target - xi);
@@ -224,6 +193,80 @@ __device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double c
     }
 }
 
+// ---- warp-staged row groups ------------------------------------------------------------------
+// A warp takes 32 consecutive rows (one per lane).  Its lanes first form the products of the
+// group's nonzeros lane-strided (coalesced value/column loads, up to kWarpBuf independent gathers
+// in flight per warp) into a warp-private shared buffer, then each lane sums its own row and
+// runs the epilogue with all 32 lanes active.  No block-wide barrier: warps run independently.
+// Groups with more than kWarpBuf nonzeros are summed directly, one lane per row.
+// Per-warp buffer: 1024 entries of the product type (4 KB for FP32, 8 KB for 8-byte types),
+// in dynamic shared memory.
+// Buffer entries per warp: 1024 for 4-byte products (4 KB), 768 for 8-byte ones (6 KB).
+template <class T>
+__host__ __device__ constexpr int warp_entries() { return sizeof(T) == 4 ? 1024 : 768; }
+template <class T>
+__host__ __device__ constexpr int smem_bytes() { return warp_entries<T>() * static_cast<int>(sizeof(T)) * (kBlock / 32); }
+template <class T>
+__device__ __forceinline__ T* warp_buffer() {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    return reinterpret_cast<T*>(dyn_smem) + (threadIdx.x >> 5) * warp_entries<T>();
+}
+
+template <class T, class Prod, class Add, class Epi>
+__device__ __forceinline__ void warp_groups(const int32_t* __restrict__ rowptr, int rb, int re, T* buf, Prod prod,
+                                            Add add, T zero, Epi epi) {
+    constexpr int kWarpBuf = warp_entries<T>();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int g = rb + warp * 32; g < re; g += kBlock) {
+        const int r = g + lane;
+        const bool valid = r < re;
+        const int a = valid ? __ldg(rowptr + r) : 0;
+        const int b = valid ? __ldg(rowptr + r + 1) : 0;
+        const int last = (re - g < 32 ? re - g : 32) - 1;
+        const int kb = __shfl_sync(0xffffffffu, a, 0);
+        const int ke = __shfl_sync(0xffffffffu, b, last);
+        T acc = zero;
+        if (ke - kb <= kWarpBuf) {
+#pragma unroll 4
+            for (int k = kb + lane; k < ke; k += 32) buf[k - kb] = prod(k);
+            __syncwarp();
+            if (valid)
+                for (int k = a; k < b; ++k) acc = add(acc, buf[k - kb]);
+            __syncwarp();
+        } else if (valid) {
+            for (int k = a; k < b; ++k) acc = add(acc, prod(k));
+        }
+        if (valid) epi(r, acc);
+    }
+}
+
+// FP32 "double-float" arithmetic: an unevaluated pair (hi, lo) carries ~46 significant bits.
+// The products of the mixed engine's checks and polish run on the FP32 pipes with it, since
+// GB300's FP64 rate is 1/64 of its FP32 rate; FP64 is used once per row.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float bb = __fsub_rn(s, a.x);
+    const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+    return make_float2(s, __fadd_rn(e, __fadd_rn(a.y, b.y)));
+}
+// (h + l) * x exactly up to the lo-part products: h*x via FMA two-product.
+__device__ __forceinline__ float2 df_prod(float h, float l, float x) {
+    const float p = __fmul_rn(h, x);
+    const float e = __fmaf_rn(h, x, -p);
+    return make_float2(p, __fmaf_rn(l, x, e));
+}
+// (h + l) * (xh + xl)
+__device__ __forceinline__ float2 df_prod2(float h, float l, float2 x) {
+    const float p = __fmul_rn(h, x.x);
+    const float e = __fmaf_rn(h, x.x, -p);
+    return make_float2(p, __fmaf_rn(h, x.y, __fmaf_rn(l, x.x, e)));
+}
+__device__ __forceinline__ double df_value(float2 a) { return static_cast<double>(a.x) + static_cast<double>(a.y); }
+__device__ __forceinline__ float2 df_split(double x) {
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - static_cast<double>(h)));
+}
+
 // Sources of one check: MODE 0 FP64 values + x64; 1 hi/lo values + x32; 2 hi/lo values + xp.
 struct CheckSrc {
     const int32_t* rowptr;
@@ -234,6 +277,7 @@ struct CheckSrc {
     const double* x64;
     const float* x32;
     const double* xp;
+    const float2* xp2;
     const double* c;
     const double* l;
     const double* u;
@@ -243,73 +287,60 @@ struct CheckSrc {
     int gate;
 };
 
-template <int MODE>
-__device__ __forceinline__ double check_value(const CheckSrc& s, int k) {
-    if constexpr (MODE == 0) return __ldg(s.val64 + k);
-    else return static_cast<double>(__ldg(s.vhi + k)) + static_cast<double>(__ldg(s.vlo + k));
-}
-template <int MODE>
-__device__ __forceinline__ double check_x(const CheckSrc& s, int k) {
-    if constexpr (MODE == 0) return s.x64[k];
-    else if constexpr (MODE == 1) return static_cast<double>(s.x32[k]);
-    else return s.xp[k];
+__device__ __forceinline__ double gate_diag(const CheckSrc& s, int r, double fallback) {
+    if (!s.gate) return 1.0;
+    if (s.diag) return s.diag[r];
+    return fallback;
 }
 
-template <int LANES, int MODE>
+// Check of rows [rb, re): accumulates check_row terms into a.
+template <int MODE>
 __device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
-    constexpr int RPW = 32 / LANES;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sub = lane / LANES, sl = lane % LANES;
-    for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
-        const int r = base + sub;
-        double acc = 0;
-        if (r < re) {
-            const int ks = __ldg(s.rowptr + r), ke = __ldg(s.rowptr + r + 1);
-            for (int k = ks + sl; k < ke; k += LANES) acc = fma(check_value<MODE>(s, k), check_x<MODE>(s, __ldg(s.col + k)), acc);
-        }
-        acc = group_sum<LANES>(acc);
-        if (r < re && sl == 0) {
-            const double xi = check_x<MODE>(s, r);
-            bool atl, atu;
-            if constexpr (MODE == 1) {
+    const int32_t* __restrict__ col = s.col;
+    if constexpr (MODE == 0) {
+        double* buf = warp_buffer<double>();
+        warp_groups<double>(
+            s.rowptr, rb, re, buf, [&](int k) { return __ldg(s.val64 + k) * s.x64[__ldg(col + k)]; },
+            [](double x, double y) { return x + y; }, 0.0,
+            [&](int r, double gq) {
+                const double xi = s.x64[r];
+                const int ks = __ldg(s.rowptr + r);
+                const double di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? __ldg(s.val64 + ks) : 0.0);
+                check_row(a, xi, gq, s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
+            });
+    } else if constexpr (MODE == 1) {
+        float2* buf = warp_buffer<float2>();
+        warp_groups<float2>(
+            s.rowptr, rb, re, buf,
+            [&](int k) { return df_prod(__ldg(s.vhi + k), __ldg(s.vlo + k), s.x32[__ldg(col + k)]); },
+            [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
+            [&](int r, float2 acc) {
                 const float xf = s.x32[r];
-                atl = xf <= s.l32[r];
-                atu = xf >= s.u32[r];
-            } else {
-                atl = xi <= s.l[r];
-                atu = xi >= s.u[r];
-            }
-            double di = 1.0;
-            if (s.gate) {
-                if (s.diag) {
-                    di = s.diag[r];
-                } else {
-                    // a diagonal Hessian has exactly its diagonal entry in each non-empty row
-                    const int ks = __ldg(s.rowptr + r), ke = __ldg(s.rowptr + r + 1);
-                    di = ks < ke ? check_value<MODE>(s, ks) : 0.0;
-                }
-            }
-            check_row(a, xi, acc, s.c[r], s.l[r], s.u[r], di, s.gate, r, atl, atu);
-        }
-    }
-}
-
-template <int MODE>
-__device__ void check_rows_dispatch(const CheckSrc& s, int lanes, int rb, int re, Acc& a) {
-    switch (lanes) {
-    case 1: check_rows<1, MODE>(s, rb, re, a); break;
-    case 2: check_rows<2, MODE>(s, rb, re, a); break;
-    case 4: check_rows<4, MODE>(s, rb, re, a); break;
-    case 8: check_rows<8, MODE>(s, rb, re, a); break;
-    case 16: check_rows<16, MODE>(s, rb, re, a); break;
-    default: check_rows<32, MODE>(s, rb, re, a); break;
+                const int ks = __ldg(s.rowptr + r);
+                const double d0 = __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0;
+                check_row(a, static_cast<double>(xf), df_value(acc), s.c[r], s.l[r], s.u[r], gate_diag(s, r, d0), s.gate,
+                          r, xf <= s.l32[r], xf >= s.u32[r]);
+            });
+    } else {
+        float2* buf = warp_buffer<float2>();
+        warp_groups<float2>(
+            s.rowptr, rb, re, buf,
+            [&](int k) { return df_prod2(__ldg(s.vhi + k), __ldg(s.vlo + k), s.xp2[__ldg(col + k)]); },
+            [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
+            [&](int r, float2 acc) {
+                const double xi = s.xp[r];
+                const int ks = __ldg(s.rowptr + r);
+                const double d0 = __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0;
+                check_row(a, xi, df_value(acc), s.c[r], s.l[r], s.u[r], gate_diag(s, r, d0), s.gate, r, xi <= s.l[r],
+                          xi >= s.u[r]);
+            });
     }
 }
 
 __device__ __forceinline__ CheckSrc source_of(const InstDev& I) {
     CheckSrc s;
     s.rowptr = I.rowptr; s.col = I.col; s.val64 = I.val64; s.vhi = I.vhi; s.vlo = I.vlo;
-    s.x64 = I.x64; s.x32 = I.x32; s.xp = I.xp; s.c = I.c; s.l = I.l; s.u = I.u;
+    s.x64 = I.x64; s.x32 = I.x32; s.xp = I.xp; s.xp2 = I.xp2; s.c = I.c; s.l = I.l; s.u = I.u;
     s.l32 = I.l32; s.u32 = I.u32; s.diag = I.diag; s.gate = I.diag_gate;
     return s;
 }
@@ -334,7 +365,7 @@ __device__ void finish(InstDev& I, int status, int src) {
     I.end_ns = now_ns();
 }
 
-__device__ void after_check(InstDev& I, const AccDD& tot) {
+__device__ void after_check(InstDev& I, const Acc& tot) {
     const int64_t it_check = I.it_next;
     const int ph = I.phase;
     I.checks++;
@@ -343,12 +374,11 @@ __device__ void after_check(InstDev& I, const AccDD& tot) {
         obj = __longlong_as_double(0x7ff8000000000000LL);
         stat = kInf; prim = kInf; bound = -kInf; gap = kInf;
     } else {
-        DD value = dd_add(tot.obj, DD{I.offset, 0.0});
-        obj = dd_value(value);
-        stat = tot.stat;
-        prim = tot.prim;
-        if (I.diag_gate) bound = dd_value(dd_add(tot.sep, DD{I.offset, 0.0}));
-        else bound = (tot.flags & 2) ? -kInf : dd_value(dd_add(value, tot.bnd));
+        obj = tot.obj + I.offset;
+        stat = bdouble(tot.stat);
+        prim = bdouble(tot.prim);
+        if (I.diag_gate) bound = tot.sep + I.offset;
+        else bound = (tot.flags & 2) ? -kInf : obj + tot.bnd;
         gap = isfinite(bound) ? fabs(obj - bound) / (1.0 + fabs(obj)) : kInf;
     }
     const double worst = smax(prim, smax(stat, 0.0));
@@ -393,14 +423,39 @@ __device__ void after_check(InstDev& I, const AccDD& tot) {
 }
 
 // ---- step kernel ------------------------------------------------------------------------------
-template <int LANES, int PREC>
-__device__ void step_rows(const InstDev& I, int rb, int re, int j) {
+// EXACT precision: one thread per row, products and sums rounded separately in column order from
+// 0.0 and division by L -- the reference CPU loop's arithmetic exactly.
+__device__ void step_rows_exact(const InstDev& I, int rb, int re, int j) {
     const int64_t it = I.it0 + j;
     const int in = static_cast<int>(it & 1), out = in ^ 1;
-    constexpr int RPW = 32 / LANES;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sub = lane / LANES, sl = lane % LANES;
     const int32_t* __restrict__ rowptr = I.rowptr;
+    const int32_t* __restrict__ col = I.col;
+    const double* __restrict__ val = I.val64;
+    const double* __restrict__ win = I.w64[in];
+    double* __restrict__ wout = I.w64[out];
+    double* __restrict__ x = I.x64;
+    const double* __restrict__ c = I.c;
+    const double* __restrict__ l = I.l;
+    const double* __restrict__ u = I.u;
+    const double beta = I.beta[j];
+    const double L = I.L;
+    for (int r = rb + static_cast<int>(threadIdx.x); r < re; r += kBlock) {
+        double acc = 0.0;
+        const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+        for (int k = ks; k < ke; ++k) acc = __dadd_rn(acc, __dmul_rn(__ldg(val + k), __ldg(win + __ldg(col + k))));
+        const double v = __dsub_rn(__ldg(win + r), __ddiv_rn(__dadd_rn(acc, __ldg(c + r)), L));
+        const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
+        wout[r] = __dadd_rn(nx, __dmul_rn(beta, __dsub_rn(nx, x[r])));
+        x[r] = nx;
+    }
+}
+
+// FISTA step of rows [rb, re) with warp-staged products: g = Q w, then
+// x+ = clip(w - (g + c) / L), w+ = x+ + beta (x+ - x).
+template <int PREC>
+__device__ void step_rows_staged(const InstDev& I, int rb, int re, int j) {
+    const int64_t it = I.it0 + j;
+    const int in = static_cast<int>(it & 1), out = in ^ 1;
     const int32_t* __restrict__ col = I.col;
     if constexpr (PREC == PREC_MIXED) {
         const float* __restrict__ val = I.vhi;
@@ -412,22 +467,17 @@ __device__ void step_rows(const InstDev& I, int rb, int re, int j) {
         const float* __restrict__ u = I.u32;
         const float beta = static_cast<float>(I.beta[j]);
         const float invL = I.invLf;
-        for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
-            const int r = base + sub;
-            float acc = 0.f;
-            if (r < re) {
-                const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
-                for (int k = ks + sl; k < ke; k += LANES) acc = fmaf(__ldg(val + k), __ldg(win + __ldg(col + k)), acc);
-            }
-            acc = group_sum<LANES>(acc);
-            if (r < re && sl == 0) {
-                const float v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+        float* buf = warp_buffer<float>();
+        warp_groups<float>(
+            I.rowptr, rb, re, buf, [&](int k) { return __ldg(val + k) * __ldg(win + __ldg(col + k)); },
+            [](float a, float b) { return a + b; }, 0.f,
+            [&](int r, float g) {
+                const float v = __ldg(win + r) - (g + __ldg(c + r)) * invL;
                 const float nx = smaxf(__ldg(l + r), sminf(__ldg(u + r), v));
                 wout[r] = nx + beta * (nx - x[r]);
                 x[r] = nx;
-            }
-        }
-    } else if constexpr (PREC == PREC_FP64) {
+            });
+    } else {
         const double* __restrict__ val = I.val64;
         const double* __restrict__ win = I.w64[in];
         double* __restrict__ wout = I.w64[out];
@@ -437,43 +487,106 @@ __device__ void step_rows(const InstDev& I, int rb, int re, int j) {
         const double* __restrict__ u = I.u;
         const double beta = I.beta[j];
         const double invL = I.invL;
-        for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
-            const int r = base + sub;
-            double acc = 0.0;
-            if (r < re) {
-                const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
-                for (int k = ks + sl; k < ke; k += LANES) acc = fma(__ldg(val + k), __ldg(win + __ldg(col + k)), acc);
-            }
-            acc = group_sum<LANES>(acc);
-            if (r < re && sl == 0) {
-                const double v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+        double* buf = warp_buffer<double>();
+        warp_groups<double>(
+            I.rowptr, rb, re, buf, [&](int k) { return __ldg(val + k) * __ldg(win + __ldg(col + k)); },
+            [](double a, double b) { return a + b; }, 0.0,
+            [&](int r, double g) {
+                const double v = __ldg(win + r) - (g + __ldg(c + r)) * invL;
                 const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
                 wout[r] = nx + beta * (nx - x[r]);
                 x[r] = nx;
-            }
-        }
+            });
+    }
+}
+
+// Sub-warp rows: LANES lanes per row, a group of 32 / LANES rows per warp pass.
+template <int LANES, int PREC>
+__device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j) {
+    using T = typename std::conditional<PREC == PREC_MIXED, float, double>::type;
+    const int64_t it = I.it0 + j;
+    const int in = static_cast<int>(it & 1), out = in ^ 1;
+    constexpr int RPW = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    const int32_t* __restrict__ rowptr = I.rowptr;
+    const int32_t* __restrict__ col = I.col;
+    const T* __restrict__ val;
+    const T* __restrict__ win;
+    T* __restrict__ wout;
+    T* __restrict__ x;
+    const T* __restrict__ c;
+    const T* __restrict__ l;
+    const T* __restrict__ u;
+    T beta, invL;
+    if constexpr (PREC == PREC_MIXED) {
+        val = I.vhi; win = I.w32[in]; wout = I.w32[out]; x = I.x32; c = I.c32; l = I.l32; u = I.u32;
+        beta = static_cast<float>(I.beta[j]); invL = I.invLf;
     } else {
-        // PREC_FP64_EXACT: one thread per row, products and sums rounded separately in column
-        // order from 0.0 and division by L -- the reference CPU loop's arithmetic exactly.
-        const double* __restrict__ val = I.val64;
-        const double* __restrict__ win = I.w64[in];
-        double* __restrict__ wout = I.w64[out];
-        double* __restrict__ x = I.x64;
-        const double* __restrict__ c = I.c;
-        const double* __restrict__ l = I.l;
-        const double* __restrict__ u = I.u;
-        const double beta = I.beta[j];
-        const double L = I.L;
-        for (int r = rb + static_cast<int>(threadIdx.x); r < re; r += kBlock) {
-            double acc = 0.0;
+        val = I.val64; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
+        beta = I.beta[j]; invL = I.invL;
+    }
+    for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
+        const int r = base + sub;
+        T acc = 0;
+        if (r < re) {
             const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
-            for (int k = ks; k < ke; ++k) acc = __dadd_rn(acc, __dmul_rn(__ldg(val + k), __ldg(win + __ldg(col + k))));
-            const double v = __dsub_rn(__ldg(win + r), __ddiv_rn(__dadd_rn(acc, __ldg(c + r)), L));
-            const double nx = smax(__ldg(l + r), smin(__ldg(u + r), v));
-            wout[r] = __dadd_rn(nx, __dmul_rn(beta, __dsub_rn(nx, x[r])));
+#pragma unroll 4
+            for (int k = ks + sl; k < ke; k += LANES) acc += __ldg(val + k) * __ldg(win + __ldg(col + k));
+        }
+        acc = group_sum<LANES>(acc);
+        if (r < re && sl == 0) {
+            const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+            const T lo = __ldg(l + r), up = __ldg(u + r);
+            const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
+            wout[r] = nx + beta * (nx - x[r]);
             x[r] = nx;
         }
     }
+}
+
+// Block-staged tile (nnz <= kTileNnz): the tile's products are formed by all threads at once
+// (kTileNnz / kBlock independent gathers per thread), then one thread per row sums and updates.
+template <int PREC>
+__device__ void step_tile_block(const InstDev& I, int rb, int re, int j) {
+    using T = typename std::conditional<PREC == PREC_MIXED, float, double>::type;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    T* prod = reinterpret_cast<T*>(dyn_smem);
+    const int64_t it = I.it0 + j;
+    const int in = static_cast<int>(it & 1), out = in ^ 1;
+    const int32_t* __restrict__ rowptr = I.rowptr;
+    const int kb = __ldg(rowptr + rb), ke = __ldg(rowptr + re);
+    const int cnt = ke - kb;
+    const int32_t* __restrict__ cl = I.col + kb;
+    const T* __restrict__ val;
+    const T* __restrict__ win;
+    T* __restrict__ wout;
+    T* __restrict__ x;
+    const T* __restrict__ c;
+    const T* __restrict__ l;
+    const T* __restrict__ u;
+    T beta, invL;
+    if constexpr (PREC == PREC_MIXED) {
+        val = I.vhi + kb; win = I.w32[in]; wout = I.w32[out]; x = I.x32; c = I.c32; l = I.l32; u = I.u32;
+        beta = static_cast<float>(I.beta[j]); invL = I.invLf;
+    } else {
+        val = I.val64 + kb; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
+        beta = I.beta[j]; invL = I.invL;
+    }
+#pragma unroll 8
+    for (int k = threadIdx.x; k < cnt; k += kBlock) prod[k] = __ldg(val + k) * __ldg(win + __ldg(cl + k));
+    __syncthreads();
+    for (int r = rb + static_cast<int>(threadIdx.x); r < re; r += kBlock) {
+        const int a = __ldg(rowptr + r) - kb, b = __ldg(rowptr + r + 1) - kb;
+        T acc = 0;
+        for (int k = a; k < b; ++k) acc += prod[k];
+        const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+        const T lo = __ldg(l + r), up = __ldg(u + r);
+        const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
+        wout[r] = nx + beta * (nx - x[r]);
+        x[r] = nx;
+    }
+    __syncthreads();  // prod is reused by the next tile
 }
 
 template <int PREC>
@@ -485,15 +598,22 @@ __global__ void __launch_bounds__(kBlock) step_kernel(View v, int j) {
         if (I.status != ST_RUNNING || I.phase != PH_FISTA || I.precision != PREC) continue;
         if (I.it0 + j >= I.it_next) continue;
         if constexpr (PREC == PREC_FP64_EXACT) {
-            step_rows<1, PREC>(I, T.row_begin, T.row_end, j);
+            step_rows_exact(I, T.row_begin, T.row_end, j);
         } else {
-            switch (T.lanes) {
-            case 1: step_rows<1, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 2: step_rows<2, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 4: step_rows<4, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 8: step_rows<8, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 16: step_rows<16, PREC>(I, T.row_begin, T.row_end, j); break;
-            default: step_rows<32, PREC>(I, T.row_begin, T.row_end, j); break;
+            switch (T.variant) {
+            case VAR_TILE:
+                if (__ldg(I.rowptr + T.row_end) - __ldg(I.rowptr + T.row_begin) <= kTileNnz)
+                    step_tile_block<PREC>(I, T.row_begin, T.row_end, j);
+                else
+                    step_rows_staged<PREC>(I, T.row_begin, T.row_end, j);
+                break;
+            case VAR_WARP: step_rows_staged<PREC>(I, T.row_begin, T.row_end, j); break;
+            case 1: step_rows_subwarp<1, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 2: step_rows_subwarp<2, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 4: step_rows_subwarp<4, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 8: step_rows_subwarp<8, PREC>(I, T.row_begin, T.row_end, j); break;
+            case 16: step_rows_subwarp<16, PREC>(I, T.row_begin, T.row_end, j); break;
+            default: step_rows_subwarp<32, PREC>(I, T.row_begin, T.row_end, j); break;
             }
         }
     }
@@ -511,15 +631,15 @@ __global__ void __launch_bounds__(kBlock) check_kernel(View v) {
         const CheckSrc s = source_of(I);
         Acc a = acc_identity();
         if (I.precision == PREC_MIXED) {
-            if (ph == PH_POLISH_FINISH) check_rows_dispatch<2>(s, T.lanes, T.row_begin, T.row_end, a);
-            else check_rows_dispatch<1>(s, T.lanes, T.row_begin, T.row_end, a);
+            if (ph == PH_POLISH_FINISH) check_rows<2>(s, T.row_begin, T.row_end, a);
+            else check_rows<1>(s, T.row_begin, T.row_end, a);
         } else {
-            check_rows_dispatch<0>(s, T.lanes, T.row_begin, T.row_end, a);
+            check_rows<0>(s, T.row_begin, T.row_end, a);
         }
-        AccDD total = block_reduce(to_dd(a));
+        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance(v, R.x, R.y);
             if (threadIdx.x == 0) after_check(I, inst_total);
             __syncthreads();
         }
@@ -527,6 +647,10 @@ __global__ void __launch_bounds__(kBlock) check_kernel(View v) {
 }
 
 // ---- FP64 free-set polish ---------------------------------------------------------------------
+// Solves Q_FF x_F = -c_F - Q_FA x_A by Jacobi-preconditioned conjugate gradients, the free set F
+// being the variables the FP32 iterate holds strictly inside its bounds.  Vectors are FP64; the
+// matrix products are formed in FP32 double-float arithmetic from the hi/lo values and the FP32
+// pairs xp2 / p2 kept beside xp / p.
 __device__ __forceinline__ bool polish_phase(const InstDev& I, int phase) {
     return I.status == ST_RUNNING && I.phase == phase;
 }
@@ -545,61 +669,42 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
             else if (xf >= I.u32[r]) xv = I.u[r];
             else { xv = static_cast<double>(xf); fixed = 0; }
             I.xp[r] = xv;
+            I.xp2[r] = df_split(xv);
             I.fixed[r] = fixed;
         }
     }
 }
 
-template <int LANES>
-__device__ void hilo_matvec_rows(const InstDev& I, int rb, int re, const double* __restrict__ src,
-                                 bool residual, Acc& a) {
-    constexpr int RPW = 32 / LANES;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sub = lane / LANES, sl = lane % LANES;
-    for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
-        const int r = base + sub;
-        double acc = 0;
-        const bool live = r < re && !I.fixed[r];
-        if (live) {
-            const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
-            for (int k = ks + sl; k < ke; k += LANES) {
-                const double vk = static_cast<double>(__ldg(I.vhi + k)) + static_cast<double>(__ldg(I.vlo + k));
-                acc = fma(vk, src[__ldg(I.col + k)], acc);
-            }
-        }
-        acc = group_sum<LANES>(acc);
-        if (r < re && sl == 0) {
-            if (residual) {
-                // r = -(Q xp + c) on the free set, z = D^-1 r, p = z
+// q = Q src on the free rows (0 on fixed rows), src given as FP32 pairs.  residual = true:
+// r = -(Q xp + c), z = D^-1 r, p = z on free rows, accumulating r.z and max |r|/(1+|x|).
+template <bool RESIDUAL>
+__device__ void polish_matvec_rows(const InstDev& I, int rb, int re, const float2* __restrict__ src, Acc& a) {
+    const int32_t* __restrict__ col = I.col;
+    float2* buf = warp_buffer<float2>();
+    warp_groups<float2>(
+        I.rowptr, rb, re, buf, [&](int k) { return df_prod2(__ldg(I.vhi + k), __ldg(I.vlo + k), src[__ldg(col + k)]); },
+        [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
+        [&](int r, float2 acc) {
+            const bool live = !I.fixed[r];
+            if constexpr (RESIDUAL) {
                 double rr = 0, zz = 0;
                 if (live) {
-                    rr = -(acc + I.c[r]);
-                    const double d = I.diag[r];
-                    zz = d > 0 ? rr / d : rr;
+                    rr = -(df_value(acc) + I.c[r]);
+                    zz = rr * I.dinv[r];
                     a.a = fma(rr, zz, a.a);
-                    a.b = smax(a.b, fabs(rr) / (1.0 + fabs(I.xp[r])));
+                    a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) /
+                                                                 (1.0f + fabsf(static_cast<float>(I.xp[r]))))));
                 }
                 I.r[r] = rr;
                 I.z[r] = zz;
                 I.p[r] = zz;
+                I.p2[r] = df_split(zz);
             } else {
-                const double qq = live ? acc : 0.0;
+                const double qq = live ? df_value(acc) : 0.0;
                 I.q[r] = qq;
                 if (live) a.a = fma(I.p[r], qq, a.a);
             }
-        }
-    }
-}
-
-__device__ void hilo_matvec_dispatch(const InstDev& I, int lanes, int rb, int re, const double* src, bool residual, Acc& a) {
-    switch (lanes) {
-    case 1: hilo_matvec_rows<1>(I, rb, re, src, residual, a); break;
-    case 2: hilo_matvec_rows<2>(I, rb, re, src, residual, a); break;
-    case 4: hilo_matvec_rows<4>(I, rb, re, src, residual, a); break;
-    case 8: hilo_matvec_rows<8>(I, rb, re, src, residual, a); break;
-    case 16: hilo_matvec_rows<16>(I, rb, re, src, residual, a); break;
-    default: hilo_matvec_rows<32>(I, rb, re, src, residual, a); break;
-    }
+        });
 }
 
 __global__ void __launch_bounds__(kBlock) polish_residual_kernel(View v) {
@@ -609,16 +714,16 @@ __global__ void __launch_bounds__(kBlock) polish_residual_kernel(View v) {
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
         Acc a = acc_identity();
-        hilo_matvec_dispatch(I, T.lanes, T.row_begin, T.row_end, I.xp, true, a);
-        AccDD total = block_reduce(to_dd(a));
+        polish_matvec_rows<true>(I, T.row_begin, T.row_end, I.xp2, a);
+        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance(v, R.x, R.y);
             if (threadIdx.x == 0) {
-                I.rz = dd_value(inst_total.a);
-                I.cg_res = inst_total.b;
+                I.rz = inst_total.a;
+                I.cg_res = bdouble(inst_total.b);
                 I.cg_it = 0;
-                I.phase = (inst_total.b <= I.cg_tol || !(I.rz > 0)) ? PH_POLISH_FINISH : PH_POLISH_CG;
+                I.phase = (I.cg_res <= I.cg_tol || !(I.rz > 0)) ? PH_POLISH_FINISH : PH_POLISH_CG;
             }
             __syncthreads();
         }
@@ -632,13 +737,13 @@ __global__ void __launch_bounds__(kBlock) cg_matvec_kernel(View v) {
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         Acc a = acc_identity();
-        hilo_matvec_dispatch(I, T.lanes, T.row_begin, T.row_end, I.p, false, a);
-        AccDD total = block_reduce(to_dd(a));
+        polish_matvec_rows<false>(I, T.row_begin, T.row_end, I.p2, a);
+        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance(v, R.x, R.y);
             if (threadIdx.x == 0) {
-                const double pq = dd_value(inst_total.a);
+                const double pq = inst_total.a;
                 if (pq > 0 && isfinite(pq)) {
                     I.alpha = I.rz / pq;
                 } else {
@@ -663,26 +768,25 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
             if (I.fixed[r]) continue;
             const double xv = fma(alpha, I.p[r], I.xp[r]);
             const double rr = fma(-alpha, I.q[r], I.r[r]);
-            const double d = I.diag[r];
-            const double zz = d > 0 ? rr / d : rr;
+            const double zz = rr * I.dinv[r];
             I.xp[r] = xv;
             I.r[r] = rr;
             I.z[r] = zz;
             a.a = fma(rr, zz, a.a);
-            a.b = smax(a.b, fabs(rr) / (1.0 + fabs(xv)));
+            a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) / (1.0f + fabsf(static_cast<float>(xv))))));
         }
-        AccDD total = block_reduce(to_dd(a));
+        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            AccDD inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance(v, R.x, R.y);
             if (threadIdx.x == 0) {
-                const double rz_new = dd_value(inst_total.a);
+                const double rz_new = inst_total.a;
                 I.beta_cg = I.rz > 0 ? rz_new / I.rz : 0.0;
                 I.rz = rz_new;
-                I.cg_res = inst_total.b;
+                I.cg_res = bdouble(inst_total.b);
                 I.cg_it++;
                 I.cg_total++;
-                if (inst_total.b <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) I.phase = PH_POLISH_FINISH;
+                if (I.cg_res <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) I.phase = PH_POLISH_FINISH;
             }
             __syncthreads();
         }
@@ -697,11 +801,18 @@ __global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v) {
         if (I.status != ST_RUNNING) continue;
         if (I.phase == PH_POLISH_CG) {
             const double beta = I.beta_cg;
-            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock)
-                if (!I.fixed[r]) I.p[r] = fma(beta, I.p[r], I.z[r]);
+            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
+                if (I.fixed[r]) continue;
+                const double pv = fma(beta, I.p[r], I.z[r]);
+                I.p[r] = pv;
+                I.p2[r] = df_split(pv);
+            }
         } else if (I.phase == PH_POLISH_FINISH) {
-            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock)
-                I.xp[r] = smax(I.l[r], smin(I.u[r], I.xp[r]));
+            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
+                const double xv = smax(I.l[r], smin(I.u[r], I.xp[r]));
+                I.xp[r] = xv;
+                I.xp2[r] = df_split(xv);
+            }
         }
     }
 }
@@ -827,6 +938,7 @@ __global__ void prepare_kernel(View v, int slot, int n, const double* __restrict
         for (int k = ks; k < ke; ++k) if (I.col[k] == r) d += val[k];
         diag[r] = d;
         if (I.precision == PREC_MIXED) {
+            const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
             const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
             const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
             const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
@@ -856,8 +968,8 @@ __global__ void __launch_bounds__(kBlock) check_standalone_kernel(CheckSrc s, in
     const int rb = blockIdx.x * rows_per_block;
     const int re = min(n, rb + rows_per_block);
     Acc a = acc_identity();
-    if (rb < re) check_rows<4, 0>(s, rb, re, a);
-    AccDD total = block_reduce(to_dd(a));
+    if (rb < re) check_rows<0>(s, rb, re, a);
+    Acc total = block_reduce(a);
     __shared__ int is_last;
     if (threadIdx.x == 0) {
         store_partial(&partial[blockIdx.x], total);
@@ -867,9 +979,9 @@ __global__ void __launch_bounds__(kBlock) check_standalone_kernel(CheckSrc s, in
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    AccDD acc = to_dd(acc_identity());
+    Acc acc = acc_identity();
     for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += kBlock) acc = combine(acc, load_partial(&partial[k]));
-    AccDD tot = block_reduce(acc);
+    Acc tot = block_reduce(acc);
     if (threadIdx.x == 0) {
         scr->done = 0;
         double obj, stat, prim, bound, gap;
@@ -877,12 +989,11 @@ __global__ void __launch_bounds__(kBlock) check_standalone_kernel(CheckSrc s, in
             obj = __longlong_as_double(0x7ff8000000000000LL);
             stat = kInf; prim = kInf; bound = -kInf; gap = kInf;
         } else {
-            DD value = dd_add(tot.obj, DD{offset, 0.0});
-            obj = dd_value(value);
-            stat = tot.stat;
-            prim = tot.prim;
-            if (s.gate) bound = dd_value(dd_add(tot.sep, DD{offset, 0.0}));
-            else bound = (tot.flags & 2) ? -kInf : dd_value(dd_add(value, tot.bnd));
+            obj = tot.obj + offset;
+            stat = bdouble(tot.stat);
+            prim = bdouble(tot.prim);
+            if (s.gate) bound = tot.sep + offset;
+            else bound = (tot.flags & 2) ? -kInf : obj + tot.bnd;
             gap = isfinite(bound) ? fabs(obj - bound) / (1.0 + fabs(obj)) : kInf;
         }
         bool verified = isfinite(obj) && smax(prim, smax(stat, 0.0)) <= tol;
@@ -921,21 +1032,66 @@ __global__ void __launch_bounds__(kBlock) box_step_kernel(int n, const int32_t* 
 }  // namespace
 
 // ---- launch wrappers -----------------------------------------------------------------------------
-void launch_check(const View& v, int grid, cudaStream_t s) { check_kernel<<<grid, kBlock, 0, s>>>(v); }
+namespace {
+// One full wave (SMs x resident blocks per SM) per tile kernel, computed once per process.
+struct Waves {
+    int step[3] = {0, 0, 0};
+    int check = 0, polish = 0, matvec = 0;
+};
+Waves g_waves;
+
+template <class K>
+int wave_of(K kernel, int sms, int dyn_smem) {
+    if (dyn_smem > 0) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem);
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kBlock, dyn_smem);
+    return sms * (b < 1 ? 1 : b);
+}
+constexpr int kSmemF32 = smem_bytes<float>() > kTileNnz * 4 ? smem_bytes<float>() : kTileNnz * 4;
+constexpr int kSmem8 = smem_bytes<double>() > kTileNnz * 8 ? smem_bytes<double>() : kTileNnz * 8;
+inline int pick(int cap, int wave) { return cap < wave ? (cap < 1 ? 1 : cap) : wave; }
+}  // namespace
+
+int tile_grid(int sms) {
+    g_waves.step[PREC_FP64] = wave_of(step_kernel<PREC_FP64>, sms, kSmem8);
+    g_waves.step[PREC_MIXED] = wave_of(step_kernel<PREC_MIXED>, sms, kSmemF32);
+    g_waves.step[PREC_FP64_EXACT] = wave_of(step_kernel<PREC_FP64_EXACT>, sms, 0);
+    g_waves.check = wave_of(check_kernel, sms, kSmem8);
+    g_waves.matvec = wave_of(cg_matvec_kernel, sms, kSmem8);
+    wave_of(polish_residual_kernel, sms, kSmem8);
+    wave_of(check_standalone_kernel, sms, kSmem8);
+    g_waves.polish = wave_of(cg_update_kernel, sms, 0);
+    int m = 0;
+    for (int w : {g_waves.step[0], g_waves.step[1], g_waves.step[2], g_waves.check, g_waves.matvec, g_waves.polish})
+        m = w > m ? w : m;
+    return m;
+}
+
+void launch_check(const View& v, int grid, cudaStream_t s) { check_kernel<<<pick(grid, g_waves.check), kBlock, kSmem8, s>>>(v); }
 
 void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s) {
     switch (precision) {
-    case PREC_MIXED: step_kernel<PREC_MIXED><<<grid, kBlock, 0, s>>>(v, j); break;
-    case PREC_FP64_EXACT: step_kernel<PREC_FP64_EXACT><<<grid, kBlock, 0, s>>>(v, j); break;
-    default: step_kernel<PREC_FP64><<<grid, kBlock, 0, s>>>(v, j); break;
+    case PREC_MIXED: step_kernel<PREC_MIXED><<<pick(grid, g_waves.step[PREC_MIXED]), kBlock, kSmemF32, s>>>(v, j); break;
+    case PREC_FP64_EXACT:
+        step_kernel<PREC_FP64_EXACT><<<pick(grid, g_waves.step[PREC_FP64_EXACT]), kBlock, 0, s>>>(v, j);
+        break;
+    default: step_kernel<PREC_FP64><<<pick(grid, g_waves.step[PREC_FP64]), kBlock, kSmem8, s>>>(v, j); break;
     }
 }
 
-void launch_polish_init(const View& v, int grid, cudaStream_t s) { polish_init_kernel<<<grid, kBlock, 0, s>>>(v); }
-void launch_polish_residual(const View& v, int grid, cudaStream_t s) { polish_residual_kernel<<<grid, kBlock, 0, s>>>(v); }
-void launch_cg_matvec(const View& v, int grid, cudaStream_t s) { cg_matvec_kernel<<<grid, kBlock, 0, s>>>(v); }
-void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<grid, kBlock, 0, s>>>(v); }
-void launch_cg_direction(const View& v, int grid, cudaStream_t s) { cg_direction_kernel<<<grid, kBlock, 0, s>>>(v); }
+void launch_polish_init(const View& v, int grid, cudaStream_t s) {
+    polish_init_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v);
+}
+void launch_polish_residual(const View& v, int grid, cudaStream_t s) {
+    polish_residual_kernel<<<pick(grid, g_waves.matvec), kBlock, kSmem8, s>>>(v);
+}
+void launch_cg_matvec(const View& v, int grid, cudaStream_t s) {
+    cg_matvec_kernel<<<pick(grid, g_waves.matvec), kBlock, kSmem8, s>>>(v);
+}
+void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v); }
+void launch_cg_direction(const View& v, int grid, cudaStream_t s) {
+    cg_direction_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v);
+}
 
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish, int steps,
                  int polish_kernels, cudaStream_t s) {
@@ -984,7 +1140,7 @@ void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* co
     const int grid = check_grid(n);
     auto* scr = static_cast<StandaloneScratch*>(scratch);
     auto* partial = reinterpret_cast<Partial*>(static_cast<char*>(scratch) + 256);
-    check_standalone_kernel<<<grid, kBlock, 0, s>>>(src, static_cast<int>(n), tol, offset, partial, scr, result);
+    check_standalone_kernel<<<grid, kBlock, kSmem8, s>>>(src, static_cast<int>(n), tol, offset, partial, scr, result);
 }
 
 void launch_box_step(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,

@@ -4,6 +4,10 @@
 
 namespace bqp {
 
+// Computes each tile kernel's full wave (SMs x resident blocks per SM); returns the largest.
+// Call once before launching.  The `grid` argument of the launchers below is a cap: each
+// kernel launches min(cap, its own full wave) blocks.
+int tile_grid(int sms);
 // Tile kernels: grid-stride over the tile table (the grid size is fixed at capture).
 void launch_check(const View& v, int grid, cudaStream_t s);
 void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s);

@@ -73,6 +73,9 @@ typedef struct bqp_options {
     int32_t diagonal_gate;    /* -1 auto from the CSR; 0/1 force the reference's positive-diagonal
                                  dual-gap gate (src/qp_admm.cpp:72-78,106-116)                  */
     double  offset;           /* constant term of the objective (LinearProblem::offset)          */
+    int32_t kernel_variant;   /* SpMV structure of the FISTA step: -1 auto (tuning default), 0 block-
+                                 staged tile, 64 warp-staged rows, 1/2/4/8/16/32 lanes per row     */
+    int32_t reserved;         /* must be 0                                                       */
 } bqp_options;
 
 /* Result of one solve (the numeric fields of QpResult plus engine accounting). */

@@ -162,8 +162,10 @@ def test_iteration_and_time_limits(engine):
     inst = boxqp.planted('grid', seed=2, n=128 * 128)
     x, st = solve(engine, inst, 'fp64', 1e-12, iteration_limit=37)
     assert boxqp.STATUS_NAMES[st.status] == 'iteration_limit' and st.iterations == 37
-    x, st = solve(engine, inst, 'fp64', 1e-14, iteration_limit=10 ** 9, time_limit=0.05)
+    big = boxqp.planted('graph1m', seed=3, n=300000)
+    x, st = solve(engine, big, 'fp64', 1e-300, iteration_limit=10 ** 9, time_limit=0.05)
     assert boxqp.STATUS_NAMES[st.status] == 'time_limit'
+    assert 0.05 <= st.device_seconds < 5.0
     assert np.all(np.isfinite(x))
 
 
