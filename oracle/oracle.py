@@ -57,6 +57,18 @@ def build_reference(ref_dir='/root/reference/02-software/solver'):
     return proc.returncode == 0 and REF_LIB.exists()
 
 
+def build_level_a(ref_dir='/root/reference/02-software/solver'):
+    """Links the reference's own CLI and scale harness with the GB300 plugin (Level A); returns the
+    path of the scale harness, or None where the reference checkout is absent."""
+    if not Path(ref_dir).is_dir():
+        return None
+    proc = subprocess.run(['make', '-s', '-j8', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}', 'level_a'],
+                          cwd=str(HERE.parent), capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(proc.stdout + proc.stderr)
+    return HERE / '_ref' / 'solver_scale_gb300'
+
+
 _orc = None
 _ref = None
 

@@ -31,3 +31,28 @@ $(OUT)/libsovereign_ref.so: $(OBJS)
 	$(CXX) -shared -fopenmp -o $@ $(OBJS)
 
 .PHONY: all
+
+# Level-A drop-in check: the reference's library with SOVEREIGN_CUDA defined (so its CPU stub of
+# make_cuda_box drops out), the GB300 plugin hypergrey-sih-26_gb300/plugin/cuda_box_gb300.cpp in
+# place of src/cuda_box.cu, and the reference's own CLI and scale harness linked against
+# libboxqp.so.  Built from the reference's sources where they lie; outputs only into oracle/_ref.
+PKG := hypergrey-sih-26_gb300
+LIBDIR := $(abspath $(PKG)/boxqp)
+LVL_FLAGS := $(CXXFLAGS) -DSOVEREIGN_CUDA=1 -Iinclude
+LVL_OBJS := $(addprefix $(OUT)/lvl_,$(SRCS:.cpp=.o)) $(OUT)/lvl_plugin.o
+
+$(OUT)/lvl_%.o: $(REF)/src/%.cpp | $(OUT)
+	$(CXX) $(LVL_FLAGS) -c $< -o $@
+
+$(OUT)/lvl_plugin.o: $(PKG)/plugin/cuda_box_gb300.cpp | $(OUT)
+	$(CXX) $(LVL_FLAGS) -c $< -o $@
+
+$(OUT)/solver_scale_gb300: $(LVL_OBJS) $(REF)/src/scale_benchmark.cpp
+	$(CXX) $(LVL_FLAGS) $(REF)/src/scale_benchmark.cpp $(LVL_OBJS) -L$(LIBDIR) -lboxqp -Wl,-rpath,$(LIBDIR) -o $@
+
+$(OUT)/solver_cli_gb300: $(LVL_OBJS) $(REF)/src/main.cpp
+	$(CXX) $(LVL_FLAGS) $(REF)/src/main.cpp $(LVL_OBJS) -L$(LIBDIR) -lboxqp -Wl,-rpath,$(LIBDIR) -o $@
+
+level_a: $(OUT)/solver_scale_gb300 $(OUT)/solver_cli_gb300
+
+.PHONY: level_a

@@ -202,3 +202,15 @@ def test_splitmix64_reference_values():
     assert out == 0xE220A8397B1DCDAF
     out2, _ = boxqp.splitmix64(state)
     assert out2 == 0x6E789E6AA1B965F4
+
+
+def test_level_a_plugin_links_into_the_reference():
+    """The reference's own scale harness, linked with the GB300 plugin in place of its CUDA file,
+    reaches the plugin: without a GPU it reports the reference's message and exit code 2."""
+    import subprocess
+    exe = O.build_level_a()
+    if exe is None:
+        pytest.skip('reference checkout not present on this host')
+    out = subprocess.run([str(exe), '1000', 'cuda', '1', '30'], capture_output=True, text=True, timeout=120,
+                         env={'CUDA_VISIBLE_DEVICES': '', 'PATH': '/usr/bin:/bin'})
+    assert out.returncode == 2 and 'No CUDA device available' in out.stderr
