@@ -17,6 +17,7 @@
 // FP64 arithmetic is kept out of the FP32 iterations (GB300's FP64 rate is ~1/64 of FP32).
 #include "kernels.cuh"
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <type_traits>
@@ -1138,6 +1139,15 @@ void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* co
     src.diag = nullptr;  // a diagonal Hessian's only entry per row is its diagonal
     src.gate = gate;
     const int grid = check_grid(n);
+    // The kernel's dynamic shared memory plus its static reduction buffer exceed the default
+    // 48 KB: opt in once per device (the engine's set-up does the same for its kernels).
+    static std::atomic<bool> opted[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !opted[dev].load()) {
+        cudaFuncSetAttribute(check_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem8);
+        opted[dev].store(true);
+    }
     auto* scr = static_cast<StandaloneScratch*>(scratch);
     auto* partial = reinterpret_cast<Partial*>(static_cast<char*>(scratch) + 256);
     check_standalone_kernel<<<grid, kBlock, kSmem8, s>>>(src, static_cast<int>(n), tol, offset, partial, scr, result);
