@@ -13,6 +13,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,37 @@ bool ok(cudaError_t e, std::string& why) {
     if (e == cudaSuccess) return true;
     why = std::string("CUDA: ") + cudaGetErrorString(e);
     return false;
+}
+// ---- scratch of bqp_check_device_noalloc ------------------------------------------------------
+// The verification reduction needs global scratch for its per-block partials, its completion
+// counter and its 8 result values.  bqp_check_device_noalloc takes that scratch from this
+// file-scope device array instead of cudaMalloc: 96 KiB on every device that loads the library,
+// held until the process exits.  At most 1024 blocks of partials fit, which bounds n to
+// kNoAllocMaxRows.  In host code the name of the array is only a host-side stand-in, so the
+// device address is looked up once per device with cudaGetSymbolAddress.
+constexpr int64_t kNoAllocMaxRows = 4194304;
+constexpr size_t kNoAllocBytes = 96 * 1024;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_address[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (set up on the first call per device).
+cudaError_t noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_address[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_address[dev] = p;
+    }
+    *out = g_noalloc_address[dev];
+    return cudaSuccess;
 }
 }  // namespace
 
@@ -161,6 +193,59 @@ int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, c
     cudaFree(scratch);
     cudaStreamDestroy(s);
     if (e != cudaSuccess) return BQP_ERR_CUDA;
+    std::memset(stats, 0, sizeof(*stats));
+    stats->objective = host[0];
+    stats->primal_residual = host[1];
+    stats->stationarity_residual = host[2];
+    stats->complementarity_residual = host[3];
+    stats->dual_bound = host[4];
+    stats->relative_gap = host[5];
+    stats->verified = host[6] != 0 ? 1 : 0;
+    stats->status = stats->verified ? BQP_STATUS_OPTIMAL : BQP_STATUS_RUNNING;
+    return BQP_OK;
+}
+
+int bqp_check_device_noalloc(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
+                             const double* d_x, const double* d_c, const double* d_lower, const double* d_upper,
+                             double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats) {
+    if (n <= 0 || !d_rowptr || !d_x || !d_c || !d_lower || !d_upper || !stats || !(tolerance > 0) ||
+        !std::isfinite(offset)) {
+        g_box_error = "invalid argument";
+        return BQP_ERR_INVALID;
+    }
+    if (n > kNoAllocMaxRows) {
+        g_box_error = "bqp_check_device_noalloc: n = " + std::to_string(n) + " exceeds the limit of " +
+                      std::to_string(kNoAllocMaxRows) + " rows of its static scratch; use bqp_check_device";
+        return BQP_ERR_INVALID;
+    }
+    const size_t head = bqp::check_scratch_bytes(n);
+    const size_t bytes = head + 8 * sizeof(double);
+    if (bytes > kNoAllocBytes) {
+        g_box_error = "bqp_check_device_noalloc: scratch size exceeds the static array";
+        return BQP_ERR_INVALID;
+    }
+    void* scratch = nullptr;
+    cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) {
+        g_box_error = std::string("CUDA: ") + cudaGetErrorString(e);
+        return BQP_ERR_CUDA;
+    }
+    double* result = reinterpret_cast<double*>(static_cast<char*>(scratch) + head);
+    double host[8];
+    // The array keeps the previous call's contents: clear the completion counter, partials and
+    // result before the launch.  All calls use the legacy default stream.
+    e = cudaMemsetAsync(scratch, 0, bytes, 0);
+    if (e == cudaSuccess) {
+        bqp::launch_check_standalone(n, d_rowptr, d_col, d_val, d_x, d_c, d_lower, d_upper, tolerance, offset,
+                                     diagonal_gate > 0 ? 1 : 0, scratch, result, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, result, sizeof(host), cudaMemcpyDeviceToHost, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) {
+        g_box_error = std::string("CUDA: ") + cudaGetErrorString(e);
+        return BQP_ERR_CUDA;
+    }
     std::memset(stats, 0, sizeof(*stats));
     stats->objective = host[0];
     stats->primal_residual = host[1];

@@ -176,6 +176,22 @@ int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, c
                      const double* d_x, const double* d_c, const double* d_lower, const double* d_upper,
                      double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats);
 
+/* ---- verification without any device allocation -------------------------------------------
+ * No counterpart in the reference.  Same computation and arguments as bqp_check_device, for
+ * callers that cannot allocate device memory: a serving loop in which cudaMalloc/cudaFree would
+ * synchronize the device and stall the solves in flight, or a process whose device memory is
+ * already reserved by another allocator (a framework's caching pool), where cudaMalloc fails.
+ * It allocates nothing: its scratch is a 96 KiB static device array in libboxqp.so that every
+ * GPU loading the library holds until exit, which limits n to 4,194,304 rows (larger n returns
+ * BQP_ERR_INVALID with a message from bqp_box_last_error(NULL)).  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress) for the current device; make that
+ * first call before any stream capture.  All calls share the one array and run on the legacy
+ * default stream: calls that overlap on the GPU (from several host threads) race.            */
+int bqp_check_device_noalloc(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
+                             const double* d_x, const double* d_c, const double* d_lower,
+                             const double* d_upper, double tolerance, double offset,
+                             int32_t diagonal_gate, bqp_stats* stats);
+
 /* ---- host helpers ---------------------------------------------------------------------------
  * Full symmetric CSR from lower-triangle triplets, as CsrMatrix(n, rows) builds it after the
  * mirroring in src/accelerated_qp.cpp:20-24 (columns ascending, duplicates summed in input
