@@ -304,13 +304,205 @@ def run_ours(args, world, rank, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local, pg):
+    """4,096 planted box QPs of uneven size (n log-uniform [64, 16384], 2..6 edges/vertex) solved in
+    one running batch (mixed precision, each to its own KKT <= 1e-6), against a loop of single-instance
+    solves of the plain FP64 engine and against the CPU reference algorithm."""
+    import numpy as np
+    import boxqp
+    from boxqp import options_struct
+    count = args.instances
+    t0 = time.perf_counter()
+    insts = [boxqp.planted('batch', seed=3 + 1000 * rank, index=i) for i in range(count)]
+    gen_s = time.perf_counter() - t0
+    n_tot = sum(p['n'] for p in insts)
+    nnz_tot = sum(p['nnz'] for p in insts)
+    eng = boxqp.Engine(local)
+    opts = options_struct(args.tol, 60.0, 200000, 'mixed')
+    ids = [eng.submit(p['rowptr'], p['col'], p['val'], p['c'], p['lower'], p['upper'], opts) for p in insts]
+    for i in ids:
+        eng.wait(i)
+    for _ in range(args.warmup):
+        eng.resolve(ids)
+        for i in ids:
+            eng.wait(i)
+    barrier(pg)
+    eng.timer(reset=True)
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.resolve(ids)
+            for i in ids:
+                eng.wait(i)
+        wall = time.perf_counter() - t0
+    dev_ms, kernels, launches = eng.timer()
+    dev_s = allreduce_max(pg, dev_ms / 1e3)
+    solves = allreduce_sum(pg, args.steps * count)
+    value = solves / dev_s
+    statuses, iters, bytes_total, worst_kkt, worst_obj = {}, [], 0.0, 0.0, 0.0
+    for p, i in zip(insts, ids):
+        x, st = eng.fetch(i, p['n'])
+        name = boxqp.STATUS_NAMES[st.status]
+        statuses[name] = statuses.get(name, 0) + 1
+        iters.append(int(st.iterations))
+        bytes_total += st.bytes
+        worst_kkt = max(worst_kkt, st.stationarity_residual)
+        worst_obj = max(worst_obj, abs(st.objective - p['fstar']) / (1 + abs(p['fstar'])))
+    # plain FP64 engine, one instance at a time
+    o64 = options_struct(args.tol, 60.0, 200000, 'fp64')
+    sample = list(range(0, count, args.fp64_stride))
+    eng.timer(reset=True)
+    t0 = time.perf_counter()
+    for k in sample:
+        p = insts[k]
+        eng.solve(p['rowptr'], p['col'], p['val'], p['c'], p['lower'], p['upper'], o64)
+    fp64_wall = time.perf_counter() - t0
+    fp64_dev, _, _ = eng.timer()
+    fp64 = {'solves_per_s': len(sample) / (fp64_dev / 1e3), 'wall_solves_per_s': len(sample) / fp64_wall,
+            'sample': f'every {args.fp64_stride}th instance ({len(sample)} solves), one at a time through bqp_solve_sync'}
+    # e2e: submit every instance from host buffers, collect every primal
+    h2d = sum(p['rowptr'].nbytes + p['col'].nbytes + p['val'].nbytes + 3 * p['c'].nbytes for p in insts)
+    d2h = 8 * n_tot
+    for i in ids:
+        eng.release(i)
+    t0 = time.perf_counter()
+    ids2 = [eng.submit(p['rowptr'], p['col'], p['val'], p['c'], p['lower'], p['upper'], opts) for p in insts]
+    for p, i in zip(insts, ids2):
+        eng.wait(i)
+        eng.fetch(i, p['n'])
+    e2e_s = allreduce_max(pg, time.perf_counter() - t0)
+    for i in ids2:
+        eng.release(i)
+    e2e = {'value': allreduce_sum(pg, count) / e2e_s, 'unit': 'solves/s', 'h2d_bytes_per_step': int(h2d),
+           'd2h_bytes_per_step': int(d2h), 'api': 'bqp_submit x4096 + bqp_wait + bqp_fetch (pageable host buffers)'}
+    cpu = None
+    if rank == 0 and world == 1 and not args.quick:
+        from oracle import oracle as O
+        cs = list(range(0, count, args.cpu_stride))
+        t0 = time.perf_counter()
+        for k in cs:
+            p = boxqp.planted('batch', seed=3, index=k, lower_triplets=True)
+            O.solve_box(p['hrow'], p['hcol'], p['hval'], p['c'], p['lower'], p['upper'], tol=args.tol, threads=1)
+        cpu_s = time.perf_counter() - t0
+        cpu = {'value': len(cs) / cpu_s, 'unit': 'solves/s', 'cores': 1, 'kind': 'port',
+               'sample': f'every {args.cpu_stride}th instance ({len(cs)} FP64 reference-FISTA solves, 1 thread each, '
+                         'sequential); instances are too small for OpenMP rows'}
+    peak, kind = load_peaks()
+    achieved = bytes_total / (dev_s / args.steps) / 1e9
+    eng.close()
+    if rank != 0:
+        return
+    line = {'metric': METRIC, 'value': value, 'unit': 'solves/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 * dev_s / args.steps, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32+f64', 'data': 'synthetic',
+            'config': {'workload': f'uneven batch: {count} planted box QPs, n log-uniform [64,16384], 2..6 '
+                                   'edges/vertex, l=0, u~U[0.5,2], one running batch, mixed precision',
+                       'instances': count, 'sum_n': n_tot, 'sum_nnz': nnz_tot, 'tolerance': args.tol,
+                       'generation_s': gen_s,
+                       'l2': f'inputs larger than L2: {(8 * nnz_tot + 32 * n_tot) / 1e6:.0f} MB per batch iteration'},
+            'batch': {'statuses': statuses, 'iterations_mean': float(np.mean(iters)),
+                      'iterations_max': int(np.max(iters)), 'worst_kkt': worst_kkt, 'worst_objective_rel_err': worst_obj},
+            'hbm_gbs': achieved, 'wall_ms_per_step': 1e3 * wall / args.steps,
+            'fp64_single_instance_loop': fp64, 'speedup_vs_fp64_single_loop': value / fp64['solves_per_s'],
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                         'traffic': None, 'peak_kind': kind, 'scope': 'whole batch solve (algorithmic bytes / device time)'},
+            'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': int(kernels), 'graph_launches': int(launches),
+            'clocks': clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args, world, rank, local, pg):
+    """Poisson stream of box-QP requests (n log-uniform [1000, 200000], tolerance 1e-4 or 1e-8 by a
+    seeded coin) into the continuous-batching request loop under a 40 GB admission cap."""
+    import queue
+    import numpy as np
+    import boxqp
+    from boxqp.serve import BoxQPServer
+    rate, duration = args.rate, args.duration
+    st = 4 + 7919 * rank
+    arrivals, t, k = [], 0.0, 0
+    while True:
+        out, st = boxqp.splitmix64(st)
+        t += -np.log(1.0 - (out >> 11) * 2.0 ** -53) / rate
+        if t >= duration:
+            break
+        coin, st = boxqp.splitmix64(st)
+        arrivals.append((t, k, 1e-4 if coin & 1 else 1e-8))
+        k += 1
+    ready = queue.Queue(maxsize=512)
+
+    def produce(start):
+        for i in range(start, len(arrivals), 3):
+            t_i, idx, tol = arrivals[i]
+            ready.put((i, boxqp.planted('serve', seed=4 + rank, index=idx)))
+    producers = [threading.Thread(target=produce, args=(s,), daemon=True) for s in range(3)]
+    for p in producers:
+        p.start()
+    server = BoxQPServer(local, mem_cap_bytes=40 << 30, latency_ms=args.latency_ms)
+    made = {}
+    results = []
+    lag = []
+    barrier(pg)
+    t_start = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for i, (t_i, idx, tol) in enumerate(arrivals):
+            while i not in made:
+                j, inst = ready.get()
+                made[j] = inst
+            inst = made.pop(i)
+            now = time.perf_counter() - t_start
+            if now < t_i:
+                time.sleep(t_i - now)
+            lag.append(max(0.0, time.perf_counter() - t_start - t_i))
+            fut = server.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], tol)
+            results.append((inst['n'], inst['fstar'], tol, fut))
+        done = []
+        for n, fstar, tol, fut in results:
+            r = fut.result(timeout=300)
+            done.append((n, fstar, tol, r))
+        elapsed = time.perf_counter() - t_start
+    load = server.load()
+    server.close()
+    lat = np.array([r.latency for _, _, _, r in done]) * 1e3
+    ok = sum(1 for _, _, _, r in done if r.status == 'optimal')
+    worst = {}
+    for tol in (1e-4, 1e-8):
+        sel = [(n, f, r) for n, f, tt, r in done if tt == tol]
+        if sel:
+            worst[f'{tol:g}'] = {'requests': len(sel), 'worst_kkt': max(r.stationarity for _, _, r in sel),
+                                 'worst_objective_rel_err': max(abs(r.objective - f) / (1 + abs(f)) for _, f, r in sel)}
+    thr = allreduce_sum(pg, len(done)) / allreduce_max(pg, elapsed)
+    if rank != 0:
+        return
+    line = {'metric': METRIC, 'value': thr, 'unit': 'solves/s', 'n_gpus': world, 'steps': len(done), 'warmup': 0,
+            'ms_per_step': float(np.median(lat)), 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32+f64', 'data': 'synthetic',
+            'config': {'workload': f'serving stream: Poisson arrivals {rate:g}/s for {duration:g} s, n log-uniform '
+                                   '[1000, 200000], 5 edges/vertex, tolerance 1e-4 or 1e-8, 40 GB admission cap',
+                       'latency_target_ms': args.latency_ms, 'requests': len(arrivals)},
+            'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99)),
+                           'p99.9': float(np.percentile(lat, 99.9)), 'max': float(lat.max()), 'mean': float(lat.mean())},
+            'arrival_lag_ms_p99': float(np.percentile(np.array(lag) * 1e3, 99)),
+            'optimal': ok, 'peak_resident': load['peak_resident'], 'errors_vs_fp64_checks': worst,
+            'e2e': {'value': thr, 'unit': 'solves/s', 'h2d_bytes_per_step': None, 'd2h_bytes_per_step': None,
+                    'api': 'BoxQPServer.submit (bqp_submit) from host buffers, latency from submission to result'},
+            'clocks': clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
-    ap.add_argument('--workload', default='graph1m', choices=['graph1m', 'grid', 'graph10k'])
+    ap.add_argument('--workload', default='graph1m', choices=['graph1m', 'grid', 'graph10k', 'batch', 'serve'])
+    ap.add_argument('--instances', type=int, default=4096, help='batch: number of instances')
+    ap.add_argument('--fp64-stride', type=int, default=1, help='batch: FP64 single-solve loop over every k-th')
+    ap.add_argument('--cpu-stride', type=int, default=32, help='batch: CPU baseline over every k-th instance')
+    ap.add_argument('--rate', type=float, default=200.0, help='serve: arrivals per second')
+    ap.add_argument('--duration', type=float, default=60.0, help='serve: seconds of arrivals')
+    ap.add_argument('--latency-ms', type=float, default=2.0, help='serve: device launch length target')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--tol', type=float, default=1e-6)
     ap.add_argument('--quick', action='store_true', help='skip e2e, FP64 and CPU legs')
@@ -318,6 +510,10 @@ def main():
     world, rank, local, pg = dist_setup(args)
     if args.impl == 'reference':
         run_reference(args, world, rank, pg)
+    elif args.workload == 'batch':
+        run_batch(args, world, rank, local, pg)
+    elif args.workload == 'serve':
+        run_serve(args, world, rank, local, pg)
     else:
         run_ours(args, world, rank, local, pg)
     if pg:

@@ -21,7 +21,7 @@ class Options(ctypes.Structure):
     _fields_ = [('tolerance', c_double), ('time_limit', c_double), ('iteration_limit', c_int64),
                 ('precision', c_int32), ('lipschitz', c_int32), ('check_interval', c_int32),
                 ('diagonal_gate', c_int32), ('offset', c_double), ('kernel_variant', c_int32),
-                ('reserved', c_int32)]
+                ('reserved', c_int32), ('polish_switch', c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -63,6 +63,7 @@ PROTOTYPES = {
                            POINTER(Options), _U64P]),
     'bqp_poll': (c_int, [c_void_p, c_uint64, _I32P]),
     'bqp_wait': (c_int, [c_void_p, c_uint64, c_double]),
+    'bqp_wait_any': (c_int, [c_void_p, c_double, _U64P]),
     'bqp_fetch': (c_int, [c_void_p, c_uint64, _F64P, POINTER(Stats)]),
     'bqp_release': (c_int, [c_void_p, c_uint64]),
     'bqp_resolve': (c_int, [c_void_p, _U64P, c_int64]),

@@ -94,7 +94,7 @@ def _i64(a):
 
 
 def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, precision='fp64',
-                   check_interval=25, diagonal_gate=-1, offset=0.0, kernel_variant=-1):
+                   check_interval=25, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None):
     o = Options()
     lib().bqp_options_default(o)
     o.tolerance = float(tolerance)
@@ -105,6 +105,8 @@ def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, prec
     o.diagonal_gate = int(diagonal_gate)
     o.offset = float(offset)
     o.kernel_variant = int(kernel_variant)
+    if polish_switch is not None:
+        o.polish_switch = float(polish_switch)
     return o
 
 
@@ -201,6 +203,15 @@ class Engine:
             return False
         self._check(rc)
         return True
+
+    def wait_any(self, timeout=-1.0):
+        """Id of the next finished asynchronous solve, or None on timeout."""
+        ident = N.c_uint64(0)
+        rc = lib().bqp_wait_any(self._ctx, float(timeout), N.ctypes.byref(ident))
+        if rc == 6:
+            return None
+        self._check(rc)
+        return ident.value
 
     def fetch(self, ident, n):
         x = np.empty(n, dtype=np.float64)

@@ -128,6 +128,7 @@ struct Job {
     std::vector<Tile> tiles;  // local tiles (inst field filled at admission)
     int state = JOB_QUEUED;
     bool resolve = false;     // re-run of a resident solve
+    bool notify = false;      // report completion through the completion queue (bqp_wait_any)
     bool resident = false;
     int slot = -1;
     void* slab = nullptr;
@@ -212,6 +213,7 @@ public:
     int fetch(uint64_t id, double* x, bqp_stats* stats);
     int release(uint64_t id);
     int resolve(const uint64_t* ids, int64_t count);
+    int wait_any(double timeout, uint64_t* id);
     int load(int64_t* queued, int64_t* running, int64_t* peak, int64_t* resident_bytes);
     int timer(int reset, double* ms, int64_t* kernels, int64_t* launches) {
         std::lock_guard<std::mutex> g(mu_);
@@ -307,6 +309,7 @@ private:
     std::condition_variable cv_work_, cv_done_;
     std::map<uint64_t, std::unique_ptr<Job>> jobs_;
     std::deque<Job*> queue_;
+    std::deque<uint64_t> completed_;  // finished notify-jobs, in completion order
     std::vector<std::pair<int, void*>> pending_free_;
     uint64_t next_id_ = 1;
     int64_t n_running_ = 0, peak_resident_ = 0;
@@ -490,7 +493,7 @@ bool Engine::run_stream(int cap, std::string& why) {
         if (profile_phases_) cudaEventRecord(pev_[0], stream_);
         launch_check(v, grid, stream_);
         launch_gate_plain(v, stream_);
-        kernels += 2;
+        kernels += 3;
         cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
         if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine check")) return false;
         if (profile_phases_) cudaEventRecord(pev_[1], stream_);
@@ -630,10 +633,25 @@ int Engine::submit(Job* raw, uint64_t* id) {
     if (id) *id = j->id;
     const bool done = j->state == JOB_DONE;
     jobs_[j->id] = std::move(job);
+    if (done && j->notify) {
+        completed_.push_back(j->id);
+        cv_done_.notify_all();
+    }
     if (!done) {
         queue_.push_back(j);
         cv_work_.notify_all();
     }
+    return BQP_OK;
+}
+
+int Engine::wait_any(double timeout, uint64_t* id) {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto pred = [&] { return !completed_.empty() || stop_; };
+    if (timeout < 0) cv_done_.wait(lk, pred);
+    else if (!cv_done_.wait_for(lk, std::chrono::duration<double>(timeout), pred)) return BQP_ERR_NOT_READY;
+    if (completed_.empty()) return BQP_ERR_NOT_READY;
+    *id = completed_.front();
+    completed_.pop_front();
     return BQP_OK;
 }
 
@@ -685,6 +703,7 @@ int Engine::release(uint64_t id) {
     } else if (j.state != JOB_DONE) {
         return BQP_ERR_NOT_READY;
     }
+    completed_.erase(std::remove(completed_.begin(), completed_.end(), id), completed_.end());
     if (j.resident) {
         pending_free_.emplace_back(j.slot, j.slab);
         resident_bytes_ -= j.layout.total;
@@ -706,6 +725,7 @@ int Engine::resolve(const uint64_t* ids, int64_t count) {
         Job& j = *jobs_[ids[k]];
         j.state = JOB_QUEUED;
         j.resolve = true;
+        j.notify = true;
         j.error = BQP_OK;
         j.t_submit = host_seconds();
         queue_.push_back(&j);
@@ -791,6 +811,7 @@ bool Engine::admit(Job& j, std::string& why) {
         R.polish = prec == PREC_MIXED ? 1 : 0;
         R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
         R.cg_tol = 0.1 * j.opt.tolerance;
+        R.polish_switch = j.opt.polish_switch;
         // tiles
         for (Tile& t : j.tiles) t.inst = slot;
         const int begin = static_cast<int>(h_tiles_.size());
@@ -994,6 +1015,7 @@ void Engine::collect(std::unique_lock<std::mutex>& lk) {
         j->state = JOB_DONE;
         j->resolve = false;
         n_running_--;
+        if (j->notify) completed_.push_back(j->id);
     }
     cv_done_.notify_all();
 }
@@ -1056,6 +1078,7 @@ void Engine::loop() {
                     j->error = BQP_ERR_ADMISSION;
                     j->error_text = "solve does not fit under the device-memory cap";
                     j->state = JOB_DONE;
+                    if (j->notify) completed_.push_back(j->id);
                     cv_done_.notify_all();
                     continue;
                 }
@@ -1081,6 +1104,7 @@ void Engine::loop() {
                 j->error = BQP_ERR_CUDA;
                 j->error_text = why;
                 j->state = JOB_DONE;
+                if (j->notify) completed_.push_back(j->id);
                 set_error(why);
                 cv_done_.notify_all();
             }
@@ -1102,6 +1126,7 @@ void Engine::loop() {
                     j->error = BQP_ERR_CUDA;
                     j->error_text = why;
                     n_running_--;
+                    if (j->notify) completed_.push_back(j->id);
                 }
             }
             cv_done_.notify_all();
@@ -1135,7 +1160,7 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
     if (!o || !(o->tolerance > 0) || !std::isfinite(o->tolerance) || o->time_limit < 0 || !std::isfinite(o->time_limit) ||
         o->iteration_limit < 0 || o->check_interval < 1 || o->check_interval > bqp::kMaxInterval ||
         (o->precision != BQP_PRECISION_FP64 && o->precision != BQP_PRECISION_MIXED && o->precision != BQP_PRECISION_FP64_EXACT) ||
-        !std::isfinite(o->offset) ||
+        !std::isfinite(o->offset) || !(o->polish_switch >= 0) || !std::isfinite(o->polish_switch) ||
         (o->kernel_variant >= 0 && o->kernel_variant != 0 && o->kernel_variant != 64 && o->kernel_variant != 1 &&
          o->kernel_variant != 2 && o->kernel_variant != 4 && o->kernel_variant != 8 && o->kernel_variant != 16 &&
          o->kernel_variant != 32)) {
@@ -1250,6 +1275,7 @@ void bqp_options_default(bqp_options* o) {
     o->offset = 0;
     o->kernel_variant = -1;
     o->reserved = 0;
+    o->polish_switch = 3e-2;
 }
 
 bqp_ctx* bqp_create(int device, size_t mem_cap_bytes) {
@@ -1310,7 +1336,13 @@ int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, cons
     std::string why;
     int rc = make_job(n, nnz, rowptr, col, val, c, lower, upper, options, true, &j, why);
     if (rc != BQP_OK) return fail(ctx, rc, why);
+    j->notify = true;
     return ctx->engine->submit(j, id);
+}
+
+int bqp_wait_any(bqp_ctx* ctx, double timeout_seconds, uint64_t* id) {
+    if (!ctx || !id) return BQP_ERR_INVALID;
+    return ctx->engine->wait_any(timeout_seconds, id);
 }
 
 int bqp_poll(bqp_ctx* ctx, uint64_t id, int32_t* status) {

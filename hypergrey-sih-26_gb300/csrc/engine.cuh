@@ -135,6 +135,7 @@ struct __align__(16) InstDev {
     double beta_cg;
     double cg_res;
     double cg_tol;
+    double polish_switch;  // stationarity that triggers the first polish attempt
     int64_t cg_it;
     int64_t cg_total;
     int64_t cg_max;

@@ -59,8 +59,9 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 
 struct Acc {
     double obj, bnd, sep, a;
-    unsigned long long stat, prim, b, hash;
-    long long nact;
+    unsigned long long stat, prim, b;
+    unsigned hash;
+    int nact;
     int flags;
 };
 __device__ __forceinline__ Acc acc_identity() {
@@ -123,8 +124,8 @@ __device__ __forceinline__ Acc load_partial(const Partial* p) {
     r.stat = __ldcg(reinterpret_cast<const unsigned long long*>(&p->stat));
     r.prim = __ldcg(reinterpret_cast<const unsigned long long*>(&p->prim));
     r.b = __ldcg(reinterpret_cast<const unsigned long long*>(&p->b));
-    r.hash = __ldcg(reinterpret_cast<const unsigned long long*>(&p->hash));
-    r.nact = __ldcg(reinterpret_cast<const long long*>(&p->n_active));
+    r.hash = static_cast<unsigned>(__ldcg(reinterpret_cast<const unsigned long long*>(&p->hash)));
+    r.nact = static_cast<int>(__ldcg(reinterpret_cast<const long long*>(&p->n_active)));
     r.flags = __ldcg(&p->flags);
     return r;
 }
@@ -154,11 +155,11 @@ __device__ Acc reduce_instance(const View& v, int tb, int te) {
 }
 
 // ---- one row of check_qp_solution ------------------------------------------------------------
-__device__ __forceinline__ uint64_t mix_index(uint64_t k) {
-    k = (k + 1) * 0x9E3779B97F4A7C15ULL;
-    k ^= k >> 31;
-    k *= 0xBF58476D1CE4E5B9ULL;
-    return k ^ (k >> 29);
+__device__ __forceinline__ unsigned mix_index(unsigned k) {
+    k = (k + 1u) * 0x9E3779B9u;
+    k ^= k >> 16;
+    k *= 0x85EBCA6Bu;
+    return k ^ (k >> 13);
 }
 
 __device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double ci, double li, double ui, double di,
@@ -186,10 +187,10 @@ __device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double c
         a.sep += 0.5 * di * m * m + ci * m;
     }
     if (at_lower) {
-        a.hash ^= mix_index(2ull * static_cast<uint64_t>(row));
+        a.hash ^= mix_index(2u * static_cast<unsigned>(row));
         a.nact++;
     } else if (at_upper) {
-        a.hash ^= mix_index(2ull * static_cast<uint64_t>(row) + 1);
+        a.hash ^= mix_index(2u * static_cast<unsigned>(row) + 1u);
         a.nact++;
     }
 }
@@ -305,8 +306,11 @@ __device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
             [](double x, double y) { return x + y; }, 0.0,
             [&](int r, double gq) {
                 const double xi = s.x64[r];
-                const int ks = __ldg(s.rowptr + r);
-                const double di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? __ldg(s.val64 + ks) : 0.0);
+                double di = 1.0;
+                if (s.gate) {
+                    const int ks = __ldg(s.rowptr + r);
+                    di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? __ldg(s.val64 + ks) : 0.0);
+                }
                 check_row(a, xi, gq, s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
             });
     } else if constexpr (MODE == 1) {
@@ -317,10 +321,13 @@ __device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
             [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
             [&](int r, float2 acc) {
                 const float xf = s.x32[r];
-                const int ks = __ldg(s.rowptr + r);
-                const double d0 = __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0;
-                check_row(a, static_cast<double>(xf), df_value(acc), s.c[r], s.l[r], s.u[r], gate_diag(s, r, d0), s.gate,
-                          r, xf <= s.l32[r], xf >= s.u32[r]);
+                double di = 1.0;
+                if (s.gate) {
+                    const int ks = __ldg(s.rowptr + r);
+                    di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0);
+                }
+                check_row(a, static_cast<double>(xf), df_value(acc), s.c[r], s.l[r], s.u[r], di, s.gate, r,
+                          xf <= s.l32[r], xf >= s.u32[r]);
             });
     } else {
         float2* buf = warp_buffer<float2>();
@@ -330,10 +337,12 @@ __device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
             [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
             [&](int r, float2 acc) {
                 const double xi = s.xp[r];
-                const int ks = __ldg(s.rowptr + r);
-                const double d0 = __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0;
-                check_row(a, xi, df_value(acc), s.c[r], s.l[r], s.u[r], gate_diag(s, r, d0), s.gate, r, xi <= s.l[r],
-                          xi >= s.u[r]);
+                double di = 1.0;
+                if (s.gate) {
+                    const int ks = __ldg(s.rowptr + r);
+                    di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0);
+                }
+                check_row(a, xi, df_value(acc), s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
             });
     }
 }
@@ -407,7 +416,7 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
         I.stable_checks = stable ? I.stable_checks + 1 : 0;
         I.active_hash = tot.hash;
         I.n_active = tot.nact;
-        double sw = 1e-3;
+        double sw = I.polish_switch;
         for (int k = 0; k < I.polish_rounds; ++k) sw *= 0.1;
         if (I.stable_checks >= 1 && stat <= sw) {
             I.phase = PH_POLISH_INIT;
@@ -621,17 +630,24 @@ __global__ void __launch_bounds__(kBlock) step_kernel(View v, int j) {
 }
 
 // ---- check kernel -----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) check_kernel(View v) {
+// One kernel per precision family (FAMILY_MIXED: FP32 iterate or polished point; FAMILY_FP64:
+// fp64 and fp64_exact), so each carries only its own check path and its own register budget.
+constexpr int FAMILY_FP64 = 0;
+constexpr int FAMILY_MIXED = 1;
+
+template <int FAMILY>
+__global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (I.status != ST_RUNNING) continue;
+        if ((I.precision == PREC_MIXED) != (FAMILY == FAMILY_MIXED)) continue;
         const int ph = I.phase;
         if (ph != PH_FISTA && ph != PH_POLISH_FINISH) continue;
         const CheckSrc s = source_of(I);
         Acc a = acc_identity();
-        if (I.precision == PREC_MIXED) {
+        if constexpr (FAMILY == FAMILY_MIXED) {
             if (ph == PH_POLISH_FINISH) check_rows<2>(s, T.row_begin, T.row_end, a);
             else check_rows<1>(s, T.row_begin, T.row_end, a);
         } else {
@@ -865,7 +881,7 @@ __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraph
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
-        long long launched = 2;  // check + gate
+        long long launched = 3;  // two check kernels + gate
         for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps : 0;
         launched += c.polish > 0 ? polish_kernels : 0;
         v.ctrl->kernels += launched;
@@ -1037,7 +1053,7 @@ namespace {
 // One full wave (SMs x resident blocks per SM) per tile kernel, computed once per process.
 struct Waves {
     int step[3] = {0, 0, 0};
-    int check = 0, polish = 0, matvec = 0;
+    int check = 0, check_mixed = 0, polish = 0, matvec = 0;
 };
 Waves g_waves;
 
@@ -1057,7 +1073,8 @@ int tile_grid(int sms) {
     g_waves.step[PREC_FP64] = wave_of(step_kernel<PREC_FP64>, sms, kSmem8);
     g_waves.step[PREC_MIXED] = wave_of(step_kernel<PREC_MIXED>, sms, kSmemF32);
     g_waves.step[PREC_FP64_EXACT] = wave_of(step_kernel<PREC_FP64_EXACT>, sms, 0);
-    g_waves.check = wave_of(check_kernel, sms, kSmem8);
+    g_waves.check = wave_of(check_kernel<FAMILY_FP64>, sms, kSmem8);
+    g_waves.check_mixed = wave_of(check_kernel<FAMILY_MIXED>, sms, kSmem8);
     g_waves.matvec = wave_of(cg_matvec_kernel, sms, kSmem8);
     wave_of(polish_residual_kernel, sms, kSmem8);
     wave_of(check_standalone_kernel, sms, kSmem8);
@@ -1068,7 +1085,10 @@ int tile_grid(int sms) {
     return m;
 }
 
-void launch_check(const View& v, int grid, cudaStream_t s) { check_kernel<<<pick(grid, g_waves.check), kBlock, kSmem8, s>>>(v); }
+void launch_check(const View& v, int grid, cudaStream_t s) {
+    check_kernel<FAMILY_MIXED><<<pick(grid, g_waves.check_mixed), kBlock, kSmem8, s>>>(v);
+    check_kernel<FAMILY_FP64><<<pick(grid, g_waves.check), kBlock, kSmem8, s>>>(v);
+}
 
 void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s) {
     switch (precision) {

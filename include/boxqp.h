@@ -76,6 +76,9 @@ typedef struct bqp_options {
     int32_t kernel_variant;   /* SpMV structure of the FISTA step: -1 auto (tuning default), 0 block-
                                  staged tile, 64 warp-staged rows, 1/2/4/8/16/32 lanes per row     */
     int32_t reserved;         /* must be 0                                                       */
+    double  polish_switch;    /* mixed: stationarity at or below which, with the active set
+                                 unchanged since the previous check, the FP64 free-set polish is
+                                 attempted (default 3e-2; x0.1 after each failed attempt)        */
 } bqp_options;
 
 /* Result of one solve (the numeric fields of QpResult plus engine accounting). */
@@ -123,6 +126,10 @@ int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, cons
 int bqp_poll(bqp_ctx* ctx, uint64_t id, int32_t* status);
 /* Blocks until the solve is finished (timeout_seconds < 0: no timeout).                      */
 int bqp_wait(bqp_ctx* ctx, uint64_t id, double timeout_seconds);
+/* Blocks until some solve submitted with bqp_submit (or re-armed with bqp_resolve) finishes and
+ * returns its id; each finished solve is reported once, in completion order.  BQP_ERR_NOT_READY
+ * on timeout (timeout_seconds < 0: no timeout).                                              */
+int bqp_wait_any(bqp_ctx* ctx, double timeout_seconds, uint64_t* id);
 /* Copies the primal (n doubles, caller-owned) and the statistics of a finished solve.        */
 int bqp_fetch(bqp_ctx* ctx, uint64_t id, double* x, bqp_stats* stats);
 /* Frees the solve's device memory; the id becomes unknown.                                   */
