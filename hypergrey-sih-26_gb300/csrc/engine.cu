@@ -493,7 +493,7 @@ bool Engine::run_stream(int cap, std::string& why) {
         if (profile_phases_) cudaEventRecord(pev_[0], stream_);
         launch_check(v, grid, stream_);
         launch_gate_plain(v, stream_);
-        kernels += 3;
+        kernels += 4;
         cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
         if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine check")) return false;
         if (profile_phases_) cudaEventRecord(pev_[1], stream_);

@@ -41,6 +41,16 @@ __device__ __forceinline__ float sminf(float a, float b) { return (b < a) ? b : 
 
 template <class T>
 __device__ __forceinline__ T shfl_xor(T v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+template <class T>
+__device__ __forceinline__ T shfl_idx(T v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+template <>
+__device__ __forceinline__ float2 shfl_xor<float2>(float2 v, int o) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+}
+template <>
+__device__ __forceinline__ float2 shfl_idx<float2>(float2 v, int src) {
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
 
 template <int LANES, class T>
 __device__ __forceinline__ T group_sum(T v) {
@@ -242,6 +252,55 @@ __device__ __forceinline__ void warp_groups(const int32_t* __restrict__ rowptr, 
     }
 }
 
+// Sub-warp products, full-warp epilogue: a warp takes 32 consecutive rows; in each of LANES passes
+// its 32 / LANES sub-groups of LANES lanes form one row sum each (the memory pattern of the tuned
+// sub-warp step kernel), and shuffles hand every row sum to its own lane, so the epilogue of the
+// 32 rows runs with all 32 lanes active.  Fixed summation order (lane-strided partials, xor tree).
+template <int LANES, class T, class Prod, class Add, class Epi>
+__device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr, int rb, int re, Prod prod, Add add,
+                                             T zero, Epi epi) {
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    for (int base = rb + warp * 32; base < re; base += kBlock) {
+        T mine = zero;
+#pragma unroll
+        for (int pass = 0; pass < LANES; ++pass) {
+            const int r = base + pass * R + sub;
+            T acc = zero;
+            if (r < re) {
+                const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+#pragma unroll 4
+                for (int k = ks + sl; k < ke; k += LANES) acc = add(acc, prod(k));
+            }
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1) acc = add(acc, shfl_xor(acc, o));
+            const int g = lane - pass * R;
+            const bool mine_now = g >= 0 && g < R;
+            const T got = shfl_idx(acc, (mine_now ? g : 0) * LANES);
+            if (mine_now) mine = got;
+        }
+        const int r = base + lane;
+        if (r < re) epi(r, mine);
+    }
+}
+
+// Runs rows [rb, re) with the tile's SpMV structure: sub-warp rows for 1..32 lanes, warp-staged
+// rows (shared-memory buffer) for the block- and warp-staged variants.
+template <class T, class Prod, class Add, class Epi>
+__device__ __forceinline__ void tile_rows(int variant, const int32_t* __restrict__ rowptr, int rb, int re, Prod prod,
+                                          Add add, T zero, Epi epi) {
+    switch (variant) {
+    case 1: subwarp_rows<1, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    case 2: subwarp_rows<2, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    case 4: subwarp_rows<4, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    case 8: subwarp_rows<8, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    case 16: subwarp_rows<16, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    case 32: subwarp_rows<32, T>(rowptr, rb, re, prod, add, zero, epi); break;
+    default: warp_groups<T>(rowptr, rb, re, warp_buffer<T>(), prod, add, zero, epi); break;
+    }
+}
+
 // FP32 "double-float" arithmetic: an unevaluated pair (hi, lo) carries ~46 significant bits.
 // The products of the mixed engine's checks and polish run on the FP32 pipes with it, since
 // GB300's FP64 rate is 1/64 of its FP32 rate; FP64 is used once per row.
@@ -267,6 +326,37 @@ __device__ __forceinline__ double df_value(float2 a) { return static_cast<double
 __device__ __forceinline__ float2 df_split(double x) {
     const float h = __double2float_rn(x);
     return make_float2(h, __double2float_rn(x - static_cast<double>(h)));
+}
+
+// check_row for the FP32 iterate of the mixed engine: the iterate lies in [l32, u32], a subset of
+// [l, u], by construction, so its scaled bound violation is 0; the stationarity ratio is divided
+// in FP32 (7 significant digits of the reported residual); sums stay FP64.
+__device__ __forceinline__ void check_row_f32(Acc& a, float xf, double gq, double ci, double li, double ui, int row,
+                                              bool at_lower, bool at_upper) {
+    if (!isfinite(xf)) {
+        a.flags |= 1;
+        return;
+    }
+    const double xi = static_cast<double>(xf);
+    a.obj = fma(0.5 * xi, gq, a.obj);
+    a.obj = fma(ci, xi, a.obj);
+    const double g = gq + ci;
+    const double num = fabs(xi - smax(li, smin(ui, xi - g)));
+    double res = static_cast<double>(__fdiv_rn(static_cast<float>(num), 1.0f + fabsf(xf)));
+    if (!isfinite(g) || !isfinite(num)) res = kInf;
+    a.stat = umax64(a.stat, dbits(res));
+    if (g != 0) {
+        double target = g > 0 ? li : ui;
+        if (isfinite(target)) a.bnd += g * (target - xi);
+        else a.flags |= 2;
+    }
+    if (at_lower) {
+        a.hash ^= mix_index(2u * static_cast<unsigned>(row));
+        a.nact++;
+    } else if (at_upper) {
+        a.hash ^= mix_index(2u * static_cast<unsigned>(row) + 1u);
+        a.nact++;
+    }
 }
 
 // Sources of one check: MODE 0 FP64 values + x64; 1 hi/lo values + x32; 2 hi/lo values + xp.
@@ -297,12 +387,11 @@ __device__ __forceinline__ double gate_diag(const CheckSrc& s, int r, double fal
 
 // Check of rows [rb, re): accumulates check_row terms into a.
 template <int MODE>
-__device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
+__device__ void check_rows(const CheckSrc& s, int variant, int rb, int re, Acc& a) {
     const int32_t* __restrict__ col = s.col;
     if constexpr (MODE == 0) {
-        double* buf = warp_buffer<double>();
-        warp_groups<double>(
-            s.rowptr, rb, re, buf, [&](int k) { return __ldg(s.val64 + k) * s.x64[__ldg(col + k)]; },
+        tile_rows<double>(
+            variant, s.rowptr, rb, re, [&](int k) { return __ldg(s.val64 + k) * s.x64[__ldg(col + k)]; },
             [](double x, double y) { return x + y; }, 0.0,
             [&](int r, double gq) {
                 const double xi = s.x64[r];
@@ -314,25 +403,24 @@ __device__ void check_rows(const CheckSrc& s, int rb, int re, Acc& a) {
                 check_row(a, xi, gq, s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
             });
     } else if constexpr (MODE == 1) {
-        float2* buf = warp_buffer<float2>();
-        warp_groups<float2>(
-            s.rowptr, rb, re, buf,
+        tile_rows<float2>(
+            variant, s.rowptr, rb, re,
             [&](int k) { return df_prod(__ldg(s.vhi + k), __ldg(s.vlo + k), s.x32[__ldg(col + k)]); },
             [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
             [&](int r, float2 acc) {
                 const float xf = s.x32[r];
-                double di = 1.0;
                 if (s.gate) {
                     const int ks = __ldg(s.rowptr + r);
-                    di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0);
+                    const double d0 = __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0;
+                    check_row(a, static_cast<double>(xf), df_value(acc), s.c[r], s.l[r], s.u[r], gate_diag(s, r, d0),
+                              1, r, xf <= s.l32[r], xf >= s.u32[r]);
+                } else {
+                    check_row_f32(a, xf, df_value(acc), s.c[r], s.l[r], s.u[r], r, xf <= s.l32[r], xf >= s.u32[r]);
                 }
-                check_row(a, static_cast<double>(xf), df_value(acc), s.c[r], s.l[r], s.u[r], di, s.gate, r,
-                          xf <= s.l32[r], xf >= s.u32[r]);
             });
     } else {
-        float2* buf = warp_buffer<float2>();
-        warp_groups<float2>(
-            s.rowptr, rb, re, buf,
+        tile_rows<float2>(
+            variant, s.rowptr, rb, re,
             [&](int k) { return df_prod2(__ldg(s.vhi + k), __ldg(s.vlo + k), s.xp2[__ldg(col + k)]); },
             [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
             [&](int r, float2 acc) {
@@ -633,7 +721,8 @@ __global__ void __launch_bounds__(kBlock) step_kernel(View v, int j) {
 // One kernel per precision family (FAMILY_MIXED: FP32 iterate or polished point; FAMILY_FP64:
 // fp64 and fp64_exact), so each carries only its own check path and its own register budget.
 constexpr int FAMILY_FP64 = 0;
-constexpr int FAMILY_MIXED = 1;
+constexpr int FAMILY_MIXED = 1;    // FP32 iterate of the mixed engine (FISTA phase)
+constexpr int FAMILY_VERIFY = 2;   // polished point of the mixed engine (once per polish)
 
 template <int FAMILY>
 __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
@@ -642,17 +731,14 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (I.status != ST_RUNNING) continue;
-        if ((I.precision == PREC_MIXED) != (FAMILY == FAMILY_MIXED)) continue;
+        if ((I.precision == PREC_MIXED) != (FAMILY != FAMILY_FP64)) continue;
         const int ph = I.phase;
-        if (ph != PH_FISTA && ph != PH_POLISH_FINISH) continue;
+        if (FAMILY == FAMILY_VERIFY ? ph != PH_POLISH_FINISH : ph != PH_FISTA) continue;
         const CheckSrc s = source_of(I);
         Acc a = acc_identity();
-        if constexpr (FAMILY == FAMILY_MIXED) {
-            if (ph == PH_POLISH_FINISH) check_rows<2>(s, T.row_begin, T.row_end, a);
-            else check_rows<1>(s, T.row_begin, T.row_end, a);
-        } else {
-            check_rows<0>(s, T.row_begin, T.row_end, a);
-        }
+        if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a);
+        else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, T.variant, T.row_begin, T.row_end, a);
+        else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a);
         Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
@@ -695,43 +781,55 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
 // q = Q src on the free rows (0 on fixed rows), src given as FP32 pairs.  residual = true:
 // r = -(Q xp + c), z = D^-1 r, p = z on free rows, accumulating r.z and max |r|/(1+|x|).
 template <bool RESIDUAL>
-__device__ void polish_matvec_rows(const InstDev& I, int rb, int re, const float2* __restrict__ src, Acc& a) {
+__device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re, const float2* __restrict__ src, Acc& a) {
+    // Local copies: the epilogue stores through other pointers of the same record, which would
+    // otherwise force the matrix pointers to be reloaded for every product.
     const int32_t* __restrict__ col = I.col;
-    float2* buf = warp_buffer<float2>();
-    warp_groups<float2>(
-        I.rowptr, rb, re, buf, [&](int k) { return df_prod2(__ldg(I.vhi + k), __ldg(I.vlo + k), src[__ldg(col + k)]); },
+    const float* __restrict__ vhi = I.vhi;
+    const float* __restrict__ vlo = I.vlo;
+    const uint8_t* __restrict__ fixed = I.fixed;
+    const double* __restrict__ c = I.c;
+    const double* __restrict__ dinv = I.dinv;
+    const double* __restrict__ xp = I.xp;
+    double* __restrict__ r_out = I.r;
+    double* __restrict__ z_out = I.z;
+    double* __restrict__ p_out = I.p;
+    float2* __restrict__ p2_out = I.p2;
+    double* __restrict__ q_out = I.q;
+    tile_rows<float2>(
+        variant, I.rowptr, rb, re, [&](int k) { return df_prod2(__ldg(vhi + k), __ldg(vlo + k), src[__ldg(col + k)]); },
         [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
         [&](int r, float2 acc) {
-            const bool live = !I.fixed[r];
+            const bool live = !fixed[r];
             if constexpr (RESIDUAL) {
                 double rr = 0, zz = 0;
                 if (live) {
-                    rr = -(df_value(acc) + I.c[r]);
-                    zz = rr * I.dinv[r];
+                    rr = -(df_value(acc) + c[r]);
+                    zz = rr * dinv[r];
                     a.a = fma(rr, zz, a.a);
                     a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) /
-                                                                 (1.0f + fabsf(static_cast<float>(I.xp[r]))))));
+                                                                 (1.0f + fabsf(static_cast<float>(xp[r]))))));
                 }
-                I.r[r] = rr;
-                I.z[r] = zz;
-                I.p[r] = zz;
-                I.p2[r] = df_split(zz);
+                r_out[r] = rr;
+                z_out[r] = zz;
+                p_out[r] = zz;
+                p2_out[r] = df_split(zz);
             } else {
                 const double qq = live ? df_value(acc) : 0.0;
-                I.q[r] = qq;
-                if (live) a.a = fma(I.p[r], qq, a.a);
+                q_out[r] = qq;
+                if (live) a.a = fma(p_out[r], qq, a.a);
             }
         });
 }
 
-__global__ void __launch_bounds__(kBlock) polish_residual_kernel(View v) {
+__global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
         Acc a = acc_identity();
-        polish_matvec_rows<true>(I, T.row_begin, T.row_end, I.xp2, a);
+        polish_matvec_rows<true>(I, T.variant, T.row_begin, T.row_end, I.xp2, a);
         Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
@@ -747,14 +845,14 @@ __global__ void __launch_bounds__(kBlock) polish_residual_kernel(View v) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) cg_matvec_kernel(View v) {
+__global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         Acc a = acc_identity();
-        polish_matvec_rows<false>(I, T.row_begin, T.row_end, I.p2, a);
+        polish_matvec_rows<false>(I, T.variant, T.row_begin, T.row_end, I.p2, a);
         Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
@@ -881,7 +979,7 @@ __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraph
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
-        long long launched = 3;  // two check kernels + gate
+        long long launched = 4;  // three check kernels + gate
         for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps : 0;
         launched += c.polish > 0 ? polish_kernels : 0;
         v.ctrl->kernels += launched;
@@ -985,7 +1083,7 @@ __global__ void __launch_bounds__(kBlock) check_standalone_kernel(CheckSrc s, in
     const int rb = blockIdx.x * rows_per_block;
     const int re = min(n, rb + rows_per_block);
     Acc a = acc_identity();
-    if (rb < re) check_rows<0>(s, rb, re, a);
+    if (rb < re) check_rows<0>(s, VAR_WARP, rb, re, a);
     Acc total = block_reduce(a);
     __shared__ int is_last;
     if (threadIdx.x == 0) {
@@ -1053,7 +1151,7 @@ namespace {
 // One full wave (SMs x resident blocks per SM) per tile kernel, computed once per process.
 struct Waves {
     int step[3] = {0, 0, 0};
-    int check = 0, check_mixed = 0, polish = 0, matvec = 0;
+    int check = 0, check_mixed = 0, check_verify = 0, polish = 0, matvec = 0;
 };
 Waves g_waves;
 
@@ -1075,6 +1173,7 @@ int tile_grid(int sms) {
     g_waves.step[PREC_FP64_EXACT] = wave_of(step_kernel<PREC_FP64_EXACT>, sms, 0);
     g_waves.check = wave_of(check_kernel<FAMILY_FP64>, sms, kSmem8);
     g_waves.check_mixed = wave_of(check_kernel<FAMILY_MIXED>, sms, kSmem8);
+    g_waves.check_verify = wave_of(check_kernel<FAMILY_VERIFY>, sms, kSmem8);
     g_waves.matvec = wave_of(cg_matvec_kernel, sms, kSmem8);
     wave_of(polish_residual_kernel, sms, kSmem8);
     wave_of(check_standalone_kernel, sms, kSmem8);
@@ -1087,6 +1186,7 @@ int tile_grid(int sms) {
 
 void launch_check(const View& v, int grid, cudaStream_t s) {
     check_kernel<FAMILY_MIXED><<<pick(grid, g_waves.check_mixed), kBlock, kSmem8, s>>>(v);
+    check_kernel<FAMILY_VERIFY><<<pick(grid, g_waves.check_verify), kBlock, kSmem8, s>>>(v);
     check_kernel<FAMILY_FP64><<<pick(grid, g_waves.check), kBlock, kSmem8, s>>>(v);
 }
 
