@@ -1171,17 +1171,75 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
         why = "Invalid CSR row pointers";
         return BQP_ERR_INVALID;
     }
-    for (int64_t i = 0; i < n; ++i) {
-        if (rowptr[i + 1] < rowptr[i]) { why = "Invalid CSR row pointers"; return BQP_ERR_INVALID; }
-        if (!std::isfinite(c[i]) || std::isnan(l[i]) || std::isnan(u[i]) || l[i] == HUGE_VAL || u[i] == -HUGE_VAL) {
-            why = "Invalid variable coefficient or bound";
-            return BQP_ERR_INVALID;
-        }
-    }
-    for (int64_t k = 0; k < nnz; ++k) {
-        if (col[k] < 0 || col[k] >= n || !std::isfinite(val[k])) { why = "Invalid Hessian"; return BQP_ERR_INVALID; }
-    }
     return BQP_OK;
+}
+
+// One pass over the problem, split over host threads by row ranges: the reference's input checks
+// (validate_linear_problem, src/mps.cpp:47-60, plus CSR sanity), the Gershgorin bound
+// (src/accelerated_qp.cpp:25-26), the positive-diagonal gate (src/qp_admm.cpp:72-78) and
+// infeasible bounds.  Every row checks its own pointers before touching its entries.
+struct Scan {
+    int error = 0;  // 1 row pointers, 2 coefficient/bound, 3 Hessian entry
+    double lipschitz = 0;
+    bool diagonal = true;
+    bool positive = true;
+    bool infeasible = false;
+};
+
+Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+               const double* c, const double* l, const double* u) {
+    Scan s;
+    for (int64_t i = r0; i < r1; ++i) {
+        const int64_t a = rowptr[i], b = rowptr[i + 1];
+        if (a < 0 || b < a || b > nnz) { s.error = 1; return s; }
+        if (!std::isfinite(c[i]) || std::isnan(l[i]) || std::isnan(u[i]) || l[i] == HUGE_VAL || u[i] == -HUGE_VAL) {
+            s.error = 2;
+            return s;
+        }
+        if (l[i] > u[i]) s.infeasible = true;
+        double abs_sum = 0, d = 0;
+        for (int64_t k = a; k < b; ++k) {
+            const int32_t cc = col[k];
+            const double v = val[k];
+            if (cc < 0 || cc >= n || !std::isfinite(v)) {
+                s.error = 3;
+                return s;
+            }
+            abs_sum += std::abs(v);
+            if (cc == i) d += v;
+            else s.diagonal = false;
+        }
+        if (!(d > 0)) s.positive = false;
+        s.lipschitz = std::max(s.lipschitz, abs_sum);
+    }
+    return s;
+}
+
+Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
+                  const double* c, const double* l, const double* u) {
+    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    int64_t threads = std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, nnz / 500000));
+    std::vector<Scan> part(static_cast<size_t>(threads));
+    auto work = [&](int64_t t) {
+        const int64_t r0 = n * t / threads, r1 = n * (t + 1) / threads;
+        part[t] = scan_rows(r0, r1, n, nnz, rowptr, col, val, c, l, u);
+    };
+    if (threads == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int64_t t = 0; t < threads; ++t) pool.emplace_back(work, t);
+        for (auto& th : pool) th.join();
+    }
+    Scan s;
+    for (const Scan& p : part) {
+        if (p.error && !s.error) s.error = p.error;
+        s.lipschitz = std::max(s.lipschitz, p.lipschitz);
+        s.diagonal = s.diagonal && p.diagonal;
+        s.positive = s.positive && p.positive;
+        s.infeasible = s.infeasible || p.infeasible;
+    }
+    return s;
 }
 
 // Builds a job: validation, Gershgorin L, diagonal gate, tiles; infeasible bounds finish at once.
@@ -1193,7 +1251,13 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     else bqp_options_default(&o);
     int rc = validate_problem(n, nnz, rowptr, col, val, c, l, u, &o, why);
     if (rc != BQP_OK) return rc;
-    double lipschitz = bqp_gershgorin(n, rowptr, val);
+    const Scan scan = scan_problem(n, nnz, rowptr, col, val, c, l, u);
+    if (scan.error) {
+        why = scan.error == 1 ? "Invalid CSR row pointers"
+                              : scan.error == 2 ? "Invalid variable coefficient or bound" : "Invalid Hessian";
+        return BQP_ERR_INVALID;
+    }
+    const double lipschitz = scan.lipschitz;
     if (lipschitz == 0) {
         why = "Zero-Hessian models use the CPU LP path";
         return BQP_ERR_UNSUPPORTED;
@@ -1203,32 +1267,17 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     j->nnz = nnz;
     j->opt = o;
     j->lipschitz = lipschitz;
-    if (o.diagonal_gate >= 0) {
-        j->diag_gate = o.diagonal_gate ? 1 : 0;
-    } else {
-        bool diagonal = true;
-        for (int64_t i = 0; i < n && diagonal; ++i)
-            for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
-                if (col[k] != i) { diagonal = false; break; }
-        bool positive = diagonal;
-        for (int64_t i = 0; i < n && positive; ++i) {
-            double d = 0;
-            for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) d += val[k];
-            if (!(d > 0)) positive = false;
-        }
-        j->diag_gate = positive ? 1 : 0;
-    }
-    for (int64_t i = 0; i < n; ++i) {
-        if (l[i] > u[i]) {
-            j->state = bqp::JOB_DONE;
-            j->stats.status = BQP_STATUS_INFEASIBLE_BOUNDS;
-            j->stats.objective = std::numeric_limits<double>::quiet_NaN();
-            j->stats.primal_residual = j->stats.stationarity_residual = HUGE_VAL;
-            j->stats.complementarity_residual = j->stats.relative_gap = HUGE_VAL;
-            j->stats.dual_bound = -HUGE_VAL;
-            *out = j.release();
-            return BQP_OK;
-        }
+    if (o.diagonal_gate >= 0) j->diag_gate = o.diagonal_gate ? 1 : 0;
+    else j->diag_gate = (scan.diagonal && scan.positive) ? 1 : 0;
+    if (scan.infeasible) {
+        j->state = bqp::JOB_DONE;
+        j->stats.status = BQP_STATUS_INFEASIBLE_BOUNDS;
+        j->stats.objective = std::numeric_limits<double>::quiet_NaN();
+        j->stats.primal_residual = j->stats.stationarity_residual = HUGE_VAL;
+        j->stats.complementarity_residual = j->stats.relative_gap = HUGE_VAL;
+        j->stats.dual_bound = -HUGE_VAL;
+        *out = j.release();
+        return BQP_OK;
     }
     if (o.precision == BQP_PRECISION_FP64_EXACT) j->variant = 1;
     else if (o.kernel_variant >= 0) j->variant = o.kernel_variant;
