@@ -51,11 +51,11 @@ struct Layout {
     size_t c32 = kNone, l32 = kNone, u32 = kNone, x32 = kNone, w32a = kNone, w32b = kNone;
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
-    size_t xp2 = kNone, p2 = kNone, dinv = kNone;
+    size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t total = 0;
 };
 
-Layout make_layout(int64_t n, int64_t nnz, int precision) {
+Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
     Layout L;
     size_t o = 0;
     // 64 bytes of slack behind every array keep 16-byte vector loads of a tail in bounds.
@@ -93,6 +93,8 @@ Layout make_layout(int64_t n, int64_t nnz, int precision) {
         L.p2 = take(N * 8);
         L.dinv = take(N * 8);
         L.fixed = take(N);
+        L.free_rows = take(N * 4);
+        L.free_cnt = take(static_cast<size_t>(tiles) * 4);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
@@ -548,11 +550,12 @@ bool Engine::build_graph(std::string& why) {
     const View v = view();
 
     if (!cuda_ok(cudaGraphCreate(&graph_, 0), why, "graph create")) return false;
-    cudaGraphConditionalHandle h_loop, h_f[3], h_pol;
+    cudaGraphConditionalHandle h_loop, h_f[3], h_pol, h_cg;
     if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_loop, graph_, 1, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
     for (int k = 0; k < 3; ++k)
         if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_f[k], graph_, 0, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
     if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_pol, graph_, 0, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
+    if (!cuda_ok(cudaGraphConditionalHandleCreate(&h_cg, graph_, 0, cudaGraphCondAssignDefault), why, "conditional handle")) return false;
 
     cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
     wp.conditional.handle = h_loop;
@@ -577,20 +580,24 @@ bool Engine::build_graph(std::string& why) {
         if (!cuda_ok(cudaStreamEndCapture(capture_, &out), why, "end capture")) return false;
         return cuda_ok(cudaGetLastError(), why, "captured launch");
     };
-    auto add_if = [&](cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraphNode_t* node, cudaGraph_t* inner) -> bool {
+    auto add_cond = [&](cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                        cudaGraphNode_t* node, cudaGraph_t* inner) -> bool {
         cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
         p.conditional.handle = h;
-        p.conditional.type = cudaGraphCondTypeIf;
+        p.conditional.type = type;
         p.conditional.size = 1;
-        if (!cuda_ok(cudaGraphAddNode(node, body, &dep, nullptr, 1, &p), why, "if node")) return false;
+        if (!cuda_ok(cudaGraphAddNode(node, g, &dep, nullptr, dep ? 1 : 0, &p), why, "conditional node")) return false;
         *inner = p.conditional.phGraph_out[0];
         return true;
+    };
+    auto add_if = [&](cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraphNode_t* node, cudaGraph_t* inner) {
+        return add_cond(body, dep, h, cudaGraphCondTypeIf, node, inner);
     };
 
     cudaGraphNode_t last = nullptr;
     if (!capture(body, nullptr, 0, [&] {
             launch_check(v, grid, capture_);
-            launch_gate(v, h_f, h_pol, K, 2 + 3 * kCgPerBody, capture_);
+            launch_gate(v, h_f, h_pol, h_cg, K, capture_);
         }, &last)) return false;
     const int precisions[3] = {PREC_FP64, PREC_MIXED, PREC_FP64_EXACT};
     for (int k = 0; k < 3; ++k) {
@@ -606,14 +613,19 @@ bool Engine::build_graph(std::string& why) {
         cudaGraphNode_t node;
         cudaGraph_t inner;
         if (!add_if(last, h_pol, &node, &inner)) return false;
+        // polish: init + residual, then WHILE (an instance is iterating, < kCgPerBody iterations)
+        // { matvec, update, direction }; the direction kernel sets the loop's condition.
+        cudaGraphNode_t head = nullptr, loop_node;
+        cudaGraph_t loop_body;
         if (!capture(inner, nullptr, 0, [&] {
                 launch_polish_init(v, grid, capture_);
                 launch_polish_residual(v, grid, capture_);
-                for (int j = 0; j < kCgPerBody; ++j) {
-                    launch_cg_matvec(v, grid, capture_);
-                    launch_cg_update(v, grid, capture_);
-                    launch_cg_direction(v, grid, capture_);
-                }
+            }, &head)) return false;
+        if (!add_cond(inner, head, h_cg, cudaGraphCondTypeWhile, &loop_node, &loop_body)) return false;
+        if (!capture(loop_body, nullptr, 0, [&] {
+                launch_cg_matvec(v, grid, capture_);
+                launch_cg_update(v, grid, capture_);
+                launch_cg_direction(v, grid, capture_, h_cg, kCgPerBody);
             }, nullptr)) return false;
         last = node;
     }
@@ -747,7 +759,7 @@ int Engine::load(int64_t* queued, int64_t* running, int64_t* peak, int64_t* resi
 bool Engine::admit(Job& j, std::string& why) {
     const int prec = j.opt.precision;
     if (!j.resolve) {
-        j.layout = make_layout(j.n, j.nnz, prec);
+        j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
         void* slab = nullptr;
         if (!cuda_ok(cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, stream_), why, "allocate solve")) return false;
         j.slab = slab;
@@ -798,6 +810,8 @@ bool Engine::admit(Job& j, std::string& why) {
         R.xp2 = at<float2>(slab, L.xp2);
         R.p2 = at<float2>(slab, L.p2);
         R.dinv = at<double>(slab, L.dinv);
+        R.free_rows = at<int32_t>(slab, L.free_rows);
+        R.free_cnt = at<int32_t>(slab, L.free_cnt);
         R.n = static_cast<int32_t>(j.n);
         R.diag_gate = j.diag_gate;
         R.precision = prec;
@@ -1071,7 +1085,7 @@ void Engine::loop() {
         // admission: FIFO while the head fits under the cap
         while (!queue_.empty()) {
             Job* j = queue_.front();
-            const size_t need = j->resolve ? 0 : make_layout(j->n, j->nnz, j->opt.precision).total;
+            const size_t need = j->resolve ? 0 : make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
             if (!j->resolve && resident_bytes_ + need > cap_) {
                 if (n_running_ == 0) {
                     queue_.pop_front();

@@ -93,6 +93,8 @@ struct __align__(16) InstDev {
     double* q;
     double* z;
     uint8_t* fixed;        // polish: 1 = held at a bound
+    int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row
+    int32_t* free_cnt;     // polish: free rows per tile (index within the instance's tiles)
     // geometry (the instance's tile range lives in View::ranges)
     int32_t n;
     int32_t diag_gate;
@@ -153,6 +155,8 @@ struct Ctrl {
     int32_t n_fista[3];    // instances in the FISTA phase, per precision
     int32_t n_polish;
     int32_t error;         // non-zero: a kernel detected an inconsistency
+    int32_t n_cg;          // instances that may still run CG iterations in this body
+    int32_t cg_iters;      // CG iterations run in this body
     long long kernels;     // engine kernels executed by this launch (counted by gate/control)
 };
 

@@ -157,11 +157,75 @@ __device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles
     return last;
 }
 
-// Reduces the partials of tiles [tb, te) in a fixed order; valid in thread 0.
+// Reduces the partials of tiles [tb, te) in a fixed order; valid in thread 0.  Pairs of partials
+// are loaded before they are combined (same order, two loads in flight).
 __device__ Acc reduce_instance(const View& v, int tb, int te) {
     Acc acc = acc_identity();
-    for (int k = tb + threadIdx.x; k < te; k += kBlock) acc = combine(acc, load_partial(&v.partial[k]));
+    int k = tb + static_cast<int>(threadIdx.x);
+    for (; k + kBlock < te; k += 2 * kBlock) {
+        const Acc p0 = load_partial(&v.partial[k]);
+        const Acc p1 = load_partial(&v.partial[k + kBlock]);
+        acc = combine(acc, p0);
+        acc = combine(acc, p1);
+    }
+    if (k < te) acc = combine(acc, load_partial(&v.partial[k]));
     return block_reduce(acc);
+}
+
+// The CG reductions carry one sum (a) and one maximum (b): the same fixed order on those two
+// fields alone, eight partials in flight per thread.
+__device__ Acc block_reduce_ab(Acc v) {
+    __shared__ double part_a[kBlock / 32];
+    __shared__ unsigned long long part_b[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.a += shfl_xor(v.a, o);
+        v.b = umax64(v.b, shfl_xor(v.b, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        part_a[warp] = v.a;
+        part_b[warp] = v.b;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double a = lane < kBlock / 32 ? part_a[lane] : 0.0;
+        unsigned long long b = lane < kBlock / 32 ? part_b[lane] : 0ull;
+#pragma unroll
+        for (int o = (kBlock / 64); o > 0; o >>= 1) {
+            a += shfl_xor(a, o);
+            b = umax64(b, shfl_xor(b, o));
+        }
+        v.a = a;
+        v.b = b;
+    }
+    __syncthreads();
+    return v;
+}
+
+__device__ Acc reduce_instance_ab(const View& v, int tb, int te) {
+    constexpr int kAhead = 8;
+    Acc acc = acc_identity();
+    int k = tb + static_cast<int>(threadIdx.x);
+    for (; k + (kAhead - 1) * kBlock < te; k += kAhead * kBlock) {
+        double a[kAhead];
+        unsigned long long b[kAhead];
+#pragma unroll
+        for (int i = 0; i < kAhead; ++i) {
+            a[i] = __ldcg(&v.partial[k + i * kBlock].a);
+            b[i] = __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k + i * kBlock].b));
+        }
+#pragma unroll
+        for (int i = 0; i < kAhead; ++i) {
+            acc.a += a[i];
+            acc.b = umax64(acc.b, b[i]);
+        }
+    }
+    for (; k < te; k += kBlock) {
+        acc.a += __ldcg(&v.partial[k].a);
+        acc.b = umax64(acc.b, __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k].b)));
+    }
+    return block_reduce_ab(acc);
 }
 
 // ---- one row of check_qp_solution ------------------------------------------------------------
@@ -256,9 +320,15 @@ __device__ __forceinline__ void warp_groups(const int32_t* __restrict__ rowptr, 
 // its 32 / LANES sub-groups of LANES lanes form one row sum each (the memory pattern of the tuned
 // sub-warp step kernel), and shuffles hand every row sum to its own lane, so the epilogue of the
 // 32 rows runs with all 32 lanes active.  Fixed summation order (lane-strided partials, xor tree).
-template <int LANES, class T, class Prod, class Add, class Epi>
+struct SameRow {
+    __device__ __forceinline__ int operator()(int j) const { return j; }
+};
+
+// Positions [rb, re) name rows through row(j): the identity for a tile's row range, or a list of
+// rows (the free rows of a polish tile).  The summation order of one row does not depend on it.
+template <int LANES, class T, class Prod, class Add, class Epi, class Map = SameRow>
 __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr, int rb, int re, Prod prod, Add add,
-                                             T zero, Epi epi) {
+                                             T zero, Epi epi, Map row = Map()) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -266,9 +336,10 @@ __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr,
         T mine = zero;
 #pragma unroll
         for (int pass = 0; pass < LANES; ++pass) {
-            const int r = base + pass * R + sub;
+            const int j = base + pass * R + sub;
             T acc = zero;
-            if (r < re) {
+            if (j < re) {
+                const int r = row(j);
                 const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
 #pragma unroll 4
                 for (int k = ks + sl; k < ke; k += LANES) acc = add(acc, prod(k));
@@ -280,8 +351,8 @@ __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr,
             const T got = shfl_idx(acc, (mine_now ? g : 0) * LANES);
             if (mine_now) mine = got;
         }
-        const int r = base + lane;
-        if (r < re) epi(r, mine);
+        const int j = base + lane;
+        if (j < re) epi(row(j), mine);
     }
 }
 
@@ -754,34 +825,84 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // being the variables the FP32 iterate holds strictly inside its bounds.  Vectors are FP64; the
 // matrix products are formed in FP32 double-float arithmetic from the hi/lo values and the FP32
 // pairs xp2 / p2 kept beside xp / p.
+// polish_init lists each tile's free rows in ascending order at free_rows[row_begin ...] and
+// their count at free_cnt[tile index within the instance]; the CG kernels visit only those rows
+// (an instance's tiling depends on the instance alone, so the list survives changes of the batch).
+// Fixed rows hold r = z = p = 0, so the products of the CG matvec over all columns are exact.
 __device__ __forceinline__ bool polish_phase(const InstDev& I, int phase) {
     return I.status == ST_RUNNING && I.phase == phase;
 }
 
 __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
+    __shared__ int warp_free[kBlock / 32];
     const int nt = v.ctrl->n_tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         const InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
-        for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-            const float xf = I.x32[r];
-            uint8_t fixed = 1;
-            double xv;
-            if (xf <= I.l32[r]) xv = I.l[r];
-            else if (xf >= I.u32[r]) xv = I.u[r];
-            else { xv = static_cast<double>(xf); fixed = 0; }
-            I.xp[r] = xv;
-            I.xp2[r] = df_split(xv);
-            I.fixed[r] = fixed;
+        const float* __restrict__ x32 = I.x32;
+        const float* __restrict__ l32 = I.l32;
+        const float* __restrict__ u32 = I.u32;
+        const double* __restrict__ l = I.l;
+        const double* __restrict__ u = I.u;
+        double* __restrict__ xp = I.xp;
+        float2* __restrict__ xp2 = I.xp2;
+        uint8_t* __restrict__ fixed_out = I.fixed;
+        double* __restrict__ r_out = I.r;
+        double* __restrict__ z_out = I.z;
+        double* __restrict__ p_out = I.p;
+        float2* __restrict__ p2_out = I.p2;
+        int32_t* __restrict__ list = I.free_rows + T.row_begin;
+        int count = 0;
+        for (int r0 = T.row_begin; r0 < T.row_end; r0 += kBlock) {
+            const int r = r0 + static_cast<int>(threadIdx.x);
+            bool is_free = false;
+            if (r < T.row_end) {
+                const float xf = x32[r];
+                double xv;
+                if (xf <= l32[r]) xv = l[r];
+                else if (xf >= u32[r]) xv = u[r];
+                else { xv = static_cast<double>(xf); is_free = true; }
+                xp[r] = xv;
+                xp2[r] = df_split(xv);
+                fixed_out[r] = is_free ? 0 : 1;
+                if (!is_free) {
+                    r_out[r] = 0.0;
+                    z_out[r] = 0.0;
+                    p_out[r] = 0.0;
+                    p2_out[r] = make_float2(0.f, 0.f);
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, is_free);
+            if (lane == 0) warp_free[warp] = __popc(m);
+            __syncthreads();
+            int before = count, total = count;
+#pragma unroll
+            for (int w = 0; w < kBlock / 32; ++w) {
+                before += w < warp ? warp_free[w] : 0;
+                total += warp_free[w];
+            }
+            if (is_free) list[before + __popc(m & ((1u << lane) - 1u))] = r;
+            __syncthreads();
+            count = total;
         }
+        if (threadIdx.x == 0) I.free_cnt[t - v.ranges[T.inst].x] = count;
     }
 }
 
-// q = Q src on the free rows (0 on fixed rows), src given as FP32 pairs.  residual = true:
-// r = -(Q xp + c), z = D^-1 r, p = z on free rows, accumulating r.z and max |r|/(1+|x|).
+struct ListRow {
+    const int32_t* list;
+    __device__ __forceinline__ int operator()(int j) const { return list[j]; }
+};
+
+// q = Q src on the tile's free rows, src given as FP32 pairs.  residual = true: r = -(Q xp + c),
+// z = D^-1 r, p = z on the free rows, accumulating r.z and max |r|/(1+|x|).  The sub-warp variants
+// visit the free-row list; the staged variants (long rows) run every row and skip fixed ones in
+// the epilogue.
 template <bool RESIDUAL>
-__device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re, const float2* __restrict__ src, Acc& a) {
+__device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re, int n_free,
+                                   const float2* __restrict__ src, Acc& a) {
     // Local copies: the epilogue stores through other pointers of the same record, which would
     // otherwise force the matrix pointers to be reloaded for every product.
     const int32_t* __restrict__ col = I.col;
@@ -796,30 +917,37 @@ __device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re
     double* __restrict__ p_out = I.p;
     float2* __restrict__ p2_out = I.p2;
     double* __restrict__ q_out = I.q;
-    tile_rows<float2>(
-        variant, I.rowptr, rb, re, [&](int k) { return df_prod2(__ldg(vhi + k), __ldg(vlo + k), src[__ldg(col + k)]); },
-        [](float2 x, float2 y) { return df_add(x, y); }, make_float2(0.f, 0.f),
-        [&](int r, float2 acc) {
-            const bool live = !fixed[r];
-            if constexpr (RESIDUAL) {
-                double rr = 0, zz = 0;
-                if (live) {
-                    rr = -(df_value(acc) + c[r]);
-                    zz = rr * dinv[r];
-                    a.a = fma(rr, zz, a.a);
-                    a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) /
-                                                                 (1.0f + fabsf(static_cast<float>(xp[r]))))));
-                }
-                r_out[r] = rr;
-                z_out[r] = zz;
-                p_out[r] = zz;
-                p2_out[r] = df_split(zz);
-            } else {
-                const double qq = live ? df_value(acc) : 0.0;
-                q_out[r] = qq;
-                if (live) a.a = fma(p_out[r], qq, a.a);
-            }
-        });
+    auto prod = [&](int k) { return df_prod2(__ldg(vhi + k), __ldg(vlo + k), src[__ldg(col + k)]); };
+    auto add = [](float2 x, float2 y) { return df_add(x, y); };
+    auto epi = [&](int r, float2 acc) {
+        if (fixed[r]) return;
+        if constexpr (RESIDUAL) {
+            const double rr = -(df_value(acc) + c[r]);
+            const double zz = rr * dinv[r];
+            a.a = fma(rr, zz, a.a);
+            a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) /
+                                                         (1.0f + fabsf(static_cast<float>(xp[r]))))));
+            r_out[r] = rr;
+            z_out[r] = zz;
+            p_out[r] = zz;
+            p2_out[r] = df_split(zz);
+        } else {
+            const double qq = df_value(acc);
+            q_out[r] = qq;
+            a.a = fma(p_out[r], qq, a.a);
+        }
+    };
+    const float2 zero = make_float2(0.f, 0.f);
+    const ListRow list{I.free_rows + rb};
+    switch (variant) {
+    case 1: subwarp_rows<1, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 2: subwarp_rows<2, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 4: subwarp_rows<4, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 8: subwarp_rows<8, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 16: subwarp_rows<16, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 32: subwarp_rows<32, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    default: warp_groups<float2>(I.rowptr, rb, re, warp_buffer<float2>(), prod, add, zero, epi); break;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
@@ -828,17 +956,18 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
-        Acc a = acc_identity();
-        polish_matvec_rows<true>(I, T.variant, T.row_begin, T.row_end, I.xp2, a);
-        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
+        Acc a = acc_identity();
+        polish_matvec_rows<true>(I, T.variant, T.row_begin, T.row_end, I.free_cnt[t - R.x], I.xp2, a);
+        Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
                 I.rz = inst_total.a;
                 I.cg_res = bdouble(inst_total.b);
                 I.cg_it = 0;
                 I.phase = (I.cg_res <= I.cg_tol || !(I.rz > 0)) ? PH_POLISH_FINISH : PH_POLISH_CG;
+                if (I.phase == PH_POLISH_FINISH) atomicSub(&v.ctrl->n_cg, 1);
             }
             __syncthreads();
         }
@@ -851,12 +980,12 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
-        Acc a = acc_identity();
-        polish_matvec_rows<false>(I, T.variant, T.row_begin, T.row_end, I.p2, a);
-        Acc total = block_reduce(a);
         const int2 R = v.ranges[T.inst];
+        Acc a = acc_identity();
+        polish_matvec_rows<false>(I, T.variant, T.row_begin, T.row_end, I.free_cnt[t - R.x], I.p2, a);
+        Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
                 const double pq = inst_total.a;
                 if (pq > 0 && isfinite(pq)) {
@@ -877,23 +1006,31 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
+        const int2 R = v.ranges[T.inst];
         const double alpha = I.alpha;
+        const int32_t* __restrict__ list = I.free_rows + T.row_begin;
+        const int n_free = I.free_cnt[t - R.x];
+        const double* __restrict__ p = I.p;
+        const double* __restrict__ q = I.q;
+        const double* __restrict__ dinv = I.dinv;
+        double* __restrict__ xp = I.xp;
+        double* __restrict__ rr_v = I.r;
+        double* __restrict__ z = I.z;
         Acc a = acc_identity();
-        for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-            if (I.fixed[r]) continue;
-            const double xv = fma(alpha, I.p[r], I.xp[r]);
-            const double rr = fma(-alpha, I.q[r], I.r[r]);
-            const double zz = rr * I.dinv[r];
-            I.xp[r] = xv;
-            I.r[r] = rr;
-            I.z[r] = zz;
+        for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+            const int r = list[j];
+            const double xv = fma(alpha, p[r], xp[r]);
+            const double rr = fma(-alpha, q[r], rr_v[r]);
+            const double zz = rr * dinv[r];
+            xp[r] = xv;
+            rr_v[r] = rr;
+            z[r] = zz;
             a.a = fma(rr, zz, a.a);
             a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) / (1.0f + fabsf(static_cast<float>(xv))))));
         }
-        Acc total = block_reduce(a);
-        const int2 R = v.ranges[T.inst];
+        Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
                 const double rz_new = inst_total.a;
                 I.beta_cg = I.rz > 0 ? rz_new / I.rz : 0.0;
@@ -901,14 +1038,26 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
                 I.cg_res = bdouble(inst_total.b);
                 I.cg_it++;
                 I.cg_total++;
-                if (I.cg_res <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) I.phase = PH_POLISH_FINISH;
+                if (I.cg_res <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) {
+                    I.phase = PH_POLISH_FINISH;
+                    atomicSub(&v.ctrl->n_cg, 1);
+                }
             }
             __syncthreads();
         }
     }
 }
 
-__global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v) {
+// In a graph, block 0 also decides whether the CG loop of this body runs another iteration:
+// while an instance is still iterating and fewer than `cap` iterations ran (the instances
+// leaving CG were counted down by the update kernel, which completed before this launch).
+__global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v, cudaGraphConditionalHandle h_cg, int cap) {
+    if (cap > 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctrl* ctrl = v.ctrl;
+        const int it = ++ctrl->cg_iters;
+        ctrl->kernels += 3;
+        cudaGraphSetConditional(h_cg, (ctrl->n_cg > 0 && it < cap) ? 1u : 0u);
+    }
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
@@ -916,17 +1065,26 @@ __global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v) {
         if (I.status != ST_RUNNING) continue;
         if (I.phase == PH_POLISH_CG) {
             const double beta = I.beta_cg;
-            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-                if (I.fixed[r]) continue;
-                const double pv = fma(beta, I.p[r], I.z[r]);
-                I.p[r] = pv;
-                I.p2[r] = df_split(pv);
+            const int32_t* __restrict__ list = I.free_rows + T.row_begin;
+            const int n_free = I.free_cnt[t - v.ranges[T.inst].x];
+            const double* __restrict__ z = I.z;
+            double* __restrict__ p = I.p;
+            float2* __restrict__ p2 = I.p2;
+            for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                const int r = list[j];
+                const double pv = fma(beta, p[r], z[r]);
+                p[r] = pv;
+                p2[r] = df_split(pv);
             }
         } else if (I.phase == PH_POLISH_FINISH) {
+            const double* __restrict__ l = I.l;
+            const double* __restrict__ u = I.u;
+            double* __restrict__ xp = I.xp;
+            float2* __restrict__ xp2 = I.xp2;
             for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-                const double xv = smax(I.l[r], smin(I.u[r], I.xp[r]));
-                I.xp[r] = xv;
-                I.xp2[r] = df_split(xv);
+                const double xv = smax(l[r], smin(u[r], xp[r]));
+                xp[r] = xv;
+                xp2[r] = df_split(xv);
             }
         }
     }
@@ -972,21 +1130,26 @@ __device__ Counts count_phases(const View& v, bool mirror) {
     return c;
 }
 
+// The polish branch runs polish_init and the residual, then a CG loop whose iterations the
+// direction kernel counts into Ctrl::kernels.
 __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraphConditionalHandle h_mixed,
-                            cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish, int steps,
-                            int polish_kernels) {
+                            cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish,
+                            cudaGraphConditionalHandle h_cg, int steps) {
     const Counts c = count_phases(v, false);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
+        v.ctrl->n_cg = c.polish;
+        v.ctrl->cg_iters = 0;
         long long launched = 4;  // three check kernels + gate
         for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps : 0;
-        launched += c.polish > 0 ? polish_kernels : 0;
+        launched += c.polish > 0 ? 2 : 0;
         v.ctrl->kernels += launched;
         cudaGraphSetConditional(h_fp64, c.fista[0] > 0 ? 1u : 0u);
         cudaGraphSetConditional(h_mixed, c.fista[1] > 0 ? 1u : 0u);
         cudaGraphSetConditional(h_exact, c.fista[2] > 0 ? 1u : 0u);
         cudaGraphSetConditional(h_polish, c.polish > 0 ? 1u : 0u);
+        cudaGraphSetConditional(h_cg, c.polish > 0 ? 1u : 0u);
     }
 }
 
@@ -1006,6 +1169,8 @@ __global__ void gate_plain_kernel(View v) {
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
+        v.ctrl->n_cg = c.polish;
+        v.ctrl->cg_iters = 0;
     }
 }
 
@@ -1210,13 +1375,13 @@ void launch_cg_matvec(const View& v, int grid, cudaStream_t s) {
     cg_matvec_kernel<<<pick(grid, g_waves.matvec), kBlock, kSmem8, s>>>(v);
 }
 void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v); }
-void launch_cg_direction(const View& v, int grid, cudaStream_t s) {
-    cg_direction_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v);
+void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop, int cap) {
+    cg_direction_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v, cg_loop, cap);
 }
 
-void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish, int steps,
-                 int polish_kernels, cudaStream_t s) {
-    gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, steps, polish_kernels);
+void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
+                 cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s) {
+    gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, cg_loop, steps);
 }
 void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s) {
     control_kernel<<<1, 1024, 0, s>>>(v, loop);

@@ -15,12 +15,14 @@ void launch_polish_init(const View& v, int grid, cudaStream_t s);
 void launch_polish_residual(const View& v, int grid, cudaStream_t s);
 void launch_cg_matvec(const View& v, int grid, cudaStream_t s);
 void launch_cg_update(const View& v, int grid, cudaStream_t s);
-void launch_cg_direction(const View& v, int grid, cudaStream_t s);
+// cap > 0 (inside a graph): also sets cg_loop, the WHILE handle of the CG loop, allowing at
+// most `cap` iterations per body.  cap = 0: no handle is touched (host-driven launches).
+void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop = 0, int cap = 0);
 // Single-block control kernels that steer the conditional graph nodes.
-// fista[k]: handle of the IF node of the precision-k step launches.
-// `steps` / `polish_kernels`: kernels inside each FISTA / the polish IF body (for the count).
-void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish, int steps,
-                 int polish_kernels, cudaStream_t s);
+// fista[k]: handle of the IF node of the precision-k step launches; polish: the IF node of the
+// polish branch; cg_loop: the WHILE node of its CG loop.  `steps`: kernels inside each FISTA body.
+void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
+                 cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s);
 void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s);
 // Host-driven variants of the control kernels (no conditional handles).
 void launch_gate_plain(const View& v, cudaStream_t s);
