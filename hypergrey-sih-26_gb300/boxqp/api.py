@@ -58,7 +58,7 @@ class QpOptions:
     threads: int = 1
     scaling: bool = True
     precision: str = 'fp64'
-    check_interval: int = 25
+    check_interval: int = 0  # 0: engine default (25, the reference's cadence, for the FP64 engines)
 
 
 @dataclass
@@ -94,7 +94,7 @@ def _i64(a):
 
 
 def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, precision='fp64',
-                   check_interval=25, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None):
+                   check_interval=0, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None):
     o = Options()
     lib().bqp_options_default(o)
     o.tolerance = float(tolerance)

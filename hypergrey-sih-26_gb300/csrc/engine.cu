@@ -852,6 +852,7 @@ bool Engine::admit(Job& j, std::string& why) {
     R.fista_iters = 0;
     R.checks = 0;
     R.iterations = 0;
+    R.skip_check = (prec == PREC_MIXED && R.max_iter > 0) ? 1 : 0;
     if (!cuda_ok(cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_), why, "instance record")) return false;
     if (tables_dirty_) {
         if (!h_tiles_.empty())
@@ -888,8 +889,13 @@ bool Engine::admit(Job& j, std::string& why) {
         timer_ms_ += ms;
         timer_kernels_ += 1;
     }
-    if (j.opt.check_interval > graph_interval_) {
-        graph_interval_ = std::min(j.opt.check_interval, kMaxInterval);
+    // steps per body: the longest check interval among the resident solves
+    int steps = j.rec.interval;
+    for (const Job* r : slot_job_)
+        if (r && r != &j) steps = std::max(steps, r->rec.interval);
+    steps = std::min(steps, kMaxInterval);
+    if (steps != graph_interval_) {
+        graph_interval_ = steps;
         graph_valid_ = false;
     }
     const int grid_max = grid_max_;
@@ -1172,7 +1178,7 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
         return BQP_ERR_INVALID;
     }
     if (!o || !(o->tolerance > 0) || !std::isfinite(o->tolerance) || o->time_limit < 0 || !std::isfinite(o->time_limit) ||
-        o->iteration_limit < 0 || o->check_interval < 1 || o->check_interval > bqp::kMaxInterval ||
+        o->iteration_limit < 0 || o->check_interval < 0 || o->check_interval > bqp::kMaxInterval ||
         (o->precision != BQP_PRECISION_FP64 && o->precision != BQP_PRECISION_MIXED && o->precision != BQP_PRECISION_FP64_EXACT) ||
         !std::isfinite(o->offset) || !(o->polish_switch >= 0) || !std::isfinite(o->polish_switch) ||
         (o->kernel_variant >= 0 && o->kernel_variant != 0 && o->kernel_variant != 64 && o->kernel_variant != 1 &&
@@ -1280,6 +1286,13 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     j->n = n;
     j->nnz = nnz;
     j->opt = o;
+    // Engine defaults (0 = auto).  FP64 engines check every 25 iterations, the reference's
+    // cadence.  The mixed engine checks only to find its polish point: on instances whose rows
+    // average 8 or more nonzeros (FISTA steps bound by their random gathers) every 10 iterations
+    // with a polish switch at stationarity 0.1, else every 25 with a switch at 0.03.
+    const bool gather_heavy = o.precision == BQP_PRECISION_MIXED && nnz >= 8 * n;
+    if (j->opt.check_interval == 0) j->opt.check_interval = gather_heavy ? 10 : 25;
+    if (j->opt.polish_switch == 0) j->opt.polish_switch = j->opt.check_interval <= 10 ? 0.1 : 3e-2;
     j->lipschitz = lipschitz;
     if (o.diagonal_gate >= 0) j->diag_gate = o.diagonal_gate ? 1 : 0;
     else j->diag_gate = (scan.diagonal && scan.positive) ? 1 : 0;
@@ -1333,12 +1346,12 @@ void bqp_options_default(bqp_options* o) {
     o->iteration_limit = 200000;
     o->precision = BQP_PRECISION_FP64;
     o->lipschitz = BQP_LIPSCHITZ_GERSHGORIN;
-    o->check_interval = 25;
+    o->check_interval = 0;
     o->diagonal_gate = -1;
     o->offset = 0;
     o->kernel_variant = -1;
     o->reserved = 0;
-    o->polish_switch = 3e-2;
+    o->polish_switch = 0;
 }
 
 bqp_ctx* bqp_create(int device, size_t mem_cap_bytes) {

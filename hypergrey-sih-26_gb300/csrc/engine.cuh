@@ -105,6 +105,8 @@ struct __align__(16) InstDev {
     int32_t polish_rounds;
     int32_t precision;
     int32_t polish;        // mixed: free-set polish enabled
+    int32_t skip_check;    // 1: the first body runs its steps without checking x0 (mixed)
+    int32_t pad_skip;
     int64_t it0;          // iteration of the step j = 0 of the current chunk
     int64_t it_next;       // iteration of the next check
     int64_t max_iter;

@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
-        if (I.status != ST_RUNNING) continue;
+        if (I.status != ST_RUNNING || I.skip_check) continue;
         if ((I.precision == PREC_MIXED) != (FAMILY != FAMILY_FP64)) continue;
         const int ph = I.phase;
         if (FAMILY == FAMILY_VERIFY ? ph != PH_POLISH_FINISH : ph != PH_FISTA) continue;
@@ -1130,12 +1130,21 @@ __device__ Counts count_phases(const View& v, bool mirror) {
     return c;
 }
 
+// The check kernels of this body have run: instances that skipped their first check take part
+// from the next body on.
+__device__ void clear_skip(const View& v) {
+    const int n = v.ctrl->n_inst;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (v.inst[i].skip_check) v.inst[i].skip_check = 0;
+}
+
 // The polish branch runs polish_init and the residual, then a CG loop whose iterations the
 // direction kernel counts into Ctrl::kernels.
 __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraphConditionalHandle h_mixed,
                             cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish,
                             cudaGraphConditionalHandle h_cg, int steps) {
     const Counts c = count_phases(v, false);
+    clear_skip(v);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
@@ -1166,6 +1175,7 @@ __global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h) {
 
 __global__ void gate_plain_kernel(View v) {
     const Counts c = count_phases(v, false);
+    clear_skip(v);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
@@ -1200,6 +1210,14 @@ __global__ void init_instance_kernel(View v, int slot, int n, int precision) {
         I.start_ns = start;
         I.deadline_ns = start + I.deadline_ns;  // host stores the budget in nanoseconds
         I.end_ns = 0;
+        if (I.skip_check) {
+            // mixed precision: x0 = clip(0) is not checked; the first chunk of steps is armed here
+            // as a check of x0 would arm it (the first check then comes after `interval` steps)
+            I.it0 = 0;
+            I.it_next = I.interval < I.max_iter ? I.interval : I.max_iter;
+            fista_betas(I, I.it_next);
+            I.fista_iters += I.it_next;
+        }
     }
 }
 

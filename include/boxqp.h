@@ -69,7 +69,9 @@ typedef struct bqp_options {
     int64_t iteration_limit;  /* FISTA iterations, default 200000                                */
     int32_t precision;        /* BQP_PRECISION_*, default BQP_PRECISION_FP64                      */
     int32_t lipschitz;        /* BQP_LIPSCHITZ_*, default BQP_LIPSCHITZ_GERSHGORIN                */
-    int32_t check_interval;   /* iterations between verifications, default 25 (reference)        */
+    int32_t check_interval;   /* iterations between checks, 1..32; default 0 = auto: 25 for the FP64
+                                 engines (the reference's cadence, src/accelerated_qp.cpp:40);
+                                 mixed: 10 when nnz >= 8 n, else 25                              */
     int32_t diagonal_gate;    /* -1 auto from the CSR; 0/1 force the reference's positive-diagonal
                                  dual-gap gate (src/qp_admm.cpp:72-78,106-116)                  */
     double  offset;           /* constant term of the objective (LinearProblem::offset)          */
@@ -78,7 +80,8 @@ typedef struct bqp_options {
     int32_t reserved;         /* must be 0                                                       */
     double  polish_switch;    /* mixed: stationarity at or below which, with the active set
                                  unchanged since the previous check, the FP64 free-set polish is
-                                 attempted (default 3e-2; x0.1 after each failed attempt)        */
+                                 attempted (x0.1 after each failed attempt); default 0 = auto:
+                                 0.1 with a check interval <= 10, else 3e-2                      */
 } bqp_options;
 
 /* Result of one solve (the numeric fields of QpResult plus engine accounting). */

@@ -37,7 +37,10 @@ def test_bindings_cover_the_header():
 def test_options_defaults_mirror_qpoptions():
     o = N.Options()
     boxqp.lib().bqp_options_default(o)
-    assert (o.tolerance, o.time_limit, o.iteration_limit, o.check_interval) == (1e-7, 30.0, 200000, 25)
+    # check_interval 0 and polish_switch 0 select the engine defaults (25 = the reference's cadence
+    # for the FP64 engines)
+    assert (o.tolerance, o.time_limit, o.iteration_limit, o.check_interval) == (1e-7, 30.0, 200000, 0)
+    assert o.polish_switch == 0
     assert o.precision == 0 and o.diagonal_gate == -1
 
 

@@ -29,7 +29,10 @@ def test_staggered_requests_overlap_and_match_solo_runs():
         for k, (inst, tol) in enumerate(reqs):
             futs.append(server.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'],
                                       inst['upper'], tol))
-            time.sleep(0.002 * (k % 3))
+            # a burst of six (queued behind the first launch, so admitted together), then arrivals
+            # staggered into the running batch
+            if k >= 6:
+                time.sleep(0.001 * (k % 3))
         mixed = [f.result(timeout=120) for f in futs]
         load = server.load()
     finally:
