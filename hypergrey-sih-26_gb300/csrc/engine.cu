@@ -247,6 +247,9 @@ public:
 private:
     void loop();
     bool admit(Job& j, std::string& why);
+    bool rearm(const std::vector<Job*>& batch, std::string& why);
+    void reset_record(Job& j);
+    void update_steps();
     bool run_once(std::string& why);
     bool run_stream(int cap, std::string& why);
     void update_grid();
@@ -290,6 +293,14 @@ private:
     Ctrl* h_ctrl_ = nullptr;       // pinned
     int32_t* h_status_ = nullptr;  // pinned
     int inst_cap_ = 0, tile_cap_ = 0;
+    // re-arm staging (pinned host / device): records, slots, row spans
+    InstDev* h_stage_ = nullptr;
+    InstDev* d_stage_ = nullptr;
+    int32_t* h_stage_slots_ = nullptr;
+    int32_t* d_stage_slots_ = nullptr;
+    int2* h_spans_ = nullptr;
+    int2* d_spans_ = nullptr;
+    int stage_cap_ = 0, span_cap_ = 0;
 
     // host mirrors
     std::vector<Tile> h_tiles_;
@@ -407,6 +418,14 @@ void Engine::shutdown() {
     d_inst_ = nullptr; d_ranges_ = nullptr; d_tile_done_ = nullptr; d_status_ = nullptr;
     d_tiles_ = nullptr; d_partial_ = nullptr; d_ctrl_ = nullptr;
     if (h_ctrl_) cudaFreeHost(h_ctrl_);
+    if (h_stage_) cudaFreeHost(h_stage_);
+    if (h_stage_slots_) cudaFreeHost(h_stage_slots_);
+    if (h_spans_) cudaFreeHost(h_spans_);
+    cudaFree(d_stage_);
+    cudaFree(d_stage_slots_);
+    cudaFree(d_spans_);
+    h_stage_ = nullptr; h_stage_slots_ = nullptr; h_spans_ = nullptr;
+    d_stage_ = nullptr; d_stage_slots_ = nullptr; d_spans_ = nullptr;
     if (h_status_) cudaFreeHost(h_status_);
     h_ctrl_ = nullptr;
     h_status_ = nullptr;
@@ -516,7 +535,7 @@ bool Engine::run_stream(int cap, std::string& why) {
             kernels += 2 + 3 * kCgPerBody;
         }
         if (profile_phases_) cudaEventRecord(pev_[3], stream_);
-        launch_control_plain(v, stream_);
+        launch_control_plain(v, K, stream_);
         kernels += 1;
         if (profile_phases_) cudaEventRecord(pev_[4], stream_);
         cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
@@ -629,7 +648,7 @@ bool Engine::build_graph(std::string& why) {
             }, nullptr)) return false;
         last = node;
     }
-    if (!capture(body, &last, 1, [&] { launch_control(v, h_loop, capture_); }, nullptr)) return false;
+    if (!capture(body, &last, 1, [&] { launch_control(v, h_loop, K, capture_); }, nullptr)) return false;
     if (!cuda_ok(cudaGraphInstantiate(&exec_, graph_, 0), why, "graph instantiate")) return false;
     graph_valid_ = true;
     return true;
@@ -755,7 +774,105 @@ int Engine::load(int64_t* queued, int64_t* running, int64_t* peak, int64_t* resi
     return BQP_OK;
 }
 
-// Uploads (or re-arms) one solve and appends its tiles.  Engine thread only.
+// Control state of a solve at its start (a new upload or a re-arm of a resident solve).
+void Engine::reset_record(Job& j) {
+    InstDev& R = j.rec;
+    R.status = ST_RUNNING;
+    R.phase = PH_FISTA;
+    R.polish_rounds = 0;
+    R.it0 = 0;
+    R.it_cur = 0;
+    R.it_next = 0;
+    R.t = 1.0;
+    R.deadline_ns = static_cast<int64_t>(std::min(j.opt.time_limit, 1e9) * 1e9);  // budget; made absolute on device
+    R.verified = 0;
+    R.stable_checks = 0;
+    R.active_hash = 0;
+    R.n_active = -1;
+    R.result_src = 0;
+    R.cg_it = 0;
+    R.cg_total = 0;
+    R.fista_iters = 0;
+    R.checks = 0;
+    R.iterations = 0;
+    R.arm_chunk = (j.opt.precision == PREC_MIXED && R.max_iter > 0) ? 1 : 0;
+}
+
+// Re-arms resident solves (bqp_resolve): one upload of the staged records and one kernel for the
+// whole batch.  Engine thread only.
+bool Engine::rearm(const std::vector<Job*>& batch, std::string& why) {
+    const int count = static_cast<int>(batch.size());
+    int spans = 0;
+    for (const Job* j : batch) spans += static_cast<int>((j->n + kRearmRows - 1) / kRearmRows);
+    if (count > stage_cap_) {
+        const int cap = std::max(count, std::max(256, 2 * stage_cap_));
+        if (h_stage_) cudaFreeHost(h_stage_);
+        if (h_stage_slots_) cudaFreeHost(h_stage_slots_);
+        cudaFree(d_stage_);
+        cudaFree(d_stage_slots_);
+        h_stage_ = nullptr; h_stage_slots_ = nullptr; d_stage_ = nullptr; d_stage_slots_ = nullptr;
+        stage_cap_ = 0;
+        if (!cuda_ok(cudaMallocHost(&h_stage_, sizeof(InstDev) * cap), why, "re-arm staging")) return false;
+        if (!cuda_ok(cudaMallocHost(&h_stage_slots_, sizeof(int32_t) * cap), why, "re-arm staging")) return false;
+        if (!cuda_ok(cudaMalloc(&d_stage_, sizeof(InstDev) * cap), why, "re-arm staging")) return false;
+        if (!cuda_ok(cudaMalloc(&d_stage_slots_, sizeof(int32_t) * cap), why, "re-arm staging")) return false;
+        stage_cap_ = cap;
+    }
+    if (spans > span_cap_) {
+        const int cap = std::max(spans, std::max(256, 2 * span_cap_));
+        if (h_spans_) cudaFreeHost(h_spans_);
+        cudaFree(d_spans_);
+        h_spans_ = nullptr; d_spans_ = nullptr;
+        span_cap_ = 0;
+        if (!cuda_ok(cudaMallocHost(&h_spans_, sizeof(int2) * cap), why, "re-arm staging")) return false;
+        if (!cuda_ok(cudaMalloc(&d_spans_, sizeof(int2) * cap), why, "re-arm staging")) return false;
+        span_cap_ = cap;
+    }
+    // the staging buffers are reused: the previous re-arm has completed (it was synchronized)
+    int s = 0;
+    for (int k = 0; k < count; ++k) {
+        Job& j = *batch[k];
+        reset_record(j);
+        h_stage_[k] = j.rec;
+        h_stage_slots_[k] = j.slot;
+        for (int64_t r = 0; r < j.n; r += kRearmRows) h_spans_[s++] = int2{k, static_cast<int>(r)};
+    }
+    cudaEventRecord(ev0_, stream_);
+    cudaMemcpyAsync(d_stage_, h_stage_, sizeof(InstDev) * count, cudaMemcpyHostToDevice, stream_);
+    cudaMemcpyAsync(d_stage_slots_, h_stage_slots_, sizeof(int32_t) * count, cudaMemcpyHostToDevice, stream_);
+    cudaMemcpyAsync(d_spans_, h_spans_, sizeof(int2) * spans, cudaMemcpyHostToDevice, stream_);
+    launch_rearm(view(), d_stage_, d_stage_slots_, d_spans_, spans, stream_);
+    cudaEventRecord(ev1_, stream_);
+    if (!cuda_ok(cudaEventSynchronize(ev1_), why, "re-arm")) return false;
+    if (!cuda_ok(cudaGetLastError(), why, "re-arm kernel")) return false;
+    // re-arming resident solves is part of their device time: count it in the timer
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    std::lock_guard<std::mutex> g(mu_);
+    timer_ms_ += ms;
+    timer_kernels_ += 1;
+    return true;
+}
+
+// Steps per body: the shortest check interval among the running solves (a longer chunk spans
+// several bodies; each solve checks at its own iterations whatever the batch).
+void Engine::update_steps() {
+    int steps = kMaxInterval;
+    bool any = false;
+    for (const Job* r : slot_job_)
+        if (r && r->state == JOB_RUNNING) {
+            steps = std::min(steps, r->rec.interval);
+            any = true;
+        }
+    if (!any) return;
+    steps = std::max(1, steps);
+    if (steps != graph_interval_) {
+        graph_interval_ = steps;
+        graph_valid_ = false;
+    }
+}
+
+// Uploads one new solve and appends its tiles.  Engine thread only.
 bool Engine::admit(Job& j, std::string& why) {
     const int prec = j.opt.precision;
     if (!j.resolve) {
@@ -834,25 +951,8 @@ bool Engine::admit(Job& j, std::string& why) {
         h_ranges_[slot] = int2{begin, static_cast<int>(h_tiles_.size())};
         tables_dirty_ = true;
     }
+    reset_record(j);
     InstDev& R = j.rec;
-    R.status = ST_RUNNING;
-    R.phase = PH_FISTA;
-    R.polish_rounds = 0;
-    R.it0 = 0;
-    R.it_next = 0;
-    R.t = 1.0;
-    R.deadline_ns = static_cast<int64_t>(std::min(j.opt.time_limit, 1e9) * 1e9);  // budget; made absolute on device
-    R.verified = 0;
-    R.stable_checks = 0;
-    R.active_hash = 0;
-    R.n_active = -1;
-    R.result_src = 0;
-    R.cg_it = 0;
-    R.cg_total = 0;
-    R.fista_iters = 0;
-    R.checks = 0;
-    R.iterations = 0;
-    R.skip_check = (prec == PREC_MIXED && R.max_iter > 0) ? 1 : 0;
     if (!cuda_ok(cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_), why, "instance record")) return false;
     if (tables_dirty_) {
         if (!h_tiles_.empty())
@@ -876,28 +976,8 @@ bool Engine::admit(Job& j, std::string& why) {
             launch_prepare_instance(v, j.slot, j.n, j.nnz, val, stream_);
         }
     }
-    if (j.resolve) cudaEventRecord(ev0_, stream_);
     launch_init_instance(v, j.slot, static_cast<int>(j.n), prec, stream_);
     if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
-    if (j.resolve) {
-        // re-arming a resident solve is part of its device time: count it in the timer
-        cudaEventRecord(ev1_, stream_);
-        cudaEventSynchronize(ev1_);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ev0_, ev1_);
-        std::lock_guard<std::mutex> g(mu_);
-        timer_ms_ += ms;
-        timer_kernels_ += 1;
-    }
-    // steps per body: the longest check interval among the resident solves
-    int steps = j.rec.interval;
-    for (const Job* r : slot_job_)
-        if (r && r != &j) steps = std::max(steps, r->rec.interval);
-    steps = std::min(steps, kMaxInterval);
-    if (steps != graph_interval_) {
-        graph_interval_ = steps;
-        graph_valid_ = false;
-    }
     const int grid_max = grid_max_;
     if (graph_grid_ < grid_max && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
     return true;
@@ -1059,6 +1139,7 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     R.status = ST_RUNNING;
     R.phase = PH_FISTA;
     R.it0 = 0;
+    R.it_cur = 0;
     R.it_next = 1LL << 40;
     for (int k = 0; k < kMaxInterval; ++k) R.beta[k] = 0.5;
     cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
@@ -1088,9 +1169,41 @@ void Engine::loop() {
     std::unique_lock<std::mutex> lk(mu_);
     while (!stop_) {
         if (!pending_free_.empty()) process_frees();
-        // admission: FIFO while the head fits under the cap
+        // admission: FIFO while the head fits under the cap; consecutive re-arms of resident
+        // solves go together in one upload and one kernel
+        bool admitted = false;
         while (!queue_.empty()) {
             Job* j = queue_.front();
+            if (j->resolve) {
+                std::vector<Job*> batch;
+                while (!queue_.empty() && queue_.front()->resolve) {
+                    batch.push_back(queue_.front());
+                    queue_.pop_front();
+                }
+                for (Job* b : batch) b->state = JOB_ADMITTING;
+                lk.unlock();
+                std::string why;
+                const bool ok = rearm(batch, why);
+                lk.lock();
+                for (Job* b : batch) {
+                    if (ok) {
+                        b->state = JOB_RUNNING;
+                        slot_job_[b->slot] = b;
+                        n_running_++;
+                    } else {
+                        b->error = BQP_ERR_CUDA;
+                        b->error_text = why;
+                        b->state = JOB_DONE;
+                        if (b->notify) completed_.push_back(b->id);
+                    }
+                }
+                if (!ok) {
+                    set_error(why);
+                    cv_done_.notify_all();
+                }
+                admitted = true;
+                continue;
+            }
             const size_t need = j->resolve ? 0 : make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
             if (!j->resolve && resident_bytes_ + need > cap_) {
                 if (n_running_ == 0) {
@@ -1116,9 +1229,7 @@ void Engine::loop() {
                 j->state = JOB_RUNNING;
                 slot_job_[j->slot] = j;
                 n_running_++;
-                int64_t resident = 0;
-                for (Job* s : slot_job_) if (s && s->state == JOB_RUNNING) resident++;
-                peak_resident_ = std::max(peak_resident_, resident);
+                admitted = true;
             } else {
                 resident_bytes_ -= need;
                 j->error = BQP_ERR_CUDA;
@@ -1128,6 +1239,10 @@ void Engine::loop() {
                 set_error(why);
                 cv_done_.notify_all();
             }
+        }
+        if (admitted) {
+            peak_resident_ = std::max(peak_resident_, n_running_);
+            update_steps();
         }
         if (n_running_ == 0) {
             if (queue_.empty() && pending_free_.empty()) cv_work_.wait(lk);

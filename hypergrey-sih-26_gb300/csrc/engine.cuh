@@ -15,6 +15,7 @@ constexpr int kBlock = 256;          // threads per CTA of every tile kernel
 constexpr int kMaxInterval = 32;     // maximum check interval (iterations per chunk)
 constexpr int kTileNnz = 4096;       // target nonzeros per tile
 constexpr int kTileRows = 512;       // maximum rows per tile
+constexpr int kRearmRows = 8192;     // rows per block when re-arming resident solves
 
 enum Phase : int32_t {
     PH_FISTA = 0,        // FISTA iterations (FP64 or FP32 per precision)
@@ -105,9 +106,10 @@ struct __align__(16) InstDev {
     int32_t polish_rounds;
     int32_t precision;
     int32_t polish;        // mixed: free-set polish enabled
-    int32_t skip_check;    // 1: the first body runs its steps without checking x0 (mixed)
-    int32_t pad_skip;
-    int64_t it0;          // iteration of the step j = 0 of the current chunk
+    int32_t arm_chunk;     // 1: admission arms the first chunk without a check of x0 (mixed)
+    int32_t pad_arm;
+    int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)
+    int64_t it_cur;        // iteration of the body's first step launch; a chunk may span bodies
     int64_t it_next;       // iteration of the next check
     int64_t max_iter;
     int64_t deadline_ns;   // %globaltimer deadline

@@ -585,6 +585,7 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
     }
     I.phase = PH_FISTA;
     I.it0 = it_check;
+    I.it_cur = it_check;
     I.it_next = it_check + I.interval < I.max_iter ? it_check + I.interval : I.max_iter;
     const int64_t count = I.it_next - I.it0;
     fista_betas(I, count);
@@ -758,14 +759,17 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j) {
     __syncthreads();  // prod is reused by the next tile
 }
 
+// Launch j0 of a body performs iteration it_cur + j0 of every instance whose chunk is not done.
 template <int PREC>
-__global__ void __launch_bounds__(kBlock) step_kernel(View v, int j) {
+__global__ void __launch_bounds__(kBlock) step_kernel(View v, int j0) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         const InstDev& I = v.inst[T.inst];
         if (I.status != ST_RUNNING || I.phase != PH_FISTA || I.precision != PREC) continue;
-        if (I.it0 + j >= I.it_next) continue;
+        const int64_t it = I.it_cur + j0;
+        if (it >= I.it_next) continue;
+        const int j = static_cast<int>(it - I.it0);  // position in the chunk
         if constexpr (PREC == PREC_FP64_EXACT) {
             step_rows_exact(I, T.row_begin, T.row_end, j);
         } else {
@@ -801,7 +805,8 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
         InstDev& I = v.inst[T.inst];
-        if (I.status != ST_RUNNING || I.skip_check) continue;
+        if (I.status != ST_RUNNING) continue;
+        if (I.phase == PH_FISTA && I.it_cur < I.it_next) continue;  // chunk still running
         if ((I.precision == PREC_MIXED) != (FAMILY != FAMILY_FP64)) continue;
         const int ph = I.phase;
         if (FAMILY == FAMILY_VERIFY ? ph != PH_POLISH_FINISH : ph != PH_FISTA) continue;
@@ -1130,12 +1135,16 @@ __device__ Counts count_phases(const View& v, bool mirror) {
     return c;
 }
 
-// The check kernels of this body have run: instances that skipped their first check take part
-// from the next body on.
-__device__ void clear_skip(const View& v) {
+// End of a body: every instance that stepped in it (FISTA phase) advances by the steps it ran.
+__device__ void advance_chunks(const View& v, int steps) {
     const int n = v.ctrl->n_inst;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (v.inst[i].skip_check) v.inst[i].skip_check = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        InstDev& I = v.inst[i];
+        if (I.status != ST_RUNNING || I.phase != PH_FISTA) continue;
+        const int64_t to = I.it_cur + steps;
+        I.it_cur = to < I.it_next ? to : I.it_next;
+    }
+    __syncthreads();
 }
 
 // The polish branch runs polish_init and the residual, then a CG loop whose iterations the
@@ -1144,7 +1153,6 @@ __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraph
                             cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish,
                             cudaGraphConditionalHandle h_cg, int steps) {
     const Counts c = count_phases(v, false);
-    clear_skip(v);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
@@ -1162,7 +1170,8 @@ __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraph
     }
 }
 
-__global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h) {
+__global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h, int steps) {
+    advance_chunks(v, steps);
     const Counts c = count_phases(v, true);
     if (threadIdx.x == 0) {
         Ctrl* ctrl = v.ctrl;
@@ -1175,7 +1184,6 @@ __global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h) {
 
 __global__ void gate_plain_kernel(View v) {
     const Counts c = count_phases(v, false);
-    clear_skip(v);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
         v.ctrl->n_polish = c.polish;
@@ -1184,7 +1192,8 @@ __global__ void gate_plain_kernel(View v) {
     }
 }
 
-__global__ void control_plain_kernel(View v) {
+__global__ void control_plain_kernel(View v, int steps) {
+    advance_chunks(v, steps);
     const Counts c = count_phases(v, true);
     if (threadIdx.x == 0) {
         v.ctrl->bodies++;
@@ -1192,32 +1201,58 @@ __global__ void control_plain_kernel(View v) {
     }
 }
 
-__global__ void init_instance_kernel(View v, int slot, int n, int precision) {
-    InstDev& I = v.inst[slot];
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-        if (precision == PREC_MIXED) {
-            const float x0 = smaxf(I.l32[r], sminf(I.u32[r], 0.0f));
-            I.x32[r] = x0;
-            I.w32[0][r] = x0;
-        } else {
-            const double x0 = smax(I.l[r], smin(I.u[r], 0.0));
-            I.x64[r] = x0;
-            I.w64[0][r] = x0;
-        }
+// x0 = clip(0, l, u) and w = x0 for row r (the pointers of a record do not change on re-arming).
+__device__ __forceinline__ void init_row(const InstDev& I, int r) {
+    if (I.precision == PREC_MIXED) {
+        const float x0 = smaxf(I.l32[r], sminf(I.u32[r], 0.0f));
+        I.x32[r] = x0;
+        I.w32[0][r] = x0;
+    } else {
+        const double x0 = smax(I.l[r], smin(I.u[r], 0.0));
+        I.x64[r] = x0;
+        I.w64[0][r] = x0;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+}
+
+// Start of a solve: clock, deadline and (mixed) the first chunk.  One thread.
+__device__ void start_instance(InstDev& I) {
         const int64_t start = now_ns();
         I.start_ns = start;
         I.deadline_ns = start + I.deadline_ns;  // host stores the budget in nanoseconds
         I.end_ns = 0;
-        if (I.skip_check) {
+        if (I.arm_chunk) {
             // mixed precision: x0 = clip(0) is not checked; the first chunk of steps is armed here
             // as a check of x0 would arm it (the first check then comes after `interval` steps)
             I.it0 = 0;
+            I.it_cur = 0;
             I.it_next = I.interval < I.max_iter ? I.interval : I.max_iter;
             fista_betas(I, I.it_next);
             I.fista_iters += I.it_next;
         }
+}
+
+__global__ void init_instance_kernel(View v, int slot, int n) {
+    InstDev& I = v.inst[slot];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) init_row(I, r);
+    if (blockIdx.x == 0 && threadIdx.x == 0) start_instance(I);
+}
+
+// Re-arms a list of resident solves in one launch.  Block b takes rows [span.y, span.y + kRearmRows)
+// of staged record span.x; the block holding row 0 also installs the record in its slot and
+// starts the solve.
+__global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __restrict__ stage,
+                                                       const int32_t* __restrict__ slots, const int2* __restrict__ spans) {
+    const int2 sp = spans[blockIdx.x];
+    const InstDev& S = stage[sp.x];
+    const int end = S.n < sp.y + kRearmRows ? S.n : sp.y + kRearmRows;
+    for (int r = sp.y + static_cast<int>(threadIdx.x); r < end; r += kBlock) init_row(S, r);
+    if (sp.y == 0) {
+        InstDev& I = v.inst[slots[sp.x]];
+        const uint4* src = reinterpret_cast<const uint4*>(&S);
+        uint4* dst = reinterpret_cast<uint4*>(&I);
+        for (int w = threadIdx.x; w < static_cast<int>(sizeof(InstDev) / 16); w += kBlock) dst[w] = src[w];
+        __syncthreads();
+        if (threadIdx.x == 0) start_instance(I);
     }
 }
 
@@ -1401,17 +1436,23 @@ void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGra
                  cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s) {
     gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, cg_loop, steps);
 }
-void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s) {
-    control_kernel<<<1, 1024, 0, s>>>(v, loop);
+void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s) {
+    control_kernel<<<1, 1024, 0, s>>>(v, loop, steps);
 }
 void launch_gate_plain(const View& v, cudaStream_t s) { gate_plain_kernel<<<1, 1024, 0, s>>>(v); }
-void launch_control_plain(const View& v, cudaStream_t s) { control_plain_kernel<<<1, 1024, 0, s>>>(v); }
+void launch_control_plain(const View& v, int steps, cudaStream_t s) { control_plain_kernel<<<1, 1024, 0, s>>>(v, steps); }
 
 void launch_init_instance(const View& v, int slot, int n, int precision, cudaStream_t s) {
     int grid = (n + kBlock - 1) / kBlock;
     if (grid > 4096) grid = 4096;
     if (grid < 1) grid = 1;
-    init_instance_kernel<<<grid, kBlock, 0, s>>>(v, slot, n, precision);
+    (void)precision;
+    init_instance_kernel<<<grid, kBlock, 0, s>>>(v, slot, n);
+}
+
+void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, const int2* spans, int n_spans,
+                  cudaStream_t s) {
+    if (n_spans > 0) rearm_kernel<<<n_spans, kBlock, 0, s>>>(v, stage, slots, spans);
 }
 
 void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {

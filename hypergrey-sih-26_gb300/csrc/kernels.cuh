@@ -23,13 +23,18 @@ void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphCondi
 // polish branch; cg_loop: the WHILE node of its CG loop.  `steps`: kernels inside each FISTA body.
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
                  cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s);
-void launch_control(const View& v, cudaGraphConditionalHandle loop, cudaStream_t s);
+// `steps`: step launches per body; FISTA-phase instances advance it_cur by up to that many.
+void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s);
 // Host-driven variants of the control kernels (no conditional handles).
 void launch_gate_plain(const View& v, cudaStream_t s);
-void launch_control_plain(const View& v, cudaStream_t s);
+void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
 void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
 // Admission: x0 = clip(0, l, u), w = x0, start clock; one instance.
+// Re-arm of resident solves: records staged on the device, spans (staged index, first row) of
+// kRearmRows rows each, one block per span.
+void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, const int2* spans, int n_spans,
+                  cudaStream_t s);
 void launch_init_instance(const View& v, int slot, int n, int precision, cudaStream_t s);
 
 // Standalone FP64 check on caller device arrays (one instance, block partials in scratch).
