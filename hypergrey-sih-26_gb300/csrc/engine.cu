@@ -164,14 +164,21 @@ int default_variant(int64_t n, int64_t nnz, int precision) {
 }
 
 // Row tiles of one instance: contiguous rows with about kTileNnz nonzeros and at most
-// kTileRows rows.  Depends on the instance alone, so its reductions are the same whether it
-// runs alone or inside any batch.
+// kTileRows rows, the row count rounded down to a multiple of 256 (one 32-row group per warp of
+// a block) or else of 32 where that many fit, so that the warps of a block finish a tile together.
+// Depends on the instance alone, so its reductions are the same whether it runs alone or inside
+// any batch.
 std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int variant) {
     std::vector<Tile> t;
     int64_t r = 0;
     while (r < n) {
         int64_t e = r + 1;
         while (e < n && e - r < kTileRows && static_cast<int64_t>(rowptr[e + 1]) - rowptr[r] <= kTileNnz) ++e;
+        if (e < n) {
+            const int64_t rows = e - r;
+            if (rows >= kBlock) e = r + rows / kBlock * kBlock;
+            else if (rows >= 32) e = r + rows / 32 * 32;
+        }
         t.push_back(Tile{0, static_cast<int32_t>(r), static_cast<int32_t>(e), variant});
         r = e;
     }
@@ -527,12 +534,18 @@ bool Engine::run_stream(int cap, std::string& why) {
         if (h_ctrl_->n_polish > 0) {
             launch_polish_init(v, grid, stream_);
             launch_polish_residual(v, grid, stream_);
+            kernels += 2;
+            // the CG loop as the graph runs it: stop once no instance iterates (read back after
+            // every iteration; this mode serves per-kernel profiling, not speed)
             for (int j = 0; j < kCgPerBody; ++j) {
                 launch_cg_matvec(v, grid, stream_);
                 launch_cg_update(v, grid, stream_);
                 launch_cg_direction(v, grid, stream_);
+                kernels += 3;
+                cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
+                if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine polish")) return false;
+                if (h_ctrl_->n_cg <= 0) break;
             }
-            kernels += 2 + 3 * kCgPerBody;
         }
         if (profile_phases_) cudaEventRecord(pev_[3], stream_);
         launch_control_plain(v, K, stream_);

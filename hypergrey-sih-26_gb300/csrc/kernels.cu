@@ -320,15 +320,9 @@ __device__ __forceinline__ void warp_groups(const int32_t* __restrict__ rowptr, 
 // its 32 / LANES sub-groups of LANES lanes form one row sum each (the memory pattern of the tuned
 // sub-warp step kernel), and shuffles hand every row sum to its own lane, so the epilogue of the
 // 32 rows runs with all 32 lanes active.  Fixed summation order (lane-strided partials, xor tree).
-struct SameRow {
-    __device__ __forceinline__ int operator()(int j) const { return j; }
-};
-
-// Positions [rb, re) name rows through row(j): the identity for a tile's row range, or a list of
-// rows (the free rows of a polish tile).  The summation order of one row does not depend on it.
-template <int LANES, class T, class Prod, class Add, class Epi, class Map = SameRow>
+template <int LANES, class T, class Prod, class Add, class Epi>
 __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr, int rb, int re, Prod prod, Add add,
-                                             T zero, Epi epi, Map row = Map()) {
+                                             T zero, Epi epi) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -336,10 +330,9 @@ __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr,
         T mine = zero;
 #pragma unroll
         for (int pass = 0; pass < LANES; ++pass) {
-            const int j = base + pass * R + sub;
+            const int r = base + pass * R + sub;
             T acc = zero;
-            if (j < re) {
-                const int r = row(j);
+            if (r < re) {
                 const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
 #pragma unroll 4
                 for (int k = ks + sl; k < ke; k += LANES) acc = add(acc, prod(k));
@@ -351,8 +344,8 @@ __device__ __forceinline__ void subwarp_rows(const int32_t* __restrict__ rowptr,
             const T got = shfl_idx(acc, (mine_now ? g : 0) * LANES);
             if (mine_now) mine = got;
         }
-        const int j = base + lane;
-        if (j < re) epi(row(j), mine);
+        const int r = base + lane;
+        if (r < re) epi(r, mine);
     }
 }
 
@@ -896,15 +889,36 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
     }
 }
 
-struct ListRow {
-    const int32_t* list;
-    __device__ __forceinline__ int operator()(int j) const { return list[j]; }
-};
+// Rows of a free-row list, LANES lanes per row: the warps of the block take the list in turns of
+// 32 / LANES rows (one pass each), so a tile's few hundred free rows spread evenly over the block,
+// and the leading lane of each group runs the row's epilogue.  Per row the same summation as
+// subwarp_rows: lane-strided partial sums, then an xor tree over the group.
+template <int LANES, class Prod, class Epi>
+__device__ __forceinline__ void list_rows(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ list, int n,
+                                          Prod prod, Epi epi) {
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
+        const int j = g * R + sub;
+        float2 acc = make_float2(0.f, 0.f);
+        int r = -1;
+        if (j < n) {
+            r = list[j];
+            const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+#pragma unroll 4
+            for (int k = ks + sl; k < ke; k += LANES) acc = df_add(acc, prod(k));
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
+        if (sl == 0 && r >= 0) epi(r, acc);
+    }
+}
 
 // q = Q src on the tile's free rows, src given as FP32 pairs.  residual = true: r = -(Q xp + c),
 // z = D^-1 r, p = z on the free rows, accumulating r.z and max |r|/(1+|x|).  The sub-warp variants
-// visit the free-row list; the staged variants (long rows) run every row and skip fixed ones in
-// the epilogue.
+// visit the free-row list (list_rows); the staged variants (long rows) run every row and skip
+// fixed ones in the epilogue.
 template <bool RESIDUAL>
 __device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re, int n_free,
                                    const float2* __restrict__ src, Acc& a) {
@@ -943,14 +957,14 @@ __device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re
         }
     };
     const float2 zero = make_float2(0.f, 0.f);
-    const ListRow list{I.free_rows + rb};
+    const int32_t* list = I.free_rows + rb;
     switch (variant) {
-    case 1: subwarp_rows<1, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
-    case 2: subwarp_rows<2, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
-    case 4: subwarp_rows<4, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
-    case 8: subwarp_rows<8, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
-    case 16: subwarp_rows<16, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
-    case 32: subwarp_rows<32, float2>(I.rowptr, 0, n_free, prod, add, zero, epi, list); break;
+    case 1: list_rows<1>(I.rowptr, list, n_free, prod, epi); break;
+    case 2: list_rows<2>(I.rowptr, list, n_free, prod, epi); break;
+    case 4: list_rows<4>(I.rowptr, list, n_free, prod, epi); break;
+    case 8: list_rows<8>(I.rowptr, list, n_free, prod, epi); break;
+    case 16: list_rows<16>(I.rowptr, list, n_free, prod, epi); break;
+    case 32: list_rows<32>(I.rowptr, list, n_free, prod, epi); break;
     default: warp_groups<float2>(I.rowptr, rb, re, warp_buffer<float2>(), prod, add, zero, epi); break;
     }
 }
