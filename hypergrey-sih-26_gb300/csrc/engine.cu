@@ -809,6 +809,8 @@ void Engine::reset_record(Job& j) {
     R.checks = 0;
     R.iterations = 0;
     R.arm_chunk = (j.opt.precision == PREC_MIXED && R.max_iter > 0) ? 1 : 0;
+    R.moved[0] = 0;
+    R.moved[1] = 0;
 }
 
 // Re-arms resident solves (bqp_resolve): one upload of the staged records and one kernel for the

@@ -108,6 +108,7 @@ struct __align__(16) InstDev {
     int32_t polish;        // mixed: free-set polish enabled
     int32_t arm_chunk;     // 1: admission arms the first chunk without a check of x0 (mixed)
     int32_t pad_arm;
+    int32_t moved[2];      // mixed: a variable entered or left a bound in the chunk's last two steps
     int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)
     int64_t it_cur;        // iteration of the body's first step launch; a chunk may span bodies
     int64_t it_next;       // iteration of the next check

@@ -570,7 +570,9 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
         I.n_active = tot.nact;
         double sw = I.polish_switch;
         for (int k = 0; k < I.polish_rounds; ++k) sw *= 0.1;
-        if (I.stable_checks >= 1 && stat <= sw) {
+        // the chunk's last three iterates share their active set (no move in its last two steps)
+        const bool step_stable = it_check - I.it0 >= 2 && I.moved[0] == 0 && I.moved[1] == 0;
+        if ((I.stable_checks >= 1 && stat <= sw) || (step_stable && stat <= 3.0 * sw)) {
             I.phase = PH_POLISH_INIT;
             I.cg_it = 0;
             return;
@@ -579,6 +581,8 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
     I.phase = PH_FISTA;
     I.it0 = it_check;
     I.it_cur = it_check;
+    I.moved[0] = 0;
+    I.moved[1] = 0;
     I.it_next = it_check + I.interval < I.max_iter ? it_check + I.interval : I.max_iter;
     const int64_t count = I.it_next - I.it0;
     fista_betas(I, count);
@@ -586,6 +590,19 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
 }
 
 // ---- step kernel ------------------------------------------------------------------------------
+// Active-set motion (mixed precision): in the last two steps of a chunk the step kernel records
+// whether any variable entered or left a bound (track = 0 / 1; -1 elsewhere).  A chunk whose last
+// three iterates share their active set is "step-stable", which lets the check start the polish
+// without waiting for a second check with the same active set.
+__device__ __forceinline__ int bound_state(float x, float lo, float up) { return x <= lo ? 1 : (x >= up ? 2 : 0); }
+__device__ __forceinline__ void flag_moves(const InstDev& I, int track, bool moved) {
+    if (track < 0) return;
+    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) {
+        volatile int32_t* f = const_cast<volatile int32_t*>(&I.moved[track]);
+        if (*f == 0) *f = 1;
+    }
+}
+
 // EXACT precision: one thread per row, products and sums rounded separately in column order from
 // 0.0 and division by L -- the reference CPU loop's arithmetic exactly.
 __device__ void step_rows_exact(const InstDev& I, int rb, int re, int j) {
@@ -616,7 +633,7 @@ __device__ void step_rows_exact(const InstDev& I, int rb, int re, int j) {
 // FISTA step of rows [rb, re) with warp-staged products: g = Q w, then
 // x+ = clip(w - (g + c) / L), w+ = x+ + beta (x+ - x).
 template <int PREC>
-__device__ void step_rows_staged(const InstDev& I, int rb, int re, int j) {
+__device__ void step_rows_staged(const InstDev& I, int rb, int re, int j, int track) {
     const int64_t it = I.it0 + j;
     const int in = static_cast<int>(it & 1), out = in ^ 1;
     const int32_t* __restrict__ col = I.col;
@@ -631,15 +648,20 @@ __device__ void step_rows_staged(const InstDev& I, int rb, int re, int j) {
         const float beta = static_cast<float>(I.beta[j]);
         const float invL = I.invLf;
         float* buf = warp_buffer<float>();
+        bool moved = false;
         warp_groups<float>(
             I.rowptr, rb, re, buf, [&](int k) { return __ldg(val + k) * __ldg(win + __ldg(col + k)); },
             [](float a, float b) { return a + b; }, 0.f,
             [&](int r, float g) {
                 const float v = __ldg(win + r) - (g + __ldg(c + r)) * invL;
-                const float nx = smaxf(__ldg(l + r), sminf(__ldg(u + r), v));
-                wout[r] = nx + beta * (nx - x[r]);
+                const float lo = __ldg(l + r), up = __ldg(u + r);
+                const float nx = smaxf(lo, sminf(up, v));
+                const float xo = x[r];
+                wout[r] = nx + beta * (nx - xo);
                 x[r] = nx;
+                moved |= bound_state(xo, lo, up) != bound_state(nx, lo, up);
             });
+        flag_moves(I, track, moved);
     } else {
         const double* __restrict__ val = I.val64;
         const double* __restrict__ win = I.w64[in];
@@ -665,7 +687,7 @@ __device__ void step_rows_staged(const InstDev& I, int rb, int re, int j) {
 
 // Sub-warp rows: LANES lanes per row, a group of 32 / LANES rows per warp pass.
 template <int LANES, int PREC>
-__device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j) {
+__device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j, int track) {
     using T = typename std::conditional<PREC == PREC_MIXED, float, double>::type;
     const int64_t it = I.it0 + j;
     const int in = static_cast<int>(it & 1), out = in ^ 1;
@@ -689,6 +711,7 @@ __device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j) {
         val = I.val64; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
         beta = I.beta[j]; invL = I.invL;
     }
+    bool moved = false;
     for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
         const int r = base + sub;
         T acc = 0;
@@ -702,16 +725,19 @@ __device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j) {
             const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
             const T lo = __ldg(l + r), up = __ldg(u + r);
             const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
-            wout[r] = nx + beta * (nx - x[r]);
+            const T xo = x[r];
+            wout[r] = nx + beta * (nx - xo);
             x[r] = nx;
+            if constexpr (PREC == PREC_MIXED) moved |= bound_state(xo, lo, up) != bound_state(nx, lo, up);
         }
     }
+    if constexpr (PREC == PREC_MIXED) flag_moves(I, track, moved);
 }
 
 // Block-staged tile (nnz <= kTileNnz): the tile's products are formed by all threads at once
 // (kTileNnz / kBlock independent gathers per thread), then one thread per row sums and updates.
 template <int PREC>
-__device__ void step_tile_block(const InstDev& I, int rb, int re, int j) {
+__device__ void step_tile_block(const InstDev& I, int rb, int re, int j, int track) {
     using T = typename std::conditional<PREC == PREC_MIXED, float, double>::type;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     T* prod = reinterpret_cast<T*>(dyn_smem);
@@ -739,6 +765,7 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j) {
 #pragma unroll 8
     for (int k = threadIdx.x; k < cnt; k += kBlock) prod[k] = __ldg(val + k) * __ldg(win + __ldg(cl + k));
     __syncthreads();
+    bool moved = false;
     for (int r = rb + static_cast<int>(threadIdx.x); r < re; r += kBlock) {
         const int a = __ldg(rowptr + r) - kb, b = __ldg(rowptr + r + 1) - kb;
         T acc = 0;
@@ -746,9 +773,12 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j) {
         const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
         const T lo = __ldg(l + r), up = __ldg(u + r);
         const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
-        wout[r] = nx + beta * (nx - x[r]);
+        const T xo = x[r];
+        wout[r] = nx + beta * (nx - xo);
         x[r] = nx;
+        if constexpr (PREC == PREC_MIXED) moved |= bound_state(xo, lo, up) != bound_state(nx, lo, up);
     }
+    if constexpr (PREC == PREC_MIXED) flag_moves(I, track, moved);
     __syncthreads();  // prod is reused by the next tile
 }
 
@@ -763,23 +793,25 @@ __global__ void __launch_bounds__(kBlock) step_kernel(View v, int j0) {
         const int64_t it = I.it_cur + j0;
         if (it >= I.it_next) continue;
         const int j = static_cast<int>(it - I.it0);  // position in the chunk
+        const int count = static_cast<int>(I.it_next - I.it0);
+        const int track = (PREC == PREC_MIXED && count >= 2 && j >= count - 2) ? j - (count - 2) : -1;
         if constexpr (PREC == PREC_FP64_EXACT) {
             step_rows_exact(I, T.row_begin, T.row_end, j);
         } else {
             switch (T.variant) {
             case VAR_TILE:
                 if (__ldg(I.rowptr + T.row_end) - __ldg(I.rowptr + T.row_begin) <= kTileNnz)
-                    step_tile_block<PREC>(I, T.row_begin, T.row_end, j);
+                    step_tile_block<PREC>(I, T.row_begin, T.row_end, j, track);
                 else
-                    step_rows_staged<PREC>(I, T.row_begin, T.row_end, j);
+                    step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track);
                 break;
-            case VAR_WARP: step_rows_staged<PREC>(I, T.row_begin, T.row_end, j); break;
-            case 1: step_rows_subwarp<1, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 2: step_rows_subwarp<2, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 4: step_rows_subwarp<4, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 8: step_rows_subwarp<8, PREC>(I, T.row_begin, T.row_end, j); break;
-            case 16: step_rows_subwarp<16, PREC>(I, T.row_begin, T.row_end, j); break;
-            default: step_rows_subwarp<32, PREC>(I, T.row_begin, T.row_end, j); break;
+            case VAR_WARP: step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track); break;
+            case 1: step_rows_subwarp<1, PREC>(I, T.row_begin, T.row_end, j, track); break;
+            case 2: step_rows_subwarp<2, PREC>(I, T.row_begin, T.row_end, j, track); break;
+            case 4: step_rows_subwarp<4, PREC>(I, T.row_begin, T.row_end, j, track); break;
+            case 8: step_rows_subwarp<8, PREC>(I, T.row_begin, T.row_end, j, track); break;
+            case 16: step_rows_subwarp<16, PREC>(I, T.row_begin, T.row_end, j, track); break;
+            default: step_rows_subwarp<32, PREC>(I, T.row_begin, T.row_end, j, track); break;
             }
         }
     }
@@ -1239,6 +1271,8 @@ __device__ void start_instance(InstDev& I) {
             // as a check of x0 would arm it (the first check then comes after `interval` steps)
             I.it0 = 0;
             I.it_cur = 0;
+            I.moved[0] = 0;
+            I.moved[1] = 0;
             I.it_next = I.interval < I.max_iter ? I.interval : I.max_iter;
             fista_betas(I, I.it_next);
             I.fista_iters += I.it_next;
