@@ -41,6 +41,16 @@ double host_seconds() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// BOXQP_PROFILE=1 also prints host-side times of each submission and admission to stderr.
+bool host_profile() {
+    static const bool on = [] {
+        const char* m = std::getenv("BOXQP_PROFILE");
+        return m && std::string(m) == "1";
+    }();
+    return on;
+}
+
+
 size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 constexpr int kCgPerBody = 25;  // CG iterations per polish body
 constexpr size_t kNone = std::numeric_limits<size_t>::max();
@@ -111,13 +121,58 @@ T* at(void* base, size_t off) {
 
 enum JobState { JOB_QUEUED = 0, JOB_ADMITTING = 1, JOB_RUNNING = 2, JOB_DONE = 3 };
 
+// Host copies of submitted inputs (asynchronous submit) live in buffers kept for reuse: a fresh
+// allocation of a few hundred MB costs more in first-touch page faults than the copy itself.
+class HostBufferCache {
+public:
+    static HostBufferCache& get() {
+        static HostBufferCache* cache = new HostBufferCache;  // never destroyed: usable at exit
+        return *cache;
+    }
+    char* acquire(size_t bytes, size_t* got) {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            size_t best = free_.size();
+            for (size_t k = 0; k < free_.size(); ++k)
+                if (free_[k].second >= bytes && free_[k].second <= 2 * bytes + (1 << 20) &&
+                    (best == free_.size() || free_[k].second < free_[best].second))
+                    best = k;
+            if (best != free_.size()) {
+                char* p = free_[best].first;
+                *got = free_[best].second;
+                cached_ -= *got;
+                free_.erase(free_.begin() + static_cast<std::ptrdiff_t>(best));
+                return p;
+            }
+        }
+        *got = bytes;
+        return static_cast<char*>(std::malloc(bytes ? bytes : 1));
+    }
+    void release(char* p, size_t bytes) {
+        if (!p) return;
+        std::lock_guard<std::mutex> g(mu_);
+        if (cached_ + bytes > kLimit) {
+            std::free(p);
+            return;
+        }
+        free_.emplace_back(p, bytes);
+        cached_ += bytes;
+    }
+
+private:
+    static constexpr size_t kLimit = size_t(4) << 30;
+    std::mutex mu_;
+    std::vector<std::pair<char*, size_t>> free_;
+    size_t cached_ = 0;
+};
+
 struct Job {
     uint64_t id = 0;
     int64_t n = 0, nnz = 0;
     bqp_options opt{};
-    // owned copies (asynchronous submit) or borrowed pointers (synchronous solve)
-    std::vector<int32_t> own_rowptr, own_col;
-    std::vector<double> own_val, own_c, own_l, own_u;
+    // owned copy in one cached host buffer (asynchronous submit) or borrowed pointers (synchronous solve)
+    char* own = nullptr;
+    size_t own_bytes = 0;
     const int32_t* rowptr = nullptr;
     const int32_t* col = nullptr;
     const double* val = nullptr;
@@ -142,15 +197,13 @@ struct Job {
     std::vector<double> x;
     std::vector<float> x32_tmp;
     double t_submit = 0, t_done = 0;
+    ~Job() { HostBufferCache::get().release(own, own_bytes); }
 };
 
 void free_inputs(Job& j) {
-    std::vector<int32_t>().swap(j.own_rowptr);
-    std::vector<int32_t>().swap(j.own_col);
-    std::vector<double>().swap(j.own_val);
-    std::vector<double>().swap(j.own_c);
-    std::vector<double>().swap(j.own_l);
-    std::vector<double>().swap(j.own_u);
+    HostBufferCache::get().release(j.own, j.own_bytes);
+    j.own = nullptr;
+    j.own_bytes = 0;
     j.rowptr = nullptr; j.col = nullptr; j.val = nullptr; j.c = nullptr; j.l = nullptr; j.u = nullptr;
 }
 
@@ -889,6 +942,7 @@ void Engine::update_steps() {
 
 // Uploads one new solve and appends its tiles.  Engine thread only.
 bool Engine::admit(Job& j, std::string& why) {
+    const double t0 = host_seconds();
     const int prec = j.opt.precision;
     if (!j.resolve) {
         j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
@@ -993,6 +1047,12 @@ bool Engine::admit(Job& j, std::string& why) {
     }
     launch_init_instance(v, j.slot, static_cast<int>(j.n), prec, stream_);
     if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
+    if (host_profile()) {
+        const double t1 = host_seconds();
+        cudaStreamSynchronize(stream_);
+        std::fprintf(stderr, "[boxqp] admit n=%lld: enqueue %.3f ms, device done %.3f ms\n", static_cast<long long>(j.n),
+                     1e3 * (t1 - t0), 1e3 * (host_seconds() - t0));
+    }
     const int grid_max = grid_max_;
     if (graph_grid_ < grid_max && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
     return true;
@@ -1336,8 +1396,18 @@ struct Scan {
     bool infeasible = false;
 };
 
+// Destination of the host copy taken during the scan (asynchronous submit), or all null.
+struct InputCopy {
+    int32_t* rowptr = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+    double* c = nullptr;
+    double* l = nullptr;
+    double* u = nullptr;
+};
+
 Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
-               const double* c, const double* l, const double* u) {
+               const double* c, const double* l, const double* u, const InputCopy& dst) {
     Scan s;
     for (int64_t i = r0; i < r1; ++i) {
         const int64_t a = rowptr[i], b = rowptr[i + 1];
@@ -1362,17 +1432,27 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
         if (!(d > 0)) s.positive = false;
         s.lipschitz = std::max(s.lipschitz, abs_sum);
     }
+    if (dst.rowptr && r1 > r0) {
+        // rows [r0, r1) validated: their nonzeros are [rowptr[r0], rowptr[r1]) within [0, nnz]
+        const int64_t k0 = rowptr[r0], k1 = rowptr[r1];
+        std::memcpy(dst.rowptr + r0, rowptr + r0, sizeof(int32_t) * static_cast<size_t>(r1 - r0 + (r1 == n ? 1 : 0)));
+        std::memcpy(dst.col + k0, col + k0, sizeof(int32_t) * static_cast<size_t>(k1 - k0));
+        std::memcpy(dst.val + k0, val + k0, sizeof(double) * static_cast<size_t>(k1 - k0));
+        std::memcpy(dst.c + r0, c + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
+        std::memcpy(dst.l + r0, l + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
+        std::memcpy(dst.u + r0, u + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
+    }
     return s;
 }
 
 Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
-                  const double* c, const double* l, const double* u) {
+                  const double* c, const double* l, const double* u, const InputCopy& dst) {
     unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     int64_t threads = std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, nnz / 500000));
     std::vector<Scan> part(static_cast<size_t>(threads));
     auto work = [&](int64_t t) {
         const int64_t r0 = n * t / threads, r1 = n * (t + 1) / threads;
-        part[t] = scan_rows(r0, r1, n, nnz, rowptr, col, val, c, l, u);
+        part[t] = scan_rows(r0, r1, n, nnz, rowptr, col, val, c, l, u, dst);
     };
     if (threads == 1) {
         work(0);
@@ -1396,23 +1476,48 @@ Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* 
 int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
              const double* c, const double* l, const double* u, const bqp_options* options, bool copy,
              Job** out, std::string& why) {
+    using bqp::host_seconds;
+    using bqp::host_profile;
+    using bqp::align_up;
+    using bqp::HostBufferCache;
+    const double t0 = host_seconds();
     bqp_options o;
     if (options) o = *options;
     else bqp_options_default(&o);
     int rc = validate_problem(n, nnz, rowptr, col, val, c, l, u, &o, why);
     if (rc != BQP_OK) return rc;
-    const Scan scan = scan_problem(n, nnz, rowptr, col, val, c, l, u);
+    std::unique_ptr<Job> j(new Job);
+    InputCopy dst;
+    if (copy) {
+        // one cached host buffer: rowptr, col, val, c, l, u (64-byte aligned sections)
+        const size_t N = static_cast<size_t>(n), Z = static_cast<size_t>(nnz);
+        const size_t o_col = align_up((N + 1) * 4, 64), o_val = o_col + align_up(Z * 4, 64);
+        const size_t o_c = o_val + align_up(Z * 8, 64), o_l = o_c + align_up(N * 8, 64), o_u = o_l + align_up(N * 8, 64);
+        const size_t bytes = o_u + N * 8;
+        j->own = HostBufferCache::get().acquire(bytes, &j->own_bytes);
+        if (!j->own) {
+            why = "host memory for the input copy";
+            return BQP_ERR_NO_MEMORY;
+        }
+        dst.rowptr = reinterpret_cast<int32_t*>(j->own);
+        dst.col = reinterpret_cast<int32_t*>(j->own + o_col);
+        dst.val = reinterpret_cast<double*>(j->own + o_val);
+        dst.c = reinterpret_cast<double*>(j->own + o_c);
+        dst.l = reinterpret_cast<double*>(j->own + o_l);
+        dst.u = reinterpret_cast<double*>(j->own + o_u);
+    }
+    const Scan scan = scan_problem(n, nnz, rowptr, col, val, c, l, u, dst);
     if (scan.error) {
         why = scan.error == 1 ? "Invalid CSR row pointers"
                               : scan.error == 2 ? "Invalid variable coefficient or bound" : "Invalid Hessian";
         return BQP_ERR_INVALID;
     }
+    const double t_scan = host_seconds();
     const double lipschitz = scan.lipschitz;
     if (lipschitz == 0) {
         why = "Zero-Hessian models use the CPU LP path";
         return BQP_ERR_UNSUPPORTED;
     }
-    std::unique_ptr<Job> j(new Job);
     j->n = n;
     j->nnz = nnz;
     j->opt = o;
@@ -1440,22 +1545,16 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     else if (o.kernel_variant >= 0) j->variant = o.kernel_variant;
     else j->variant = bqp::default_variant(n, nnz, o.precision);
     j->tiles = bqp::make_tiles(n, rowptr, j->variant);
+    const double t_tiles = host_seconds();
     if (copy) {
-        j->own_rowptr.assign(rowptr, rowptr + n + 1);
-        j->own_col.assign(col, col + nnz);
-        j->own_val.assign(val, val + nnz);
-        j->own_c.assign(c, c + n);
-        j->own_l.assign(l, l + n);
-        j->own_u.assign(u, u + n);
-        j->rowptr = j->own_rowptr.data();
-        j->col = j->own_col.data();
-        j->val = j->own_val.data();
-        j->c = j->own_c.data();
-        j->l = j->own_l.data();
-        j->u = j->own_u.data();
+        j->rowptr = dst.rowptr; j->col = dst.col; j->val = dst.val; j->c = dst.c; j->l = dst.l; j->u = dst.u;
     } else {
         j->rowptr = rowptr; j->col = col; j->val = val; j->c = c; j->l = l; j->u = u;
     }
+    if (host_profile())
+        std::fprintf(stderr, "[boxqp] submit n=%lld: validate+scan %.3f ms, tiles %.3f ms, copy %.3f ms\n",
+                     static_cast<long long>(n), 1e3 * (t_scan - t0), 1e3 * (t_tiles - t_scan),
+                     1e3 * (host_seconds() - t_tiles));
     *out = j.release();
     return BQP_OK;
 }
