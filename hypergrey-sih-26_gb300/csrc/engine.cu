@@ -62,6 +62,7 @@ struct Layout {
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
+    size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone;
     size_t total = 0;
 };
 
@@ -105,6 +106,10 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.fixed = take(N);
         L.free_rows = take(N * 4);
         L.free_cnt = take(static_cast<size_t>(tiles) * 4);
+        L.col_ff = take(Z * 4);
+        L.hi_ff = take(Z * 4);
+        L.lo_ff = take(Z * 4);
+        L.cnt_ff = take(N * 4);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
@@ -802,6 +807,10 @@ int Engine::release(uint64_t id) {
     }
     completed_.erase(std::remove(completed_.begin(), completed_.end(), id), completed_.end());
     if (j.resident) {
+        // the job object dies below: the engine thread must not see it through its slot (its
+        // slot, tiles and slab are reclaimed at the next loop iteration)
+        if (j.slot >= 0 && j.slot < static_cast<int>(slot_job_.size()) && slot_job_[j.slot] == &j)
+            slot_job_[j.slot] = nullptr;
         pending_free_.emplace_back(j.slot, j.slab);
         resident_bytes_ -= j.layout.total;
         j.slab = nullptr;
@@ -998,6 +1007,19 @@ bool Engine::admit(Job& j, std::string& why) {
         R.dinv = at<double>(slab, L.dinv);
         R.free_rows = at<int32_t>(slab, L.free_rows);
         R.free_cnt = at<int32_t>(slab, L.free_cnt);
+        R.col_ff = at<int32_t>(slab, L.col_ff);
+        R.hi_ff = at<float>(slab, L.hi_ff);
+        R.lo_ff = at<float>(slab, L.lo_ff);
+        R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
+        // polish lanes per row: about a quarter of the average row length, a power of two
+        auto lanes_for = [](double avg) {
+            int lanes = 1;
+            while (lanes < 32 && 4.0 * lanes * 1.5 <= avg) lanes *= 2;
+            return lanes;
+        };
+        const double avg_row = static_cast<double>(j.nnz) / static_cast<double>(std::max<int64_t>(j.n, 1));
+        R.lanes_res = lanes_for(avg_row);
+        R.lanes_cg = lanes_for(0.5 * avg_row);
         R.n = static_cast<int32_t>(j.n);
         R.diag_gate = j.diag_gate;
         R.precision = prec;

@@ -96,6 +96,10 @@ struct __align__(16) InstDev {
     uint8_t* fixed;        // polish: 1 = held at a bound
     int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row
     int32_t* free_cnt;     // polish: free rows per tile (index within the instance's tiles)
+    int32_t* col_ff;       // polish: a free row's free-column entries, packed at the start of the
+    float* hi_ff;          //   row's own extent [rowptr[r], rowptr[r] + cnt_ff[r]) of these arrays
+    float* lo_ff;
+    int32_t* cnt_ff;
     // geometry (the instance's tile range lives in View::ranges)
     int32_t n;
     int32_t diag_gate;
@@ -109,6 +113,8 @@ struct __align__(16) InstDev {
     int32_t arm_chunk;     // 1: admission arms the first chunk without a check of x0 (mixed)
     int32_t pad_arm;
     int32_t moved[2];      // mixed: a variable entered or left a bound in the chunk's last two steps
+    int32_t lanes_res;     // polish: lanes per row of the residual pass (full rows)
+    int32_t lanes_cg;      // polish: lanes per row of the CG products (free-free rows)
     int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)
     int64_t it_cur;        // iteration of the body's first step launch; a chunk may span bodies
     int64_t it_next;       // iteration of the next check

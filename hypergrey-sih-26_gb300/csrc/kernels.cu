@@ -921,58 +921,76 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
     }
 }
 
-// Rows of a free-row list, LANES lanes per row: the warps of the block take the list in turns of
-// 32 / LANES rows (one pass each), so a tile's few hundred free rows spread evenly over the block,
-// and the leading lane of each group runs the row's epilogue.  Per row the same summation as
-// subwarp_rows: lane-strided partial sums, then an xor tree over the group.
-template <int LANES, class Prod, class Epi>
-__device__ __forceinline__ void list_rows(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ list, int n,
-                                          Prod prod, Epi epi) {
+// Polish products over a tile's free-row list, LANES lanes per row (chosen from the average row
+// length at admission): the warps of the block take the list in turns of 32 / LANES
+// rows, so a tile's few hundred free rows spread evenly over the block, and the leading lane of
+// each group runs the row's epilogue.  Per row: lane-strided partial sums, then an xor tree.
+
+// Residual pass: r = -(Q xp + c) over the full rows (xp2 holds the snapped point), and each
+// free row's entries in free columns packed, in column order, at the start of the row's own
+// extent of col_ff / hi_ff / lo_ff with their count in cnt_ff: the CG products then read only
+// Q_FF (p is zero on the fixed rows, so the omitted entries contribute nothing).
+template <int LANES>
+__device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list, int n, Acc& a) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
-    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
-        const int j = g * R + sub;
-        float2 acc = make_float2(0.f, 0.f);
-        int r = -1;
-        if (j < n) {
-            r = list[j];
-            const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
-#pragma unroll 4
-            for (int k = ks + sl; k < ke; k += LANES) acc = df_add(acc, prod(k));
-        }
-#pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
-        if (sl == 0 && r >= 0) epi(r, acc);
-    }
-}
-
-// q = Q src on the tile's free rows, src given as FP32 pairs.  residual = true: r = -(Q xp + c),
-// z = D^-1 r, p = z on the free rows, accumulating r.z and max |r|/(1+|x|).  The sub-warp variants
-// visit the free-row list (list_rows); the staged variants (long rows) run every row and skip
-// fixed ones in the epilogue.
-template <bool RESIDUAL>
-__device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re, int n_free,
-                                   const float2* __restrict__ src, Acc& a) {
-    // Local copies: the epilogue stores through other pointers of the same record, which would
-    // otherwise force the matrix pointers to be reloaded for every product.
+    const unsigned group = (LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u)) << (sub * LANES);
+    const unsigned below = (1u << lane) - 1u;
+    const int32_t* __restrict__ rowptr = I.rowptr;
     const int32_t* __restrict__ col = I.col;
     const float* __restrict__ vhi = I.vhi;
     const float* __restrict__ vlo = I.vlo;
     const uint8_t* __restrict__ fixed = I.fixed;
+    const float2* __restrict__ xp2 = I.xp2;
     const double* __restrict__ c = I.c;
     const double* __restrict__ dinv = I.dinv;
     const double* __restrict__ xp = I.xp;
+    int32_t* __restrict__ col_ff = I.col_ff;
+    float* __restrict__ hi_ff = I.hi_ff;
+    float* __restrict__ lo_ff = I.lo_ff;
+    int32_t* __restrict__ cnt_ff = I.cnt_ff;
     double* __restrict__ r_out = I.r;
     double* __restrict__ z_out = I.z;
     double* __restrict__ p_out = I.p;
     float2* __restrict__ p2_out = I.p2;
-    double* __restrict__ q_out = I.q;
-    auto prod = [&](int k) { return df_prod2(__ldg(vhi + k), __ldg(vlo + k), src[__ldg(col + k)]); };
-    auto add = [](float2 x, float2 y) { return df_add(x, y); };
-    auto epi = [&](int r, float2 acc) {
-        if (fixed[r]) return;
-        if constexpr (RESIDUAL) {
+    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
+        const int j = g * R + sub;
+        int r = -1, ks = 0, len = 0;
+        if (j < n) {
+            r = list[j];
+            ks = __ldg(rowptr + r);
+            len = __ldg(rowptr + r + 1) - ks;
+        }
+        const int wmax = __reduce_max_sync(0xffffffffu, len);
+        float2 acc = make_float2(0.f, 0.f);
+        int kept = 0;
+        for (int i = 0; i < wmax; i += LANES) {  // warp-uniform
+            const bool valid = i + sl < len;
+            bool keep = false;
+            int cc = 0;
+            float h = 0.f, lo = 0.f;
+            if (valid) {
+                const int k = ks + i + sl;
+                cc = __ldg(col + k);
+                h = __ldg(vhi + k);
+                lo = __ldg(vlo + k);
+                acc = df_add(acc, df_prod2(h, lo, xp2[cc]));
+                keep = !fixed[cc];
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int pos = ks + kept + __popc(m & group & below);
+                col_ff[pos] = cc;
+                hi_ff[pos] = h;
+                lo_ff[pos] = lo;
+            }
+            kept += __popc(m & group);
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
+        if (sl == 0 && r >= 0) {
+            cnt_ff[r] = kept;
             const double rr = -(df_value(acc) + c[r]);
             const double zz = rr * dinv[r];
             a.a = fma(rr, zz, a.a);
@@ -982,26 +1000,58 @@ __device__ void polish_matvec_rows(const InstDev& I, int variant, int rb, int re
             z_out[r] = zz;
             p_out[r] = zz;
             p2_out[r] = df_split(zz);
-        } else {
-            const double qq = df_value(acc);
-            q_out[r] = qq;
-            a.a = fma(p_out[r], qq, a.a);
         }
-    };
-    const float2 zero = make_float2(0.f, 0.f);
-    const int32_t* list = I.free_rows + rb;
-    switch (variant) {
-    case 1: list_rows<1>(I.rowptr, list, n_free, prod, epi); break;
-    case 2: list_rows<2>(I.rowptr, list, n_free, prod, epi); break;
-    case 4: list_rows<4>(I.rowptr, list, n_free, prod, epi); break;
-    case 8: list_rows<8>(I.rowptr, list, n_free, prod, epi); break;
-    case 16: list_rows<16>(I.rowptr, list, n_free, prod, epi); break;
-    case 32: list_rows<32>(I.rowptr, list, n_free, prod, epi); break;
-    default: warp_groups<float2>(I.rowptr, rb, re, warp_buffer<float2>(), prod, add, zero, epi); break;
     }
 }
 
-__global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
+// CG product q = Q_FF p on a tile's free rows, accumulating p.q.
+template <int LANES>
+__device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, int n, Acc& a) {
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    const int32_t* __restrict__ rowptr = I.rowptr;
+    const int32_t* __restrict__ col = I.col_ff;
+    const float* __restrict__ vhi = I.hi_ff;
+    const float* __restrict__ vlo = I.lo_ff;
+    const int32_t* __restrict__ cnt = I.cnt_ff;
+    const float2* __restrict__ p2 = I.p2;
+    const double* __restrict__ p = I.p;
+    double* __restrict__ q_out = I.q;
+    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
+        const int j = g * R + sub;
+        float2 acc = make_float2(0.f, 0.f);
+        int r = -1;
+        if (j < n) {
+            r = list[j];
+            const int ks = __ldg(rowptr + r), ke = ks + cnt[r];
+#pragma unroll 4
+            for (int k = ks + sl; k < ke; k += LANES) acc = df_add(acc, df_prod2(__ldg(vhi + k), __ldg(vlo + k), p2[__ldg(col + k)]));
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
+        if (sl == 0 && r >= 0) {
+            const double qq = df_value(acc);
+            q_out[r] = qq;
+            a.a = fma(p[r], qq, a.a);
+        }
+    }
+}
+
+template <bool RESIDUAL>
+__device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
+    const int32_t* list = I.free_rows + rb;
+    switch (RESIDUAL ? I.lanes_res : I.lanes_cg) {
+    case 1: RESIDUAL ? residual_rows<1>(I, list, n_free, a) : matvec_rows<1>(I, list, n_free, a); break;
+    case 2: RESIDUAL ? residual_rows<2>(I, list, n_free, a) : matvec_rows<2>(I, list, n_free, a); break;
+    case 4: RESIDUAL ? residual_rows<4>(I, list, n_free, a) : matvec_rows<4>(I, list, n_free, a); break;
+    case 8: RESIDUAL ? residual_rows<8>(I, list, n_free, a) : matvec_rows<8>(I, list, n_free, a); break;
+    case 16: RESIDUAL ? residual_rows<16>(I, list, n_free, a) : matvec_rows<16>(I, list, n_free, a); break;
+    default: RESIDUAL ? residual_rows<32>(I, list, n_free, a) : matvec_rows<32>(I, list, n_free, a); break;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
@@ -1009,7 +1059,7 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
-        polish_matvec_rows<true>(I, T.variant, T.row_begin, T.row_end, I.free_cnt[t - R.x], I.xp2, a);
+        polish_rows<true>(I, T.row_begin, I.free_cnt[t - R.x], a);
         Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
@@ -1033,7 +1083,7 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
-        polish_matvec_rows<false>(I, T.variant, T.row_begin, T.row_end, I.free_cnt[t - R.x], I.p2, a);
+        polish_rows<false>(I, T.row_begin, I.free_cnt[t - R.x], a);
         Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
@@ -1417,7 +1467,7 @@ namespace {
 // One full wave (SMs x resident blocks per SM) per tile kernel, computed once per process.
 struct Waves {
     int step[3] = {0, 0, 0};
-    int check = 0, check_mixed = 0, check_verify = 0, polish = 0, matvec = 0;
+    int check = 0, check_mixed = 0, check_verify = 0, polish = 0, matvec = 0, residual = 0;
 };
 Waves g_waves;
 
@@ -1440,8 +1490,8 @@ int tile_grid(int sms) {
     g_waves.check = wave_of(check_kernel<FAMILY_FP64>, sms, kSmem8);
     g_waves.check_mixed = wave_of(check_kernel<FAMILY_MIXED>, sms, kSmem8);
     g_waves.check_verify = wave_of(check_kernel<FAMILY_VERIFY>, sms, kSmem8);
-    g_waves.matvec = wave_of(cg_matvec_kernel, sms, kSmem8);
-    wave_of(polish_residual_kernel, sms, kSmem8);
+    g_waves.matvec = wave_of(cg_matvec_kernel, sms, 0);
+    g_waves.residual = wave_of(polish_residual_kernel, sms, 0);
     wave_of(check_standalone_kernel, sms, kSmem8);
     g_waves.polish = wave_of(cg_update_kernel, sms, 0);
     int m = 0;
@@ -1470,10 +1520,10 @@ void launch_polish_init(const View& v, int grid, cudaStream_t s) {
     polish_init_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v);
 }
 void launch_polish_residual(const View& v, int grid, cudaStream_t s) {
-    polish_residual_kernel<<<pick(grid, g_waves.matvec), kBlock, kSmem8, s>>>(v);
+    polish_residual_kernel<<<pick(grid, g_waves.residual), kBlock, 0, s>>>(v);
 }
 void launch_cg_matvec(const View& v, int grid, cudaStream_t s) {
-    cg_matvec_kernel<<<pick(grid, g_waves.matvec), kBlock, kSmem8, s>>>(v);
+    cg_matvec_kernel<<<pick(grid, g_waves.matvec), kBlock, 0, s>>>(v);
 }
 void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v); }
 void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop, int cap) {
