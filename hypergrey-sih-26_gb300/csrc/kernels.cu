@@ -1318,12 +1318,15 @@ __device__ void start_instance(InstDev& I) {
         I.end_ns = 0;
         if (I.arm_chunk) {
             // mixed precision: x0 = clip(0) is not checked; the first chunk of steps is armed here
-            // as a check of x0 would arm it (the first check then comes after `interval` steps)
+            // as a check of x0 would arm it.  With a short interval the first chunk is two
+            // intervals long: the active set still moves in the first steps, so a check there
+            // could not start the polish.
             I.it0 = 0;
             I.it_cur = 0;
             I.moved[0] = 0;
             I.moved[1] = 0;
-            I.it_next = I.interval < I.max_iter ? I.interval : I.max_iter;
+            const int64_t first = 2 * I.interval <= kMaxInterval ? 2 * I.interval : I.interval;
+            I.it_next = first < I.max_iter ? first : I.max_iter;
             fista_betas(I, I.it_next);
             I.fista_iters += I.it_next;
         }
