@@ -1034,6 +1034,10 @@ bool Engine::admit(Job& j, std::string& why) {
         R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
         R.cg_tol = 0.1 * j.opt.tolerance;
         R.polish_switch = j.opt.polish_switch;
+        // a step-stable chunk (its last three iterates share their active set) starts the polish at
+        // 3x the switch, except on chain-like rows of fewer than 4 nonzeros (tridiagonal: the free
+        // runs are long, and an early polish costs more CG iterations than the FISTA steps it saves)
+        R.step_switch = j.nnz >= 4 * j.n ? 3.0 * j.opt.polish_switch : 0.0;
         // tiles
         for (Tile& t : j.tiles) t.inst = slot;
         const int begin = static_cast<int>(h_tiles_.size());

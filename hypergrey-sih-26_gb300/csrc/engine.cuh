@@ -149,6 +149,7 @@ struct __align__(16) InstDev {
     double cg_res;
     double cg_tol;
     double polish_switch;  // stationarity that triggers the first polish attempt
+    double step_switch;    // the same after a step-stable chunk (see after_check)
     int64_t cg_it;
     int64_t cg_total;
     int64_t cg_max;

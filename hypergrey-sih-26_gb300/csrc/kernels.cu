@@ -572,7 +572,8 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
         for (int k = 0; k < I.polish_rounds; ++k) sw *= 0.1;
         // the chunk's last three iterates share their active set (no move in its last two steps)
         const bool step_stable = it_check - I.it0 >= 2 && I.moved[0] == 0 && I.moved[1] == 0;
-        if ((I.stable_checks >= 1 && stat <= sw) || (step_stable && stat <= 3.0 * sw)) {
+        const double step_sw = I.polish_switch > 0 ? sw * (I.step_switch / I.polish_switch) : 0.0;
+        if ((I.stable_checks >= 1 && stat <= sw) || (step_stable && stat <= step_sw)) {
             I.phase = PH_POLISH_INIT;
             I.cg_it = 0;
             return;
