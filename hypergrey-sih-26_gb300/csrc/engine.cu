@@ -62,7 +62,7 @@ struct Layout {
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
-    size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone;
+    size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
     size_t total = 0;
 };
 
@@ -110,6 +110,7 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.hi_ff = take(Z * 4);
         L.lo_ff = take(Z * 4);
         L.cnt_ff = take(N * 4);
+        L.start_ff = take(N * 4);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
@@ -1011,6 +1012,7 @@ bool Engine::admit(Job& j, std::string& why) {
         R.hi_ff = at<float>(slab, L.hi_ff);
         R.lo_ff = at<float>(slab, L.lo_ff);
         R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
+        R.start_ff = at<int32_t>(slab, L.start_ff);
         // polish lanes per row: about a quarter of the average row length, a power of two
         auto lanes_for = [](double avg) {
             int lanes = 1;

@@ -96,10 +96,11 @@ struct __align__(16) InstDev {
     uint8_t* fixed;        // polish: 1 = held at a bound
     int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row
     int32_t* free_cnt;     // polish: free rows per tile (index within the instance's tiles)
-    int32_t* col_ff;       // polish: a free row's free-column entries, packed at the start of the
-    float* hi_ff;          //   row's own extent [rowptr[r], rowptr[r] + cnt_ff[r]) of these arrays
-    float* lo_ff;
+    int32_t* col_ff;       // polish: the free-column entries of a tile's free rows, packed row
+    float* hi_ff;          //   after row (list order) from the start of the tile's own extent
+    float* lo_ff;          //   [rowptr[row_begin], ...): row r at [start_ff[r], + cnt_ff[r])
     int32_t* cnt_ff;
+    int32_t* start_ff;
     // geometry (the instance's tile range lives in View::ranges)
     int32_t n;
     int32_t diag_gate;

@@ -927,12 +927,72 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
 // rows, so a tile's few hundred free rows spread evenly over the block, and the leading lane of
 // each group runs the row's epilogue.  Per row: lane-strided partial sums, then an xor tree.
 
-// Residual pass: r = -(Q xp + c) over the full rows (xp2 holds the snapped point), and each
-// free row's entries in free columns packed, in column order, at the start of the row's own
-// extent of col_ff / hi_ff / lo_ff with their count in cnt_ff: the CG products then read only
-// Q_FF (p is zero on the fixed rows, so the omitted entries contribute nothing).
+// Residual pass: r = -(Q xp + c) over the full rows (xp2 holds the snapped point), and the
+// tile's Q_FF entries (free rows, free columns; p is zero on the fixed rows, so the omitted
+// entries contribute nothing to the CG products) packed densely from the start of the tile's
+// extent: a first pass counts each free row's kept entries, a block scan places the rows, and
+// the product pass writes them in column order.
 template <int LANES>
-__device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list, int n, Acc& a) {
+__device__ void count_kept(const InstDev& I, const int32_t* __restrict__ list, int n, int32_t* kept_of) {
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / LANES, sl = lane % LANES;
+    const int32_t* __restrict__ rowptr = I.rowptr;
+    const int32_t* __restrict__ col = I.col;
+    const uint8_t* __restrict__ fixed = I.fixed;
+    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
+        const int j = g * R + sub;
+        int cnt = 0;
+        if (j < n) {
+            const int r = list[j];
+            const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+#pragma unroll 4
+            for (int k = ks + sl; k < ke; k += LANES) cnt += fixed[__ldg(col + k)] ? 0 : 1;
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (sl == 0 && j < n) kept_of[j] = cnt;
+    }
+}
+
+// Exclusive prefix sum of v[0..n) in place (n <= kTileRows), block-wide; returns the total.
+__device__ int block_exclusive_scan(int32_t* v, int n) {
+    __shared__ int warp_tot[kBlock / 32];
+    __shared__ int total;
+    constexpr int kPer = kTileRows / kBlock;  // entries per thread
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int mine[kPer], sum = 0;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int idx = threadIdx.x * kPer + i;
+        mine[i] = idx < n ? v[idx] : 0;
+        sum += mine[i];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_tot[w];
+    if (threadIdx.x == kBlock - 1) total = before + incl;
+    int run = before + incl - sum;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int idx = threadIdx.x * kPer + i;
+        if (idx < n) v[idx] = run;
+        run += mine[i];
+    }
+    __syncthreads();
+    return total;
+}
+
+template <int LANES>
+__device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list, int n, int base,
+                              const int32_t* __restrict__ start_of, Acc& a) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -951,17 +1011,19 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     float* __restrict__ hi_ff = I.hi_ff;
     float* __restrict__ lo_ff = I.lo_ff;
     int32_t* __restrict__ cnt_ff = I.cnt_ff;
+    int32_t* __restrict__ start_ff = I.start_ff;
     double* __restrict__ r_out = I.r;
     double* __restrict__ z_out = I.z;
     double* __restrict__ p_out = I.p;
     float2* __restrict__ p2_out = I.p2;
     for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
         const int j = g * R + sub;
-        int r = -1, ks = 0, len = 0;
+        int r = -1, ks = 0, len = 0, dst = 0;
         if (j < n) {
             r = list[j];
             ks = __ldg(rowptr + r);
             len = __ldg(rowptr + r + 1) - ks;
+            dst = base + start_of[j];
         }
         const int wmax = __reduce_max_sync(0xffffffffu, len);
         float2 acc = make_float2(0.f, 0.f);
@@ -981,7 +1043,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
             }
             const unsigned m = __ballot_sync(0xffffffffu, keep);
             if (keep) {
-                const int pos = ks + kept + __popc(m & group & below);
+                const int pos = dst + kept + __popc(m & group & below);
                 col_ff[pos] = cc;
                 hi_ff[pos] = h;
                 lo_ff[pos] = lo;
@@ -992,6 +1054,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
         for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
         if (sl == 0 && r >= 0) {
             cnt_ff[r] = kept;
+            start_ff[r] = dst;
             const double rr = -(df_value(acc) + c[r]);
             const double zz = rr * dinv[r];
             a.a = fma(rr, zz, a.a);
@@ -1011,11 +1074,11 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
-    const int32_t* __restrict__ rowptr = I.rowptr;
     const int32_t* __restrict__ col = I.col_ff;
     const float* __restrict__ vhi = I.hi_ff;
     const float* __restrict__ vlo = I.lo_ff;
     const int32_t* __restrict__ cnt = I.cnt_ff;
+    const int32_t* __restrict__ start = I.start_ff;
     const float2* __restrict__ p2 = I.p2;
     const double* __restrict__ p = I.p;
     double* __restrict__ q_out = I.q;
@@ -1025,7 +1088,7 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
         int r = -1;
         if (j < n) {
             r = list[j];
-            const int ks = __ldg(rowptr + r), ke = ks + cnt[r];
+            const int ks = start[r], ke = ks + cnt[r];
 #pragma unroll 4
             for (int k = ks + sl; k < ke; k += LANES) acc = df_add(acc, df_prod2(__ldg(vhi + k), __ldg(vlo + k), p2[__ldg(col + k)]));
         }
@@ -1039,16 +1102,38 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     }
 }
 
+template <int LANES>
+__device__ void residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, Acc& a) {
+    __shared__ int32_t start_of[kTileRows];
+    count_kept<LANES>(I, list, n_free, start_of);
+    __syncthreads();
+    block_exclusive_scan(start_of, n_free);
+    residual_rows<LANES>(I, list, n_free, base, start_of, a);
+}
+
+// Residual (with the packing of Q_FF) or CG product over tile rows [rb, ...) of one instance.
 template <bool RESIDUAL>
 __device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
     const int32_t* list = I.free_rows + rb;
-    switch (RESIDUAL ? I.lanes_res : I.lanes_cg) {
-    case 1: RESIDUAL ? residual_rows<1>(I, list, n_free, a) : matvec_rows<1>(I, list, n_free, a); break;
-    case 2: RESIDUAL ? residual_rows<2>(I, list, n_free, a) : matvec_rows<2>(I, list, n_free, a); break;
-    case 4: RESIDUAL ? residual_rows<4>(I, list, n_free, a) : matvec_rows<4>(I, list, n_free, a); break;
-    case 8: RESIDUAL ? residual_rows<8>(I, list, n_free, a) : matvec_rows<8>(I, list, n_free, a); break;
-    case 16: RESIDUAL ? residual_rows<16>(I, list, n_free, a) : matvec_rows<16>(I, list, n_free, a); break;
-    default: RESIDUAL ? residual_rows<32>(I, list, n_free, a) : matvec_rows<32>(I, list, n_free, a); break;
+    if constexpr (RESIDUAL) {
+        const int base = __ldg(I.rowptr + rb);
+        switch (I.lanes_res) {
+        case 1: residual_tile<1>(I, list, n_free, base, a); break;
+        case 2: residual_tile<2>(I, list, n_free, base, a); break;
+        case 4: residual_tile<4>(I, list, n_free, base, a); break;
+        case 8: residual_tile<8>(I, list, n_free, base, a); break;
+        case 16: residual_tile<16>(I, list, n_free, base, a); break;
+        default: residual_tile<32>(I, list, n_free, base, a); break;
+        }
+    } else {
+        switch (I.lanes_cg) {
+        case 1: matvec_rows<1>(I, list, n_free, a); break;
+        case 2: matvec_rows<2>(I, list, n_free, a); break;
+        case 4: matvec_rows<4>(I, list, n_free, a); break;
+        case 8: matvec_rows<8>(I, list, n_free, a); break;
+        case 16: matvec_rows<16>(I, list, n_free, a); break;
+        default: matvec_rows<32>(I, list, n_free, a); break;
+        }
     }
 }
 
