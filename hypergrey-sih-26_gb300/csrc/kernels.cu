@@ -860,6 +860,14 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // their count at free_cnt[tile index within the instance]; the CG kernels visit only those rows
 // (an instance's tiling depends on the instance alone, so the list survives changes of the batch).
 // Fixed rows hold r = z = p = 0, so the products of the CG matvec over all columns are exact.
+// CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with 0.1 tol), as the
+// bit pattern of a non-negative float: maxima reduce on the integer pipes, and the FP64 pipe
+// (1/64 of the FP32 rate on this GPU) only converts r and x.
+__device__ __forceinline__ unsigned long long cg_ratio_bits(double r, double x) {
+    const float ratio = __fdividef(fabsf(static_cast<float>(r)), 1.0f + fabsf(static_cast<float>(x)));
+    return static_cast<unsigned long long>(__float_as_uint(ratio));
+}
+
 __device__ __forceinline__ bool polish_phase(const InstDev& I, int phase) {
     return I.status == ST_RUNNING && I.phase == phase;
 }
@@ -1058,8 +1066,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
             const double rr = -(df_value(acc) + c[r]);
             const double zz = rr * dinv[r];
             a.a = fma(rr, zz, a.a);
-            a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) /
-                                                         (1.0f + fabsf(static_cast<float>(xp[r]))))));
+            a.b = umax64(a.b, cg_ratio_bits(rr, xp[r]));
             r_out[r] = rr;
             z_out[r] = zz;
             p_out[r] = zz;
@@ -1151,7 +1158,7 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
                 I.rz = inst_total.a;
-                I.cg_res = bdouble(inst_total.b);
+                I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
                 I.cg_it = 0;
                 I.phase = (I.cg_res <= I.cg_tol || !(I.rz > 0)) ? PH_POLISH_FINISH : PH_POLISH_CG;
                 if (I.phase == PH_POLISH_FINISH) atomicSub(&v.ctrl->n_cg, 1);
@@ -1213,7 +1220,7 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
             rr_v[r] = rr;
             z[r] = zz;
             a.a = fma(rr, zz, a.a);
-            a.b = umax64(a.b, dbits(static_cast<double>(fabsf(static_cast<float>(rr)) / (1.0f + fabsf(static_cast<float>(xv))))));
+            a.b = umax64(a.b, cg_ratio_bits(rr, xv));
         }
         Acc total = block_reduce_ab(a);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
@@ -1222,7 +1229,7 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
                 const double rz_new = inst_total.a;
                 I.beta_cg = I.rz > 0 ? rz_new / I.rz : 0.0;
                 I.rz = rz_new;
-                I.cg_res = bdouble(inst_total.b);
+                I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
                 I.cg_it++;
                 I.cg_total++;
                 if (I.cg_res <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) {
