@@ -1405,6 +1405,11 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
         why = "Invalid box QP options";
         return BQP_ERR_INVALID;
     }
+    if (o->lipschitz != BQP_LIPSCHITZ_GERSHGORIN) {
+        why = o->lipschitz == BQP_LIPSCHITZ_POWER ? "the power-iteration Lipschitz estimate is not implemented"
+                                                   : "Invalid box QP options";
+        return o->lipschitz == BQP_LIPSCHITZ_POWER ? BQP_ERR_UNSUPPORTED : BQP_ERR_INVALID;
+    }
     if (rowptr[0] != 0 || rowptr[n] != nnz) {
         why = "Invalid CSR row pointers";
         return BQP_ERR_INVALID;

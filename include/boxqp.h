@@ -57,8 +57,8 @@ extern "C" {
 
 /* ---- step size ------------------------------------------------------------------------- */
 #define BQP_LIPSCHITZ_GERSHGORIN  0  /* L = max_i sum_k |Q_ik|, as src/accelerated_qp.cpp:25-26      */
-#define BQP_LIPSCHITZ_POWER       1  /* FP64 power-iteration estimate of lambda_max, safety factor,
-                                        never above Gershgorin; divergence falls back to Gershgorin   */
+#define BQP_LIPSCHITZ_POWER       1  /* reserved for a power-iteration estimate of lambda_max; not
+                                        implemented: submissions asking for it get BQP_ERR_UNSUPPORTED */
 
 typedef struct bqp_ctx bqp_ctx;
 

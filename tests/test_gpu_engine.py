@@ -192,3 +192,12 @@ def test_check_device_matches_oracle_checker():
 
 def test_device_name():
     assert 'GB300' in boxqp.cuda_device_name() or len(boxqp.cuda_device_name()) > 0
+
+
+def test_power_lipschitz_option_is_rejected_as_unsupported(engine):
+    inst = boxqp.planted('graph10k', seed=1, n=500)
+    o = boxqp.options_struct(1e-6, 10.0, 1000, 'mixed')
+    o.lipschitz = 1  # BQP_LIPSCHITZ_POWER: declared, not implemented
+    with pytest.raises(boxqp.EngineError) as err:
+        engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+    assert err.value.code == 7 and 'not implemented' in str(err.value)
