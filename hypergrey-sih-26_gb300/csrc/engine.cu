@@ -312,7 +312,23 @@ public:
 
 private:
     void loop();
-    bool admit(Job& j, std::string& why);
+    bool upload(Job& j, std::string& why);
+    static void CUDART_CB on_launch_done(void* self) {
+        Engine* e = static_cast<Engine*>(self);
+        {
+            std::lock_guard<std::mutex> g(e->mu_);
+            e->launch_done_ = true;
+        }
+        e->cv_work_.notify_all();
+    }
+    // a new solve at the head of the queue that fits under the cap (caller holds mu_)
+    bool uploadable_head() const {
+        if (queue_.empty() || queue_.front()->resolve) return false;
+        const Job* j = queue_.front();
+        return resident_bytes_ + make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total <= cap_;
+    }
+    bool install(std::vector<Job*>& jobs, std::string& why);
+    void upload_waiting();
     bool rearm(const std::vector<Job*>& batch, std::string& why);
     void reset_record(Job& j);
     void update_steps();
@@ -346,6 +362,10 @@ private:
     int grid_max_ = 152 * 8;
     cudaStream_t stream_ = nullptr;
     cudaStream_t capture_ = nullptr;
+    cudaStream_t ustream_ = nullptr;   // uploads of new solves, overlapping the running graph
+    cudaEvent_t uev_ = nullptr;        // end of the latest upload on ustream_
+    std::vector<Job*> uploaded_;       // uploaded, not yet installed (engine thread only)
+    bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
     cudaMemPool_t pool_ = nullptr;
 
     // device tables
@@ -430,6 +450,8 @@ bool Engine::init(std::string& why) {
     grid_max_ = tile_grid(sms_);
     if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&ustream_, cudaStreamNonBlocking), why, "stream")) return false;
+    if (!cuda_ok(cudaEventCreateWithFlags(&uev_, cudaEventDisableTiming), why, "event")) return false;
     cudaMemPoolProps props;
     std::memset(&props, 0, sizeof(props));
     props.allocType = cudaMemAllocationTypePinned;
@@ -469,6 +491,7 @@ void Engine::shutdown() {
     if (thread_.joinable()) thread_.join();
     if (stream_) {
         cudaSetDevice(device_);
+        if (ustream_) cudaStreamSynchronize(ustream_);
         cudaStreamSynchronize(stream_);
         for (auto& kv : jobs_) if (kv.second->slab) cudaFreeAsync(kv.second->slab, stream_);
         for (auto& pf : pending_free_) if (pf.second) cudaFreeAsync(pf.second, stream_);
@@ -508,8 +531,12 @@ void Engine::shutdown() {
     ev1_ = nullptr;
     if (stream_) cudaStreamDestroy(stream_);
     if (capture_) cudaStreamDestroy(capture_);
+    if (ustream_) cudaStreamDestroy(ustream_);
+    if (uev_) cudaEventDestroy(uev_);
     stream_ = nullptr;
     capture_ = nullptr;
+    ustream_ = nullptr;
+    uev_ = nullptr;
 }
 
 // Grows the device tables (instance records, tile table, partials); invalidates the graph.
@@ -950,23 +977,113 @@ void Engine::update_steps() {
     }
 }
 
-// Uploads one new solve and appends its tiles.  Engine thread only.
-bool Engine::admit(Job& j, std::string& why) {
+// Uploads one new solve on the upload stream (inputs, slab, device-side forms), without touching
+// the tables the running graph reads; install() makes it part of the batch.  Engine thread only.
+bool Engine::upload(Job& j, std::string& why) {
     const double t0 = host_seconds();
     const int prec = j.opt.precision;
-    if (!j.resolve) {
-        j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
-        void* slab = nullptr;
-        if (!cuda_ok(cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, stream_), why, "allocate solve")) return false;
-        j.slab = slab;
-        const Layout& L = j.layout;
-        const size_t N = static_cast<size_t>(j.n), Z = static_cast<size_t>(j.nnz);
-        cudaMemcpyAsync(at<int32_t>(slab, L.rowptr), j.rowptr, (N + 1) * 4, cudaMemcpyHostToDevice, stream_);
-        if (Z) cudaMemcpyAsync(at<int32_t>(slab, L.col), j.col, Z * 4, cudaMemcpyHostToDevice, stream_);
-        cudaMemcpyAsync(at<double>(slab, L.c), j.c, N * 8, cudaMemcpyHostToDevice, stream_);
-        cudaMemcpyAsync(at<double>(slab, L.l), j.l, N * 8, cudaMemcpyHostToDevice, stream_);
-        cudaMemcpyAsync(at<double>(slab, L.u), j.u, N * 8, cudaMemcpyHostToDevice, stream_);
-        // slot
+    j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
+    void* slab = nullptr;
+    if (!cuda_ok(cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, ustream_), why, "allocate solve")) return false;
+    j.slab = slab;
+    j.resident = true;
+    const Layout& L = j.layout;
+    const size_t N = static_cast<size_t>(j.n), Z = static_cast<size_t>(j.nnz);
+    cudaMemcpyAsync(at<int32_t>(slab, L.rowptr), j.rowptr, (N + 1) * 4, cudaMemcpyHostToDevice, ustream_);
+    if (Z) cudaMemcpyAsync(at<int32_t>(slab, L.col), j.col, Z * 4, cudaMemcpyHostToDevice, ustream_);
+    cudaMemcpyAsync(at<double>(slab, L.c), j.c, N * 8, cudaMemcpyHostToDevice, ustream_);
+    cudaMemcpyAsync(at<double>(slab, L.l), j.l, N * 8, cudaMemcpyHostToDevice, ustream_);
+    cudaMemcpyAsync(at<double>(slab, L.u), j.u, N * 8, cudaMemcpyHostToDevice, ustream_);
+    InstDev& R = j.rec;
+    std::memset(&R, 0, sizeof(R));
+    R.rowptr = at<int32_t>(slab, L.rowptr);
+    R.col = at<int32_t>(slab, L.col);
+    R.val64 = at<double>(slab, L.val64);
+    R.vhi = at<float>(slab, L.vhi);
+    R.vlo = at<float>(slab, L.vlo);
+    R.c = at<double>(slab, L.c);
+    R.l = at<double>(slab, L.l);
+    R.u = at<double>(slab, L.u);
+    R.c32 = at<float>(slab, L.c32);
+    R.l32 = at<float>(slab, L.l32);
+    R.u32 = at<float>(slab, L.u32);
+    R.diag = at<double>(slab, L.diag);
+    R.x64 = at<double>(slab, L.x64);
+    R.w64[0] = at<double>(slab, L.w64a);
+    R.w64[1] = at<double>(slab, L.w64b);
+    R.x32 = at<float>(slab, L.x32);
+    R.w32[0] = at<float>(slab, L.w32a);
+    R.w32[1] = at<float>(slab, L.w32b);
+    R.xp = at<double>(slab, L.xp);
+    R.r = at<double>(slab, L.r);
+    R.p = at<double>(slab, L.p);
+    R.q = at<double>(slab, L.q);
+    R.z = at<double>(slab, L.z);
+    R.fixed = at<uint8_t>(slab, L.fixed);
+    R.xp2 = at<float2>(slab, L.xp2);
+    R.p2 = at<float2>(slab, L.p2);
+    R.dinv = at<double>(slab, L.dinv);
+    R.free_rows = at<int32_t>(slab, L.free_rows);
+    R.free_cnt = at<int32_t>(slab, L.free_cnt);
+    R.col_ff = at<int32_t>(slab, L.col_ff);
+    R.hi_ff = at<float>(slab, L.hi_ff);
+    R.lo_ff = at<float>(slab, L.lo_ff);
+    R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
+    R.start_ff = at<int32_t>(slab, L.start_ff);
+    // polish lanes per row: about a quarter of the average row length, a power of two
+    auto lanes_for = [](double avg) {
+        int lanes = 1;
+        while (lanes < 32 && 4.0 * lanes * 1.5 <= avg) lanes *= 2;
+        return lanes;
+    };
+    const double avg_row = static_cast<double>(j.nnz) / static_cast<double>(std::max<int64_t>(j.n, 1));
+    R.lanes_res = lanes_for(avg_row);
+    R.lanes_cg = lanes_for(0.5 * avg_row);
+    R.n = static_cast<int32_t>(j.n);
+    R.diag_gate = j.diag_gate;
+    R.precision = prec;
+    R.L = j.lipschitz;
+    R.invL = 1.0 / j.lipschitz;
+    R.invLf = static_cast<float>(1.0 / j.lipschitz);
+    R.tol = j.opt.tolerance;
+    R.offset = j.opt.offset;
+    R.interval = j.opt.check_interval;
+    R.max_iter = j.opt.iteration_limit;
+    R.polish = prec == PREC_MIXED ? 1 : 0;
+    R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
+    R.cg_tol = 0.1 * j.opt.tolerance;
+    R.polish_switch = j.opt.polish_switch;
+    // a step-stable chunk (its last three iterates share their active set) starts the polish at
+    // 3x the switch, except on chain-like rows of fewer than 4 nonzeros (tridiagonal: the free
+    // runs are long, and an early polish costs more CG iterations than the FISTA steps it saves)
+    R.step_switch = j.nnz >= 4 * j.n ? 3.0 * j.opt.polish_switch : 0.0;
+    if (prec == PREC_MIXED) {
+        void* tmp = nullptr;
+        if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, ustream_), why, "allocate upload buffer")) return false;
+        if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
+        launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(tmp), ustream_);
+        cudaFreeAsync(tmp, ustream_);
+    } else {
+        double* val = at<double>(slab, L.val64);
+        if (Z) cudaMemcpyAsync(val, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
+        launch_prepare_instance(R, j.n, j.nnz, val, ustream_);
+    }
+    if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
+    cudaEventRecord(uev_, ustream_);
+    if (host_profile()) {
+        const double t1 = host_seconds();
+        cudaStreamSynchronize(ustream_);
+        std::fprintf(stderr, "[boxqp] upload n=%lld: enqueue %.3f ms, device done %.3f ms\n", static_cast<long long>(j.n),
+                     1e3 * (t1 - t0), 1e3 * (host_seconds() - t0));
+    }
+    return true;
+}
+
+// Makes uploaded solves part of the batch: slots, tiles and records (one re-arm launch, after
+// the uploads on ustream_).  Engine thread, between graph launches.
+bool Engine::install(std::vector<Job*>& jobs, std::string& why) {
+    for (Job* jp : jobs) {
+        Job& j = *jp;
         int slot;
         if (!free_slots_.empty()) {
             slot = free_slots_.back();
@@ -976,71 +1093,6 @@ bool Engine::admit(Job& j, std::string& why) {
             slot = n_inst_++;
         }
         j.slot = slot;
-        j.resident = true;
-        InstDev& R = j.rec;
-        std::memset(&R, 0, sizeof(R));
-        R.rowptr = at<int32_t>(slab, L.rowptr);
-        R.col = at<int32_t>(slab, L.col);
-        R.val64 = at<double>(slab, L.val64);
-        R.vhi = at<float>(slab, L.vhi);
-        R.vlo = at<float>(slab, L.vlo);
-        R.c = at<double>(slab, L.c);
-        R.l = at<double>(slab, L.l);
-        R.u = at<double>(slab, L.u);
-        R.c32 = at<float>(slab, L.c32);
-        R.l32 = at<float>(slab, L.l32);
-        R.u32 = at<float>(slab, L.u32);
-        R.diag = at<double>(slab, L.diag);
-        R.x64 = at<double>(slab, L.x64);
-        R.w64[0] = at<double>(slab, L.w64a);
-        R.w64[1] = at<double>(slab, L.w64b);
-        R.x32 = at<float>(slab, L.x32);
-        R.w32[0] = at<float>(slab, L.w32a);
-        R.w32[1] = at<float>(slab, L.w32b);
-        R.xp = at<double>(slab, L.xp);
-        R.r = at<double>(slab, L.r);
-        R.p = at<double>(slab, L.p);
-        R.q = at<double>(slab, L.q);
-        R.z = at<double>(slab, L.z);
-        R.fixed = at<uint8_t>(slab, L.fixed);
-        R.xp2 = at<float2>(slab, L.xp2);
-        R.p2 = at<float2>(slab, L.p2);
-        R.dinv = at<double>(slab, L.dinv);
-        R.free_rows = at<int32_t>(slab, L.free_rows);
-        R.free_cnt = at<int32_t>(slab, L.free_cnt);
-        R.col_ff = at<int32_t>(slab, L.col_ff);
-        R.hi_ff = at<float>(slab, L.hi_ff);
-        R.lo_ff = at<float>(slab, L.lo_ff);
-        R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
-        R.start_ff = at<int32_t>(slab, L.start_ff);
-        // polish lanes per row: about a quarter of the average row length, a power of two
-        auto lanes_for = [](double avg) {
-            int lanes = 1;
-            while (lanes < 32 && 4.0 * lanes * 1.5 <= avg) lanes *= 2;
-            return lanes;
-        };
-        const double avg_row = static_cast<double>(j.nnz) / static_cast<double>(std::max<int64_t>(j.n, 1));
-        R.lanes_res = lanes_for(avg_row);
-        R.lanes_cg = lanes_for(0.5 * avg_row);
-        R.n = static_cast<int32_t>(j.n);
-        R.diag_gate = j.diag_gate;
-        R.precision = prec;
-        R.L = j.lipschitz;
-        R.invL = 1.0 / j.lipschitz;
-        R.invLf = static_cast<float>(1.0 / j.lipschitz);
-        R.tol = j.opt.tolerance;
-        R.offset = j.opt.offset;
-        R.interval = j.opt.check_interval;
-        R.max_iter = j.opt.iteration_limit;
-        R.polish = prec == PREC_MIXED ? 1 : 0;
-        R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
-        R.cg_tol = 0.1 * j.opt.tolerance;
-        R.polish_switch = j.opt.polish_switch;
-        // a step-stable chunk (its last three iterates share their active set) starts the polish at
-        // 3x the switch, except on chain-like rows of fewer than 4 nonzeros (tridiagonal: the free
-        // runs are long, and an early polish costs more CG iterations than the FISTA steps it saves)
-        R.step_switch = j.nnz >= 4 * j.n ? 3.0 * j.opt.polish_switch : 0.0;
-        // tiles
         for (Tile& t : j.tiles) t.inst = slot;
         const int begin = static_cast<int>(h_tiles_.size());
         if (!ensure_tables(0, begin + static_cast<int>(j.tiles.size()), why)) return false;
@@ -1048,42 +1100,40 @@ bool Engine::admit(Job& j, std::string& why) {
         h_ranges_[slot] = int2{begin, static_cast<int>(h_tiles_.size())};
         tables_dirty_ = true;
     }
-    reset_record(j);
-    InstDev& R = j.rec;
-    if (!cuda_ok(cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_), why, "instance record")) return false;
-    if (tables_dirty_) {
-        if (!h_tiles_.empty())
-            cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
-        cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * n_inst_, cudaMemcpyHostToDevice, stream_);
-        tables_dirty_ = false;
-    }
-    const View v = view();
-    if (!j.resolve) {
-        const Layout& L = j.layout;
-        const size_t Z = static_cast<size_t>(j.nnz);
-        if (prec == PREC_MIXED) {
-            void* tmp = nullptr;
-            if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, stream_), why, "allocate upload buffer")) return false;
-            if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, stream_);
-            launch_prepare_instance(v, j.slot, j.n, j.nnz, static_cast<const double*>(tmp), stream_);
-            cudaFreeAsync(tmp, stream_);
+    if (!cuda_ok(cudaStreamWaitEvent(stream_, uev_, 0), why, "upload order")) return false;
+    if (!rearm(jobs, why)) return false;
+    if (graph_grid_ < grid_max_ && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
+    return true;
+}
+
+// While a graph runs: uploads the new solves at the head of the queue that fit under the cap.
+void Engine::upload_waiting() {
+    std::unique_lock<std::mutex> lk(mu_);
+    while (!queue_.empty() && !stop_) {
+        Job* j = queue_.front();
+        if (j->resolve) break;
+        const size_t need = make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
+        if (resident_bytes_ + need > cap_) break;
+        queue_.pop_front();
+        j->state = JOB_ADMITTING;
+        resident_bytes_ += need;
+        lk.unlock();
+        std::string why;
+        const bool ok = upload(*j, why);
+        free_inputs(*j);
+        lk.lock();
+        if (ok) {
+            uploaded_.push_back(j);
         } else {
-            double* val = at<double>(j.slab, L.val64);
-            if (Z) cudaMemcpyAsync(val, j.val, Z * 8, cudaMemcpyHostToDevice, stream_);
-            launch_prepare_instance(v, j.slot, j.n, j.nnz, val, stream_);
+            resident_bytes_ -= need;
+            j->error = BQP_ERR_CUDA;
+            j->error_text = why;
+            j->state = JOB_DONE;
+            if (j->notify) completed_.push_back(j->id);
+            set_error(why);
+            cv_done_.notify_all();
         }
     }
-    launch_init_instance(v, j.slot, static_cast<int>(j.n), prec, stream_);
-    if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
-    if (host_profile()) {
-        const double t1 = host_seconds();
-        cudaStreamSynchronize(stream_);
-        std::fprintf(stderr, "[boxqp] admit n=%lld: enqueue %.3f ms, device done %.3f ms\n", static_cast<long long>(j.n),
-                     1e3 * (t1 - t0), 1e3 * (host_seconds() - t0));
-    }
-    const int grid_max = grid_max_;
-    if (graph_grid_ < grid_max && static_cast<int>(h_tiles_.size()) > graph_grid_) graph_valid_ = false;
-    return true;
 }
 
 void Engine::process_frees() {
@@ -1145,6 +1195,19 @@ bool Engine::run_once(std::string& why) {
     cudaEventRecord(ev1_, stream_);
     cudaMemcpyAsync(h_status_, d_status_, sizeof(int32_t) * std::max(n_inst_, 1), cudaMemcpyDeviceToHost, stream_);
     cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
+    // while the device runs the launch, upload the new solves that arrive (they are installed
+    // before the next launch); a host callback behind the launch ends the wait
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        launch_done_ = false;
+    }
+    if (!cuda_ok(cudaLaunchHostFunc(stream_, &Engine::on_launch_done, this), why, "launch callback")) return false;
+    for (;;) {
+        upload_waiting();
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_work_.wait(lk, [&] { return launch_done_ || stop_ || uploadable_head(); });
+        if (launch_done_ || stop_) break;
+    }
     if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine launch")) return false;
     const double dt = host_seconds() - t0;
     float ms = 0;
@@ -1307,9 +1370,9 @@ void Engine::loop() {
                 admitted = true;
                 continue;
             }
-            const size_t need = j->resolve ? 0 : make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
-            if (!j->resolve && resident_bytes_ + need > cap_) {
-                if (n_running_ == 0) {
+            const size_t need = make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
+            if (resident_bytes_ + need > cap_) {
+                if (n_running_ == 0 && uploaded_.empty()) {
                     queue_.pop_front();
                     j->error = BQP_ERR_ADMISSION;
                     j->error_text = "solve does not fit under the device-memory cap";
@@ -1325,14 +1388,11 @@ void Engine::loop() {
             resident_bytes_ += need;
             lk.unlock();
             std::string why;
-            bool ok = admit(*j, why);
-            if (!j->resolve) free_inputs(*j);
+            const bool ok = upload(*j, why);
+            free_inputs(*j);
             lk.lock();
             if (ok) {
-                j->state = JOB_RUNNING;
-                slot_job_[j->slot] = j;
-                n_running_++;
-                admitted = true;
+                uploaded_.push_back(j);
             } else {
                 resident_bytes_ -= need;
                 j->error = BQP_ERR_CUDA;
@@ -1342,6 +1402,32 @@ void Engine::loop() {
                 set_error(why);
                 cv_done_.notify_all();
             }
+        }
+        // install what was uploaded here and during the previous launch
+        if (!uploaded_.empty()) {
+            std::vector<Job*> batch;
+            batch.swap(uploaded_);
+            lk.unlock();
+            std::string why;
+            const bool ok = install(batch, why);
+            lk.lock();
+            for (Job* j : batch) {
+                if (ok) {
+                    j->state = JOB_RUNNING;
+                    slot_job_[j->slot] = j;
+                    n_running_++;
+                } else {
+                    j->error = BQP_ERR_CUDA;
+                    j->error_text = why;
+                    j->state = JOB_DONE;
+                    if (j->notify) completed_.push_back(j->id);
+                }
+            }
+            if (!ok) {
+                set_error(why);
+                cv_done_.notify_all();
+            }
+            admitted = true;
         }
         if (admitted) {
             peak_resident_ = std::max(peak_resident_, n_running_);

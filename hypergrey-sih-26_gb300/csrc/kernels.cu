@@ -1454,26 +1454,36 @@ __global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __
 // the diagonal dual-gap gate) and, for mixed precision, hi/lo FP32 values (val ~= hi + lo), the
 // FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
 // so FP32 iterates never leave the FP64 box).
-__global__ void prepare_kernel(View v, int slot, int n, const double* __restrict__ val) {
-    InstDev& I = v.inst[slot];
-    const int stride = gridDim.x * blockDim.x;
-    const int first = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const double* __restrict__ val) {
+    // diagonal (at most one entry per row after the CSR build): four lanes per row, warp-uniform passes
+    const int lane = threadIdx.x & 31, sub = lane >> 2, sl = lane & 3;
+    const int warp_id = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int warps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
     double* diag = const_cast<double*>(I.diag);
-    for (int r = first; r < n; r += stride) {
-        const int ks = I.rowptr[r], ke = I.rowptr[r + 1];
+    for (int base = warp_id * 8; base < n; base += warps * 8) {
+        const int r = base + sub;
         double d = 0;
-        for (int k = ks; k < ke; ++k) if (I.col[k] == r) d += val[k];
-        diag[r] = d;
-        if (I.precision == PREC_MIXED) {
-            const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
-            const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
-            const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
-            const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+        if (r < n) {
+            const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+            for (int k = ks + sl; k < ke; k += 4)
+                if (__ldg(I.col + k) == r) d += val[k];
+        }
+        d += __shfl_xor_sync(0xffffffffu, d, 1);
+        d += __shfl_xor_sync(0xffffffffu, d, 2);
+        if (r < n && sl == 0) {
+            diag[r] = d;
+            if (I.precision == PREC_MIXED) {
+                const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
+                const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
+                const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
+                const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+            }
         }
     }
     if (I.precision == PREC_MIXED) {
         const int nnz = I.rowptr[n];
-        for (int k = first; k < nnz; k += stride) {
+        const int stride = gridDim.x * blockDim.x;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += stride) {
             const double x = val[k];
             const float hi = __double2float_rn(x);
             const_cast<float*>(I.vhi)[k] = hi;
@@ -1649,12 +1659,12 @@ void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, con
     if (n_spans > 0) rearm_kernel<<<n_spans, kBlock, 0, s>>>(v, stage, slots, spans);
 }
 
-void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
-    int64_t work = n > nnz ? n : nnz;
+void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
+    int64_t work = n * 4 > nnz ? n * 4 : nnz;
     int64_t grid = (work + kBlock - 1) / kBlock;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid < 1) grid = 1;
-    prepare_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(v, slot, static_cast<int>(n), val);
+    prepare_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), val);
 }
 
 int check_grid(int64_t n) {

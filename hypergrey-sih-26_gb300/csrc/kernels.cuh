@@ -29,7 +29,8 @@ void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, c
 void launch_gate_plain(const View& v, cudaStream_t s);
 void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
-void launch_prepare_instance(const View& v, int slot, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
+// The record is passed by value: the instance is installed in its slot later, between graph launches.
+void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
 // Admission: x0 = clip(0, l, u), w = x0, start clock; one instance.
 // Re-arm of resident solves: records staged on the device, spans (staged index, first row) of
 // kRearmRows rows each, one block per span.
