@@ -189,7 +189,30 @@ def run_reference(args, world, rank, pg):
                              'sample': f'{args.steps} full FP64 solves of the workload at KKT<={args.tol:g} '
                                        f'({info.get("iterations")} iterations each)'},
             'e2e': {'value': value, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    gpu = reference_gpu_row(inst, args.tol)
+    if gpu:
+        line['reference_gpu'] = gpu
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_row(inst, tol):
+    """The reference's own CUDA plugin on this GPU: its kernels (src/cuda_box.cu, compiled unmodified
+    for sm_103a into oracle/_ref) under its host loop with the host check every 25 iterations.
+    Reported beside the reference arm's CPU value (which stays the arm's `value`); one solve."""
+    from oracle import oracle as O
+    if not O.REF_CUBIN.exists():
+        return {'unavailable': 'the reference CUDA module was not built (no reference checkout where build() ran)'}
+    if not O.build_ref_cuda():
+        return {'unavailable': 'the driver-API harness did not compile'}
+    try:
+        status, st, x, (solve_s, loop_s) = O.ref_cuda_solve(
+            inst['rowptr'], inst['col'], inst['val'], *oracle_args(inst), tol=tol, time_limit=120.0)
+    except Exception as exc:
+        return {'unavailable': str(exc)[:200]}
+    return {'value': 1.0 / solve_s, 'unit': 'solves/s', 'status': status, 'iterations': int(st['iterations']),
+            'seconds_per_solve': solve_s, 'loop_seconds': loop_s,
+            'kind': 'reference CUDA plugin kernels (src/cuda_box.cu, unmodified, sm_103a) under the reference host '
+                    'loop (src/accelerated_qp.cpp:36-57): 2 launches per iteration, host check every 25'}
 
 
 def run_ours(args, world, rank, local, pg):

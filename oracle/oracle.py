@@ -6,8 +6,11 @@ Two libraries:
   oracle/_ref/libsovereign_ref.so  the reference's own solver sources compiled by
                                  oracle/ref.mk plus oracle/ref_shim.cpp (only where the
                                  reference checkout exists)
-Only the tests, the smoke check and the benchmark's CPU-baseline leg use this module; the
-engine never does.
+  oracle/_build/libref_cuda.so   oracle/ref_cuda_harness.c: the reference's CUDA plugin kernels
+                                 (oracle/_ref/cuda_box_sm103a.cubin, built by oracle/ref.mk from
+                                 the reference's cuda_box.cu) under the reference's host loop
+Only the tests, the smoke check and the benchmark's CPU-baseline leg and reference arm use this
+module; the engine never does.
 """
 import ctypes
 import subprocess
@@ -20,6 +23,9 @@ HERE = Path(__file__).resolve().parent
 ORACLE_SRC = HERE / 'boxqp_oracle.c'
 ORACLE_LIB = HERE / '_build' / 'liboracle.so'
 REF_LIB = HERE / '_ref' / 'libsovereign_ref.so'
+REF_CUBIN = HERE / '_ref' / 'cuda_box_sm103a.cubin'
+REF_CUDA_SRC = HERE / 'ref_cuda_harness.c'
+REF_CUDA_LIB = HERE / '_build' / 'libref_cuda.so'
 
 STATUS = {0: 'optimal', 1: 'iteration_limit', 2: 'time_limit', 3: 'numerical_error',
           4: 'unsupported_curvature', 5: 'infeasible_bounds', 6: 'zero_hessian'}
@@ -46,6 +52,61 @@ def build_oracle(force=False):
                         str(ORACLE_SRC), '-o', str(tmp), '-lm'], check=True, capture_output=True)
         tmp.replace(ORACLE_LIB)
     return ORACLE_LIB
+
+
+def build_ref_cuda(force=False):
+    """Compiles the driver-API harness for the reference's CUDA kernels (with the oracle's checker);
+    True on success (needs the CUDA headers and a libcuda to link against)."""
+    srcs = [REF_CUDA_SRC, ORACLE_SRC]
+    if not force and REF_CUDA_LIB.exists() and all(p.stat().st_mtime <= REF_CUDA_LIB.stat().st_mtime for p in srcs):
+        return True
+    REF_CUDA_LIB.parent.mkdir(exist_ok=True)
+    tmp = REF_CUDA_LIB.with_suffix('.tmp.so')
+    cmd = ['gcc', '-O2', '-std=gnu11', '-fopenmp', '-fPIC', '-shared', '-ffp-contract=off', '-I/usr/local/cuda/include',
+           *[str(p) for p in srcs], '-o', str(tmp), '-L/usr/local/cuda/lib64/stubs', '-L/usr/local/cuda/lib64', '-lcuda',
+           '-lm']
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        return False
+    tmp.replace(REF_CUDA_LIB)
+    return True
+
+
+def build_ref_cubin(ref_dir='/root/reference/02-software/solver'):
+    """Compiles the reference's cuda_box.cu for sm_103a into oracle/_ref (only where the reference
+    checkout exists); True when the module is present afterwards."""
+    if Path(ref_dir).is_dir():
+        subprocess.run(['make', '-s', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}', 'cuda_cubin'], cwd=str(HERE.parent),
+                       capture_output=True, text=True)
+    return REF_CUBIN.exists()
+
+
+def ref_cuda_solve(rowptr, col, val, hrow, hcol, hval, cost, lower, upper, tol=1e-6, iteration_limit=200000,
+                   time_limit=120.0):
+    """The reference's CUDA plugin (its own kernels) under its host loop; returns
+    (status name, stats dict, x, (solve seconds, loop seconds))."""
+    L = ctypes.CDLL(str(REF_CUDA_LIB))
+    L.ref_cuda_solve.restype = c_int
+    L.ref_cuda_solve.argtypes = [c_char_p, c_int64, _I32P, _I32P, _F64P, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P,
+                                 _F64P, c_double, c_int64, c_double, _F64P, POINTER(OrcStats), POINTER(c_int), _F64P,
+                                 c_char_p, c_int]
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    n = cost.shape[0]
+    x = np.zeros(n)
+    st = OrcStats()
+    status = c_int(-1)
+    secs = np.zeros(2)
+    err = ctypes.create_string_buffer(512)
+    rc = L.ref_cuda_solve(str(REF_CUBIN).encode(), n, _p(rowptr, c_int32), _p(col, c_int32), _p(val, c_double),
+                          hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double), _p(cost, c_double),
+                          _p(lower, c_double), _p(upper, c_double), tol, iteration_limit, time_limit, _p(x, c_double),
+                          ctypes.byref(st), ctypes.byref(status), _p(secs, c_double), err, 512)
+    if rc != 0:
+        raise RuntimeError('reference CUDA plugin: ' + err.value.decode(errors='replace'))
+    return STATUS.get(status.value, str(status.value)), st.as_dict(), x, (float(secs[0]), float(secs[1]))
 
 
 def build_reference(ref_dir='/root/reference/02-software/solver'):

@@ -56,3 +56,13 @@ $(OUT)/solver_cli_gb300: $(LVL_OBJS) $(REF)/src/main.cpp
 level_a: $(OUT)/solver_scale_gb300 $(OUT)/solver_cli_gb300
 
 .PHONY: level_a
+
+# The reference's CUDA plugin kernels, unmodified, compiled for this GPU into a loadable module
+# (device code only; oracle/ref_cuda_harness.c drives it with the reference's host loop).
+NVCC ?= nvcc
+$(OUT)/cuda_box_sm103a.cubin: $(REF)/src/cuda_box.cu | $(OUT)
+	$(NVCC) -cubin -gencode arch=compute_103a,code=sm_103a -O3 -I$(REF)/include -w -o $@ $<
+
+cuda_cubin: $(OUT)/cuda_box_sm103a.cubin
+
+.PHONY: cuda_cubin
