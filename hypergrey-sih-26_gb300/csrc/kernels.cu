@@ -174,13 +174,20 @@ __device__ Acc reduce_instance(const View& v, int tb, int te) {
 
 // The CG reductions carry one sum (a) and one maximum (b): the same fixed order on those two
 // fields alone, eight partials in flight per thread.
-__device__ Acc block_reduce_ab(Acc v) {
+// Only lanes that are multiples of `lanes` hold values (the group leaders of a sub-warp pass),
+// and a warp without data (`warp_data` false) contributes zeros: the FP64 additions of the
+// xor tree run only where there is something to add (FP64 is 1/64 of the FP32 rate here).
+__device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true) {
     __shared__ double part_a[kBlock / 32];
     __shared__ unsigned long long part_b[kBlock / 32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        v.a += shfl_xor(v.a, o);
-        v.b = umax64(v.b, shfl_xor(v.b, o));
+    if (warp_data) {
+        for (int o = 16; o >= lanes; o >>= 1) {  // warp-uniform
+            v.a += shfl_xor(v.a, o);
+            v.b = umax64(v.b, shfl_xor(v.b, o));
+        }
+    } else {
+        v.a = 0;
+        v.b = 0;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
@@ -1153,7 +1160,7 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         polish_rows<true>(I, T.row_begin, I.free_cnt[t - R.x], a);
-        Acc total = block_reduce_ab(a);
+        Acc total = block_reduce_ab(a, I.lanes_res);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
@@ -1177,7 +1184,7 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         polish_rows<false>(I, T.row_begin, I.free_cnt[t - R.x], a);
-        Acc total = block_reduce_ab(a);
+        Acc total = block_reduce_ab(a, I.lanes_cg);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
@@ -1222,7 +1229,7 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
             a.a = fma(rr, zz, a.a);
             a.b = umax64(a.b, cg_ratio_bits(rr, xv));
         }
-        Acc total = block_reduce_ab(a);
+        Acc total = block_reduce_ab(a, 1, (threadIdx.x & ~31u) < static_cast<unsigned>(n_free));
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
@@ -1455,34 +1462,24 @@ __global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __
 // FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
 // so FP32 iterates never leave the FP64 box).
 __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const double* __restrict__ val) {
-    // diagonal (at most one entry per row after the CSR build): four lanes per row, warp-uniform passes
-    const int lane = threadIdx.x & 31, sub = lane >> 2, sl = lane & 3;
-    const int warp_id = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int warps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    // diagonal (at most one entry per row after the CSR build), one thread per row
+    const int stride = gridDim.x * blockDim.x;
     double* diag = const_cast<double*>(I.diag);
-    for (int base = warp_id * 8; base < n; base += warps * 8) {
-        const int r = base + sub;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
         double d = 0;
-        if (r < n) {
-            const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
-            for (int k = ks + sl; k < ke; k += 4)
-                if (__ldg(I.col + k) == r) d += val[k];
-        }
-        d += __shfl_xor_sync(0xffffffffu, d, 1);
-        d += __shfl_xor_sync(0xffffffffu, d, 2);
-        if (r < n && sl == 0) {
-            diag[r] = d;
-            if (I.precision == PREC_MIXED) {
-                const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
-                const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
-                const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
-                const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
-            }
+        for (int k = ks; k < ke; ++k)
+            if (__ldg(I.col + k) == r) d += val[k];
+        diag[r] = d;
+        if (I.precision == PREC_MIXED) {
+            const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
+            const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
+            const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
+            const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
         }
     }
     if (I.precision == PREC_MIXED) {
         const int nnz = I.rowptr[n];
-        const int stride = gridDim.x * blockDim.x;
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += stride) {
             const double x = val[k];
             const float hi = __double2float_rn(x);
@@ -1660,7 +1657,7 @@ void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, con
 }
 
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
-    int64_t work = n * 4 > nnz ? n * 4 : nnz;
+    int64_t work = n > nnz ? n : nnz;
     int64_t grid = (work + kBlock - 1) / kBlock;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid < 1) grid = 1;

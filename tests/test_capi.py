@@ -114,6 +114,23 @@ def test_csr_builder_matches_reference_assembly(seed):
             assert np.array_equal(x, y)
 
 
+def test_parallel_csr_builder_keeps_input_order_across_chunks():
+    """Enough triplets for the multi-threaded path (several chunks, several row blocks): repeated
+    entries of one row spread over all chunks must still be summed in input order."""
+    rng = np.random.default_rng(7)
+    n = 3000
+    k = 900000
+    r = rng.integers(0, n, k)
+    c = rng.integers(0, n, k)
+    hr, hc = np.maximum(r, c), np.minimum(r, c)
+    hv = rng.standard_normal(k) * 10.0 ** rng.integers(-8, 8, k)  # sums whose value depends on order
+    hv[rng.random(k) < 0.05] = 0.0
+    a = boxqp.csr_from_lower(n, hr, hc, hv, 1.0)
+    b = O.build_csr(n, hr, hc, hv, 1.0)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
 def test_gershgorin_matches_oracle():
     g = boxqp.planted('graph10k', seed=3, n=2000)
     assert boxqp.gershgorin(g['rowptr'], g['val']) == O.max_abs_row_sum(g['rowptr'], g['val'])
