@@ -21,7 +21,7 @@ class Options(ctypes.Structure):
     _fields_ = [('tolerance', c_double), ('time_limit', c_double), ('iteration_limit', c_int64),
                 ('precision', c_int32), ('lipschitz', c_int32), ('check_interval', c_int32),
                 ('diagonal_gate', c_int32), ('offset', c_double), ('kernel_variant', c_int32),
-                ('reserved', c_int32), ('polish_switch', c_double)]
+                ('scaling', c_int32), ('polish_switch', c_double)]
 
 
 class Stats(ctypes.Structure):

@@ -94,7 +94,8 @@ def _i64(a):
 
 
 def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, precision='fp64',
-                   check_interval=0, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None):
+                   check_interval=0, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None,
+                   scaling=0):
     o = Options()
     lib().bqp_options_default(o)
     o.tolerance = float(tolerance)
@@ -107,6 +108,7 @@ def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, prec
     o.kernel_variant = int(kernel_variant)
     if polish_switch is not None:
         o.polish_switch = float(polish_switch)
+    o.scaling = int(scaling)
     return o
 
 

@@ -63,6 +63,7 @@ struct Layout {
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
+    size_t sstep = kNone, lprec = kNone;
     size_t total = 0;
 };
 
@@ -111,6 +112,8 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.lo_ff = take(Z * 4);
         L.cnt_ff = take(N * 4);
         L.start_ff = take(N * 4);
+        L.sstep = take(N * 4);
+        L.lprec = take(8);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
@@ -1030,6 +1033,8 @@ bool Engine::upload(Job& j, std::string& why) {
     R.lo_ff = at<float>(slab, L.lo_ff);
     R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
     R.start_ff = at<int32_t>(slab, L.start_ff);
+    R.sstep = at<float>(slab, L.sstep);
+    R.lprec = at<double>(slab, L.lprec);
     // polish lanes per row: about a quarter of the average row length, a power of two
     auto lanes_for = [](double avg) {
         int lanes = 1;
@@ -1062,6 +1067,7 @@ bool Engine::upload(Job& j, std::string& why) {
         if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, ustream_), why, "allocate upload buffer")) return false;
         if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
         launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(tmp), ustream_);
+        launch_precondition(R, j.n, static_cast<const double*>(tmp), j.opt.scaling != 2, ustream_);
         cudaFreeAsync(tmp, ustream_);
     } else {
         double* val = at<double>(slab, L.val64);
@@ -1491,6 +1497,10 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
         why = "Invalid box QP options";
         return BQP_ERR_INVALID;
     }
+    if (o->scaling < 0 || o->scaling > 2) {
+        why = "Invalid box QP options";
+        return BQP_ERR_INVALID;
+    }
     if (o->lipschitz != BQP_LIPSCHITZ_GERSHGORIN) {
         why = o->lipschitz == BQP_LIPSCHITZ_POWER ? "the power-iteration Lipschitz estimate is not implemented"
                                                    : "Invalid box QP options";
@@ -1641,11 +1651,13 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     j->nnz = nnz;
     j->opt = o;
     // Engine defaults (0 = auto).  FP64 engines check every 25 iterations, the reference's
-    // cadence.  The mixed engine checks only to find its polish point: on instances whose rows
-    // average 8 or more nonzeros (FISTA steps bound by their random gathers) every 10 iterations
-    // with a polish switch at stationarity 0.1, else every 25 with a switch at 0.03.
-    const bool gather_heavy = o.precision == BQP_PRECISION_MIXED && nnz >= 8 * n;
-    if (j->opt.check_interval == 0) j->opt.check_interval = gather_heavy ? 10 : 25;
+    // cadence.  The mixed engine checks only to find its polish point.  Where a FISTA step is
+    // dear (rows of 8 or more nonzeros, bound by their random gathers, and 4M or more nonzeros)
+    // it checks every 8 iterations (the first check after 12) with a polish switch at
+    // stationarity 0.1; elsewhere a check costs several steps, and it checks every 25 with a
+    // switch at 0.03.
+    const bool dear_steps = o.precision == BQP_PRECISION_MIXED && nnz >= 8 * n && nnz >= 4000000;
+    if (j->opt.check_interval == 0) j->opt.check_interval = dear_steps ? 8 : 25;
     if (j->opt.polish_switch == 0) j->opt.polish_switch = j->opt.check_interval <= 10 ? 0.1 : 3e-2;
     j->lipschitz = lipschitz;
     if (o.diagonal_gate >= 0) j->diag_gate = o.diagonal_gate ? 1 : 0;
@@ -1698,7 +1710,7 @@ void bqp_options_default(bqp_options* o) {
     o->diagonal_gate = -1;
     o->offset = 0;
     o->kernel_variant = -1;
-    o->reserved = 0;
+    o->scaling = 0;
     o->polish_switch = 0;
 }
 

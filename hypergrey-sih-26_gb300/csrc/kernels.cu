@@ -654,14 +654,14 @@ __device__ void step_rows_staged(const InstDev& I, int rb, int re, int j, int tr
         const float* __restrict__ l = I.l32;
         const float* __restrict__ u = I.u32;
         const float beta = static_cast<float>(I.beta[j]);
-        const float invL = I.invLf;
+        const float* __restrict__ sstep = I.sstep;  // per-row step (preconditioned or 1/L)
         float* buf = warp_buffer<float>();
         bool moved = false;
         warp_groups<float>(
             I.rowptr, rb, re, buf, [&](int k) { return __ldg(val + k) * __ldg(win + __ldg(col + k)); },
             [](float a, float b) { return a + b; }, 0.f,
             [&](int r, float g) {
-                const float v = __ldg(win + r) - (g + __ldg(c + r)) * invL;
+                const float v = __ldg(win + r) - (g + __ldg(c + r)) * __ldg(sstep + r);
                 const float lo = __ldg(l + r), up = __ldg(u + r);
                 const float nx = smaxf(lo, sminf(up, v));
                 const float xo = x[r];
@@ -719,6 +719,7 @@ __device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j, int t
         val = I.val64; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
         beta = I.beta[j]; invL = I.invL;
     }
+    const float* __restrict__ sstep = I.sstep;
     bool moved = false;
     for (int base = rb + warp * RPW; base < re; base += (kBlock / 32) * RPW) {
         const int r = base + sub;
@@ -730,7 +731,10 @@ __device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j, int t
         }
         acc = group_sum<LANES>(acc);
         if (r < re && sl == 0) {
-            const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+            T step;
+            if constexpr (PREC == PREC_MIXED) step = __ldg(sstep + r);  // per-row step
+            else step = invL;
+            const T v = __ldg(win + r) - (acc + __ldg(c + r)) * step;
             const T lo = __ldg(l + r), up = __ldg(u + r);
             const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
             const T xo = x[r];
@@ -770,6 +774,7 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j, int tra
         val = I.val64 + kb; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
         beta = I.beta[j]; invL = I.invL;
     }
+    const float* __restrict__ sstep = I.sstep;
 #pragma unroll 8
     for (int k = threadIdx.x; k < cnt; k += kBlock) prod[k] = __ldg(val + k) * __ldg(win + __ldg(cl + k));
     __syncthreads();
@@ -778,7 +783,10 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j, int tra
         const int a = __ldg(rowptr + r) - kb, b = __ldg(rowptr + r + 1) - kb;
         T acc = 0;
         for (int k = a; k < b; ++k) acc += prod[k];
-        const T v = __ldg(win + r) - (acc + __ldg(c + r)) * invL;
+        T step;
+        if constexpr (PREC == PREC_MIXED) step = __ldg(sstep + r);  // per-row step
+        else step = invL;
+        const T v = __ldg(win + r) - (acc + __ldg(c + r)) * step;
         const T lo = __ldg(l + r), up = __ldg(u + r);
         const T nx = (lo < ((up < v) ? up : v)) ? ((up < v) ? up : v) : lo;
         const T xo = x[r];
@@ -1418,14 +1426,14 @@ __device__ void start_instance(InstDev& I) {
         I.end_ns = 0;
         if (I.arm_chunk) {
             // mixed precision: x0 = clip(0) is not checked; the first chunk of steps is armed here
-            // as a check of x0 would arm it.  With a short interval the first chunk is two
-            // intervals long: the active set still moves in the first steps, so a check there
-            // could not start the polish.
+            // as a check of x0 would arm it.  With a short interval the first chunk is one and a
+            // half intervals long: the active set still moves in the first steps, so a check
+            // there could not start the polish.
             I.it0 = 0;
             I.it_cur = 0;
             I.moved[0] = 0;
             I.moved[1] = 0;
-            const int64_t first = 2 * I.interval <= kMaxInterval ? 2 * I.interval : I.interval;
+            const int64_t first = I.interval <= 16 ? I.interval + I.interval / 2 : I.interval;
             I.it_next = first < I.max_iter ? first : I.max_iter;
             fista_betas(I, I.it_next);
             I.fista_iters += I.it_next;
@@ -1486,6 +1494,42 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
             const_cast<float*>(I.vhi)[k] = hi;
             const_cast<float*>(I.vlo)[k] = __double2float_rn(x - static_cast<double>(hi));
         }
+    }
+}
+
+// Diagonally preconditioned FISTA (mixed engine): FISTA on y = D^1/2 x (D = diag Q) is FISTA on
+// x with the per-row step v_i^2 / L', v_i = Q_ii^-1/2 (rows without a positive diagonal keep
+// v_i = L^-1/2, L the plain Gershgorin bound) and L' = max_i v_i sum_j |Q_ij| v_j, the Gershgorin
+// bound of V Q V.  The box stays a box, so the projection maps over unchanged.
+__device__ __forceinline__ double precond_v(const InstDev& I, int r) {
+    return I.diag[r] > 0 ? sqrt(I.dinv[r]) : 1.0 / sqrt(I.L);
+}
+
+__global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n, const double* __restrict__ val) {
+    const int stride = gridDim.x * blockDim.x;
+    unsigned long long best = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+        double sum = 0;
+        for (int k = ks; k < ke; ++k) sum += fabs(val[k]) * precond_v(I, __ldg(I.col + k));
+        best = umax64(best, dbits(sum * precond_v(I, r)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = umax64(best, shfl_xor(best, o));
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(reinterpret_cast<unsigned long long*>(I.lprec), best);
+}
+
+// scaled = 0: the scalar step 1/L in every row.
+__global__ void __launch_bounds__(kBlock) precond_step_kernel(InstDev I, int n, int scaled) {
+    const int stride = gridDim.x * blockDim.x;
+    const double lp = scaled ? *I.lprec : 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        double s = I.invL;
+        if (scaled && lp > 0) {
+            const double v = precond_v(I, r);
+            s = v * v / lp;
+        }
+        I.sstep[r] = static_cast<float>(s);
     }
 }
 
@@ -1654,6 +1698,17 @@ void launch_init_instance(const View& v, int slot, int n, int precision, cudaStr
 void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, const int2* spans, int n_spans,
                   cudaStream_t s) {
     if (n_spans > 0) rearm_kernel<<<n_spans, kBlock, 0, s>>>(v, stage, slots, spans);
+}
+
+void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, cudaStream_t s) {
+    int64_t grid = (n + kBlock - 1) / kBlock;
+    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid < 1) grid = 1;
+    if (scaled) {
+        cudaMemsetAsync(rec.lprec, 0, sizeof(double), s);
+        precond_bound_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), val);
+    }
+    precond_step_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), scaled ? 1 : 0);
 }
 
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {

@@ -31,6 +31,9 @@ void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
 // The record is passed by value: the instance is installed in its slot later, between graph launches.
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
+// Mixed engine: per-row FISTA steps (diagonally preconditioned when `scaled`, else 1/L), after
+// launch_prepare_instance on the same stream; val = the FP64 values.
+void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, cudaStream_t s);
 // Admission: x0 = clip(0, l, u), w = x0, start clock; one instance.
 // Re-arm of resident solves: records staged on the device, spans (staged index, first row) of
 // kRearmRows rows each, one block per span.

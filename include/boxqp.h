@@ -77,7 +77,11 @@ typedef struct bqp_options {
     double  offset;           /* constant term of the objective (LinearProblem::offset)          */
     int32_t kernel_variant;   /* SpMV structure of the FISTA step: -1 auto (tuning default), 0 block-
                                  staged tile, 64 warp-staged rows, 1/2/4/8/16/32 lanes per row     */
-    int32_t reserved;         /* must be 0                                                       */
+    int32_t scaling;          /* mixed engine: 0 auto (= 1), 1 diagonally preconditioned FISTA steps
+                                 (per-row step 1 / (L' Q_ii), L' the Gershgorin bound of
+                                 D^-1/2 Q D^-1/2: FISTA in Jacobi-scaled variables, with iterates,
+                                 checks and results in the original ones), 2 scalar step 1/L.
+                                 The FP64 engines always take the reference's scalar step.      */
     double  polish_switch;    /* mixed: stationarity at or below which, with the active set
                                  unchanged since the previous check, the FP64 free-set polish is
                                  attempted (x0.1 after each failed attempt); default 0 = auto:
