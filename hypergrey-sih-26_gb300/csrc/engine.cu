@@ -1056,7 +1056,7 @@ bool Engine::upload(Job& j, std::string& why) {
     R.max_iter = j.opt.iteration_limit;
     R.polish = prec == PREC_MIXED ? 1 : 0;
     R.cg_max = std::max<int64_t>(50, std::min<int64_t>(5000, j.n));
-    R.cg_tol = 0.1 * j.opt.tolerance;
+    R.cg_tol = 0.3 * j.opt.tolerance;
     R.polish_switch = j.opt.polish_switch;
     // a step-stable chunk (its last three iterates share their active set) starts the polish at
     // 3x the switch, except on chain-like rows of fewer than 4 nonzeros (tridiagonal: the free
