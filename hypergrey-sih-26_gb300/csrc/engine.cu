@@ -63,7 +63,7 @@ struct Layout {
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
-    size_t sstep = kNone, lprec = kNone;
+    size_t sstep = kNone, lprec = kNone, s = kNone;
     size_t total = 0;
 };
 
@@ -113,6 +113,7 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.cnt_ff = take(N * 4);
         L.start_ff = take(N * 4);
         L.sstep = take(N * 4);
+        L.s = take(N * 8);
         L.lprec = take(8);
     } else {
         L.x64 = take(N * 8);
@@ -628,9 +629,8 @@ bool Engine::run_stream(int cap, std::string& why) {
             // every iteration; this mode serves per-kernel profiling, not speed)
             for (int j = 0; j < kCgPerBody; ++j) {
                 launch_cg_matvec(v, grid, stream_);
-                launch_cg_update(v, grid, stream_);
-                launch_cg_direction(v, grid, stream_);
-                kernels += 3;
+                launch_cg_vector(v, grid, stream_);
+                kernels += 2;
                 cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
                 if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine polish")) return false;
                 if (h_ctrl_->n_cg <= 0) break;
@@ -745,8 +745,7 @@ bool Engine::build_graph(std::string& why) {
         if (!add_cond(inner, head, h_cg, cudaGraphCondTypeWhile, &loop_node, &loop_body)) return false;
         if (!capture(loop_body, nullptr, 0, [&] {
                 launch_cg_matvec(v, grid, capture_);
-                launch_cg_update(v, grid, capture_);
-                launch_cg_direction(v, grid, capture_, h_cg, kCgPerBody);
+                launch_cg_vector(v, grid, capture_, h_cg, kCgPerBody);
             }, nullptr)) return false;
         last = node;
     }
@@ -1034,6 +1033,7 @@ bool Engine::upload(Job& j, std::string& why) {
     R.cnt_ff = at<int32_t>(slab, L.cnt_ff);
     R.start_ff = at<int32_t>(slab, L.start_ff);
     R.sstep = at<float>(slab, L.sstep);
+    R.s = at<double>(slab, L.s);
     R.lprec = at<double>(slab, L.lprec);
     // polish lanes per row: about a quarter of the average row length, a power of two
     auto lanes_for = [](double avg) {

@@ -92,6 +92,7 @@ struct __align__(16) InstDev {
     double* r;
     double* p;
     double* q;
+    double* s;             // polish: s = Q p (Chronopoulos-Gear CG)
     double* z;
     uint8_t* fixed;        // polish: 1 = held at a bound
     int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row

@@ -177,33 +177,41 @@ __device__ Acc reduce_instance(const View& v, int tb, int te) {
 // Only lanes that are multiples of `lanes` hold values (the group leaders of a sub-warp pass),
 // and a warp without data (`warp_data` false) contributes zeros: the FP64 additions of the
 // xor tree run only where there is something to add (FP64 is 1/64 of the FP32 rate here).
+// The CG reductions carry two sums (a, obj) and one maximum (b).
 __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true) {
     __shared__ double part_a[kBlock / 32];
+    __shared__ double part_o[kBlock / 32];
     __shared__ unsigned long long part_b[kBlock / 32];
     if (warp_data) {
         for (int o = 16; o >= lanes; o >>= 1) {  // warp-uniform
             v.a += shfl_xor(v.a, o);
+            v.obj += shfl_xor(v.obj, o);
             v.b = umax64(v.b, shfl_xor(v.b, o));
         }
     } else {
         v.a = 0;
+        v.obj = 0;
         v.b = 0;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
         part_a[warp] = v.a;
+        part_o[warp] = v.obj;
         part_b[warp] = v.b;
     }
     __syncthreads();
     if (warp == 0) {
         double a = lane < kBlock / 32 ? part_a[lane] : 0.0;
+        double ob = lane < kBlock / 32 ? part_o[lane] : 0.0;
         unsigned long long b = lane < kBlock / 32 ? part_b[lane] : 0ull;
 #pragma unroll
         for (int o = (kBlock / 64); o > 0; o >>= 1) {
             a += shfl_xor(a, o);
+            ob += shfl_xor(ob, o);
             b = umax64(b, shfl_xor(b, o));
         }
         v.a = a;
+        v.obj = ob;
         v.b = b;
     }
     __syncthreads();
@@ -215,21 +223,24 @@ __device__ Acc reduce_instance_ab(const View& v, int tb, int te) {
     Acc acc = acc_identity();
     int k = tb + static_cast<int>(threadIdx.x);
     for (; k + (kAhead - 1) * kBlock < te; k += kAhead * kBlock) {
-        double a[kAhead];
+        double a[kAhead], ob[kAhead];
         unsigned long long b[kAhead];
 #pragma unroll
         for (int i = 0; i < kAhead; ++i) {
             a[i] = __ldcg(&v.partial[k + i * kBlock].a);
+            ob[i] = __ldcg(&v.partial[k + i * kBlock].obj);
             b[i] = __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k + i * kBlock].b));
         }
 #pragma unroll
         for (int i = 0; i < kAhead; ++i) {
             acc.a += a[i];
+            acc.obj += ob[i];
             acc.b = umax64(acc.b, b[i]);
         }
     }
     for (; k < te; k += kBlock) {
         acc.a += __ldcg(&v.partial[k].a);
+        acc.obj += __ldcg(&v.partial[k].obj);
         acc.b = umax64(acc.b, __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k].b)));
     }
     return block_reduce_ab(acc);
@@ -1038,6 +1049,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     double* __restrict__ r_out = I.r;
     double* __restrict__ z_out = I.z;
     double* __restrict__ p_out = I.p;
+    double* __restrict__ s_out = I.s;
     float2* __restrict__ p2_out = I.p2;
     for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
         const int j = g * R + sub;
@@ -1085,12 +1097,15 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
             r_out[r] = rr;
             z_out[r] = zz;
             p_out[r] = zz;
+            s_out[r] = 0.0;
             p2_out[r] = df_split(zz);
         }
     }
 }
 
-// CG product q = Q_FF p on a tile's free rows, accumulating p.q.
+// CG product w = Q_FF u on a tile's free rows (u gathered from its FP32 pairs), accumulating
+// gamma = r.u, delta = w.u and max |r|/(1+|x|) (the single reduction of the Chronopoulos-Gear
+// form of preconditioned CG).
 template <int LANES>
 __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, int n, Acc& a) {
     constexpr int R = 32 / LANES;
@@ -1101,9 +1116,11 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     const float* __restrict__ vlo = I.lo_ff;
     const int32_t* __restrict__ cnt = I.cnt_ff;
     const int32_t* __restrict__ start = I.start_ff;
-    const float2* __restrict__ p2 = I.p2;
-    const double* __restrict__ p = I.p;
-    double* __restrict__ q_out = I.q;
+    const float2* __restrict__ p2 = I.p2;  // u as FP32 pairs
+    const double* __restrict__ u = I.z;
+    const double* __restrict__ rr_v = I.r;
+    const double* __restrict__ xp = I.xp;
+    double* __restrict__ q_out = I.q;      // w
     for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
         const int j = g * R + sub;
         float2 acc = make_float2(0.f, 0.f);
@@ -1117,9 +1134,11 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
 #pragma unroll
         for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
         if (sl == 0 && r >= 0) {
-            const double qq = df_value(acc);
-            q_out[r] = qq;
-            a.a = fma(p[r], qq, a.a);
+            const double w = df_value(acc), ui = u[r], ri = rr_v[r];
+            q_out[r] = w;
+            a.a = fma(ri, ui, a.a);
+            a.obj = fma(w, ui, a.obj);
+            a.b = umax64(a.b, cg_ratio_bits(ri, xp[r]));
         }
     }
 }
@@ -1196,58 +1215,27 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
-                const double pq = inst_total.a;
-                if (pq > 0 && isfinite(pq)) {
-                    I.alpha = I.rz / pq;
-                } else {
-                    I.alpha = 0;
-                    I.cg_it = I.cg_max;  // breakdown: stop after this update
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
-    const int nt = v.ctrl->n_tiles;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-        const Tile T = v.tiles[t];
-        InstDev& I = v.inst[T.inst];
-        if (!polish_phase(I, PH_POLISH_CG)) continue;
-        const int2 R = v.ranges[T.inst];
-        const double alpha = I.alpha;
-        const int32_t* __restrict__ list = I.free_rows + T.row_begin;
-        const int n_free = I.free_cnt[t - R.x];
-        const double* __restrict__ p = I.p;
-        const double* __restrict__ q = I.q;
-        const double* __restrict__ dinv = I.dinv;
-        double* __restrict__ xp = I.xp;
-        double* __restrict__ rr_v = I.r;
-        double* __restrict__ z = I.z;
-        Acc a = acc_identity();
-        for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-            const int r = list[j];
-            const double xv = fma(alpha, p[r], xp[r]);
-            const double rr = fma(-alpha, q[r], rr_v[r]);
-            const double zz = rr * dinv[r];
-            xp[r] = xv;
-            rr_v[r] = rr;
-            z[r] = zz;
-            a.a = fma(rr, zz, a.a);
-            a.b = umax64(a.b, cg_ratio_bits(rr, xv));
-        }
-        Acc total = block_reduce_ab(a, 1, (threadIdx.x & ~31u) < static_cast<unsigned>(n_free));
-        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
-            if (threadIdx.x == 0) {
-                const double rz_new = inst_total.a;
-                I.beta_cg = I.rz > 0 ? rz_new / I.rz : 0.0;
-                I.rz = rz_new;
+                // Chronopoulos-Gear: gamma_i = r_i.u_i, delta_i = (Q u_i).u_i, beta_i =
+                // gamma_i / gamma_{i-1}, alpha_i = gamma_i / (delta_i - beta_i gamma_i / alpha_{i-1})
+                const double gamma = inst_total.a, delta = inst_total.obj;
                 I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
+                const bool first = I.cg_it == 0;
                 I.cg_it++;
                 I.cg_total++;
-                if (I.cg_res <= I.cg_tol || I.cg_it >= I.cg_max || !isfinite(rz_new)) {
+                bool stop = I.cg_res <= I.cg_tol || I.cg_it > I.cg_max || !isfinite(gamma) || !isfinite(delta);
+                if (!stop) {
+                    const double beta = first ? 0.0 : gamma / I.rz;
+                    const double den = first ? delta : delta - beta * gamma / I.alpha;
+                    const double alpha = gamma / den;
+                    if (alpha > 0 && isfinite(alpha)) {
+                        I.alpha = alpha;
+                        I.beta_cg = beta;
+                        I.rz = gamma;
+                    } else {
+                        stop = true;  // breakdown
+                    }
+                }
+                if (stop) {
                     I.phase = PH_POLISH_FINISH;
                     atomicSub(&v.ctrl->n_cg, 1);
                 }
@@ -1257,14 +1245,17 @@ __global__ void __launch_bounds__(kBlock) cg_update_kernel(View v) {
     }
 }
 
-// In a graph, block 0 also decides whether the CG loop of this body runs another iteration:
-// while an instance is still iterating and fewer than `cap` iterations ran (the instances
-// leaving CG were counted down by the update kernel, which completed before this launch).
-__global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v, cudaGraphConditionalHandle h_cg, int cap) {
+// CG vector step on the free rows: p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s,
+// u = D^-1 r (and its FP32 pairs for the next product).  No reduction: the product kernel's
+// finalizer already chose alpha and beta.  Instances that finished CG snap x into the box here.
+// In a graph, block 0 also decides whether the CG loop runs another iteration: while an instance
+// still iterates and fewer than `cap` iterations ran (the product kernel, which completed before
+// this launch, counted finishing instances down).
+__global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphConditionalHandle h_cg, int cap) {
     if (cap > 0 && blockIdx.x == 0 && threadIdx.x == 0) {
         Ctrl* ctrl = v.ctrl;
         const int it = ++ctrl->cg_iters;
-        ctrl->kernels += 3;
+        ctrl->kernels += 2;
         cudaGraphSetConditional(h_cg, (ctrl->n_cg > 0 && it < cap) ? 1u : 0u);
     }
     const int nt = v.ctrl->n_tiles;
@@ -1273,25 +1264,37 @@ __global__ void __launch_bounds__(kBlock) cg_direction_kernel(View v, cudaGraphC
         const InstDev& I = v.inst[T.inst];
         if (I.status != ST_RUNNING) continue;
         if (I.phase == PH_POLISH_CG) {
-            const double beta = I.beta_cg;
+            const double alpha = I.alpha, beta = I.beta_cg;
             const int32_t* __restrict__ list = I.free_rows + T.row_begin;
             const int n_free = I.free_cnt[t - v.ranges[T.inst].x];
-            const double* __restrict__ z = I.z;
+            const double* __restrict__ dinv = I.dinv;
+            const double* __restrict__ w = I.q;
+            double* __restrict__ u = I.z;
             double* __restrict__ p = I.p;
-            float2* __restrict__ p2 = I.p2;
+            double* __restrict__ s = I.s;
+            double* __restrict__ xp = I.xp;
+            double* __restrict__ rr_v = I.r;
+            float2* __restrict__ u2 = I.p2;
             for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
                 const int r = list[j];
-                const double pv = fma(beta, p[r], z[r]);
-                p[r] = pv;
-                p2[r] = df_split(pv);
+                const double pn = fma(beta, p[r], u[r]);
+                const double sn = fma(beta, s[r], w[r]);
+                const double rn = fma(-alpha, sn, rr_v[r]);
+                const double un = rn * dinv[r];
+                p[r] = pn;
+                s[r] = sn;
+                xp[r] = fma(alpha, pn, xp[r]);
+                rr_v[r] = rn;
+                u[r] = un;
+                u2[r] = df_split(un);
             }
         } else if (I.phase == PH_POLISH_FINISH) {
             const double* __restrict__ l = I.l;
-            const double* __restrict__ u = I.u;
+            const double* __restrict__ uu = I.u;
             double* __restrict__ xp = I.xp;
             float2* __restrict__ xp2 = I.xp2;
             for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-                const double xv = smax(l[r], smin(u[r], xp[r]));
+                const double xv = smax(l[r], smin(uu[r], xp[r]));
                 xp[r] = xv;
                 xp2[r] = df_split(xv);
             }
@@ -1481,6 +1484,8 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
         diag[r] = d;
         if (I.precision == PREC_MIXED) {
             const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
+            // preconditioner scale v_r, kept in s (free until the polish) for the step set-up
+            I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(I.L);
             const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
             const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
             const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
@@ -1500,10 +1505,9 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
 // Diagonally preconditioned FISTA (mixed engine): FISTA on y = D^1/2 x (D = diag Q) is FISTA on
 // x with the per-row step v_i^2 / L', v_i = Q_ii^-1/2 (rows without a positive diagonal keep
 // v_i = L^-1/2, L the plain Gershgorin bound) and L' = max_i v_i sum_j |Q_ij| v_j, the Gershgorin
-// bound of V Q V.  The box stays a box, so the projection maps over unchanged.
-__device__ __forceinline__ double precond_v(const InstDev& I, int r) {
-    return I.diag[r] > 0 ? sqrt(I.dinv[r]) : 1.0 / sqrt(I.L);
-}
+// bound of V Q V.  The box stays a box, so the projection maps over unchanged.  prepare_kernel
+// leaves v in the s array.
+__device__ __forceinline__ double precond_v(const InstDev& I, int r) { return I.s[r]; }
 
 __global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n, const double* __restrict__ val) {
     const int stride = gridDim.x * blockDim.x;
@@ -1640,7 +1644,7 @@ int tile_grid(int sms) {
     g_waves.matvec = wave_of(cg_matvec_kernel, sms, 0);
     g_waves.residual = wave_of(polish_residual_kernel, sms, 0);
     wave_of(check_standalone_kernel, sms, kSmem8);
-    g_waves.polish = wave_of(cg_update_kernel, sms, 0);
+    g_waves.polish = wave_of(cg_vector_kernel, sms, 0);
     int m = 0;
     for (int w : {g_waves.step[0], g_waves.step[1], g_waves.step[2], g_waves.check, g_waves.matvec, g_waves.polish})
         m = w > m ? w : m;
@@ -1672,9 +1676,8 @@ void launch_polish_residual(const View& v, int grid, cudaStream_t s) {
 void launch_cg_matvec(const View& v, int grid, cudaStream_t s) {
     cg_matvec_kernel<<<pick(grid, g_waves.matvec), kBlock, 0, s>>>(v);
 }
-void launch_cg_update(const View& v, int grid, cudaStream_t s) { cg_update_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v); }
-void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop, int cap) {
-    cg_direction_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v, cg_loop, cap);
+void launch_cg_vector(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop, int cap) {
+    cg_vector_kernel<<<pick(grid, g_waves.polish), kBlock, 0, s>>>(v, cg_loop, cap);
 }
 
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,

@@ -14,10 +14,9 @@ void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s);
 void launch_polish_init(const View& v, int grid, cudaStream_t s);
 void launch_polish_residual(const View& v, int grid, cudaStream_t s);
 void launch_cg_matvec(const View& v, int grid, cudaStream_t s);
-void launch_cg_update(const View& v, int grid, cudaStream_t s);
 // cap > 0 (inside a graph): also sets cg_loop, the WHILE handle of the CG loop, allowing at
 // most `cap` iterations per body.  cap = 0: no handle is touched (host-driven launches).
-void launch_cg_direction(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop = 0, int cap = 0);
+void launch_cg_vector(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop = 0, int cap = 0);
 // Single-block control kernels that steer the conditional graph nodes.
 // fista[k]: handle of the IF node of the precision-k step launches; polish: the IF node of the
 // polish branch; cg_loop: the WHILE node of its CG loop.  `steps`: kernels inside each FISTA body.
