@@ -1343,6 +1343,10 @@ __device__ Counts count_phases(const View& v, bool mirror) {
 }
 
 // End of a body: every instance that stepped in it (FISTA phase) advances by the steps it ran.
+// A mixed solve whose chunk just completed step-stable (no variable crossed a bound in its last
+// two steps) goes straight to its first polish attempt, without the check of the FP32 iterate:
+// the polished point is verified in FP64 anyway, and a failed attempt resumes FISTA from this
+// iterate through the checked path.
 __device__ void advance_chunks(const View& v, int steps) {
     const int n = v.ctrl->n_inst;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1350,6 +1354,14 @@ __device__ void advance_chunks(const View& v, int steps) {
         if (I.status != ST_RUNNING || I.phase != PH_FISTA) continue;
         const int64_t to = I.it_cur + steps;
         I.it_cur = to < I.it_next ? to : I.it_next;
+        if (I.it_cur == I.it_next && I.precision == PREC_MIXED && I.polish && I.polish_rounds == 0 &&
+            I.step_switch > 0 && I.it_next - I.it0 >= 2 && I.it_next < I.max_iter && I.moved[0] == 0 &&
+            I.moved[1] == 0) {
+            I.phase = PH_POLISH_INIT;
+            I.cg_it = 0;
+            I.stable_checks = 0;
+            I.iterations = I.it_next;
+        }
     }
     __syncthreads();
 }
