@@ -201,3 +201,18 @@ def test_power_lipschitz_option_is_rejected_as_unsupported(engine):
     with pytest.raises(boxqp.EngineError) as err:
         engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
     assert err.value.code == 7 and 'not implemented' in str(err.value)
+
+
+@pytest.mark.parametrize('scaling', [1, 2])
+@pytest.mark.parametrize('preset,n,seed', [('graph10k', 0, 5), ('graph1m', 40000, 2), ('tridiagonal', 5000, 1)])
+def test_mixed_mode_with_and_without_preconditioned_steps(engine, preset, n, seed, scaling):
+    """scaling = 1: per-row steps 1/(L' Q_ii) (the default); 2: the scalar step 1/L.  Both verify
+    and land on the planted optimum and active set."""
+    inst = boxqp.planted(preset, seed=seed, n=n, lower_triplets=True)
+    o = boxqp.options_struct(1e-7, 30.0, 200000, 'mixed', scaling=scaling)
+    x, st = engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+    chk = O.check(*planted_args(inst), x, tol=1e-7)
+    assert chk['verified'] == 1.0, chk
+    assert abs(chk['objective'] - inst['fstar']) / (1 + abs(inst['fstar'])) <= 1e-7
+    assert active_set_ok(inst, x)
