@@ -123,6 +123,50 @@ __device__ Acc block_reduce(Acc v) {
     return v;
 }
 
+// The check's reduction: the two FP64 sums it always needs (objective, tangent bound), the
+// separable bound only for the diagonal dual-gap gate (`gate`), and the integer fields; the CG
+// fields (a, b) stay out (FP64 additions run at 1/64 of the FP32 rate here).
+__device__ __forceinline__ Acc combine_check(const Acc& x, const Acc& y, bool gate) {
+    Acc r = x;
+    r.obj = x.obj + y.obj;
+    r.bnd = x.bnd + y.bnd;
+    if (gate) r.sep = x.sep + y.sep;
+    r.stat = umax64(x.stat, y.stat);
+    r.prim = umax64(x.prim, y.prim);
+    r.hash = x.hash ^ y.hash;
+    r.nact = x.nact + y.nact;
+    r.flags = x.flags | y.flags;
+    return r;
+}
+__device__ __forceinline__ Acc shfl_check(const Acc& x, int o, bool gate) {
+    Acc r = x;
+    r.obj = shfl_xor(x.obj, o);
+    r.bnd = shfl_xor(x.bnd, o);
+    if (gate) r.sep = shfl_xor(x.sep, o);
+    r.stat = shfl_xor(x.stat, o);
+    r.prim = shfl_xor(x.prim, o);
+    r.hash = shfl_xor(x.hash, o);
+    r.nact = shfl_xor(x.nact, o);
+    r.flags = shfl_xor(x.flags, o);
+    return r;
+}
+__device__ Acc block_reduce_check(Acc v, bool gate) {
+    __shared__ Acc warp_part[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = combine_check(v, shfl_check(v, o, gate), gate);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        Acc w = lane < kBlock / 32 ? warp_part[lane] : acc_identity();
+#pragma unroll
+        for (int o = (kBlock / 64); o > 0; o >>= 1) w = combine_check(w, shfl_check(w, o, gate), gate);
+        v = w;
+    }
+    __syncthreads();
+    return v;
+}
+
 __device__ __forceinline__ void store_partial(Partial* p, const Acc& v) {
     p->obj = v.obj; p->bnd = v.bnd; p->sep = v.sep; p->a = v.a;
     p->stat = v.stat; p->prim = v.prim; p->b = v.b; p->hash = v.hash;
@@ -157,19 +201,19 @@ __device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles
     return last;
 }
 
-// Reduces the partials of tiles [tb, te) in a fixed order; valid in thread 0.  Pairs of partials
-// are loaded before they are combined (same order, two loads in flight).
-__device__ Acc reduce_instance(const View& v, int tb, int te) {
+// Reduces the check partials of tiles [tb, te) in a fixed order; valid in thread 0.  Pairs of
+// partials are loaded before they are combined (same order, two loads in flight).
+__device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
     Acc acc = acc_identity();
     int k = tb + static_cast<int>(threadIdx.x);
     for (; k + kBlock < te; k += 2 * kBlock) {
         const Acc p0 = load_partial(&v.partial[k]);
         const Acc p1 = load_partial(&v.partial[k + kBlock]);
-        acc = combine(acc, p0);
-        acc = combine(acc, p1);
+        acc = combine_check(acc, p0, gate);
+        acc = combine_check(acc, p1, gate);
     }
-    if (k < te) acc = combine(acc, load_partial(&v.partial[k]));
-    return block_reduce(acc);
+    if (k < te) acc = combine_check(acc, load_partial(&v.partial[k]), gate);
+    return block_reduce_check(acc, gate);
 }
 
 // The CG reductions carry one sum (a) and one maximum (b): the same fixed order on those two
@@ -867,10 +911,10 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
         if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a);
         else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, T.variant, T.row_begin, T.row_end, a);
         else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a);
-        Acc total = block_reduce(a);
+        Acc total = block_reduce_check(a, s.gate != 0);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance(v, R.x, R.y);
+            Acc inst_total = reduce_instance(v, R.x, R.y, s.gate != 0);
             if (threadIdx.x == 0) after_check(I, inst_total);
             __syncthreads();
         }
