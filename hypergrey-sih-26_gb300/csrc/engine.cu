@@ -1523,6 +1523,8 @@ struct Scan {
     bool diagonal = true;
     bool positive = true;
     bool infeasible = false;
+    bool dominant = true;     // every row: Q_ii >= sum_j!=i |Q_ij| (PSD for a symmetric Q)
+    bool indefinite = false;  // a row with Q_ii < 0, or Q_ii = 0 beside off-diagonal entries
 };
 
 // Destination of the host copy taken during the scan (asynchronous submit), or all null.
@@ -1546,7 +1548,7 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
             return s;
         }
         if (l[i] > u[i]) s.infeasible = true;
-        double abs_sum = 0, d = 0;
+        double abs_sum = 0, d = 0, radius = 0;
         for (int64_t k = a; k < b; ++k) {
             const int32_t cc = col[k];
             const double v = val[k];
@@ -1555,10 +1557,17 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
                 return s;
             }
             abs_sum += std::abs(v);
-            if (cc == i) d += v;
-            else s.diagonal = false;
+            if (cc == i) {
+                d += v;
+            } else {
+                s.diagonal = false;
+                radius += std::abs(v);
+            }
         }
         if (!(d > 0)) s.positive = false;
+        // the diagonal-dominance fast path of check_convex_hessian (src/qp_admm.cpp:30-39)
+        if (d < 0 || (d == 0 && radius > 0)) s.indefinite = true;
+        if (d < radius) s.dominant = false;
         s.lipschitz = std::max(s.lipschitz, abs_sum);
     }
     if (dst.rowptr && r1 > r0) {
@@ -1597,6 +1606,8 @@ Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* 
         s.diagonal = s.diagonal && p.diagonal;
         s.positive = s.positive && p.positive;
         s.infeasible = s.infeasible || p.infeasible;
+        s.dominant = s.dominant && p.dominant;
+        s.indefinite = s.indefinite || p.indefinite;
     }
     return s;
 }
@@ -1642,6 +1653,35 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
         return BQP_ERR_INVALID;
     }
     const double t_scan = host_seconds();
+    // check_convex_hessian comes first, as in solve_accelerated_box (src/accelerated_qp.cpp:19):
+    // diagonal dominance decides in the scan; otherwise the sparse LDL^T of bqp_check_convex on the
+    // lower triangle of the CSR
+    bool convex = !scan.indefinite;
+    if (convex && !scan.dominant) {
+        std::vector<int64_t> tr, tc;
+        std::vector<double> tv;
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+                if (col[k] <= i) {
+                    tr.push_back(i);
+                    tc.push_back(col[k]);
+                    tv.push_back(val[k]);
+                }
+        convex = bqp_check_convex(n, static_cast<int64_t>(tr.size()), tr.data(), tc.data(), tv.data(), 0) == 1;
+    }
+    if (!convex) {
+        j->n = n;
+        j->nnz = nnz;
+        j->opt = o;
+        j->state = bqp::JOB_DONE;
+        j->stats.status = BQP_STATUS_UNSUPPORTED_CURVATURE;
+        j->stats.objective = std::numeric_limits<double>::quiet_NaN();
+        j->stats.primal_residual = j->stats.stationarity_residual = HUGE_VAL;
+        j->stats.complementarity_residual = j->stats.relative_gap = HUGE_VAL;
+        j->stats.dual_bound = -HUGE_VAL;
+        *out = j.release();
+        return BQP_OK;
+    }
     const double lipschitz = scan.lipschitz;
     if (lipschitz == 0) {
         why = "Zero-Hessian models use the CPU LP path";

@@ -216,3 +216,23 @@ def test_mixed_mode_with_and_without_preconditioned_steps(engine, preset, n, see
     assert chk['verified'] == 1.0, chk
     assert abs(chk['objective'] - inst['fstar']) / (1 + abs(inst['fstar'])) <= 1e-7
     assert active_set_ok(inst, x)
+
+
+def test_nonconvex_hessian_is_reported_before_solving(engine):
+    """check_convex_hessian runs first (src/accelerated_qp.cpp:19): an indefinite Q gets
+    unsupported_curvature from the C-ABI solve; a PSD but not diagonally dominant Q solves."""
+    # [[1, 2], [2, 1]] is indefinite (eigenvalues 3, -1) and not diagonally dominant
+    rowptr = np.array([0, 2, 4], np.int32)
+    col = np.array([0, 1, 0, 1], np.int32)
+    val = np.array([1.0, 2.0, 2.0, 1.0])
+    c = np.array([1.0, -1.0])
+    lo, up = np.full(2, -1.0), np.full(2, 1.0)
+    o = boxqp.options_struct(1e-7, 10.0, 10000, 'fp64')
+    x, st = engine.solve(rowptr, col, val, c, lo, up, o)
+    assert boxqp.STATUS_NAMES[st.status] == 'unsupported_curvature'
+    # [[2, 1.5], [1.5, 2]] is PSD but not diagonally dominant: the LDL^T path accepts it
+    val = np.array([2.0, 1.5, 1.5, 2.0])
+    for precision in ('fp64', 'mixed'):
+        o = boxqp.options_struct(1e-7, 10.0, 10000, precision)
+        x, st = engine.solve(rowptr, col, val, c, lo, up, o)
+        assert boxqp.STATUS_NAMES[st.status] == 'optimal', precision
