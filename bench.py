@@ -8,8 +8,9 @@ in FP64.  A step is one complete solve of that instance.
   value   solves/s with the problem resident in HBM: K re-solves (x0 = clip(0), no upload),
           timed with CUDA events on the engine stream (graph launches + re-arm kernels)
   e2e     solves/s through the public C-ABI with host buffers: every solve submits its CSR and
-          vectors (scan, copy, upload, admission), solves, and copies x back; asynchronous
-          submissions with two in flight (e2e.sync: bqp_solve_sync one call at a time)
+          vectors (scan, upload, admission), solves, and copies x back; asynchronous submissions
+          with three in flight through bqp_submit_borrowed (e2e.copy: bqp_submit, which copies
+          the inputs at submission; e2e.sync: bqp_solve_sync one call at a time)
   roofline  the FISTA step kernel (dominant kernel) timed alone with CUDA events on the same
           instance; algorithmic bytes per launch nnz*(4+4) + 4(n+1) + 7*4n
   cpu_baseline  the FP64 reference FISTA (CPU oracle port, all host cores) on one full solve
@@ -303,32 +304,42 @@ def run_ours(args, world, rank, local, pg):
         for _ in range(e2e_steps):
             xe, se = eng.solve(*args_host, opts)
         sync_s = allreduce_max(pg, time.perf_counter() - t0)
-        # the asynchronous API with two solves in flight: the host work of one submission (input
-        # scan and copy) overlaps the device work of the previous one; every solve still uploads
-        # its inputs and returns its primal vector
-        pipe_steps = max(4, min(args.steps, 20))
-        depth = 2
-        inflight, statuses = [], set()
-        barrier(pg)
-        t0 = time.perf_counter()
-        for k in range(pipe_steps):
-            inflight.append(eng.submit(*args_host, opts))
-            if len(inflight) >= depth:
+        # the asynchronous API with three solves in flight: the host work of one submission (input
+        # scan) overlaps the device work of the previous ones; every solve still uploads its inputs
+        # from host memory and copies its primal back.  Headline: bqp_submit_borrowed (no host
+        # copy of the inputs, the caller keeps them unchanged until the solve finishes); also
+        # timed: bqp_submit, which copies the inputs first.
+        def pipelined(copy, depth=3):
+            steps = max(6, min(args.steps, 20))
+            inflight, statuses = [], set()
+            out = [np.empty(n, dtype=np.float64) for _ in range(depth)]
+
+            def finish(k):
                 i = inflight.pop(0)
                 eng.wait(i)
-                xe, se = eng.fetch(i, n)
+                _, st = eng.fetch(i, n, out=out[k % depth])
                 eng.release(i)
-                statuses.add(boxqp.STATUS_NAMES[se.status])
-        for i in inflight:
-            eng.wait(i)
-            xe, se = eng.fetch(i, n)
-            eng.release(i)
-            statuses.add(boxqp.STATUS_NAMES[se.status])
-        pipe_s = allreduce_max(pg, time.perf_counter() - t0)
-        e2e = {'value': allreduce_sum(pg, pipe_steps) / pipe_s, 'unit': 'solves/s', 'h2d_bytes_per_step': int(h2d),
+                statuses.add(boxqp.STATUS_NAMES[st.status])
+
+            barrier(pg)
+            t0 = time.perf_counter()
+            for k in range(steps):
+                inflight.append(eng.submit(*args_host, opts, copy=copy))
+                if len(inflight) >= depth:
+                    finish(k)
+            while inflight:
+                finish(0)
+            return allreduce_sum(pg, steps) / allreduce_max(pg, time.perf_counter() - t0), statuses
+
+        pipelined(False)  # host buffers, pool threads warm
+        borrowed, st_b = pipelined(False)
+        copied, st_c = pipelined(True)
+        e2e = {'value': borrowed, 'unit': 'solves/s', 'h2d_bytes_per_step': int(h2d),
                'd2h_bytes_per_step': int(d2h),
-               'api': 'bqp_submit (2 in flight) + bqp_wait + bqp_fetch, pageable host buffers',
-               'status': ','.join(sorted(statuses)),
+               'api': 'bqp_submit_borrowed (3 in flight) + bqp_wait + bqp_fetch + bqp_release, pageable host buffers',
+               'status': ','.join(sorted(st_b)),
+               'copy': {'value': copied, 'api': 'bqp_submit (3 in flight, inputs copied at submission)',
+                        'status': ','.join(sorted(st_c))},
                'sync': {'value': allreduce_sum(pg, e2e_steps) / sync_s, 'api': 'bqp_solve_sync, one at a time',
                         'status': boxqp.STATUS_NAMES[se.status]}}
     # ---- CPU baseline (rank 0, N = 1) -----------------------------------------------------------

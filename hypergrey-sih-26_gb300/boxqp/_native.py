@@ -61,6 +61,8 @@ PROTOTYPES = {
     'bqp_device_name': (c_int, [c_int, c_char_p, c_size_t]),
     'bqp_submit': (c_int, [c_void_p, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P,
                            POINTER(Options), _U64P]),
+    'bqp_submit_borrowed': (c_int, [c_void_p, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P,
+                                    POINTER(Options), _U64P]),
     'bqp_poll': (c_int, [c_void_p, c_uint64, _I32P]),
     'bqp_wait': (c_int, [c_void_p, c_uint64, c_double]),
     'bqp_wait_any': (c_int, [c_void_p, c_double, _U64P]),

@@ -163,11 +163,13 @@ class Engine:
             msg = L.bqp_last_error(None)
             raise EngineError(2, msg.decode() if msg else 'engine creation failed')
         self.device = device
+        self._borrowed = {}  # id -> input arrays of a bqp_submit_borrowed solve, kept until release
 
     def close(self):
         if getattr(self, '_ctx', None):
             lib().bqp_destroy(self._ctx)
             self._ctx = None
+            self._borrowed = {}
 
     def __del__(self):
         try:
@@ -183,15 +185,21 @@ class Engine:
                 raise ValueError(text)
             raise EngineError(rc, text)
 
-    def submit(self, rowptr, col, val, c, lower, upper, options: Options):
+    def submit(self, rowptr, col, val, c, lower, upper, options: Options, copy=True):
+        """Queues one solve and returns its id.  copy=False (bqp_submit_borrowed) skips the host
+        copy of the inputs: the engine keeps references to the (contiguous) arrays until release,
+        and the caller must not modify them before the solve has finished."""
         rowptr, col, val = _i32(rowptr), _i32(col), _f64(val)
         c, lower, upper = _f64(c), _f64(lower), _f64(upper)
         options = _tuned(options, c.shape[0], col.shape[0])
         ident = N.c_uint64(0)
-        rc = lib().bqp_submit(self._ctx, c.shape[0], col.shape[0], ptr(rowptr, N.c_int32), ptr(col, N.c_int32),
-                              ptr(val, N.c_double), ptr(c, N.c_double), ptr(lower, N.c_double),
-                              ptr(upper, N.c_double), options, N.ctypes.byref(ident))
+        fn = lib().bqp_submit if copy else lib().bqp_submit_borrowed
+        rc = fn(self._ctx, c.shape[0], col.shape[0], ptr(rowptr, N.c_int32), ptr(col, N.c_int32),
+                ptr(val, N.c_double), ptr(c, N.c_double), ptr(lower, N.c_double),
+                ptr(upper, N.c_double), options, N.ctypes.byref(ident))
         self._check(rc)
+        if not copy:
+            self._borrowed[ident.value] = (rowptr, col, val, c, lower, upper)
         return ident.value
 
     def poll(self, ident):
@@ -215,14 +223,21 @@ class Engine:
         self._check(rc)
         return ident.value
 
-    def fetch(self, ident, n):
-        x = np.empty(n, dtype=np.float64)
+    def fetch(self, ident, n, out=None):
+        """(x, Stats) of a finished solve; `out` (float64, contiguous, n entries) receives x."""
+        if out is None:
+            x = np.empty(n, dtype=np.float64)
+        else:
+            x = out
+            if x.dtype != np.float64 or not x.flags['C_CONTIGUOUS'] or x.shape != (n,):
+                raise ValueError('out must be a contiguous float64 array of n entries')
         st = Stats()
         self._check(lib().bqp_fetch(self._ctx, ident, ptr(x, N.c_double), st))
         return x, st
 
     def release(self, ident):
         self._check(lib().bqp_release(self._ctx, ident))
+        self._borrowed.pop(ident, None)
 
     def resolve(self, idents):
         ids = np.ascontiguousarray(np.asarray(list(idents), dtype=np.uint64))

@@ -13,6 +13,7 @@
 #include "boxqp.h"
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "workers.h"
 
 #include <algorithm>
 #include <atomic>
@@ -204,8 +205,10 @@ struct Job {
     int error = BQP_OK;
     std::string error_text;
     bqp_stats stats{};
-    std::vector<double> x;
-    std::vector<float> x32_tmp;
+    std::vector<double> x;    // primal of a solve that holds no device memory (finished at submission)
+    const void* x_dev = nullptr;  // primal of a finished resident solve, in its slab
+    bool x_f32 = false;           // ... as FP32 (the mixed engine's unpolished iterate)
+    int fetching = 0;             // bqp_fetch calls copying x_dev (under the engine lock)
     double t_submit = 0, t_done = 0;
     ~Job() { HostBufferCache::get().release(own, own_bytes); }
 };
@@ -235,8 +238,13 @@ std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int variant) {
     std::vector<Tile> t;
     int64_t r = 0;
     while (r < n) {
-        int64_t e = r + 1;
-        while (e < n && e - r < kTileRows && static_cast<int64_t>(rowptr[e + 1]) - rowptr[r] <= kTileNnz) ++e;
+        // the first e in (r, min(n, r + kTileRows)) whose rows [r, e] pass kTileNnz nonzeros, else
+        // that end: a binary search over the nondecreasing row pointers
+        const int64_t hi = std::min<int64_t>(n, r + kTileRows);
+        const int64_t limit = static_cast<int64_t>(rowptr[r]) + kTileNnz;
+        const int32_t* p = std::upper_bound(rowptr + r + 2, rowptr + hi + 1, limit,
+                                            [](int64_t v, int32_t x) { return v < static_cast<int64_t>(x); });
+        int64_t e = (p - rowptr) - 1;
         if (e < n) {
             const int64_t rows = e - r;
             if (rows >= kBlock) e = r + rows / kBlock * kBlock;
@@ -367,6 +375,8 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaStream_t capture_ = nullptr;
     cudaStream_t ustream_ = nullptr;   // uploads of new solves, overlapping the running graph
+    cudaStream_t fstream_ = nullptr;   // bqp_fetch copies of finished primals (caller threads, fmu_)
+    std::mutex fmu_;
     cudaEvent_t uev_ = nullptr;        // end of the latest upload on ustream_
     std::vector<Job*> uploaded_;       // uploaded, not yet installed (engine thread only)
     bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
@@ -455,6 +465,7 @@ bool Engine::init(std::string& why) {
     if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&ustream_, cudaStreamNonBlocking), why, "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&fstream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaEventCreateWithFlags(&uev_, cudaEventDisableTiming), why, "event")) return false;
     cudaMemPoolProps props;
     std::memset(&props, 0, sizeof(props));
@@ -536,10 +547,12 @@ void Engine::shutdown() {
     if (stream_) cudaStreamDestroy(stream_);
     if (capture_) cudaStreamDestroy(capture_);
     if (ustream_) cudaStreamDestroy(ustream_);
+    if (fstream_) cudaStreamDestroy(fstream_);
     if (uev_) cudaEventDestroy(uev_);
     stream_ = nullptr;
     capture_ = nullptr;
     ustream_ = nullptr;
+    fstream_ = nullptr;
     uev_ = nullptr;
 }
 
@@ -814,19 +827,68 @@ int Engine::wait(uint64_t id, double timeout) {
 }
 
 int Engine::fetch(uint64_t id, double* x, bqp_stats* stats) {
+    const void* src = nullptr;
+    bool f32 = false;
+    int64_t n = 0;
+    int rc;
+    Job* jp = nullptr;
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        auto it = jobs_.find(id);
+        if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+        Job& j = *it->second;
+        if (j.state != JOB_DONE) return BQP_ERR_NOT_READY;
+        if (stats) *stats = j.stats;
+        if (j.error != BQP_OK) set_error(j.error_text);
+        rc = j.error;
+        if (x && j.x.empty() && j.resident && j.x_dev) {
+            src = j.x_dev;
+            f32 = j.x_f32;
+            n = j.n;
+            ++j.fetching;  // release() waits for the copy
+            jp = &j;
+        } else if (x && !j.x.empty()) {
+            std::memcpy(x, j.x.data(), sizeof(double) * j.x.size());
+        }
+    }
+    if (!src) return rc;
+    // device -> caller memory outside the engine lock, on this engine's fetch stream
+    cudaError_t e;
+    {
+        std::lock_guard<std::mutex> fg(fmu_);
+        int prev = -1;
+        cudaGetDevice(&prev);
+        if (prev != device_) cudaSetDevice(device_);
+        const size_t N = static_cast<size_t>(n);
+        if (f32) {
+            std::vector<float> tmp(N);
+            e = cudaMemcpyAsync(tmp.data(), src, sizeof(float) * N, cudaMemcpyDeviceToHost, fstream_);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(fstream_);
+            if (e == cudaSuccess)
+                for (size_t i = 0; i < N; ++i) x[i] = static_cast<double>(tmp[i]);
+        } else {
+            e = cudaMemcpyAsync(x, src, sizeof(double) * N, cudaMemcpyDeviceToHost, fstream_);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(fstream_);
+        }
+        if (prev >= 0 && prev != device_) cudaSetDevice(prev);
+    }
     std::lock_guard<std::mutex> g(mu_);
-    auto it = jobs_.find(id);
-    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
-    const Job& j = *it->second;
-    if (j.state != JOB_DONE) return BQP_ERR_NOT_READY;
-    if (stats) *stats = j.stats;
-    if (x && !j.x.empty()) std::memcpy(x, j.x.data(), sizeof(double) * j.x.size());
-    if (j.error != BQP_OK) set_error(j.error_text);
-    return j.error;
+    --jp->fetching;
+    if (jp->fetching == 0) cv_done_.notify_all();
+    if (e != cudaSuccess) {
+        set_error(std::string("CUDA: fetch primal: ") + cudaGetErrorString(e));
+        return BQP_ERR_CUDA;
+    }
+    return rc;
 }
 
 int Engine::release(uint64_t id) {
-    std::lock_guard<std::mutex> g(mu_);
+    std::unique_lock<std::mutex> lk(mu_);
+    // a bqp_fetch of this solve on another thread finishes its copy first
+    cv_done_.wait(lk, [&] {
+        auto f = jobs_.find(id);
+        return f == jobs_.end() || f->second->fetching == 0;
+    });
     auto it = jobs_.find(id);
     if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
     Job& j = *it->second;
@@ -851,7 +913,15 @@ int Engine::release(uint64_t id) {
 }
 
 int Engine::resolve(const uint64_t* ids, int64_t count) {
-    std::lock_guard<std::mutex> g(mu_);
+    std::unique_lock<std::mutex> lk(mu_);
+    // a re-run overwrites the primal: bqp_fetch copies in flight finish first
+    cv_done_.wait(lk, [&] {
+        for (int64_t k = 0; k < count; ++k) {
+            auto f = jobs_.find(ids[k]);
+            if (f != jobs_.end() && f->second->fetching != 0) return false;
+        }
+        return true;
+    });
     for (int64_t k = 0; k < count; ++k) {
         auto it = jobs_.find(ids[k]);
         if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
@@ -1241,26 +1311,37 @@ void Engine::collect(std::unique_lock<std::mutex>& lk) {
     for (size_t k = 0; k < finished.size(); ++k)
         cudaMemcpyAsync(&recs[k], &d_inst_[finished[k]->slot], sizeof(InstDev), cudaMemcpyDeviceToHost, stream_);
     cudaStreamSynchronize(stream_);
+    // Primals of up to kHostPrimal variables come back now, all behind one synchronisation; a
+    // larger one stays in the slab (final, untouched until release or re-run) and bqp_fetch
+    // copies it straight to the caller's array, off the engine thread.
+    std::vector<std::vector<float>> x32(finished.size());
+    bool small = false;
     for (size_t k = 0; k < finished.size(); ++k) {
         Job& j = *finished[k];
         const InstDev& R = recs[k];
+        j.x_f32 = R.result_src == 1;
+        j.x_dev = R.result_src == 1 ? static_cast<const void*>(R.x32)
+                                    : static_cast<const void*>(R.result_src == 2 ? R.xp : R.x64);
+        j.x.clear();
+        if (j.n > kHostPrimal) continue;
+        small = true;
         j.x.resize(static_cast<size_t>(j.n));
-        if (R.result_src == 1) {
-            j.x32_tmp.resize(static_cast<size_t>(j.n));
-            cudaMemcpyAsync(j.x32_tmp.data(), R.x32, sizeof(float) * j.n, cudaMemcpyDeviceToHost, stream_);
-        } else {
-            const double* src = R.result_src == 2 ? R.xp : R.x64;
-            cudaMemcpyAsync(j.x.data(), src, sizeof(double) * j.n, cudaMemcpyDeviceToHost, stream_);
+        void* dst = j.x.data();
+        if (j.x_f32) {
+            x32[k].resize(static_cast<size_t>(j.n));
+            dst = x32[k].data();
         }
+        cudaMemcpyAsync(dst, j.x_dev, (j.x_f32 ? 4 : 8) * static_cast<size_t>(j.n), cudaMemcpyDeviceToHost, stream_);
     }
-    cudaStreamSynchronize(stream_);
+    if (small) cudaStreamSynchronize(stream_);
     const double now = host_seconds();
     for (size_t k = 0; k < finished.size(); ++k) {
         Job& j = *finished[k];
         const InstDev& R = recs[k];
-        if (R.result_src == 1) {
-            for (int64_t i = 0; i < j.n; ++i) j.x[i] = static_cast<double>(j.x32_tmp[i]);
-            std::vector<float>().swap(j.x32_tmp);
+        if (!j.x.empty()) {
+            if (j.x_f32)
+                for (int64_t i = 0; i < j.n; ++i) j.x[i] = static_cast<double>(x32[k][i]);
+            j.x_dev = nullptr;
         }
         bqp_stats& s = j.stats;
         s.status = status_code(R.status);
@@ -1540,6 +1621,19 @@ struct InputCopy {
 Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
                const double* c, const double* l, const double* u, const InputCopy& dst) {
     Scan s;
+    // the copy follows the scan in pieces of about 16K nonzeros, while they are still in cache:
+    // the input is read from memory once
+    int64_t copied = r0;
+    auto copy_rows = [&](int64_t e) {
+        const int64_t k0 = rowptr[copied], k1 = rowptr[e];
+        std::memcpy(dst.rowptr + copied, rowptr + copied, sizeof(int32_t) * static_cast<size_t>(e - copied + (e == n ? 1 : 0)));
+        std::memcpy(dst.col + k0, col + k0, sizeof(int32_t) * static_cast<size_t>(k1 - k0));
+        std::memcpy(dst.val + k0, val + k0, sizeof(double) * static_cast<size_t>(k1 - k0));
+        std::memcpy(dst.c + copied, c + copied, sizeof(double) * static_cast<size_t>(e - copied));
+        std::memcpy(dst.l + copied, l + copied, sizeof(double) * static_cast<size_t>(e - copied));
+        std::memcpy(dst.u + copied, u + copied, sizeof(double) * static_cast<size_t>(e - copied));
+        copied = e;
+    };
     for (int64_t i = r0; i < r1; ++i) {
         const int64_t a = rowptr[i], b = rowptr[i + 1];
         if (a < 0 || b < a || b > nnz) { s.error = 1; return s; }
@@ -1569,36 +1663,25 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
         if (d < 0 || (d == 0 && radius > 0)) s.indefinite = true;
         if (d < radius) s.dominant = false;
         s.lipschitz = std::max(s.lipschitz, abs_sum);
-    }
-    if (dst.rowptr && r1 > r0) {
-        // rows [r0, r1) validated: their nonzeros are [rowptr[r0], rowptr[r1]) within [0, nnz]
-        const int64_t k0 = rowptr[r0], k1 = rowptr[r1];
-        std::memcpy(dst.rowptr + r0, rowptr + r0, sizeof(int32_t) * static_cast<size_t>(r1 - r0 + (r1 == n ? 1 : 0)));
-        std::memcpy(dst.col + k0, col + k0, sizeof(int32_t) * static_cast<size_t>(k1 - k0));
-        std::memcpy(dst.val + k0, val + k0, sizeof(double) * static_cast<size_t>(k1 - k0));
-        std::memcpy(dst.c + r0, c + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
-        std::memcpy(dst.l + r0, l + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
-        std::memcpy(dst.u + r0, u + r0, sizeof(double) * static_cast<size_t>(r1 - r0));
+        // rows [copied, i] validated: their nonzeros lie in [rowptr[copied], rowptr[i + 1]] within [0, nnz]
+        if (dst.rowptr && (b - rowptr[copied] >= 16384 || i + 1 - copied >= 4096 || i + 1 == r1)) copy_rows(i + 1);
     }
     return s;
 }
 
 Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, const double* val,
                   const double* c, const double* l, const double* u, const InputCopy& dst) {
-    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    int64_t threads = std::min<int64_t>(std::min<int64_t>(hw, 32), std::max<int64_t>(1, nnz / 500000));
-    std::vector<Scan> part(static_cast<size_t>(threads));
-    auto work = [&](int64_t t) {
-        const int64_t r0 = n * t / threads, r1 = n * (t + 1) / threads;
-        part[t] = scan_rows(r0, r1, n, nnz, rowptr, col, val, c, l, u, dst);
-    };
-    if (threads == 1) {
-        work(0);
-    } else {
-        std::vector<std::thread> pool;
-        for (int64_t t = 0; t < threads; ++t) pool.emplace_back(work, t);
-        for (auto& th : pool) th.join();
-    }
+    // pieces of about 128K nonzeros (by the average row), at least 2048 rows; below 256K
+    // nonzeros the calling thread scans alone.  The result does not depend on the pieces: the
+    // first error by row, the largest row sum, and/or of the flags.
+    const double avg = static_cast<double>(nnz) / static_cast<double>(n) + 1.0;
+    const int64_t rows = std::max<int64_t>(2048, static_cast<int64_t>(131072.0 / avg));
+    const int64_t pieces = nnz < 262144 ? 1 : (n + rows - 1) / rows;
+    std::vector<Scan> part(static_cast<size_t>(pieces));
+    bqp::WorkerPool::get().run(pieces, [&](int64_t p) {
+        const int64_t r0 = n * p / pieces, r1 = n * (p + 1) / pieces;
+        part[static_cast<size_t>(p)] = scan_rows(r0, r1, n, nnz, rowptr, col, val, c, l, u, dst);
+    });
     Scan s;
     for (const Scan& p : part) {
         if (p.error && !s.error) s.error = p.error;
@@ -1811,6 +1894,18 @@ int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, cons
     Job* j = nullptr;
     std::string why;
     int rc = make_job(n, nnz, rowptr, col, val, c, lower, upper, options, true, &j, why);
+    if (rc != BQP_OK) return fail(ctx, rc, why);
+    j->notify = true;
+    return ctx->engine->submit(j, id);
+}
+
+int bqp_submit_borrowed(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,
+                        const double* val, const double* c, const double* lower, const double* upper,
+                        const bqp_options* options, uint64_t* id) {
+    if (!ctx) return fail(nullptr, BQP_ERR_INVALID, "null context");
+    Job* j = nullptr;
+    std::string why;
+    int rc = make_job(n, nnz, rowptr, col, val, c, lower, upper, options, false, &j, why);
     if (rc != BQP_OK) return fail(ctx, rc, why);
     j->notify = true;
     return ctx->engine->submit(j, id);

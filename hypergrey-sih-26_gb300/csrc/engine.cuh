@@ -16,6 +16,7 @@ constexpr int kMaxInterval = 32;     // maximum check interval (iterations per c
 constexpr int kTileNnz = 4096;       // target nonzeros per tile
 constexpr int kTileRows = 512;       // maximum rows per tile
 constexpr int kRearmRows = 8192;     // rows per block when re-arming resident solves
+constexpr int64_t kHostPrimal = 131072;  // primals up to this size come back at completion, larger at fetch
 
 enum Phase : int32_t {
     PH_FISTA = 0,        // FISTA iterations (FP64 or FP32 per precision)

@@ -10,6 +10,7 @@
 //    diagonal proves PSD in O(nnz); otherwise the same congruence-scaled sparse LDL^T with
 //    complete fill and a 4M fill budget decides.
 #include "boxqp.h"
+#include "workers.h"
 
 #include <algorithm>
 #include <cmath>
@@ -43,13 +44,7 @@ int bqp_csr_from_lower(int64_t n, int64_t nh, const int64_t* hrow, const int64_t
             *k1 = nh * (t + 1) / T;
         };
         auto parallel = [&](auto&& fn) {
-            if (T == 1) {
-                fn(0);
-                return;
-            }
-            std::vector<std::thread> pool;
-            for (int t = 0; t < T; ++t) pool.emplace_back(fn, t);
-            for (auto& th : pool) th.join();
+            bqp::WorkerPool::get().run(T, [&](int64_t t) { fn(static_cast<int>(t)); });
         };
         parallel([&](int t) {
             int64_t k0, k1;

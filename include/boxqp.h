@@ -130,6 +130,13 @@ int         bqp_device_name(int device, char* out, size_t cap);
 int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,
                const double* val, const double* c, const double* lower, const double* upper,
                const bqp_options* options, uint64_t* id);
+/* bqp_submit without the host copy: the engine uploads straight from the caller's arrays, which
+ * must stay valid and unchanged until the solve has finished (bqp_wait / bqp_poll / bqp_wait_any
+ * report it) or until bqp_release of the still-queued solve returns.  Validation, the convexity
+ * gate and the errors are bqp_submit's.                                                      */
+int bqp_submit_borrowed(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,
+                        const double* val, const double* c, const double* lower, const double* upper,
+                        const bqp_options* options, uint64_t* id);
 int bqp_poll(bqp_ctx* ctx, uint64_t id, int32_t* status);
 /* Blocks until the solve is finished (timeout_seconds < 0: no timeout).                      */
 int bqp_wait(bqp_ctx* ctx, uint64_t id, double timeout_seconds);
@@ -137,7 +144,9 @@ int bqp_wait(bqp_ctx* ctx, uint64_t id, double timeout_seconds);
  * returns its id; each finished solve is reported once, in completion order.  BQP_ERR_NOT_READY
  * on timeout (timeout_seconds < 0: no timeout).                                              */
 int bqp_wait_any(bqp_ctx* ctx, double timeout_seconds, uint64_t* id);
-/* Copies the primal (n doubles, caller-owned) and the statistics of a finished solve.        */
+/* Copies the primal (n doubles, caller-owned) and the statistics of a finished solve.  The
+ * primal comes straight from the solve's device memory; a bqp_release or bqp_resolve of the same
+ * solve on another thread waits for the copy.                                                */
 int bqp_fetch(bqp_ctx* ctx, uint64_t id, double* x, bqp_stats* stats);
 /* Frees the solve's device memory; the id becomes unknown.                                   */
 int bqp_release(bqp_ctx* ctx, uint64_t id);

@@ -236,3 +236,33 @@ def test_nonconvex_hessian_is_reported_before_solving(engine):
         o = boxqp.options_struct(1e-7, 10.0, 10000, precision)
         x, st = engine.solve(rowptr, col, val, c, lo, up, o)
         assert boxqp.STATUS_NAMES[st.status] == 'optimal', precision
+
+
+@pytest.mark.parametrize('preset,n,seed,precision', [('graph10k', 0, 11, 'mixed'), ('graph1m', 200000, 4, 'mixed'),
+                                                     ('tridiagonal', 150000, 2, 'fp64')])
+def test_borrowed_submission_and_fetch_paths_agree(engine, preset, n, seed, precision):
+    """bqp_submit_borrowed (no host copy) gives the bits of bqp_submit and bqp_solve_sync; a primal
+    above 131072 variables is copied at bqp_fetch from device memory, into `out` if given, and a
+    second fetch and a fetch after a re-run return the same bits."""
+    inst = boxqp.planted(preset, seed=seed, n=n)
+    o = boxqp.options_struct(1e-6, 60.0, 200000, precision)
+    a = (inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'])
+    xs, ss = engine.solve(*a, o)
+    i_copy = engine.submit(*a, o)
+    i_borrow = engine.submit(*a, o, copy=False)
+    assert engine.wait(i_copy, 120.0) and engine.wait(i_borrow, 120.0)
+    xc, sc = engine.fetch(i_copy, inst['n'])
+    out = np.full(inst['n'], np.nan)
+    xb, sb = engine.fetch(i_borrow, inst['n'], out=out)
+    assert xb is out
+    xb2, _ = engine.fetch(i_borrow, inst['n'])
+    engine.resolve([i_borrow])
+    assert engine.wait(i_borrow, 120.0)
+    xb3, sb3 = engine.fetch(i_borrow, inst['n'])
+    engine.release(i_copy)
+    engine.release(i_borrow)
+    assert boxqp.STATUS_NAMES[ss.status] == 'optimal'
+    for x, st in ((xc, sc), (xb, sb), (xb2, sb), (xb3, sb3)):
+        assert np.array_equal(x, xs) and st.iterations == ss.iterations and st.objective == ss.objective
+    with pytest.raises(ValueError):
+        engine.fetch(i_copy, inst['n'], out=np.empty(inst['n'], np.float32))
