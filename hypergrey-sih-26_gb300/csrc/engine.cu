@@ -349,6 +349,31 @@ private:
     void update_grid();
     void collect(std::unique_lock<std::mutex>& lk);
     void process_frees();
+    void upload_tables();
+    // step groups of precision `prec` that a body launches (bits of graph_groups_)
+    std::vector<int> body_groups(int prec) const {
+        std::vector<int> g;
+        for (int k = 0; k < kStepGroups; ++k)
+            if (((graph_groups_ >> k) & 1u) && (k >= kVariants) == (prec == PREC_MIXED)) g.push_back(k);
+        return g;
+    }
+    void launch_body_steps(const View& v, int prec, int K, int grid, cudaStream_t s) const {
+        if (prec == PREC_FP64_EXACT) {
+            for (int j = 0; j < K; ++j) launch_step_exact(v, j, grid, s);
+            return;
+        }
+        std::vector<int> groups = body_groups(prec);
+        if (groups.empty()) groups.push_back(step_group(prec, VAR_TILE));  // no tiles: exits at once
+        for (int j = 0; j < K; ++j)
+            for (int g : groups) launch_step_group(v, g, j, grid, s);
+    }
+    StepLaunches body_launches(int K) const {
+        StepLaunches L;
+        L.n[PREC_FP64] = K * std::max<int>(1, static_cast<int>(body_groups(PREC_FP64).size()));
+        L.n[PREC_MIXED] = K * std::max<int>(1, static_cast<int>(body_groups(PREC_MIXED).size()));
+        L.n[PREC_FP64_EXACT] = K;
+        return L;
+    }
     bool ensure_tables(int need_inst, int need_tiles, std::string& why);
     bool build_graph(std::string& why);
     View view() const {
@@ -360,6 +385,7 @@ private:
         v.ctrl = d_ctrl_;
         v.status_mirror = d_status_;
         v.ranges = d_ranges_;
+        v.group_tiles = d_group_tiles_;
         return v;
     }
     bool cuda_ok(cudaError_t e, std::string& why, const char* what) {
@@ -406,6 +432,12 @@ private:
     std::vector<Tile> h_tiles_;
     std::vector<int2> h_ranges_;
     std::vector<Job*> slot_job_;
+    std::vector<int32_t> slot_prec_;      // precision of the solve in each slot
+    std::vector<int32_t> h_group_tiles_;  // tile indices ordered by step group
+    int32_t group_begin_[kStepGroups + 1] = {};
+    uint32_t groups_present_ = 0;         // step groups with tiles
+    uint32_t graph_groups_ = 0;           // step groups the graph launches
+    int32_t* d_group_tiles_ = nullptr;
     std::vector<int> free_slots_;
     int n_inst_ = 0;
     bool tables_dirty_ = false;
@@ -583,6 +615,7 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
         inst_cap_ = cap;
         h_ranges_.resize(cap, int2{0, 0});
         slot_job_.resize(cap, nullptr);
+        slot_prec_.resize(cap, 0);
         tables_dirty_ = true;
         graph_valid_ = false;
     }
@@ -590,12 +623,16 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
         int cap = std::max(need_tiles, std::max(1024, tile_cap_ * 2));
         Tile* tiles = nullptr;
         Partial* partial = nullptr;
+        int32_t* group_tiles = nullptr;
         if (!cuda_ok(cudaMalloc(&tiles, sizeof(Tile) * cap), why, "tile table")) return false;
         if (!cuda_ok(cudaMalloc(&partial, sizeof(Partial) * cap), why, "partials")) return false;
+        if (!cuda_ok(cudaMalloc(&group_tiles, sizeof(int32_t) * cap), why, "step groups")) return false;
         cudaFree(d_tiles_);
         cudaFree(d_partial_);
+        cudaFree(d_group_tiles_);
         d_tiles_ = tiles;
         d_partial_ = partial;
+        d_group_tiles_ = group_tiles;
         tile_cap_ = cap;
         tables_dirty_ = true;
         graph_valid_ = false;
@@ -614,6 +651,7 @@ void Engine::update_grid() {
 // each check and launches only the kernels those phases need.
 bool Engine::run_stream(int cap, std::string& why) {
     update_grid();
+    graph_groups_ = groups_present_;
     const int grid = graph_grid_;
     const int K = graph_interval_;
     const View v = view();
@@ -628,10 +666,11 @@ bool Engine::run_stream(int cap, std::string& why) {
         cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
         if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine check")) return false;
         if (profile_phases_) cudaEventRecord(pev_[1], stream_);
+        const StepLaunches L = body_launches(K);
         for (int k = 0; k < 3; ++k) {
             if (h_ctrl_->n_fista[k] <= 0) continue;
-            for (int j = 0; j < K; ++j) launch_step(v, precisions[k], j, grid, stream_);
-            kernels += K;
+            launch_body_steps(v, precisions[k], K, grid, stream_);
+            kernels += L.n[k];
         }
         if (profile_phases_) cudaEventRecord(pev_[2], stream_);
         if (h_ctrl_->n_polish > 0) {
@@ -679,6 +718,7 @@ bool Engine::build_graph(std::string& why) {
     exec_ = nullptr;
     graph_ = nullptr;
     update_grid();
+    graph_groups_ = groups_present_;
     const int grid = graph_grid_;
     const int K = graph_interval_;
     const View v = view();
@@ -731,16 +771,15 @@ bool Engine::build_graph(std::string& why) {
     cudaGraphNode_t last = nullptr;
     if (!capture(body, nullptr, 0, [&] {
             launch_check(v, grid, capture_);
-            launch_gate(v, h_f, h_pol, h_cg, K, capture_);
+            launch_gate(v, h_f, h_pol, h_cg, body_launches(K), capture_);
         }, &last)) return false;
     const int precisions[3] = {PREC_FP64, PREC_MIXED, PREC_FP64_EXACT};
     for (int k = 0; k < 3; ++k) {
         cudaGraphNode_t node;
         cudaGraph_t inner;
         if (!add_if(last, h_f[k], &node, &inner)) return false;
-        if (!capture(inner, nullptr, 0, [&] {
-                for (int j = 0; j < K; ++j) launch_step(v, precisions[k], j, grid, capture_);
-            }, nullptr)) return false;
+        if (!capture(inner, nullptr, 0, [&] { launch_body_steps(v, precisions[k], K, grid, capture_); }, nullptr))
+            return false;
         last = node;
     }
     {
@@ -1169,6 +1208,7 @@ bool Engine::install(std::vector<Job*>& jobs, std::string& why) {
             slot = n_inst_++;
         }
         j.slot = slot;
+        slot_prec_[slot] = j.opt.precision;
         for (Tile& t : j.tiles) t.inst = slot;
         const int begin = static_cast<int>(h_tiles_.size());
         if (!ensure_tables(0, begin + static_cast<int>(j.tiles.size()), why)) return false;
@@ -1238,13 +1278,40 @@ void Engine::process_frees() {
     tables_dirty_ = true;
 }
 
-bool Engine::run_once(std::string& why) {
-    if (tables_dirty_) {
-        if (!h_tiles_.empty())
-            cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
-        cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
-        tables_dirty_ = false;
+// Uploads the tile and range tables and the step groups (tiles ordered by (precision, variant),
+// a counting sort in table order) when they changed.  A group the graph does not launch yet
+// invalidates it.
+void Engine::upload_tables() {
+    if (!tables_dirty_) return;
+    int32_t count[kStepGroups + 1] = {};
+    for (const Tile& t : h_tiles_) {
+        const int g = step_group(slot_prec_[t.inst], t.variant);
+        if (g >= 0) count[g + 1]++;
     }
+    groups_present_ = 0;
+    for (int g = 0; g < kStepGroups; ++g) {
+        if (count[g + 1]) groups_present_ |= 1u << g;
+        count[g + 1] += count[g];
+    }
+    std::memcpy(group_begin_, count, sizeof(group_begin_));
+    h_group_tiles_.resize(static_cast<size_t>(count[kStepGroups]));
+    for (int k = 0; k < static_cast<int>(h_tiles_.size()); ++k) {
+        const int g = step_group(slot_prec_[h_tiles_[k].inst], h_tiles_[k].variant);
+        if (g >= 0) h_group_tiles_[static_cast<size_t>(count[g]++)] = k;
+    }
+    if (!h_tiles_.empty())
+        cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
+    if (!h_group_tiles_.empty())
+        cudaMemcpyAsync(d_group_tiles_, h_group_tiles_.data(), sizeof(int32_t) * h_group_tiles_.size(),
+                        cudaMemcpyHostToDevice, stream_);
+    cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
+    // the pageable sources above are copied out before cudaMemcpyAsync returns
+    if (groups_present_ & ~graph_groups_) graph_valid_ = false;
+    tables_dirty_ = false;
+}
+
+bool Engine::run_once(std::string& why) {
+    upload_tables();
     if (!stream_mode_ && !graph_valid_ && !build_graph(why)) return false;
     int cap = std::numeric_limits<int>::max() / 2;
     double latency;
@@ -1255,6 +1322,7 @@ bool Engine::run_once(std::string& why) {
     if (latency > 0) cap = std::max(1, static_cast<int>(latency / std::max(body_ms_, 1e-3)));
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
     h_ctrl_->bodies = 0;
     h_ctrl_->body_cap = cap;
     h_ctrl_->error = 0;
@@ -1396,13 +1464,20 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     R.it_next = 1LL << 40;
     for (int k = 0; k < kMaxInterval; ++k) R.beta[k] = 0.5;
     cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
+    upload_tables();
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
     cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
     const View v = view();
-    launch_step(v, j.opt.precision, 0, graph_grid_, stream_);  // warm-up
+    const int group = step_group(j.opt.precision, j.variant);
+    auto step = [&] {
+        if (group >= 0) launch_step_group(v, group, 0, graph_grid_, stream_);
+        else launch_step_exact(v, 0, graph_grid_, stream_);
+    };
+    step();  // warm-up
     cudaEventRecord(ev0_, stream_);
-    for (int k = 0; k < launches; ++k) launch_step(v, j.opt.precision, 0, graph_grid_, stream_);
+    for (int k = 0; k < launches; ++k) step();
     cudaEventRecord(ev1_, stream_);
     cudaMemcpyAsync(&d_inst_[j.slot], &saved, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
     cudaError_t e = cudaStreamSynchronize(stream_);

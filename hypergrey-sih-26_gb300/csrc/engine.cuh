@@ -43,6 +43,19 @@ enum Variant : int32_t {
     // 1, 2, 4, 8, 16, 32: sub-warp rows, that many lanes per row
 };
 
+// Step-kernel groups: one kernel per (precision, variant) for the FP64 and mixed engines, each
+// over its own list of tiles, so a kernel carries one SpMV structure and the registers of that
+// structure alone (the FP64_EXACT engine has one structure and no groups).
+constexpr int kVariants = 8;
+constexpr int kStepGroups = 2 * kVariants;
+__host__ __device__ constexpr int variant_index(int variant) {
+    return variant == VAR_WARP ? 7 : variant == 32 ? 6 : variant == 16 ? 5 : variant == 8 ? 4 : variant == 4 ? 3
+         : variant == 2 ? 2 : variant == 1 ? 1 : 0;
+}
+__host__ __device__ constexpr int step_group(int precision, int variant) {
+    return precision == PREC_FP64_EXACT ? -1 : (precision == PREC_MIXED ? kVariants : 0) + variant_index(variant);
+}
+
 struct Tile {
     int32_t inst;
     int32_t row_begin;
@@ -175,6 +188,7 @@ struct Ctrl {
     int32_t n_cg;          // instances that may still run CG iterations in this body
     int32_t cg_iters;      // CG iterations run in this body
     long long kernels;     // engine kernels executed by this launch (counted by gate/control)
+    int32_t group_begin[kStepGroups + 1];  // step groups: [begin, end) in View::group_tiles
 };
 
 // Everything a tile kernel needs, passed by value.
@@ -186,6 +200,7 @@ struct View {
     Ctrl* ctrl;
     int32_t* status_mirror;  // per-instance status, rewritten by the control kernel every body
     const int2* ranges;      // per-instance tile range [x, y) in the tile table
+    const int32_t* group_tiles;  // tile indices ordered by step group (Ctrl::group_begin)
 };
 
 }  // namespace bqp

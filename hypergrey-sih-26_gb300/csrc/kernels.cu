@@ -853,39 +853,49 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j, int tra
     __syncthreads();  // prod is reused by the next tile
 }
 
-// Launch j0 of a body performs iteration it_cur + j0 of every instance whose chunk is not done.
-template <int PREC>
-__global__ void __launch_bounds__(kBlock) step_kernel(View v, int j0) {
-    const int nt = v.ctrl->n_tiles;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-        const Tile T = v.tiles[t];
-        const InstDev& I = v.inst[T.inst];
-        if (I.status != ST_RUNNING || I.phase != PH_FISTA || I.precision != PREC) continue;
-        const int64_t it = I.it_cur + j0;
-        if (it >= I.it_next) continue;
-        const int j = static_cast<int>(it - I.it0);  // position in the chunk
-        const int count = static_cast<int>(I.it_next - I.it0);
-        const int track = (PREC == PREC_MIXED && count >= 2 && j >= count - 2) ? j - (count - 2) : -1;
-        if constexpr (PREC == PREC_FP64_EXACT) {
-            step_rows_exact(I, T.row_begin, T.row_end, j);
-        } else {
-            switch (T.variant) {
-            case VAR_TILE:
-                if (__ldg(I.rowptr + T.row_end) - __ldg(I.rowptr + T.row_begin) <= kTileNnz)
-                    step_tile_block<PREC>(I, T.row_begin, T.row_end, j, track);
-                else
-                    step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track);
-                break;
-            case VAR_WARP: step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track); break;
-            case 1: step_rows_subwarp<1, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            case 2: step_rows_subwarp<2, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            case 4: step_rows_subwarp<4, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            case 8: step_rows_subwarp<8, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            case 16: step_rows_subwarp<16, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            default: step_rows_subwarp<32, PREC>(I, T.row_begin, T.row_end, j, track); break;
-            }
-        }
+// One tile of FISTA step j0 of a body (iteration it_cur + j0 of an instance whose chunk is not
+// done) with a fixed SpMV structure.  The test is uniform over the block.
+template <int PREC, int VAR>
+__device__ __forceinline__ void step_tile(const View& v, const Tile& T, int j0) {
+    const InstDev& I = v.inst[T.inst];
+    if (I.status != ST_RUNNING || I.phase != PH_FISTA || I.precision != PREC) return;
+    const int64_t it = I.it_cur + j0;
+    if (it >= I.it_next) return;
+    const int j = static_cast<int>(it - I.it0);  // position in the chunk
+    const int count = static_cast<int>(I.it_next - I.it0);
+    const int track = (PREC == PREC_MIXED && count >= 2 && j >= count - 2) ? j - (count - 2) : -1;
+    if constexpr (PREC == PREC_FP64_EXACT) {
+        step_rows_exact(I, T.row_begin, T.row_end, j);
+    } else if constexpr (VAR == VAR_TILE) {
+        if (__ldg(I.rowptr + T.row_end) - __ldg(I.rowptr + T.row_begin) <= kTileNnz)
+            step_tile_block<PREC>(I, T.row_begin, T.row_end, j, track);
+        else
+            step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track);
+    } else if constexpr (VAR == VAR_WARP) {
+        step_rows_staged<PREC>(I, T.row_begin, T.row_end, j, track);
+    } else {
+        step_rows_subwarp<VAR, PREC>(I, T.row_begin, T.row_end, j, track);
     }
+}
+
+// Step kernel of one group (precision, SpMV structure): grid-stride over the group's tiles.
+// The sub-warp structures of 2 to 32 lanes per row run 6 blocks per SM (40 registers; measured
+// on the 1M random graph, 4 lanes: 85.9 us per step against 94.5 us at the compiler's 48
+// registers and 89.9 us at 8 blocks); one lane per row and the staged structures keep the
+// compiler's choice (the 1M tridiagonal and grid steps are faster there).
+template <int VAR>
+constexpr int step_min_blocks() { return (VAR == VAR_TILE || VAR == VAR_WARP || VAR == 1) ? 0 : 6; }
+
+template <int PREC, int VAR>
+__global__ void __launch_bounds__(kBlock, step_min_blocks<VAR>()) step_kernel(View v, int group, int j0) {
+    const int b = v.ctrl->group_begin[group], e = v.ctrl->group_begin[group + 1];
+    for (int t = b + static_cast<int>(blockIdx.x); t < e; t += gridDim.x) step_tile<PREC, VAR>(v, v.tiles[v.group_tiles[t]], j0);
+}
+
+// FP64_EXACT engine: one structure, every tile of the table (other precisions skip).
+__global__ void __launch_bounds__(kBlock) step_exact_kernel(View v, int j0) {
+    const int nt = v.ctrl->n_tiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) step_tile<PREC_FP64_EXACT, 1>(v, v.tiles[t], j0);
 }
 
 // ---- check kernel -----------------------------------------------------------------------------
@@ -1414,7 +1424,7 @@ __device__ void advance_chunks(const View& v, int steps) {
 // direction kernel counts into Ctrl::kernels.
 __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraphConditionalHandle h_mixed,
                             cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish,
-                            cudaGraphConditionalHandle h_cg, int steps) {
+                            cudaGraphConditionalHandle h_cg, StepLaunches steps) {
     const Counts c = count_phases(v, false);
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
@@ -1422,7 +1432,7 @@ __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraph
         v.ctrl->n_cg = c.polish;
         v.ctrl->cg_iters = 0;
         long long launched = 4;  // three check kernels + gate
-        for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps : 0;
+        for (int k = 0; k < 3; ++k) launched += c.fista[k] > 0 ? steps.n[k] : 0;
         launched += c.polish > 0 ? 2 : 0;
         v.ctrl->kernels += launched;
         cudaGraphSetConditional(h_fp64, c.fista[0] > 0 ? 1u : 0u);
@@ -1673,7 +1683,8 @@ __global__ void __launch_bounds__(kBlock) box_step_kernel(int n, const int32_t* 
 namespace {
 // One full wave (SMs x resident blocks per SM) per tile kernel, computed once per process.
 struct Waves {
-    int step[3] = {0, 0, 0};
+    int group[kStepGroups] = {};
+    int exact = 0;
     int check = 0, check_mixed = 0, check_verify = 0, polish = 0, matvec = 0, residual = 0;
 };
 Waves g_waves;
@@ -1688,12 +1699,55 @@ int wave_of(K kernel, int sms, int dyn_smem) {
 constexpr int kSmemF32 = smem_bytes<float>() > kTileNnz * 4 ? smem_bytes<float>() : kTileNnz * 4;
 constexpr int kSmem8 = smem_bytes<double>() > kTileNnz * 8 ? smem_bytes<double>() : kTileNnz * 8;
 inline int pick(int cap, int wave) { return cap < wave ? (cap < 1 ? 1 : cap) : wave; }
+
+// Dynamic shared memory of a step group: the block- and warp-staged structures keep their
+// products there, the sub-warp ones none.
+template <int PREC, int VAR>
+constexpr int step_smem() {
+    return (VAR == VAR_TILE || VAR == VAR_WARP) ? (PREC == PREC_MIXED ? kSmemF32 : kSmem8) : 0;
+}
+
+template <int PREC, int VAR>
+void group_wave(int sms) {
+    g_waves.group[step_group(PREC, VAR)] = wave_of(step_kernel<PREC, VAR>, sms, step_smem<PREC, VAR>());
+}
+
+template <int PREC>
+void group_waves(int sms) {
+    group_wave<PREC, VAR_TILE>(sms);
+    group_wave<PREC, 1>(sms);
+    group_wave<PREC, 2>(sms);
+    group_wave<PREC, 4>(sms);
+    group_wave<PREC, 8>(sms);
+    group_wave<PREC, 16>(sms);
+    group_wave<PREC, 32>(sms);
+    group_wave<PREC, VAR_WARP>(sms);
+}
+
+template <int PREC, int VAR>
+void launch_group(const View& v, int group, int j, int grid, cudaStream_t s) {
+    step_kernel<PREC, VAR><<<pick(grid, g_waves.group[group]), kBlock, step_smem<PREC, VAR>(), s>>>(v, group, j);
+}
+
+template <int PREC>
+void launch_group_of(const View& v, int group, int j, int grid, cudaStream_t s) {
+    switch (group % kVariants) {
+    case 0: launch_group<PREC, VAR_TILE>(v, group, j, grid, s); break;
+    case 1: launch_group<PREC, 1>(v, group, j, grid, s); break;
+    case 2: launch_group<PREC, 2>(v, group, j, grid, s); break;
+    case 3: launch_group<PREC, 4>(v, group, j, grid, s); break;
+    case 4: launch_group<PREC, 8>(v, group, j, grid, s); break;
+    case 5: launch_group<PREC, 16>(v, group, j, grid, s); break;
+    case 6: launch_group<PREC, 32>(v, group, j, grid, s); break;
+    default: launch_group<PREC, VAR_WARP>(v, group, j, grid, s); break;
+    }
+}
 }  // namespace
 
 int tile_grid(int sms) {
-    g_waves.step[PREC_FP64] = wave_of(step_kernel<PREC_FP64>, sms, kSmem8);
-    g_waves.step[PREC_MIXED] = wave_of(step_kernel<PREC_MIXED>, sms, kSmemF32);
-    g_waves.step[PREC_FP64_EXACT] = wave_of(step_kernel<PREC_FP64_EXACT>, sms, 0);
+    group_waves<PREC_FP64>(sms);
+    group_waves<PREC_MIXED>(sms);
+    g_waves.exact = wave_of(step_exact_kernel, sms, 0);
     g_waves.check = wave_of(check_kernel<FAMILY_FP64>, sms, kSmem8);
     g_waves.check_mixed = wave_of(check_kernel<FAMILY_MIXED>, sms, kSmem8);
     g_waves.check_verify = wave_of(check_kernel<FAMILY_VERIFY>, sms, kSmem8);
@@ -1701,8 +1755,9 @@ int tile_grid(int sms) {
     g_waves.residual = wave_of(polish_residual_kernel, sms, 0);
     wave_of(check_standalone_kernel, sms, kSmem8);
     g_waves.polish = wave_of(cg_vector_kernel, sms, 0);
-    int m = 0;
-    for (int w : {g_waves.step[0], g_waves.step[1], g_waves.step[2], g_waves.check, g_waves.matvec, g_waves.polish})
+    int m = g_waves.exact;
+    for (int w : g_waves.group) m = w > m ? w : m;
+    for (int w : {g_waves.check, g_waves.matvec, g_waves.polish})
         m = w > m ? w : m;
     return m;
 }
@@ -1713,14 +1768,13 @@ void launch_check(const View& v, int grid, cudaStream_t s) {
     check_kernel<FAMILY_FP64><<<pick(grid, g_waves.check), kBlock, kSmem8, s>>>(v);
 }
 
-void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s) {
-    switch (precision) {
-    case PREC_MIXED: step_kernel<PREC_MIXED><<<pick(grid, g_waves.step[PREC_MIXED]), kBlock, kSmemF32, s>>>(v, j); break;
-    case PREC_FP64_EXACT:
-        step_kernel<PREC_FP64_EXACT><<<pick(grid, g_waves.step[PREC_FP64_EXACT]), kBlock, 0, s>>>(v, j);
-        break;
-    default: step_kernel<PREC_FP64><<<pick(grid, g_waves.step[PREC_FP64]), kBlock, kSmem8, s>>>(v, j); break;
-    }
+void launch_step_group(const View& v, int group, int j, int grid, cudaStream_t s) {
+    if (group >= kVariants) launch_group_of<PREC_MIXED>(v, group, j, grid, s);
+    else launch_group_of<PREC_FP64>(v, group, j, grid, s);
+}
+
+void launch_step_exact(const View& v, int j, int grid, cudaStream_t s) {
+    step_exact_kernel<<<pick(grid, g_waves.exact), kBlock, 0, s>>>(v, j);
 }
 
 void launch_polish_init(const View& v, int grid, cudaStream_t s) {
@@ -1737,7 +1791,7 @@ void launch_cg_vector(const View& v, int grid, cudaStream_t s, cudaGraphConditio
 }
 
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
-                 cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s) {
+                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, cudaStream_t s) {
     gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, cg_loop, steps);
 }
 void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s) {

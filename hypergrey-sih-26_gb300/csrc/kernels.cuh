@@ -10,7 +10,10 @@ namespace bqp {
 int tile_grid(int sms);
 // Tile kernels: grid-stride over the tile table (the grid size is fixed at capture).
 void launch_check(const View& v, int grid, cudaStream_t s);
-void launch_step(const View& v, int precision, int j, int grid, cudaStream_t s);
+// Step j of a body: the step kernel of one group (step_group(precision, variant)) over the group's
+// tiles, or the FP64_EXACT step over the whole table.
+void launch_step_group(const View& v, int group, int j, int grid, cudaStream_t s);
+void launch_step_exact(const View& v, int j, int grid, cudaStream_t s);
 void launch_polish_init(const View& v, int grid, cudaStream_t s);
 void launch_polish_residual(const View& v, int grid, cudaStream_t s);
 void launch_cg_matvec(const View& v, int grid, cudaStream_t s);
@@ -19,9 +22,13 @@ void launch_cg_matvec(const View& v, int grid, cudaStream_t s);
 void launch_cg_vector(const View& v, int grid, cudaStream_t s, cudaGraphConditionalHandle cg_loop = 0, int cap = 0);
 // Single-block control kernels that steer the conditional graph nodes.
 // fista[k]: handle of the IF node of the precision-k step launches; polish: the IF node of the
-// polish branch; cg_loop: the WHILE node of its CG loop.  `steps`: kernels inside each FISTA body.
+// polish branch; cg_loop: the WHILE node of its CG loop.  `steps.n[k]`: kernels inside the
+// precision-k FISTA body (steps per body x step groups launched).
+struct StepLaunches {
+    int n[3];
+};
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
-                 cudaGraphConditionalHandle cg_loop, int steps, cudaStream_t s);
+                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, cudaStream_t s);
 // `steps`: step launches per body; FISTA-phase instances advance it_cur by up to that many.
 void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s);
 // Host-driven variants of the control kernels (no conditional handles).
