@@ -95,7 +95,9 @@ def _i64(a):
 
 def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, precision='fp64',
                    check_interval=0, diagonal_gate=-1, offset=0.0, kernel_variant=-1, polish_switch=None,
-                   scaling=0):
+                   scaling=0, lipschitz='gershgorin'):
+    """bqp_options from keywords; lipschitz: 'gershgorin' (the reference's bound) or 'power'
+    (device power-iteration estimate)."""
     o = Options()
     lib().bqp_options_default(o)
     o.tolerance = float(tolerance)
@@ -109,6 +111,7 @@ def options_struct(tolerance=1e-7, time_limit=30.0, iteration_limit=200000, prec
     if polish_switch is not None:
         o.polish_switch = float(polish_switch)
     o.scaling = int(scaling)
+    o.lipschitz = {'gershgorin': 0, 'power': 1}[lipschitz] if isinstance(lipschitz, str) else int(lipschitz)
     return o
 
 

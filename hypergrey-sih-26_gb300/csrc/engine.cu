@@ -115,12 +115,12 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.start_ff = take(N * 4);
         L.sstep = take(N * 4);
         L.s = take(N * 8);
-        L.lprec = take(8);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
         L.w64b = take(N * 8);
     }
+    L.lprec = take(8);
     L.total = o;
     return L;
 }
@@ -1171,18 +1171,28 @@ bool Engine::upload(Job& j, std::string& why) {
     // 3x the switch, except on chain-like rows of fewer than 4 nonzeros (tridiagonal: the free
     // runs are long, and an early polish costs more CG iterations than the FISTA steps it saves)
     R.step_switch = j.nnz >= 4 * j.n ? 3.0 * j.opt.polish_switch : 0.0;
+    R.lip_device = j.opt.lipschitz == BQP_LIPSCHITZ_POWER ? 1 : 0;
+    void* power = nullptr;
+    if (R.lip_device &&
+        !cuda_ok(cudaMallocFromPoolAsync(&power, power_scratch_bytes(j.n), pool_, ustream_), why, "allocate power scratch"))
+        return false;
     if (prec == PREC_MIXED) {
         void* tmp = nullptr;
         if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, ustream_), why, "allocate upload buffer")) return false;
         if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
         launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(tmp), ustream_);
-        launch_precondition(R, j.n, static_cast<const double*>(tmp), j.opt.scaling != 2, ustream_);
+        launch_precondition(R, j.n, static_cast<const double*>(tmp), j.opt.scaling != 2, power, ustream_);
         cudaFreeAsync(tmp, ustream_);
     } else {
         double* val = at<double>(slab, L.val64);
         if (Z) cudaMemcpyAsync(val, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
         launch_prepare_instance(R, j.n, j.nnz, val, ustream_);
+        if (R.lip_device) {
+            cudaMemcpyAsync(R.lprec, &R.L, sizeof(double), cudaMemcpyHostToDevice, ustream_);
+            launch_power_lipschitz(R, j.n, val, false, power, ustream_);
+        }
     }
+    if (power) cudaFreeAsync(power, ustream_);
     if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
     cudaEventRecord(uev_, ustream_);
     if (host_profile()) {
@@ -1657,10 +1667,9 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
         why = "Invalid box QP options";
         return BQP_ERR_INVALID;
     }
-    if (o->lipschitz != BQP_LIPSCHITZ_GERSHGORIN) {
-        why = o->lipschitz == BQP_LIPSCHITZ_POWER ? "the power-iteration Lipschitz estimate is not implemented"
-                                                   : "Invalid box QP options";
-        return o->lipschitz == BQP_LIPSCHITZ_POWER ? BQP_ERR_UNSUPPORTED : BQP_ERR_INVALID;
+    if (o->lipschitz != BQP_LIPSCHITZ_GERSHGORIN && o->lipschitz != BQP_LIPSCHITZ_POWER) {
+        why = "Invalid box QP options";
+        return BQP_ERR_INVALID;
     }
     if (rowptr[0] != 0 || rowptr[n] != nnz) {
         why = "Invalid CSR row pointers";

@@ -127,10 +127,10 @@ struct __align__(16) InstDev {
     int32_t precision;
     int32_t polish;        // mixed: free-set polish enabled
     int32_t arm_chunk;     // 1: admission arms the first chunk without a check of x0 (mixed)
-    int32_t pad_arm;
+    int32_t lip_device;    // 1: L is the device power estimate in *lprec (BQP_LIPSCHITZ_POWER)
     int32_t moved[2];      // mixed: a variable entered or left a bound in the chunk's last two steps
     float* sstep;          // mixed, preconditioned: per-row step 1 / (L' Q_ii) (null: scalar 1/L)
-    double* lprec;         // mixed, preconditioned: L' (device-computed at admission)
+    double* lprec;         // L' of the preconditioned mixed engine, or the power estimate of L (device-computed at admission)
     int32_t lanes_res;     // polish: lanes per row of the residual pass (full rows)
     int32_t lanes_cg;      // polish: lanes per row of the CG products (free-free rows)
     int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)

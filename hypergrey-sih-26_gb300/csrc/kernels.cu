@@ -1530,7 +1530,16 @@ __global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __
         uint4* dst = reinterpret_cast<uint4*>(&I);
         for (int w = threadIdx.x; w < static_cast<int>(sizeof(InstDev) / 16); w += kBlock) dst[w] = src[w];
         __syncthreads();
-        if (threadIdx.x == 0) start_instance(I);
+        if (threadIdx.x == 0) {
+            // the power estimate replaces the host's Gershgorin L (the mixed engine's steps
+            // already carry it in sstep; its L is then the estimate for the matrix they scale)
+            if (I.lip_device) {
+                I.L = *I.lprec;
+                I.invL = 1.0 / I.L;
+                I.invLf = static_cast<float>(I.invL);
+            }
+            start_instance(I);
+        }
     }
 }
 
@@ -1589,17 +1598,184 @@ __global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n,
     if ((threadIdx.x & 31) == 0 && best) atomicMax(reinterpret_cast<unsigned long long*>(I.lprec), best);
 }
 
-// scaled = 0: the scalar step 1/L in every row.
+// scaled = 0: the scalar step 1/L in every row (L from lprec under the power estimate).
 __global__ void __launch_bounds__(kBlock) precond_step_kernel(InstDev I, int n, int scaled) {
     const int stride = gridDim.x * blockDim.x;
-    const double lp = scaled ? *I.lprec : 0.0;
+    const double lp = (scaled || I.lip_device) ? *I.lprec : 0.0;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        double s = I.invL;
+        double s = (I.lip_device && lp > 0) ? 1.0 / lp : I.invL;
         if (scaled && lp > 0) {
             const double v = precond_v(I, r);
             s = v * v / lp;
         }
         I.sstep[r] = static_cast<float>(s);
+    }
+}
+
+// ---- power-iteration (Lanczos) Lipschitz estimate (BQP_LIPSCHITZ_POWER) ---------------------------
+// Estimates lambda_max of M = S Q S (S = diag(v) for the preconditioned mixed engine, else the
+// identity) in FP64 at admission.  The power iteration's Krylov space {y0, M y0, M^2 y0, ...}
+// from a fixed positive pseudo-random y0 is spanned by the Lanczos process (the power iteration
+// alone converges too slowly where the top eigenvalues cluster, as on graph Laplacians):
+//     v_k = w_k / beta_k,  z = M v_k,  alpha_k = v_k'z,  w_k+1 = z - alpha_k v_k - beta_k v_k-1,
+// kLanczosSteps steps, two kernels per step (product with alpha; update with beta).  The last
+// block of the final update takes the largest eigenvalue theta of the tridiagonal T (Sturm
+// bisection) and its residual |beta_K s_K| (s the unit eigenvector of T), and writes
+//     L = min(Gershgorin bound of M, max(theta + residual, 1.001 theta))
+// to lprec: theta <= lambda_max, and some eigenvalue of M lies within the residual of theta.
+// An invariant subspace (beta ~ 0, e.g. n < kLanczosSteps) ends the process early.
+// Deterministic: fixed grid, fixed shuffle trees, the last block adds the block partials in order.
+constexpr int kLanczosSteps = 32;
+constexpr int kLanczosBlocks = 152 * 4;
+struct LanczosState {
+    double alpha[kLanczosSteps];
+    double beta[kLanczosSteps + 1];  // beta[0] = |y0|, beta[k + 1] = |w_k+1|
+    unsigned ticket;
+    int steps;                       // alpha's computed; the process stops early at a zero beta
+    int stopped;
+    int pad;
+};
+
+__device__ __forceinline__ double lanczos_start(int r) {
+    return 0.5 + static_cast<double>(mix_index(static_cast<unsigned>(r) * 2654435761u + 12345u) >> 8) * (1.0 / 16777216.0);
+}
+
+// Block sum of one double in a fixed order; the last block (ticket) returns true with the grid
+// total in *total (thread 0 only).
+__device__ bool lanczos_reduce(double x, double* partial, LanczosState* st, double* total) {
+    __shared__ double red[kBlock / 32];
+    __shared__ int last;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += shfl_xor(x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0;
+        for (int w = 0; w < kBlock / 32; ++w) b += red[w];
+        partial[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1 ? 1 : 0;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return false;
+    __threadfence();
+    double t = 0;
+    for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(partial + k);
+    st->ticket = 0;
+    *total = t;
+    return true;
+}
+
+// w = y0, beta_0 = |y0|
+__global__ void __launch_bounds__(kBlock) lanczos_init_kernel(int n, double* __restrict__ w, double* __restrict__ partial,
+                                                              LanczosState* st) {
+    double b = 0;
+    for (int r = blockIdx.x * kBlock + threadIdx.x; r < n; r += gridDim.x * kBlock) {
+        const double y = lanczos_start(r);
+        w[r] = y;
+        b += y * y;
+    }
+    double t;
+    if (lanczos_reduce(b, partial, st, &t)) st->beta[0] = sqrt(t);
+}
+
+// step k: v_k = w / beta_k (stored), z = M v_k, alpha_k = v_k' z
+__global__ void __launch_bounds__(kBlock) lanczos_product_kernel(InstDev I, int n, const double* __restrict__ val, int scaled,
+                                                                 const double* __restrict__ w, double* __restrict__ vk,
+                                                                 double* __restrict__ z, double* __restrict__ partial,
+                                                                 LanczosState* st, int k) {
+    if (st->stopped) return;
+    const double scale = 1.0 / st->beta[k];
+    const double* __restrict__ v = I.s;
+    double a = 0;
+    for (int r = blockIdx.x * kBlock + threadIdx.x; r < n; r += gridDim.x * kBlock) {
+        const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+        double acc = 0;
+        for (int q = ks; q < ke; ++q) {
+            const int j = __ldg(I.col + q);
+            acc += val[q] * (scaled ? v[j] * w[j] : w[j]);
+        }
+        if (scaled) acc *= v[r];
+        const double zr = acc * scale, vr = w[r] * scale;
+        z[r] = zr;
+        vk[r] = vr;
+        a += vr * zr;
+    }
+    double t;
+    if (lanczos_reduce(a, partial, st, &t)) {
+        st->alpha[k] = t;
+        st->steps = k + 1;
+    }
+}
+
+// Largest eigenvalue of the m x m tridiagonal (alpha, beta[1..m-1]) and the residual of its Ritz
+// pair, |beta_m s_m| with s the unit eigenvector.  One thread.
+__device__ void lanczos_ritz(const LanczosState* st, int m, double* theta_out, double* resid_out) {
+    const double* a = st->alpha;
+    const double* b = st->beta;  // off-diagonal i (between i-1 and i) is b[i], i = 1..m-1
+    double lo = a[0], hi = a[0];
+    for (int i = 0; i < m; ++i) {
+        const double rad = (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < m ? fabs(b[i + 1]) : 0.0);
+        lo = fmin(lo, a[i] - rad);
+        hi = fmax(hi, a[i] + rad);
+    }
+    // Sturm count of eigenvalues > x: negative pivots of T - x I counted from the bottom
+    for (int it = 0; it < 200 && hi - lo > 1e-15 * fmax(fabs(hi), fabs(lo)); ++it) {
+        const double x = 0.5 * (lo + hi);
+        int below = 0;
+        double d = 1.0;
+        for (int i = 0; i < m; ++i) {
+            const double off = i > 0 ? b[i] * b[i] : 0.0;
+            d = (a[i] - x) - (i > 0 ? off / (d != 0.0 ? d : 1e-300) : 0.0);
+            if (d < 0) ++below;
+        }
+        if (below < m) lo = x;  // some eigenvalue lies above x
+        else hi = x;
+    }
+    const double theta = hi;
+    // eigenvector of T for theta by the three-term recurrence from s_0 = 1, kept normalised
+    double s_prev = 0.0, s_cur = 1.0, norm2 = 1.0;
+    for (int i = 0; i + 1 < m; ++i) {
+        double s_next = ((theta - a[i]) * s_cur - (i > 0 ? b[i] * s_prev : 0.0)) / (b[i + 1] != 0.0 ? b[i + 1] : 1e-300);
+        norm2 += s_next * s_next;
+        s_prev = s_cur;
+        s_cur = s_next;
+        if (norm2 > 1e200) {
+            const double f = 1.0 / sqrt(norm2);
+            s_prev *= f;
+            s_cur *= f;
+            norm2 = 1.0;
+        }
+    }
+    *theta_out = theta;
+    *resid_out = fabs(b[m]) * fabs(s_cur) / sqrt(norm2);
+}
+
+// w_k+1 = z - alpha_k v_k - beta_k v_k-1, beta_k+1 = |w_k+1|; the final step writes the estimate
+__global__ void __launch_bounds__(kBlock) lanczos_update_kernel(InstDev I, int n, const double* __restrict__ z,
+                                                                const double* __restrict__ vk,
+                                                                const double* __restrict__ vprev, double* __restrict__ w,
+                                                                double* __restrict__ partial, LanczosState* st, int k) {
+    if (st->stopped) return;
+    const double al = st->alpha[k], be = k > 0 ? st->beta[k] : 0.0;
+    double b = 0;
+    for (int r = blockIdx.x * kBlock + threadIdx.x; r < n; r += gridDim.x * kBlock) {
+        const double x = z[r] - al * vk[r] - (k > 0 ? be * vprev[r] : 0.0);
+        w[r] = x;
+        b += x * x;
+    }
+    double t;
+    if (!lanczos_reduce(b, partial, st, &t)) return;
+    const double beta = sqrt(t);
+    st->beta[k + 1] = beta;
+    const bool invariant = !(beta > 1e-12 * fmax(fabs(al), 1e-300));
+    if (invariant) st->stopped = 1;
+    if (invariant || k + 1 == kLanczosSteps) {
+        if (invariant) st->beta[k + 1] = 0.0;
+        double theta, resid;
+        lanczos_ritz(st, k + 1, &theta, &resid);
+        const double est = fmax(theta + resid, 1.001 * theta);
+        if (isfinite(est) && est > 0) *I.lprec = fmin(*I.lprec, est);  // lprec: the Gershgorin bound of M
     }
 }
 
@@ -1813,7 +1989,8 @@ void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, con
     if (n_spans > 0) rearm_kernel<<<n_spans, kBlock, 0, s>>>(v, stage, slots, spans);
 }
 
-void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, cudaStream_t s) {
+void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, void* power_scratch,
+                         cudaStream_t s) {
     int64_t grid = (n + kBlock - 1) / kBlock;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid < 1) grid = 1;
@@ -1821,7 +1998,42 @@ void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool 
         cudaMemsetAsync(rec.lprec, 0, sizeof(double), s);
         precond_bound_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), val);
     }
+    if (rec.lip_device) {
+        if (!scaled) cudaMemcpyAsync(rec.lprec, &rec.L, sizeof(double), cudaMemcpyHostToDevice, s);
+        launch_power_lipschitz(rec, n, val, scaled, power_scratch, s);
+    }
     precond_step_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), scaled ? 1 : 0);
+}
+
+inline size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+size_t power_scratch_bytes(int64_t n) {
+    return 1024 + round256(sizeof(double) * kLanczosBlocks) + 4 * round256(sizeof(double) * static_cast<size_t>(n));
+}
+
+void launch_power_lipschitz(const InstDev& rec, int64_t n, const double* val, bool scaled, void* scratch, cudaStream_t s) {
+    char* base = static_cast<char*>(scratch);
+    LanczosState* st = reinterpret_cast<LanczosState*>(base);
+    static_assert(sizeof(LanczosState) <= 1024, "state size");
+    double* partial = reinterpret_cast<double*>(base + 1024);
+    const size_t vec = round256(sizeof(double) * static_cast<size_t>(n));
+    char* vecs = base + 1024 + round256(sizeof(double) * kLanczosBlocks);
+    double* w = reinterpret_cast<double*>(vecs);
+    double* z = reinterpret_cast<double*>(vecs + vec);
+    double* va = reinterpret_cast<double*>(vecs + 2 * vec);
+    double* vb = reinterpret_cast<double*>(vecs + 3 * vec);
+    cudaMemsetAsync(st, 0, sizeof(LanczosState), s);
+    int64_t g = (n + kBlock - 1) / kBlock;
+    if (g > kLanczosBlocks) g = kLanczosBlocks;
+    if (g < 1) g = 1;
+    const int grid = static_cast<int>(g), ni = static_cast<int>(n);
+    lanczos_init_kernel<<<grid, kBlock, 0, s>>>(ni, w, partial, st);
+    for (int k = 0; k < kLanczosSteps; ++k) {
+        double* vk = (k & 1) ? vb : va;
+        double* vprev = (k & 1) ? va : vb;
+        lanczos_product_kernel<<<grid, kBlock, 0, s>>>(rec, ni, val, scaled ? 1 : 0, w, vk, z, partial, st, k);
+        lanczos_update_kernel<<<grid, kBlock, 0, s>>>(rec, ni, z, vk, vprev, w, partial, st, k);
+    }
 }
 
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {

@@ -38,8 +38,15 @@ void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // The record is passed by value: the instance is installed in its slot later, between graph launches.
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
 // Mixed engine: per-row FISTA steps (diagonally preconditioned when `scaled`, else 1/L), after
-// launch_prepare_instance on the same stream; val = the FP64 values.
-void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, cudaStream_t s);
+// launch_prepare_instance on the same stream; val = the FP64 values.  With rec.lip_device the
+// power estimate replaces the Gershgorin bound (power_scratch: power_scratch_bytes()).
+void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, void* power_scratch,
+                         cudaStream_t s);
+// BQP_LIPSCHITZ_POWER: Lanczos on the power iteration's Krylov space of S Q S (S = diag(rec.s)
+// when `scaled`), FP64, at admission; *rec.lprec holds the Gershgorin bound of that matrix before
+// and the estimate after.  scratch: power_scratch_bytes(n) bytes of device memory, 256-aligned.
+size_t power_scratch_bytes(int64_t n);
+void launch_power_lipschitz(const InstDev& rec, int64_t n, const double* val, bool scaled, void* scratch, cudaStream_t s);
 // Admission: x0 = clip(0, l, u), w = x0, start clock; one instance.
 // Re-arm of resident solves: records staged on the device, spans (staged index, first row) of
 // kRearmRows rows each, one block per span.

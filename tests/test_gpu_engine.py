@@ -194,13 +194,41 @@ def test_device_name():
     assert 'GB300' in boxqp.cuda_device_name() or len(boxqp.cuda_device_name()) > 0
 
 
-def test_power_lipschitz_option_is_rejected_as_unsupported(engine):
-    inst = boxqp.planted('graph10k', seed=1, n=500)
-    o = boxqp.options_struct(1e-6, 10.0, 1000, 'mixed')
-    o.lipschitz = 1  # BQP_LIPSCHITZ_POWER: declared, not implemented
-    with pytest.raises(boxqp.EngineError) as err:
-        engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
-    assert err.value.code == 7 and 'not implemented' in str(err.value)
+def _lambda_max(inst, scaled):
+    """Largest eigenvalue of Q (or of V Q V, V = diag(Q)^-1/2) by scipy's Lanczos, on the CPU."""
+    sp = pytest.importorskip('scipy.sparse')
+    la = pytest.importorskip('scipy.sparse.linalg')
+    n = inst['n']
+    q = sp.csr_matrix((inst['val'], inst['col'], inst['rowptr']), shape=(n, n))
+    if scaled:
+        v = 1.0 / np.sqrt(q.diagonal())
+        q = sp.diags(v) @ q @ sp.diags(v)
+    return float(la.eigsh(q, k=1, which='LA', tol=1e-10, return_eigenvectors=False)[0])
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp64_exact', 'mixed'])
+def test_power_lipschitz_estimate(engine, precision):
+    """BQP_LIPSCHITZ_POWER: the device estimate lies between lambda_max (scipy Lanczos) and the
+    Gershgorin bound, the solve verifies with no more iterations than under Gershgorin, and it is
+    deterministic."""
+    inst = boxqp.planted('graph10k', seed=21)
+    a = (inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'])
+    og = boxqp.options_struct(1e-7, 60.0, 200000, precision)
+    op = boxqp.options_struct(1e-7, 60.0, 200000, precision, lipschitz='power')
+    xg, sg = engine.solve(*a, og)
+    xp, sp_ = engine.solve(*a, op)
+    xp2, _ = engine.solve(*a, op)
+    assert boxqp.STATUS_NAMES[sg.status] == 'optimal' and boxqp.STATUS_NAMES[sp_.status] == 'optimal'
+    assert np.array_equal(xp, xp2)
+    lam = _lambda_max(inst, scaled=precision == 'mixed')
+    gersh = boxqp.gershgorin(inst['rowptr'], inst['val'])
+    assert lam * (1 - 1e-9) <= sp_.lipschitz <= (gersh if precision != 'mixed' else 2.0 * gersh)
+    if precision != 'mixed':
+        assert sp_.lipschitz < sg.lipschitz == gersh
+        assert sp_.iterations <= sg.iterations
+    chk = O.check(*planted_args(boxqp.planted('graph10k', seed=21, lower_triplets=True)), xp, tol=1e-7)
+    assert chk['verified']
+    assert abs(sp_.objective - sg.objective) <= 1e-9 * max(1.0, abs(sg.objective))
 
 
 @pytest.mark.parametrize('scaling', [1, 2])
