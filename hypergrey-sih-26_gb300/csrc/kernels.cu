@@ -1256,7 +1256,7 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
+__global__ void __launch_bounds__(kBlock, 5) cg_matvec_kernel(View v) {
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
