@@ -40,7 +40,7 @@ def _stale(target, sources):
 
 def build(force=False, verbose=False):
     """Compiles the engine if any source is newer than the library; returns the library path."""
-    headers = list(CSRC.glob('*.cuh')) + [ROOT / 'include' / 'boxqp.h']
+    headers = list(CSRC.glob('*.cuh')) + list(CSRC.glob('*.h')) + [ROOT / 'include' / 'boxqp.h']
     sources = [CSRC / s for s in CU_SOURCES + CPP_SOURCES]
     if not force and not _stale(LIB, sources + headers + [Path(__file__)]):
         return LIB
