@@ -222,34 +222,39 @@ __device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
 // and a warp without data (`warp_data` false) contributes zeros: the FP64 additions of the
 // xor tree run only where there is something to add (FP64 is 1/64 of the FP32 rate here).
 // The CG reductions carry two sums (a, obj) and one maximum (b).
+// Block sums of a and obj (FP64) and the maximum of b, in a fixed order: every thread's values go
+// to shared memory, one warp adds each lane's 8 (thread t: lane t % 32, in order of t), then an
+// xor tree over the warp.  GB300 issues an FP64 warp instruction at 1/64 of the FP32 rate whatever
+// its active lanes, so this takes 13 FP64 additions per field instead of one per tree level in
+// every warp (a lanes-strided layout leaves zeros in the other lanes; adding them is exact).
+// `lanes` is kept for the callers' layouts; the maximum reduces over all lanes.
 __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true) {
-    __shared__ double part_a[kBlock / 32];
-    __shared__ double part_o[kBlock / 32];
+    (void)lanes;
+    __shared__ double part_a[kBlock];
+    __shared__ double part_o[kBlock];
     __shared__ unsigned long long part_b[kBlock / 32];
-    if (warp_data) {
-        for (int o = 16; o >= lanes; o >>= 1) {  // warp-uniform
-            v.a += shfl_xor(v.a, o);
-            v.obj += shfl_xor(v.obj, o);
-            v.b = umax64(v.b, shfl_xor(v.b, o));
-        }
-    } else {
+    if (!warp_data) {
         v.a = 0;
         v.obj = 0;
         v.b = 0;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v.b = umax64(v.b, shfl_xor(v.b, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        part_a[warp] = v.a;
-        part_o[warp] = v.obj;
-        part_b[warp] = v.b;
-    }
+    part_a[threadIdx.x] = v.a;
+    part_o[threadIdx.x] = v.obj;
+    if (lane == 0) part_b[warp] = v.b;
     __syncthreads();
     if (warp == 0) {
-        double a = lane < kBlock / 32 ? part_a[lane] : 0.0;
-        double ob = lane < kBlock / 32 ? part_o[lane] : 0.0;
+        double a = part_a[lane], ob = part_o[lane];
+#pragma unroll
+        for (int w = 1; w < kBlock / 32; ++w) {
+            a += part_a[lane + 32 * w];
+            ob += part_o[lane + 32 * w];
+        }
         unsigned long long b = lane < kBlock / 32 ? part_b[lane] : 0ull;
 #pragma unroll
-        for (int o = (kBlock / 64); o > 0; o >>= 1) {
+        for (int o = 16; o > 0; o >>= 1) {
             a += shfl_xor(a, o);
             ob += shfl_xor(ob, o);
             b = umax64(b, shfl_xor(b, o));
