@@ -216,11 +216,6 @@ __device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
     return block_reduce_check(acc, gate);
 }
 
-// The CG reductions carry one sum (a) and one maximum (b): the same fixed order on those two
-// fields alone, eight partials in flight per thread.
-// Only lanes that are multiples of `lanes` hold values (the group leaders of a sub-warp pass),
-// and a warp without data (`warp_data` false) contributes zeros: the FP64 additions of the
-// xor tree run only where there is something to add (FP64 is 1/64 of the FP32 rate here).
 // The CG reductions carry two sums (a, obj) and one maximum (b).
 // Block sums of a and obj (FP64) and the maximum of b, in a fixed order: every thread's values go
 // to shared memory, one warp adds each lane's 8 (thread t: lane t % 32, in order of t), then an
