@@ -1547,26 +1547,67 @@ __global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __
 // the diagonal dual-gap gate) and, for mixed precision, hi/lo FP32 values (val ~= hi + lo), the
 // FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
 // so FP32 iterates never leave the FP64 box).
+// A warp takes 32 consecutive rows; in each of LANES passes its groups of LANES lanes search one
+// row each (consecutive entries, so the column loads of a group coalesce) for the diagonal by
+// integer compares alone, and a shuffle hands every row's diagonal to its own lane, so the FP64
+// epilogue (1/d, 1/sqrt(d), FP32 roundings) runs once per 32 rows on full warps.  A row with
+// several diagonal entries (a CSR with duplicates) sums them in column order.
+template <int LANES>
 __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const double* __restrict__ val) {
-    // diagonal (at most one entry per row after the CSR build), one thread per row
-    const int stride = gridDim.x * blockDim.x;
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, sub = lane / LANES, sl = lane % LANES;
+    const int warps = gridDim.x * (kBlock / 32);
     double* diag = const_cast<double*>(I.diag);
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
-        double d = 0;
-        for (int k = ks; k < ke; ++k)
-            if (__ldg(I.col + k) == r) d += val[k];
-        diag[r] = d;
-        if (I.precision == PREC_MIXED) {
-            const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
-            // preconditioner scale v_r, kept in s (free until the polish) for the step set-up
-            I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(I.L);
-            const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
-            const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
-            const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+    for (int base = (blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)) * 32; base < n; base += warps * 32) {
+        double mine = 0;
+#pragma unroll
+        for (int pass = 0; pass < LANES; ++pass) {
+            const int r = base + pass * R + sub;
+            int first = 0x7fffffff, count = 0, ks = 0, ke = 0;
+            if (r < n) {
+                ks = __ldg(I.rowptr + r);
+                ke = __ldg(I.rowptr + r + 1);
+                for (int k = ks + sl; k < ke; k += LANES)
+                    if (__ldg(I.col + k) == r) {
+                        first = min(first, k);
+                        ++count;
+                    }
+            }
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1) {
+                first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+                count += __shfl_xor_sync(0xffffffffu, count, o);
+            }
+            double d = 0;
+            if (r < n && sl == 0 && count > 0) {
+                if (count == 1) {
+                    d = val[first];
+                } else {
+                    for (int k = first; k < ke; ++k)
+                        if (__ldg(I.col + k) == r) d += val[k];
+                }
+            }
+            const int g = lane - pass * R;
+            const bool mine_now = g >= 0 && g < R;
+            const double got = shfl_idx(d, (mine_now ? g : 0) * LANES);
+            if (mine_now) mine = got;
+        }
+        const int r = base + lane;
+        if (r < n) {
+            const double d = mine;
+            diag[r] = d;
+            if (I.precision == PREC_MIXED) {
+                const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
+                // preconditioner scale v_r, kept in s (free until the polish) for the step set-up
+                I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(I.L);
+                const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
+                const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
+                const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+            }
         }
     }
     if (I.precision == PREC_MIXED) {
+        const int stride = gridDim.x * blockDim.x;
         const int nnz = I.rowptr[n];
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += stride) {
             const double x = val[k];
@@ -1584,14 +1625,21 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
 // leaves v in the s array.
 __device__ __forceinline__ double precond_v(const InstDev& I, int r) { return I.s[r]; }
 
+template <int LANES>
 __global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n, const double* __restrict__ val) {
-    const int stride = gridDim.x * blockDim.x;
+    constexpr int R = 32 / LANES;
+    const int lane = threadIdx.x & 31, sl = lane % LANES;
+    const int groups = gridDim.x * (kBlock / 32) * R;
     unsigned long long best = 0;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+    for (int base = (blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)) * R; base < n; base += groups) {
+        const int r = base + lane / LANES;
         double sum = 0;
-        for (int k = ks; k < ke; ++k) sum += fabs(val[k]) * precond_v(I, __ldg(I.col + k));
-        best = umax64(best, dbits(sum * precond_v(I, r)));
+        if (r < n) {
+            const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
+            for (int k = ks + sl; k < ke; k += LANES) sum += fabs(val[k]) * precond_v(I, __ldg(I.col + k));
+        }
+        sum = group_sum<LANES>(sum);
+        if (r < n && sl == 0) best = umax64(best, dbits(sum * precond_v(I, r)));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = umax64(best, shfl_xor(best, o));
@@ -1989,6 +2037,10 @@ void launch_rearm(const View& v, const InstDev* stage, const int32_t* slots, con
     if (n_spans > 0) rearm_kernel<<<n_spans, kBlock, 0, s>>>(v, stage, slots, spans);
 }
 
+// Lanes per row of the admission kernels: the residual pass's choice (about a sixth of the
+// average row length), clamped to 2..8.
+inline int row_lanes(const InstDev& rec) { return rec.lanes_res >= 8 ? 8 : rec.lanes_res >= 4 ? 4 : 2; }
+
 void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool scaled, void* power_scratch,
                          cudaStream_t s) {
     int64_t grid = (n + kBlock - 1) / kBlock;
@@ -1996,7 +2048,14 @@ void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool 
     if (grid < 1) grid = 1;
     if (scaled) {
         cudaMemsetAsync(rec.lprec, 0, sizeof(double), s);
-        precond_bound_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), val);
+        const int lanes = row_lanes(rec);
+        int64_t g = (n * lanes + kBlock - 1) / kBlock;
+        if (g > 152 * 16) g = 152 * 16;
+        if (g < 1) g = 1;
+        const int gi = static_cast<int>(g), ni = static_cast<int>(n);
+        if (lanes == 8) precond_bound_kernel<8><<<gi, kBlock, 0, s>>>(rec, ni, val);
+        else if (lanes == 4) precond_bound_kernel<4><<<gi, kBlock, 0, s>>>(rec, ni, val);
+        else precond_bound_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni, val);
     }
     if (rec.lip_device) {
         if (!scaled) cudaMemcpyAsync(rec.lprec, &rec.L, sizeof(double), cudaMemcpyHostToDevice, s);
@@ -2037,11 +2096,15 @@ void launch_power_lipschitz(const InstDev& rec, int64_t n, const double* val, bo
 }
 
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
-    int64_t work = n > nnz ? n : nnz;
+    const int lanes = row_lanes(rec);
+    const int64_t work = n * lanes > nnz ? n * lanes : nnz;
     int64_t grid = (work + kBlock - 1) / kBlock;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid < 1) grid = 1;
-    prepare_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), val);
+    const int gi = static_cast<int>(grid), ni = static_cast<int>(n);
+    if (lanes == 8) prepare_kernel<8><<<gi, kBlock, 0, s>>>(rec, ni, val);
+    else if (lanes == 4) prepare_kernel<4><<<gi, kBlock, 0, s>>>(rec, ni, val);
+    else prepare_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni, val);
 }
 
 int check_grid(int64_t n) {
