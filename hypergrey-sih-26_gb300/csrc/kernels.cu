@@ -1080,7 +1080,7 @@ __device__ int block_exclusive_scan(int32_t* v, int n) {
 
 template <int LANES>
 __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list, int n, int base,
-                              const int32_t* __restrict__ start_of, Acc& a) {
+                              const int32_t* __restrict__ start_of, float2* rowsum, Acc& a) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -1144,16 +1144,23 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
         if (sl == 0 && r >= 0) {
             cnt_ff[r] = kept;
             start_ff[r] = dst;
-            const double rr = -(df_value(acc) + c[r]);
-            const double zz = rr * dinv[r];
-            a.a = fma(rr, zz, a.a);
-            a.b = umax64(a.b, cg_ratio_bits(rr, xp[r]));
-            r_out[r] = rr;
-            z_out[r] = zz;
-            p_out[r] = zz;
-            s_out[r] = 0.0;
-            p2_out[r] = df_split(zz);
+            rowsum[j] = acc;
         }
+    }
+    // the FP64 epilogue, one free row per thread (full warps: an FP64 warp instruction costs the
+    // same with 1 or 32 active lanes)
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += kBlock) {
+        const int r = list[t];
+        const double rr = -(df_value(rowsum[t]) + c[r]);
+        const double zz = rr * dinv[r];
+        a.a = fma(rr, zz, a.a);
+        a.b = umax64(a.b, cg_ratio_bits(rr, xp[r]));
+        r_out[r] = rr;
+        z_out[r] = zz;
+        p_out[r] = zz;
+        s_out[r] = 0.0;
+        p2_out[r] = df_split(zz);
     }
 }
 
@@ -1161,7 +1168,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
 // gamma = r.u, delta = w.u and max |r|/(1+|x|) (the single reduction of the Chronopoulos-Gear
 // form of preconditioned CG).
 template <int LANES>
-__device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, int n, Acc& a) {
+__device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, int n, float2* rowsum, Acc& a) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -1187,47 +1194,55 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
         }
 #pragma unroll
         for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
-        if (sl == 0 && r >= 0) {
-            const double w = df_value(acc), ui = u[r], ri = rr_v[r];
-            q_out[r] = w;
-            a.a = fma(ri, ui, a.a);
-            a.obj = fma(w, ui, a.obj);
-            a.b = umax64(a.b, cg_ratio_bits(ri, xp[r]));
-        }
+        if (sl == 0 && r >= 0) rowsum[j] = acc;
+    }
+    // the FP64 epilogue, one free row per thread on full warps
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += kBlock) {
+        const int r = list[t];
+        const double w = df_value(rowsum[t]), ui = u[r], ri = rr_v[r];
+        q_out[r] = w;
+        a.a = fma(ri, ui, a.a);
+        a.obj = fma(w, ui, a.obj);
+        a.b = umax64(a.b, cg_ratio_bits(ri, xp[r]));
     }
 }
 
 template <int LANES>
-__device__ void residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, Acc& a) {
-    __shared__ int32_t start_of[kTileRows];
+__device__ void residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, int32_t* start_of,
+                              float2* rowsum, Acc& a) {
     count_kept<LANES>(I, list, n_free, start_of);
     __syncthreads();
     block_exclusive_scan(start_of, n_free);
-    residual_rows<LANES>(I, list, n_free, base, start_of, a);
+    residual_rows<LANES>(I, list, n_free, base, start_of, rowsum, a);
 }
 
 // Residual (with the packing of Q_FF) or CG product over tile rows [rb, ...) of one instance.
 template <bool RESIDUAL>
 __device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
+    // one copy per kernel, shared by every lane count: free-list positions of the packed rows
+    // (residual) and row sums handed to the FP64 epilogue
+    __shared__ int32_t start_of[RESIDUAL ? kTileRows : 1];
+    __shared__ float2 rowsum[kTileRows];
     const int32_t* list = I.free_rows + rb;
     if constexpr (RESIDUAL) {
         const int base = __ldg(I.rowptr + rb);
         switch (I.lanes_res) {
-        case 1: residual_tile<1>(I, list, n_free, base, a); break;
-        case 2: residual_tile<2>(I, list, n_free, base, a); break;
-        case 4: residual_tile<4>(I, list, n_free, base, a); break;
-        case 8: residual_tile<8>(I, list, n_free, base, a); break;
-        case 16: residual_tile<16>(I, list, n_free, base, a); break;
-        default: residual_tile<32>(I, list, n_free, base, a); break;
+        case 1: residual_tile<1>(I, list, n_free, base, start_of, rowsum, a); break;
+        case 2: residual_tile<2>(I, list, n_free, base, start_of, rowsum, a); break;
+        case 4: residual_tile<4>(I, list, n_free, base, start_of, rowsum, a); break;
+        case 8: residual_tile<8>(I, list, n_free, base, start_of, rowsum, a); break;
+        case 16: residual_tile<16>(I, list, n_free, base, start_of, rowsum, a); break;
+        default: residual_tile<32>(I, list, n_free, base, start_of, rowsum, a); break;
         }
     } else {
         switch (I.lanes_cg) {
-        case 1: matvec_rows<1>(I, list, n_free, a); break;
-        case 2: matvec_rows<2>(I, list, n_free, a); break;
-        case 4: matvec_rows<4>(I, list, n_free, a); break;
-        case 8: matvec_rows<8>(I, list, n_free, a); break;
-        case 16: matvec_rows<16>(I, list, n_free, a); break;
-        default: matvec_rows<32>(I, list, n_free, a); break;
+        case 1: matvec_rows<1>(I, list, n_free, rowsum, a); break;
+        case 2: matvec_rows<2>(I, list, n_free, rowsum, a); break;
+        case 4: matvec_rows<4>(I, list, n_free, rowsum, a); break;
+        case 8: matvec_rows<8>(I, list, n_free, rowsum, a); break;
+        case 16: matvec_rows<16>(I, list, n_free, rowsum, a); break;
+        default: matvec_rows<32>(I, list, n_free, rowsum, a); break;
         }
     }
 }
