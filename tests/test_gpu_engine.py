@@ -294,3 +294,43 @@ def test_borrowed_submission_and_fetch_paths_agree(engine, preset, n, seed, prec
         assert np.array_equal(x, xs) and st.iterations == ss.iterations and st.objective == ss.objective
     with pytest.raises(ValueError):
         engine.fetch(i_copy, inst['n'], out=np.empty(inst['n'], np.float32))
+
+
+@pytest.mark.parametrize('precision', ['mixed', 'fp64'])
+def test_every_spmv_structure_solves(engine, precision):
+    """Each step-kernel group (precision x SpMV structure, forced through kernel_variant) solves
+    the same instance to a verified optimum with the same objective."""
+    inst = boxqp.planted('graph10k', seed=31, n=3000)
+    a = (inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'])
+    objs = []
+    for variant in (0, 64, 1, 2, 4, 8, 16, 32):
+        o = boxqp.options_struct(1e-7, 60.0, 200000, precision, kernel_variant=variant)
+        x, st = engine.solve(*a, o)
+        assert boxqp.STATUS_NAMES[st.status] == 'optimal', (variant, st.as_dict())
+        objs.append(st.objective)
+    assert max(objs) - min(objs) <= 1e-9 * max(1.0, abs(objs[0]))
+
+
+def test_mixed_precisions_and_structures_in_one_batch_equal_solo(engine):
+    """A batch holding FP64, FP64_EXACT and mixed solves of several SpMV structures at once (one
+    step launch per group, the exact engine's own kernel) gives each solve the bits it gets alone."""
+    cases = []
+    for k, (preset, n, prec, variant) in enumerate([('graph10k', 2000, 'mixed', -1), ('grid', 64 * 64, 'mixed', -1),
+                                                    ('graph10k', 2500, 'fp64', -1), ('tridiagonal', 3000, 'fp64', 2),
+                                                    ('graph10k', 1500, 'fp64_exact', -1), ('graph10k', 1800, 'mixed', 8),
+                                                    ('grid', 48 * 48, 'fp64', 64), ('graph10k', 2200, 'mixed', 0)]):
+        inst = boxqp.planted(preset, seed=40 + k, n=n)
+        o = boxqp.options_struct(1e-7, 60.0, 200000, prec, kernel_variant=variant)
+        cases.append((inst, o))
+    solo = []
+    for inst, o in cases:
+        x, st = engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+        assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+        solo.append((x, st.iterations, st.objective))
+    ids = [engine.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+           for inst, o in cases]
+    for (inst, _), ident, (xs, its, obj) in zip(cases, ids, solo):
+        assert engine.wait(ident, 120.0)
+        x, st = engine.fetch(ident, inst['n'])
+        engine.release(ident)
+        assert np.array_equal(x, xs) and st.iterations == its and st.objective == obj
