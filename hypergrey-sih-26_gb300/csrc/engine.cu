@@ -205,6 +205,18 @@ struct Job {
     int error = BQP_OK;
     std::string error_text;
     bqp_stats stats{};
+    // upload in progress (engine thread): host -> device copies still to issue, then the
+    // admission kernels; tmp holds the FP64 values of a mixed solve, power the Lanczos scratch
+    struct Piece {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    };
+    std::vector<Piece> pieces;
+    size_t piece = 0, piece_off = 0;
+    void* tmp = nullptr;
+    void* power = nullptr;
+    double t_upload = 0;
     std::vector<double> x;    // primal of a solve that holds no device memory (finished at submission)
     const void* x_dev = nullptr;  // primal of a finished resident solve, in its slab
     bool x_f32 = false;           // ... as FP32 (the mixed engine's unpolished iterate)
@@ -325,6 +337,11 @@ public:
 private:
     void loop();
     bool upload(Job& j, std::string& why);
+    bool upload_begin(Job& j, std::string& why);
+    bool upload_copy(Job& j, size_t budget);
+    bool upload_finish(Job& j, std::string& why);
+    void fail_admission(Job* j, size_t reserved, const std::string& why);  // caller holds mu_
+    void finish_paused_upload(std::unique_lock<std::mutex>& lk);
     static void CUDART_CB on_launch_done(void* self) {
         Engine* e = static_cast<Engine*>(self);
         {
@@ -335,6 +352,7 @@ private:
     }
     // a new solve at the head of the queue that fits under the cap (caller holds mu_)
     bool uploadable_head() const {
+        if (uploading_) return true;
         if (queue_.empty() || queue_.front()->resolve) return false;
         const Job* j = queue_.front();
         return resident_bytes_ + make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total <= cap_;
@@ -405,6 +423,8 @@ private:
     std::mutex fmu_;
     cudaEvent_t uev_ = nullptr;        // end of the latest upload on ustream_
     std::vector<Job*> uploaded_;       // uploaded, not yet installed (engine thread only)
+    Job* uploading_ = nullptr;         // upload paused when a launch ended (engine thread, mu_)
+    static constexpr size_t kUploadChunk = size_t(32) << 20;  // bytes issued between launch tests
     bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
     cudaMemPool_t pool_ = nullptr;
 
@@ -1090,8 +1110,18 @@ void Engine::update_steps() {
 
 // Uploads one new solve on the upload stream (inputs, slab, device-side forms), without touching
 // the tables the running graph reads; install() makes it part of the batch.  Engine thread only.
+// Upload of one new solve on ustream_, in three steps so that the engine thread can pause it when
+// the running launch ends: upload_begin (slab, record, the list of copies), upload_copy (issues
+// copies up to a byte budget; pageable copies are staged by this thread), upload_finish
+// (admission kernels, the upload event).
 bool Engine::upload(Job& j, std::string& why) {
-    const double t0 = host_seconds();
+    if (!upload_begin(j, why)) return false;
+    upload_copy(j, static_cast<size_t>(-1));
+    return upload_finish(j, why);
+}
+
+bool Engine::upload_begin(Job& j, std::string& why) {
+    j.t_upload = host_seconds();
     const int prec = j.opt.precision;
     j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
     void* slab = nullptr;
@@ -1100,11 +1130,13 @@ bool Engine::upload(Job& j, std::string& why) {
     j.resident = true;
     const Layout& L = j.layout;
     const size_t N = static_cast<size_t>(j.n), Z = static_cast<size_t>(j.nnz);
-    cudaMemcpyAsync(at<int32_t>(slab, L.rowptr), j.rowptr, (N + 1) * 4, cudaMemcpyHostToDevice, ustream_);
-    if (Z) cudaMemcpyAsync(at<int32_t>(slab, L.col), j.col, Z * 4, cudaMemcpyHostToDevice, ustream_);
-    cudaMemcpyAsync(at<double>(slab, L.c), j.c, N * 8, cudaMemcpyHostToDevice, ustream_);
-    cudaMemcpyAsync(at<double>(slab, L.l), j.l, N * 8, cudaMemcpyHostToDevice, ustream_);
-    cudaMemcpyAsync(at<double>(slab, L.u), j.u, N * 8, cudaMemcpyHostToDevice, ustream_);
+    j.pieces.clear();
+    j.piece = j.piece_off = 0;
+    j.pieces.push_back({at<int32_t>(slab, L.rowptr), j.rowptr, (N + 1) * 4});
+    if (Z) j.pieces.push_back({at<int32_t>(slab, L.col), j.col, Z * 4});
+    j.pieces.push_back({at<double>(slab, L.c), j.c, N * 8});
+    j.pieces.push_back({at<double>(slab, L.l), j.l, N * 8});
+    j.pieces.push_back({at<double>(slab, L.u), j.u, N * 8});
     InstDev& R = j.rec;
     std::memset(&R, 0, sizeof(R));
     R.rowptr = at<int32_t>(slab, L.rowptr);
@@ -1172,34 +1204,64 @@ bool Engine::upload(Job& j, std::string& why) {
     // runs are long, and an early polish costs more CG iterations than the FISTA steps it saves)
     R.step_switch = j.nnz >= 4 * j.n ? 3.0 * j.opt.polish_switch : 0.0;
     R.lip_device = j.opt.lipschitz == BQP_LIPSCHITZ_POWER ? 1 : 0;
-    void* power = nullptr;
+    j.power = nullptr;
+    j.tmp = nullptr;
     if (R.lip_device &&
-        !cuda_ok(cudaMallocFromPoolAsync(&power, power_scratch_bytes(j.n), pool_, ustream_), why, "allocate power scratch"))
+        !cuda_ok(cudaMallocFromPoolAsync(&j.power, power_scratch_bytes(j.n), pool_, ustream_), why, "allocate power scratch"))
         return false;
     if (prec == PREC_MIXED) {
-        void* tmp = nullptr;
-        if (!cuda_ok(cudaMallocFromPoolAsync(&tmp, Z * 8 + 64, pool_, ustream_), why, "allocate upload buffer")) return false;
-        if (Z) cudaMemcpyAsync(tmp, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
-        launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(tmp), ustream_);
-        launch_precondition(R, j.n, static_cast<const double*>(tmp), j.opt.scaling != 2, power, ustream_);
-        cudaFreeAsync(tmp, ustream_);
+        // FP64 values only for the admission kernels (hi/lo split, diagonal, preconditioner)
+        if (!cuda_ok(cudaMallocFromPoolAsync(&j.tmp, Z * 8 + 64, pool_, ustream_), why, "allocate upload buffer")) return false;
+        if (Z) j.pieces.push_back({j.tmp, j.val, Z * 8});
+    } else if (Z) {
+        j.pieces.push_back({at<double>(slab, L.val64), j.val, Z * 8});
+    }
+    return true;
+}
+
+// Issues copies of up to `budget` bytes; true once every copy of the solve is issued.
+bool Engine::upload_copy(Job& j, size_t budget) {
+    while (j.piece < j.pieces.size() && budget > 0) {
+        const Job::Piece& p = j.pieces[j.piece];
+        const size_t take = std::min(budget, p.bytes - j.piece_off);
+        cudaMemcpyAsync(static_cast<char*>(p.dst) + j.piece_off, static_cast<const char*>(p.src) + j.piece_off, take,
+                        cudaMemcpyHostToDevice, ustream_);
+        budget -= take;
+        j.piece_off += take;
+        if (j.piece_off == p.bytes) {
+            ++j.piece;
+            j.piece_off = 0;
+        }
+    }
+    return j.piece == j.pieces.size();
+}
+
+bool Engine::upload_finish(Job& j, std::string& why) {
+    InstDev& R = j.rec;
+    const int prec = j.opt.precision;
+    if (prec == PREC_MIXED) {
+        launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(j.tmp), ustream_);
+        launch_precondition(R, j.n, static_cast<const double*>(j.tmp), j.opt.scaling != 2, j.power, ustream_);
+        cudaFreeAsync(j.tmp, ustream_);
     } else {
-        double* val = at<double>(slab, L.val64);
-        if (Z) cudaMemcpyAsync(val, j.val, Z * 8, cudaMemcpyHostToDevice, ustream_);
+        const double* val = R.val64;
         launch_prepare_instance(R, j.n, j.nnz, val, ustream_);
         if (R.lip_device) {
             cudaMemcpyAsync(R.lprec, &R.L, sizeof(double), cudaMemcpyHostToDevice, ustream_);
-            launch_power_lipschitz(R, j.n, val, false, power, ustream_);
+            launch_power_lipschitz(R, j.n, val, false, j.power, ustream_);
         }
     }
-    if (power) cudaFreeAsync(power, ustream_);
+    if (j.power) cudaFreeAsync(j.power, ustream_);
+    j.tmp = nullptr;
+    j.power = nullptr;
+    std::vector<Job::Piece>().swap(j.pieces);
     if (!cuda_ok(cudaGetLastError(), why, "admission kernels")) return false;
     cudaEventRecord(uev_, ustream_);
     if (host_profile()) {
         const double t1 = host_seconds();
         cudaStreamSynchronize(ustream_);
         std::fprintf(stderr, "[boxqp] upload n=%lld: enqueue %.3f ms, device done %.3f ms\n", static_cast<long long>(j.n),
-                     1e3 * (t1 - t0), 1e3 * (host_seconds() - t0));
+                     1e3 * (t1 - j.t_upload), 1e3 * (host_seconds() - j.t_upload));
     }
     return true;
 }
@@ -1232,34 +1294,79 @@ bool Engine::install(std::vector<Job*>& jobs, std::string& why) {
     return true;
 }
 
-// While a graph runs: uploads the new solves at the head of the queue that fit under the cap.
+// While a graph runs: uploads the new solves at the head of the queue that fit under the cap, in
+// chunks of kUploadChunk bytes; when the launch ends, an upload in progress pauses (uploading_)
+// so that the next launch is not held up by the host staging of a large solve.
 void Engine::upload_waiting() {
     std::unique_lock<std::mutex> lk(mu_);
-    while (!queue_.empty() && !stop_) {
-        Job* j = queue_.front();
-        if (j->resolve) break;
-        const size_t need = make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
-        if (resident_bytes_ + need > cap_) break;
-        queue_.pop_front();
-        j->state = JOB_ADMITTING;
-        resident_bytes_ += need;
+    while (!stop_ && !launch_done_) {
+        Job* j = uploading_;
+        if (!j) {
+            if (queue_.empty()) break;
+            j = queue_.front();
+            if (j->resolve) break;
+            const size_t need = make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
+            if (resident_bytes_ + need > cap_) break;
+            queue_.pop_front();
+            j->state = JOB_ADMITTING;
+            resident_bytes_ += need;
+            lk.unlock();
+            std::string why;
+            const bool ok = upload_begin(*j, why);
+            lk.lock();
+            if (!ok) {
+                fail_admission(j, need, why);
+                continue;
+            }
+            uploading_ = j;
+        }
         lk.unlock();
         std::string why;
-        const bool ok = upload(*j, why);
-        free_inputs(*j);
+        const bool copied = upload_copy(*j, kUploadChunk);
+        bool ok = true;
+        if (copied) {
+            ok = upload_finish(*j, why);
+            free_inputs(*j);
+        }
         lk.lock();
-        if (ok) {
-            uploaded_.push_back(j);
-        } else {
-            resident_bytes_ -= need;
-            j->error = BQP_ERR_CUDA;
-            j->error_text = why;
-            j->state = JOB_DONE;
-            if (j->notify) completed_.push_back(j->id);
-            set_error(why);
-            cv_done_.notify_all();
+        if (copied) {
+            uploading_ = nullptr;
+            if (ok) uploaded_.push_back(j);
+            else fail_admission(j, j->layout.total, why);
         }
     }
+}
+
+// Completes a paused upload (no launch running); caller holds mu_ through lk.
+void Engine::finish_paused_upload(std::unique_lock<std::mutex>& lk) {
+    Job* j = uploading_;
+    if (!j) return;
+    lk.unlock();
+    std::string why;
+    upload_copy(*j, static_cast<size_t>(-1));
+    const bool ok = upload_finish(*j, why);
+    free_inputs(*j);
+    lk.lock();
+    uploading_ = nullptr;
+    if (ok) uploaded_.push_back(j);
+    else fail_admission(j, j->layout.total, why);
+}
+
+// A solve whose admission failed: its reserved bytes and any slab go back, it finishes with the
+// CUDA error.  Caller holds mu_.
+void Engine::fail_admission(Job* j, size_t reserved, const std::string& why) {
+    resident_bytes_ -= reserved;
+    if (j->resident) {
+        pending_free_.emplace_back(-1, j->slab);
+        j->slab = nullptr;
+        j->resident = false;
+    }
+    j->error = BQP_ERR_CUDA;
+    j->error_text = why;
+    j->state = JOB_DONE;
+    if (j->notify) completed_.push_back(j->id);
+    set_error(why);
+    cv_done_.notify_all();
 }
 
 void Engine::process_frees() {
@@ -1507,6 +1614,9 @@ void Engine::loop() {
     std::unique_lock<std::mutex> lk(mu_);
     while (!stop_) {
         if (!pending_free_.empty()) process_frees();
+        // an upload paused when the last launch ended continues during the next launch; only
+        // when there is nothing else to run is it completed here
+        if (uploading_ && n_running_ == 0 && uploaded_.empty()) finish_paused_upload(lk);
         // admission: FIFO while the head fits under the cap; consecutive re-arms of resident
         // solves go together in one upload and one kernel
         bool admitted = false;
@@ -1542,6 +1652,7 @@ void Engine::loop() {
                 admitted = true;
                 continue;
             }
+            if (uploading_) break;  // FIFO: the paused upload goes first
             const size_t need = make_layout(j->n, j->nnz, static_cast<int64_t>(j->tiles.size()), j->opt.precision).total;
             if (resident_bytes_ + need > cap_) {
                 if (n_running_ == 0 && uploaded_.empty()) {
@@ -1563,17 +1674,8 @@ void Engine::loop() {
             const bool ok = upload(*j, why);
             free_inputs(*j);
             lk.lock();
-            if (ok) {
-                uploaded_.push_back(j);
-            } else {
-                resident_bytes_ -= need;
-                j->error = BQP_ERR_CUDA;
-                j->error_text = why;
-                j->state = JOB_DONE;
-                if (j->notify) completed_.push_back(j->id);
-                set_error(why);
-                cv_done_.notify_all();
-            }
+            if (ok) uploaded_.push_back(j);
+            else fail_admission(j, need, why);
         }
         // install what was uploaded here and during the previous launch
         if (!uploaded_.empty()) {
