@@ -347,6 +347,7 @@ private:
         {
             std::lock_guard<std::mutex> g(e->mu_);
             e->launch_done_ = true;
+            e->t_launch_done_ = host_seconds();
         }
         e->cv_work_.notify_all();
     }
@@ -426,6 +427,7 @@ private:
     Job* uploading_ = nullptr;         // upload paused when a launch ended (engine thread, mu_)
     static constexpr size_t kUploadChunk = size_t(32) << 20;  // bytes issued between launch tests
     bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
+    double t_launch_done_ = 0;         // host time of that callback (BOXQP_PROFILE: gap to the next launch)
     cudaMemPool_t pool_ = nullptr;
 
     // device tables
@@ -1452,6 +1454,11 @@ bool Engine::run_once(std::string& why) {
         cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
     } else if (!cuda_ok(cudaGraphLaunch(exec_, stream_), why, "graph launch")) {
         return false;
+    }
+    if (host_profile()) {
+        std::lock_guard<std::mutex> g(mu_);
+        std::fprintf(stderr, "[boxqp] launch: %d solves running, %.3f ms since the previous launch ended\n", n_running_,
+                     1e3 * (t0 - t_launch_done_));
     }
     cudaEventRecord(ev1_, stream_);
     cudaMemcpyAsync(h_status_, d_status_, sizeof(int32_t) * std::max(n_inst_, 1), cudaMemcpyDeviceToHost, stream_);
