@@ -2,9 +2,10 @@
 // the tile table, the captured conditional CUDA graph and the engine thread.
 //
 // The graph is one WHILE loop whose body is
-//     check -> gate -> IF(fp64) 25 x step -> IF(mixed) 25 x step -> IF(exact) 25 x step
-//           -> IF(polish) [polish_init, polish_residual, 25 x (cg_matvec, cg_update, cg_direction)]
-//           -> control
+//     check -> gate -> IF(fp64) K x (step per fp64 group) -> IF(mixed) K x (step per mixed group)
+//           -> IF(exact) K x step -> IF(polish) [polish_init, polish_residual,
+//              WHILE(an instance iterates, <= 25 per body) (cg_matvec, cg_vector)] -> control
+// (K: the shortest check interval among the running solves; a group: one SpMV structure).
 // The check kernel's per-instance finalizers decide each instance's next phase, the gate kernel
 // arms the IF nodes for the phases present, and the control kernel ends the loop when no
 // instance is running or after `body_cap` bodies (so the engine thread can admit new solves

@@ -13,8 +13,11 @@
 //   polish_*/cg_* FP64 conjugate gradient on the free set Q_FF x_F = -c_F - Q_FA x_A (mixed).
 //
 // Memory-bound design: SpMV streams values/columns once per iteration with read-only loads;
-// rows are processed by sub-warps of LANES lanes (chosen per instance from its row lengths);
-// FP64 arithmetic is kept out of the FP32 iterations (GB300's FP64 rate is ~1/64 of FP32).
+// rows are processed by the SpMV structure the tuning table picks per instance (block- or
+// warp-staged, or sub-warps of LANES lanes), one step kernel per (precision, structure);
+// FP64 arithmetic is kept out of the FP32 iterations (GB300's FP64 rate is ~1/64 of FP32), and
+// FP64 epilogues and reductions run on full warps (an FP64 warp instruction costs the same
+// whatever its active lanes).
 #include "kernels.cuh"
 
 #include <atomic>
