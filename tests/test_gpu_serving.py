@@ -45,3 +45,31 @@ def test_staggered_requests_overlap_and_match_solo_runs():
         assert chk['verified'] == 1.0
         # objective within 1e-7 relative at tight tolerances, within the tolerance at loose ones
         assert abs(chk['objective'] - inst['fstar']) <= max(1e-7, tol) * (1 + abs(inst['fstar']))
+
+
+def test_uploads_paused_by_a_finishing_launch_resume_exactly():
+    """Large solves submitted while a long launch runs upload in chunks; when the launch ends an
+    upload in progress pauses and resumes during the next launch.  Every result equals its solo
+    run bit for bit."""
+    eng = boxqp.Engine(0)
+    try:
+        long_inst = boxqp.planted('graph1m', seed=5, n=200000)
+        big = [boxqp.planted('graph1m', seed=6 + k, n=300000) for k in range(3)]
+        o_long = boxqp.options_struct(1e-9, 60.0, 200000, 'fp64')
+        o_big = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+        args = lambda i: (i['rowptr'], i['col'], i['val'], i['c'], i['lower'], i['upper'])
+        solo = [eng.solve(*args(i), o_big) for i in big]
+        ids = [eng.submit(*args(long_inst), o_long)]
+        ids += [eng.submit(*args(i), o_big, copy=(k % 2 == 0)) for k, i in enumerate(big)]
+        for ident in ids:
+            assert eng.wait(ident, 120.0)
+        for ident, inst, (xs, ss) in zip(ids[1:], big, solo):
+            x, st = eng.fetch(ident, inst['n'])
+            assert boxqp.STATUS_NAMES[st.status] == 'optimal'
+            assert np.array_equal(x, xs) and st.iterations == ss.iterations and st.objective == ss.objective
+        _, st_long = eng.fetch(ids[0], long_inst['n'])
+        assert boxqp.STATUS_NAMES[st_long.status] == 'optimal'
+        for ident in ids:
+            eng.release(ident)
+    finally:
+        eng.close()
