@@ -153,7 +153,9 @@ __device__ __forceinline__ Acc shfl_check(const Acc& x, int o, bool gate) {
     r.flags = shfl_xor(x.flags, o);
     return r;
 }
-__device__ Acc block_reduce_check(Acc v, bool gate) {
+// publishing = true: the caller passes the result to publish_and_test_last, whose barrier orders
+// warp 0's reads of warp_part before the next call's writes; the trailing barrier is skipped.
+__device__ Acc block_reduce_check(Acc v, bool gate, bool publishing = false) {
     __shared__ Acc warp_part[kBlock / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = combine_check(v, shfl_check(v, o, gate), gate);
@@ -166,7 +168,7 @@ __device__ Acc block_reduce_check(Acc v, bool gate) {
         for (int o = (kBlock / 64); o > 0; o >>= 1) w = combine_check(w, shfl_check(w, o, gate), gate);
         v = w;
     }
-    __syncthreads();
+    if (!publishing) __syncthreads();
     return v;
 }
 
@@ -226,7 +228,8 @@ __device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
 // its active lanes, so this takes 13 FP64 additions per field instead of one per tree level in
 // every warp (a lanes-strided layout leaves zeros in the other lanes; adding them is exact).
 // `lanes` is kept for the callers' layouts; the maximum reduces over all lanes.
-__device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true) {
+// publishing = true: as for block_reduce_check, the barrier of publish_and_test_last follows.
+__device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true, bool publishing = false) {
     (void)lanes;
     __shared__ double part_a[kBlock];
     __shared__ double part_o[kBlock];
@@ -261,7 +264,7 @@ __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true) {
         v.obj = ob;
         v.b = b;
     }
-    __syncthreads();
+    if (!publishing) __syncthreads();
     return v;
 }
 
@@ -924,7 +927,7 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
         if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a);
         else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, T.variant, T.row_begin, T.row_end, a);
         else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a);
-        Acc total = block_reduce_check(a, s.gate != 0);
+        Acc total = block_reduce_check(a, s.gate != 0, true);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance(v, R.x, R.y, s.gate != 0);
@@ -1259,7 +1262,7 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         polish_rows<true>(I, T.row_begin, I.free_cnt[t - R.x], a);
-        Acc total = block_reduce_ab(a, I.lanes_res);
+        Acc total = block_reduce_ab(a, I.lanes_res, true, true);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
@@ -1283,7 +1286,7 @@ __global__ void __launch_bounds__(kBlock, 5) cg_matvec_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         polish_rows<false>(I, T.row_begin, I.free_cnt[t - R.x], a);
-        Acc total = block_reduce_ab(a, I.lanes_cg);
+        Acc total = block_reduce_ab(a, I.lanes_cg, true, true);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
