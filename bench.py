@@ -566,6 +566,86 @@ def run_serve(args, world, rank, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_admm(args, world, rank, local, pg):
+    """The constrained-QP ADMM inner solve (K = H + sigma I + A' diag(rho) A, Jacobi PCG as
+    qp_admm.cpp:262-273) on a 1M-variable system: H the random-graph Hessian (15M nonzeros), A
+    500k rows of 8 entries.  A step is one inner solve from x = 0 to the reference's first-
+    iteration accuracy 1e-7 (1 + max|rhs|), through bqp_admm_solve (host rhs and x copied in and
+    out every step); value = CG iterations per second."""
+    import numpy as np
+    import boxqp
+    from boxqp.admm import AdmmSystem
+    n, m, per_row = 1000000, 500000, 8
+    inst = boxqp.planted('graph1m', seed=1 + rank)
+    rng = np.random.default_rng(11 + rank)
+    cols = np.sort(rng.integers(0, n, size=(m, per_row)), axis=1)
+    a_rowptr = (np.arange(m + 1) * per_row).astype(np.int32)
+    a_col = cols.reshape(-1).astype(np.int32)
+    a_val = rng.normal(size=m * per_row)
+    rho = np.where(rng.random(m) < 0.1, 10.0, 0.1)
+    sigma = 1e-8
+    rhs = rng.normal(size=n)
+    accuracy = 1e-7 * (1.0 + np.max(np.abs(rhs)))
+    max_inner = min(4000, 2 * n + 20)
+    sysm = AdmmSystem(inst['rowptr'], inst['col'], inst['val'], a_rowptr, a_col, a_val, n, device=local)
+    sysm.set_rho(rho, sigma)
+    x0 = np.zeros(n)
+    for _ in range(args.warmup):
+        sysm.solve(rhs, x0, accuracy, max_inner)
+    barrier(pg)
+    inner_total, resid = 0, 0.0
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            x, inner, resid = sysm.solve(rhs, x0, accuracy, max_inner)
+            inner_total += inner
+        wall = allreduce_max(pg, time.perf_counter() - t0)
+    nnz_h, nnz_a = int(inst['rowptr'][-1]), m * per_row
+    # per CG iteration: H, A and A' (values + columns), rho and t, and eight n-vectors read or written
+    it_bytes = 12.0 * nnz_h + 2 * 12.0 * nnz_a + 4.0 * (2 * n + m + 2) + 16.0 * m + 8.0 * 8 * n
+    ms_per_it = 1e3 * wall / max(inner_total, 1)
+    peak, kind = load_peaks()
+    cpu = None
+    if rank == 0 and world == 1 and not args.quick:
+        # the CPU restatement (pure-Python loops) on a 2,000-variable sample of the same recipe
+        from oracle.admm_pcg import AdmmSystemOracle
+        sn, sm = 2000, 1000
+        small = boxqp.planted('graph10k', seed=3, n=sn)
+        srng = np.random.default_rng(5)
+        scols = np.sort(srng.choice(sn, size=(sm, per_row)), axis=1)
+        sa = ((np.arange(sm + 1) * per_row).astype(np.int32), scols.reshape(-1).astype(np.int32),
+              srng.normal(size=sm * per_row))
+        o = AdmmSystemOracle((small['rowptr'], small['col'], small['val']), sa, sn)
+        o.set_rho(np.where(srng.random(sm) < 0.1, 10.0, 0.1), sigma)
+        srhs = srng.normal(size=sn)
+        t1 = time.perf_counter()
+        _, sinner, _ = o.solve(srhs, np.zeros(sn), 1e-7 * (1 + np.max(np.abs(srhs))), 30)
+        cdt = time.perf_counter() - t1
+        cpu = {'value': sinner / cdt, 'unit': 'CG iterations/s', 'cores': 1, 'kind': 'port',
+               'sample': f'{sinner} inner iterations of the CPU restatement on a {sn}-variable, {sm}-row system'}
+    if rank == 0:
+        out = {'metric': 'ADMM inner-solve CG iterations/s (K = H + sigma I + A\' diag(rho) A)',
+               'value': allreduce_sum(pg, inner_total) / wall, 'unit': 'CG iterations/s', 'n_gpus': world,
+               'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * wall / args.steps,
+               'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+               'data': 'synthetic',
+               'config': {'workload': f'ADMM x-update system: H random-graph Hessian n={n} ({nnz_h} nonzeros), '
+                                      f'A {m} rows x {per_row} entries, sigma 1e-8, rho 0.1 (10 on 10 % of rows)',
+                          'accuracy': accuracy, 'max_inner': max_inner, 'parallelism': f'replicas x{world}',
+                          'l2': 'inputs larger than L2: one iteration streams ~330 MB'},
+               'inner_per_step': inner_total / args.steps, 'final_max_residual': resid,
+               'roofline': {'bound': 'hbm', 'achieved': it_bytes / (ms_per_it * 1e-3) / 1e9, 'peak': peak,
+                            'unit': 'GB/s', 'frac': it_bytes / (ms_per_it * 1e-3) / 1e9 / peak, 'traffic': None,
+                            'peak_kind': kind, 'scope': 'one CG iteration (4 kernels), algorithmic bytes / wall time'},
+               'cpu_baseline': cpu,
+               'e2e': {'value': allreduce_sum(pg, inner_total) / wall, 'unit': 'CG iterations/s',
+                       'h2d_bytes_per_step': 16 * n, 'd2h_bytes_per_step': 8 * n,
+                       'api': 'bqp_admm_solve (rhs and x from host memory, x back)'},
+               'gpu_launches': int(inner_total * 4 + args.steps * 2), 'clocks': clocks.summary()}
+        print(json.dumps(out))
+    sysm.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -574,7 +654,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
     ap.add_argument('--workload', default='graph1m',
-                    choices=['graph1m', 'grid', 'graph10k', 'tridiagonal', 'batch', 'serve'])
+                    choices=['graph1m', 'grid', 'graph10k', 'tridiagonal', 'batch', 'serve', 'admm'])
     ap.add_argument('--instances', type=int, default=4096, help='batch: number of instances')
     ap.add_argument('--fp64-stride', type=int, default=1, help='batch: FP64 single-solve loop over every k-th')
     ap.add_argument('--cpu-stride', type=int, default=32, help='batch: CPU baseline over every k-th instance')
@@ -588,14 +668,20 @@ def main():
     if args.tol is None:
         args.tol = 1e-7 if args.workload == 'tridiagonal' else 1e-6
     if args.steps is None:
-        args.steps = 3 if args.workload == 'batch' else (10 if args.impl == 'reference' else 100)
+        args.steps = 3 if args.workload in ('batch', 'admm') else (10 if args.impl == 'reference' else 100)
     world, rank, local, pg = dist_setup(args)
-    if args.impl == 'reference':
+    if args.impl == 'reference' and args.workload == 'admm':
+        if rank == 0:
+            print(json.dumps({'impl': 'reference', 'unavailable': 'the reference runs this inner solve only inside '
+                              'its ADMM loop (qp_admm.cpp:262-273); the CPU restatement is timed as cpu_baseline'}))
+    elif args.impl == 'reference':
         run_reference(args, world, rank, pg)
     elif args.workload == 'batch':
         run_batch(args, world, rank, local, pg)
     elif args.workload == 'serve':
         run_serve(args, world, rank, local, pg)
+    elif args.workload == 'admm':
+        run_admm(args, world, rank, local, pg)
     else:
         run_ours(args, world, rank, local, pg)
     if pg:

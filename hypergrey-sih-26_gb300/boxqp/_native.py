@@ -79,6 +79,12 @@ PROTOTYPES = {
     'bqp_box_step': (c_int, [c_void_p, c_double]),
     'bqp_box_primal': (c_int, [c_void_p, _F64P]),
     'bqp_box_destroy': (None, [c_void_p]),
+    'bqp_admm_create': (c_void_p, [c_int, c_int64, c_int64, _I32P, _I32P, _F64P, _I32P, _I32P, _F64P]),
+    'bqp_admm_set_rho': (c_int, [c_void_p, _F64P, c_double]),
+    'bqp_admm_apply': (c_int, [c_void_p, _F64P, _F64P]),
+    'bqp_admm_solve': (c_int, [c_void_p, _F64P, _F64P, c_double, c_int64, _I64P, _F64P]),
+    'bqp_admm_last_error': (c_char_p, []),
+    'bqp_admm_destroy': (None, [c_void_p]),
     'bqp_box_last_error': (c_char_p, [c_void_p]),
     'bqp_check_device': (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_double, c_double, c_int32, POINTER(Stats)]),

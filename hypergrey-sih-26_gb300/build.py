@@ -20,7 +20,7 @@ LIB = PKG / 'boxqp' / 'libboxqp.so'
 CUDA_HOME = Path(os.environ.get('CUDA_HOME', '/usr/local/cuda'))
 NVCC = str(CUDA_HOME / 'bin' / 'nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-CU_SOURCES = ['kernels.cu', 'engine.cu', 'box.cu']
+CU_SOURCES = ['kernels.cu', 'engine.cu', 'box.cu', 'admm.cu']
 CPP_SOURCES = ['planted.cpp', 'host.cpp']
 
 

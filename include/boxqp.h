@@ -180,6 +180,27 @@ int bqp_solve_sync(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, 
                    const double* val, const double* c, const double* lower, const double* upper,
                    const bqp_options* options, double* x, bqp_stats* stats);
 
+/* ---- constrained-QP ADMM inner solve -----------------------------------------------------
+ * The linear system of the reference's ADMM x-update (02-software/solver/src/qp_admm.cpp:157-161)
+ *     K x = rhs,  K = H + sigma I + A' diag(rho) A,
+ * H (n x n, full symmetric CSR) and A (m x n, CSR) resident on the device.  bqp_admm_set_rho
+ * stores rho (m entries, > 0) and sigma (>= 0) and forms the Jacobi preconditioner
+ * diag(H) + sigma + sum_i rho_i a_ij^2 (qp_admm.cpp:153-156); bqp_admm_solve runs the reference's
+ * preconditioned CG (qp_admm.cpp:262-273) from the caller's x until max|r| <= accuracy, after
+ * max_inner iterations, or when d'K d is not positive and finite; x is overwritten, and the
+ * iterations and the final max|r| are returned.  bqp_admm_apply: out = K v.  Host arrays of n
+ * doubles; one call at a time per system.  NULL / BQP_ERR_* on failure (bqp_admm_last_error). */
+typedef struct bqp_admm bqp_admm;
+bqp_admm*   bqp_admm_create(int device, int64_t n, int64_t m, const int32_t* h_rowptr, const int32_t* h_col,
+                            const double* h_val, const int32_t* a_rowptr, const int32_t* a_col,
+                            const double* a_val);
+int         bqp_admm_set_rho(bqp_admm* s, const double* rho, double sigma);
+int         bqp_admm_apply(bqp_admm* s, const double* v, double* out);
+int         bqp_admm_solve(bqp_admm* s, const double* rhs, double* x, double accuracy, int64_t max_inner,
+                           int64_t* inner_out, double* residual_out);
+const char* bqp_admm_last_error(void);
+void        bqp_admm_destroy(bqp_admm* s);
+
 /* ---- plugin level: the reference's BoxIteration contract ----------------------------------
  * Mirrors sovereign::make_cuda_box / BoxIteration::step / BoxIteration::primal
  * (02-software/solver/include/accelerated_qp.hpp:9-16, src/cuda_box.cu:22-37): the problem is

@@ -1,0 +1,52 @@
+"""The CPU restatement of the reference's ADMM inner solve (oracle/admm_pcg.py), without a GPU:
+its system matrix equals H + sigma I + A' diag(rho) A formed densely, and its CG reaches the
+requested residual."""
+import numpy as np
+
+from oracle.admm_pcg import AdmmSystemOracle
+
+
+def random_case(seed, n=60, m=40, density=0.1):
+    rng = np.random.default_rng(seed)
+    # H: a symmetric diagonally dominant graph Laplacian plus a diagonal
+    dense_h = np.zeros((n, n))
+    for _ in range(3 * n):
+        i, j = rng.integers(0, n, 2)
+        if i != j:
+            w = rng.uniform(0.1, 1.0)
+            dense_h[i, j] -= w
+            dense_h[j, i] -= w
+            dense_h[i, i] += w
+            dense_h[j, j] += w
+    dense_h += np.diag(rng.uniform(0.0, 1.0, n))
+    dense_a = np.where(rng.random((m, n)) < density, rng.normal(size=(m, n)), 0.0)
+
+    def csr(dense):
+        rowptr, col, val = [0], [], []
+        for row in dense:
+            nz = np.nonzero(row)[0]
+            col.extend(nz.tolist())
+            val.extend(row[nz].tolist())
+            rowptr.append(len(col))
+        return np.array(rowptr, np.int32), np.array(col, np.int32), np.array(val)
+
+    return dense_h, dense_a, csr(dense_h), csr(dense_a), rng
+
+
+def test_restated_system_and_cg():
+    dense_h, dense_a, h, a, rng = random_case(3)
+    n, m = dense_h.shape[0], dense_a.shape[0]
+    rho = np.where(rng.random(m) < 0.2, 10.0, 0.1)
+    sigma = 1e-8
+    o = AdmmSystemOracle(h, a, n)
+    o.set_rho(rho, sigma)
+    k = dense_h + sigma * np.eye(n) + dense_a.T @ np.diag(rho) @ dense_a
+    v = rng.normal(size=n)
+    assert np.allclose(o.apply(v), k @ v, rtol=1e-12, atol=1e-12)
+    assert np.allclose(o.precond, np.diag(k), rtol=1e-13, atol=0)
+    rhs = rng.normal(size=n)
+    x, inner, resid = o.solve(rhs, np.zeros(n), 1e-10, 2 * n + 20)
+    assert resid <= 1e-10 and 0 < inner <= 2 * n + 20
+    assert np.allclose(x, np.linalg.solve(k, rhs), rtol=1e-8, atol=1e-8)
+    x0, inner0, _ = o.solve(rhs, np.ones(n), 1e-10, 0)
+    assert inner0 == 0 and np.array_equal(x0, np.ones(n))

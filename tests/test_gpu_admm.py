@@ -1,0 +1,85 @@
+"""GPU ADMM inner solve (C-ABI bqp_admm_*) against the CPU restatement of the reference's
+inner CG (oracle/admm_pcg.py, qp_admm.cpp:153-161, 262-273).
+
+Tolerances: K v to 1e-12 relative (summation order differs); the CG solve to 1e-9 relative in x
+with the iteration count within max(1, 2 %) (the reference's long double dot products are not
+reproduced, and CG amplifies rounding over long runs); the final max|r| at or below the accuracy
+when the solve converged."""
+import numpy as np
+import pytest
+
+import boxqp
+from boxqp.admm import AdmmSystem
+from oracle.admm_pcg import AdmmSystemOracle
+
+pytestmark = pytest.mark.gpu
+
+
+def close_counts(a, b):
+    return abs(a - b) <= max(1, int(0.02 * b))
+
+
+def case(seed, n, m, per_row):
+    """H: a planted graph Hessian; A: m sparse rows of per_row normal entries (some equality-like
+    rows get rho x 100, as the reference's set-up does)."""
+    inst = boxqp.planted('graph10k', seed=seed, n=n)
+    rng = np.random.default_rng(seed)
+    rowptr, col, val = [0], [], []
+    for _ in range(m):
+        cols = np.sort(rng.choice(n, size=per_row, replace=False))
+        col.extend(cols.tolist())
+        val.extend(rng.normal(size=per_row).tolist())
+        rowptr.append(len(col))
+    a = (np.array(rowptr, np.int32), np.array(col, np.int32), np.array(val))
+    h = (inst['rowptr'], inst['col'], inst['val'])
+    rho = np.where(rng.random(m) < 0.1, 10.0, 0.1)
+    return h, a, rho, rng
+
+
+@pytest.mark.parametrize('seed,n,m,per_row', [(1, 400, 150, 6), (2, 2000, 900, 12)])
+def test_admm_inner_solve_matches_restatement(seed, n, m, per_row):
+    h, a, rho, rng = case(seed, n, m, per_row)
+    sigma = 1e-8
+    gpu = AdmmSystem(*h, *a, n)
+    ref = AdmmSystemOracle(h, a, n)
+    gpu.set_rho(rho, sigma)
+    ref.set_rho(rho, sigma)
+    v = rng.normal(size=n)
+    kv, kv_ref = gpu.apply(v), ref.apply(v)
+    assert np.max(np.abs(kv - kv_ref)) <= 1e-12 * np.max(np.abs(kv_ref))
+    rhs = rng.normal(size=n)
+    x0 = rng.normal(size=n) * 0.1
+    for accuracy in (1e-6, 1e-10):
+        x, inner, resid = gpu.solve(rhs, x0, accuracy, 2 * n + 20)
+        xr, inner_r, resid_r = ref.solve(rhs, x0, accuracy, 2 * n + 20)
+        assert close_counts(inner, inner_r), (inner, inner_r)
+        assert resid <= accuracy and resid_r <= accuracy
+        assert np.max(np.abs(x - xr)) <= 1e-9 * max(1.0, np.max(np.abs(xr))) + 10 * accuracy
+        # repeated solves are deterministic
+        x2, inner2, resid2 = gpu.solve(rhs, x0, accuracy, 2 * n + 20)
+        assert np.array_equal(x, x2) and inner2 == inner and resid2 == resid
+    # the iteration cap and max_inner = 0
+    x, inner, _ = gpu.solve(rhs, x0, 0.0, 3)
+    xr, inner_r, _ = ref.solve(rhs, x0, 0.0, 3)
+    assert inner == inner_r == 3 and np.max(np.abs(x - xr)) <= 1e-10 * max(1.0, np.max(np.abs(xr)))
+    x, inner, _ = gpu.solve(rhs, x0, 1e-6, 0)
+    assert inner == 0 and np.array_equal(x, x0)
+    # a new rho rebuilds the preconditioner and the system
+    rho2 = rho * 3.0
+    gpu.set_rho(rho2, 1e-6)
+    ref.set_rho(rho2, 1e-6)
+    x, inner, resid = gpu.solve(rhs, x0, 1e-8, 2 * n + 20)
+    xr, inner_r, _ = ref.solve(rhs, x0, 1e-8, 2 * n + 20)
+    assert close_counts(inner, inner_r) and resid <= 1e-8
+    gpu.close()
+
+
+def test_admm_rejects_bad_input():
+    h, a, rho, _ = case(3, 100, 20, 4)
+    bad_col = (a[0], np.where(a[1] == a[1][0], 100, a[1]).astype(np.int32), a[2])
+    with pytest.raises(ValueError):
+        AdmmSystem(*h, *bad_col, 100)
+    gpu = AdmmSystem(*h, *a, 100)
+    with pytest.raises(ValueError):
+        gpu.set_rho(np.zeros(20), 1e-8)
+    gpu.close()
