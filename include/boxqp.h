@@ -57,11 +57,12 @@ extern "C" {
 
 /* ---- step size ------------------------------------------------------------------------- */
 #define BQP_LIPSCHITZ_GERSHGORIN  0  /* L = max_i sum_k |Q_ik|, as src/accelerated_qp.cpp:25-26      */
-#define BQP_LIPSCHITZ_POWER       1  /* FP64 power-iteration estimate of lambda_max on the device at
-                                        admission (30 products from a fixed start): L = min(Gershgorin,
-                                        max(rho + |residual|, 1.02 rho)), rho the Rayleigh quotient.
-                                        An estimate, not a bound; of V Q V for the preconditioned
-                                        mixed steps.  stats.lipschitz reports it.                      */
+#define BQP_LIPSCHITZ_POWER       1  /* FP64 estimate of lambda_max on the device at admission: Lanczos
+                                        on the power iteration's Krylov space (32 steps from a fixed
+                                        start), L = min(Gershgorin, max(theta + residual, 1.001 theta)),
+                                        theta the largest Ritz value.  An estimate, not a bound; of
+                                        V Q V for the preconditioned mixed steps.  stats.lipschitz
+                                        reports it.                                                    */
 
 typedef struct bqp_ctx bqp_ctx;
 
