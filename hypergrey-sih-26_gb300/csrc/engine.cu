@@ -684,7 +684,7 @@ bool Engine::run_stream(int cap, std::string& why) {
     for (; bodies < cap; ++bodies) {
         if (profile_phases_) cudaEventRecord(pev_[0], stream_);
         launch_check(v, grid, stream_);
-        launch_gate_plain(v, stream_);
+        launch_gate_plain(v, K, stream_);
         kernels += 4;
         cudaMemcpyAsync(h_ctrl_, d_ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream_);
         if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine check")) return false;
@@ -794,7 +794,7 @@ bool Engine::build_graph(std::string& why) {
     cudaGraphNode_t last = nullptr;
     if (!capture(body, nullptr, 0, [&] {
             launch_check(v, grid, capture_);
-            launch_gate(v, h_f, h_pol, h_cg, body_launches(K), capture_);
+            launch_gate(v, h_f, h_pol, h_cg, body_launches(K), K, capture_);
         }, &last)) return false;
     const int precisions[3] = {PREC_FP64, PREC_MIXED, PREC_FP64_EXACT};
     for (int k = 0; k < 3; ++k) {
@@ -1443,6 +1443,10 @@ bool Engine::run_once(std::string& why) {
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
     std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
+    for (int k = 0; k < 3; ++k) {
+        h_ctrl_->check_due[k] = 1;  // the first body checks whatever is due; later ones as counted
+        h_ctrl_->step_due[k] = kMaxInterval;
+    }
     h_ctrl_->bodies = 0;
     h_ctrl_->body_cap = cap;
     h_ctrl_->error = 0;
@@ -1593,6 +1597,7 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
     std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
+    for (int k = 0; k < 3; ++k) h_ctrl_->step_due[k] = kMaxInterval;
     cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
     const View v = view();
     const int group = step_group(j.opt.precision, j.variant);

@@ -189,6 +189,8 @@ struct Ctrl {
     int32_t cg_iters;      // CG iterations run in this body
     long long kernels;     // engine kernels executed by this launch (counted by gate/control)
     int32_t group_begin[kStepGroups + 1];  // step groups: [begin, end) in View::group_tiles
+    int32_t check_due[3];  // instances due for each check family in the next body (0: its kernel returns at once)
+    int32_t step_due[3];   // per precision: step launches of this body with work (later ones return at once)
 };
 
 // Everything a tile kernel needs, passed by value.

@@ -894,12 +894,14 @@ constexpr int step_min_blocks() { return (VAR == VAR_TILE || VAR == VAR_WARP || 
 
 template <int PREC, int VAR>
 __global__ void __launch_bounds__(kBlock, step_min_blocks<VAR>()) step_kernel(View v, int group, int j0) {
+    if (j0 >= v.ctrl->step_due[PREC]) return;  // every chunk of this precision ends before step j0
     const int b = v.ctrl->group_begin[group], e = v.ctrl->group_begin[group + 1];
     for (int t = b + static_cast<int>(blockIdx.x); t < e; t += gridDim.x) step_tile<PREC, VAR>(v, v.tiles[v.group_tiles[t]], j0);
 }
 
 // FP64_EXACT engine: one structure, every tile of the table (other precisions skip).
 __global__ void __launch_bounds__(kBlock) step_exact_kernel(View v, int j0) {
+    if (j0 >= v.ctrl->step_due[PREC_FP64_EXACT]) return;
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) step_tile<PREC_FP64_EXACT, 1>(v, v.tiles[t], j0);
 }
@@ -913,6 +915,7 @@ constexpr int FAMILY_VERIFY = 2;   // polished point of the mixed engine (once p
 
 template <int FAMILY>
 __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
+    if (v.ctrl->check_due[FAMILY] == 0) return;  // no instance due for this family in this body
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
@@ -1380,13 +1383,16 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
 // ---- control kernels (one block) ---------------------------------------------------------------
 struct Counts {
     int running, fista[3], polish;
+    int check_due[3];  // per check family: FP64 engines, the mixed FP32 iterate, the polished point
+    int step_due[3];   // per precision: the longest remaining chunk among FISTA instances (capped by steps)
 };
 
-__device__ Counts count_phases(const View& v, bool mirror) {
-    __shared__ int s[5];
-    if (threadIdx.x < 5) s[threadIdx.x] = 0;
+// steps > 0: also the step launches with work per precision (a chunk needs it_next - it_cur more)
+__device__ Counts count_phases(const View& v, bool mirror, int steps = 0) {
+    __shared__ int s[11];
+    if (threadIdx.x < 11) s[threadIdx.x] = 0;
     __syncthreads();
-    int nr = 0, nf0 = 0, nf1 = 0, nf2 = 0, np = 0;
+    int nr = 0, nf[3] = {0, 0, 0}, np = 0, due[3] = {0, 0, 0}, need[3] = {0, 0, 0};
     const int n = v.ctrl->n_inst;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const InstDev& I = v.inst[i];
@@ -1394,25 +1400,35 @@ __device__ Counts count_phases(const View& v, bool mirror) {
         if (mirror) v.status_mirror[i] = st;
         if (st != ST_RUNNING) continue;
         nr++;
+        const int pk = I.precision == PREC_MIXED ? 1 : I.precision == PREC_FP64_EXACT ? 2 : 0;
         if (I.phase == PH_FISTA) {
-            if (I.precision == PREC_MIXED) nf1++;
-            else if (I.precision == PREC_FP64_EXACT) nf2++;
-            else nf0++;
+            nf[pk]++;
+            if (I.it_cur >= I.it_next) due[pk == 1 ? 1 : 0]++;  // the check kernel's test
+            else if (steps > 0) {
+                const int64_t left = I.it_next - I.it_cur;
+                need[pk] = max(need[pk], left < steps ? static_cast<int>(left) : steps);
+            }
         } else if (I.phase == PH_POLISH_INIT || I.phase == PH_POLISH_CG) {
             np++;
+        } else if (I.phase == PH_POLISH_FINISH && pk == 1) {
+            due[2]++;
         }
     }
     if (nr) atomicAdd(&s[0], nr);
-    if (nf0) atomicAdd(&s[1], nf0);
-    if (nf1) atomicAdd(&s[2], nf1);
-    if (nf2) atomicAdd(&s[3], nf2);
+    for (int k = 0; k < 3; ++k) {
+        if (nf[k]) atomicAdd(&s[1 + k], nf[k]);
+        if (due[k]) atomicAdd(&s[5 + k], due[k]);
+        if (need[k]) atomicMax(&s[8 + k], need[k]);
+    }
     if (np) atomicAdd(&s[4], np);
     __syncthreads();
     Counts c;
     c.running = s[0];
-    c.fista[0] = s[1];
-    c.fista[1] = s[2];
-    c.fista[2] = s[3];
+    for (int k = 0; k < 3; ++k) {
+        c.fista[k] = s[1 + k];
+        c.check_due[k] = s[5 + k];
+        c.step_due[k] = s[8 + k];
+    }
     c.polish = s[4];
     return c;
 }
@@ -1445,10 +1461,13 @@ __device__ void advance_chunks(const View& v, int steps) {
 // direction kernel counts into Ctrl::kernels.
 __global__ void gate_kernel(View v, cudaGraphConditionalHandle h_fp64, cudaGraphConditionalHandle h_mixed,
                             cudaGraphConditionalHandle h_exact, cudaGraphConditionalHandle h_polish,
-                            cudaGraphConditionalHandle h_cg, StepLaunches steps) {
-    const Counts c = count_phases(v, false);
+                            cudaGraphConditionalHandle h_cg, StepLaunches steps, int body_steps) {
+    const Counts c = count_phases(v, false, body_steps);
     if (threadIdx.x == 0) {
-        for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
+        for (int k = 0; k < 3; ++k) {
+            v.ctrl->n_fista[k] = c.fista[k];
+            v.ctrl->step_due[k] = c.step_due[k];
+        }
         v.ctrl->n_polish = c.polish;
         v.ctrl->n_cg = c.polish;
         v.ctrl->cg_iters = 0;
@@ -1468,6 +1487,7 @@ __global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h, int st
     advance_chunks(v, steps);
     const Counts c = count_phases(v, true);
     if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) v.ctrl->check_due[k] = c.check_due[k];
         Ctrl* ctrl = v.ctrl;
         ctrl->bodies++;
         ctrl->kernels += 1;
@@ -1476,10 +1496,13 @@ __global__ void control_kernel(View v, cudaGraphConditionalHandle loop_h, int st
     }
 }
 
-__global__ void gate_plain_kernel(View v) {
-    const Counts c = count_phases(v, false);
+__global__ void gate_plain_kernel(View v, int steps) {
+    const Counts c = count_phases(v, false, steps);
     if (threadIdx.x == 0) {
-        for (int k = 0; k < 3; ++k) v.ctrl->n_fista[k] = c.fista[k];
+        for (int k = 0; k < 3; ++k) {
+            v.ctrl->n_fista[k] = c.fista[k];
+            v.ctrl->step_due[k] = c.step_due[k];
+        }
         v.ctrl->n_polish = c.polish;
         v.ctrl->n_cg = c.polish;
         v.ctrl->cg_iters = 0;
@@ -1490,6 +1513,7 @@ __global__ void control_plain_kernel(View v, int steps) {
     advance_chunks(v, steps);
     const Counts c = count_phases(v, true);
     if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) v.ctrl->check_due[k] = c.check_due[k];
         v.ctrl->bodies++;
         v.ctrl->running = c.running;
     }
@@ -2036,13 +2060,13 @@ void launch_cg_vector(const View& v, int grid, cudaStream_t s, cudaGraphConditio
 }
 
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
-                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, cudaStream_t s) {
-    gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, cg_loop, steps);
+                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, int body_steps, cudaStream_t s) {
+    gate_kernel<<<1, 1024, 0, s>>>(v, fista[0], fista[1], fista[2], polish, cg_loop, steps, body_steps);
 }
 void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s) {
     control_kernel<<<1, 1024, 0, s>>>(v, loop, steps);
 }
-void launch_gate_plain(const View& v, cudaStream_t s) { gate_plain_kernel<<<1, 1024, 0, s>>>(v); }
+void launch_gate_plain(const View& v, int steps, cudaStream_t s) { gate_plain_kernel<<<1, 1024, 0, s>>>(v, steps); }
 void launch_control_plain(const View& v, int steps, cudaStream_t s) { control_plain_kernel<<<1, 1024, 0, s>>>(v, steps); }
 
 void launch_init_instance(const View& v, int slot, int n, int precision, cudaStream_t s) {

@@ -28,11 +28,11 @@ struct StepLaunches {
     int n[3];
 };
 void launch_gate(const View& v, const cudaGraphConditionalHandle* fista, cudaGraphConditionalHandle polish,
-                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, cudaStream_t s);
+                 cudaGraphConditionalHandle cg_loop, StepLaunches steps, int body_steps, cudaStream_t s);
 // `steps`: step launches per body; FISTA-phase instances advance it_cur by up to that many.
 void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, cudaStream_t s);
 // Host-driven variants of the control kernels (no conditional handles).
-void launch_gate_plain(const View& v, cudaStream_t s);
+void launch_gate_plain(const View& v, int steps, cudaStream_t s);
 void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
 // The record is passed by value: the instance is installed in its slot later, between graph launches.
