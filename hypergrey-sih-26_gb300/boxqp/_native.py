@@ -59,6 +59,8 @@ PROTOTYPES = {
     'bqp_destroy': (None, [c_void_p]),
     'bqp_last_error': (c_char_p, [c_void_p]),
     'bqp_device_name': (c_int, [c_int, c_char_p, c_size_t]),
+    'bqp_host_register': (c_int, [c_void_p, c_size_t]),
+    'bqp_host_unregister': (c_int, [c_void_p]),
     'bqp_submit': (c_int, [c_void_p, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P,
                            POINTER(Options), _U64P]),
     'bqp_submit_borrowed': (c_int, [c_void_p, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P,

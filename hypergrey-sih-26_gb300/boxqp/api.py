@@ -147,6 +147,34 @@ def check_convex_hessian(q: QuadraticProblem) -> bool:
     return rc == 1
 
 
+class pinned:
+    """Context manager that page-locks numpy arrays (bqp_host_register) for as long as it is
+    entered: submissions from them upload by asynchronous DMA with no host staging copy.  The
+    arrays must be C-contiguous and stay alive while pinned."""
+
+    def __init__(self, *arrays):
+        self.arrays = [a for a in arrays if a is not None and a.nbytes > 0]
+        self._done = []
+
+    def __enter__(self):
+        for a in self.arrays:
+            if not a.flags['C_CONTIGUOUS']:
+                raise ValueError('pinned arrays must be C-contiguous')
+            rc = lib().bqp_host_register(a.ctypes.data, a.nbytes)
+            if rc != N.BQP_OK:
+                self.__exit__(None, None, None)
+                msg = lib().bqp_last_error(None)
+                raise EngineError(rc, msg.decode() if msg else 'host register failed')
+            self._done.append(a)
+        return self
+
+    def __exit__(self, *exc):
+        for a in self._done:
+            lib().bqp_host_unregister(a.ctypes.data)
+        self._done = []
+        return False
+
+
 def cuda_device_name(device=0):
     buf = N.ctypes.create_string_buffer(256)
     lib().bqp_device_name(device, buf, 256)

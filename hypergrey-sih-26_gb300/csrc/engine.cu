@@ -2067,6 +2067,28 @@ const char* bqp_last_error(const bqp_ctx* ctx) {
     return ctx->engine->error();
 }
 
+int bqp_host_register(void* ptr, size_t bytes) {
+    if (!ptr || !bytes) return BQP_ERR_INVALID;
+    const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g_error = std::string("CUDA: host register: ") + cudaGetErrorString(e);
+        return e == cudaErrorHostMemoryAlreadyRegistered ? BQP_ERR_INVALID : BQP_ERR_CUDA;
+    }
+    return BQP_OK;
+}
+
+int bqp_host_unregister(void* ptr) {
+    if (!ptr) return BQP_ERR_INVALID;
+    const cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g_error = std::string("CUDA: host unregister: ") + cudaGetErrorString(e);
+        return BQP_ERR_INVALID;
+    }
+    return BQP_OK;
+}
+
 int bqp_device_name(int device, char* out, size_t cap) {
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {

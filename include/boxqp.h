@@ -124,6 +124,11 @@ void        bqp_destroy(bqp_ctx* ctx);
 const char* bqp_last_error(const bqp_ctx* ctx);
 /* Name of the CUDA device, as sovereign::cuda_device_name() (src/cuda_box.cu:38).            */
 int         bqp_device_name(int device, char* out, size_t cap);
+/* Page-locks a host range the caller submits from repeatedly (cudaHostRegister, portable):
+ * uploads from it become asynchronous DMA with no staging copy on the host.  The range must
+ * stay allocated until bqp_host_unregister(ptr).                                             */
+int         bqp_host_register(void* ptr, size_t bytes);
+int         bqp_host_unregister(void* ptr);
 
 /* ---- asynchronous solves (continuous batching) -------------------------------------------
  * bqp_submit copies one problem (full symmetric CSR, int32 indices, columns ascending in each

@@ -334,3 +334,26 @@ def test_mixed_precisions_and_structures_in_one_batch_equal_solo(engine):
         x, st = engine.fetch(ident, inst['n'])
         engine.release(ident)
         assert np.array_equal(x, xs) and st.iterations == its and st.objective == obj
+
+
+def test_pinned_host_arrays_give_the_same_bits(engine):
+    """Submissions from page-locked arrays (bqp_host_register) upload by DMA and give the bits of
+    pageable ones; registering twice is refused, unregistering restores pageable behaviour."""
+    inst = boxqp.planted('graph1m', seed=9, n=150000)
+    a = (inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'])
+    o = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+    xs, ss = engine.solve(*a, o)
+    with boxqp.pinned(*a):
+        with pytest.raises(boxqp.EngineError):
+            with boxqp.pinned(a[1]):
+                pass
+        ids = [engine.submit(*a, o, copy=False) for _ in range(3)]
+        xp, sp = engine.solve(*a, o)
+        for ident in ids:
+            assert engine.wait(ident, 120.0)
+            x, st = engine.fetch(ident, inst['n'])
+            engine.release(ident)
+            assert np.array_equal(x, xs) and st.iterations == ss.iterations
+    assert np.array_equal(xp, xs) and sp.objective == ss.objective
+    x2, _ = engine.solve(*a, o)
+    assert np.array_equal(x2, xs)
