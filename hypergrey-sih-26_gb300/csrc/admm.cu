@@ -64,13 +64,11 @@ __device__ __forceinline__ double csr_row(const int32_t* __restrict__ rp, const 
     return s;
 }
 
-// Fixed-order block sums of two doubles and a maximum; the last block (ticket) gets the grid
-// totals in thread 0 and returns true there.
-__device__ bool reduce_last(double a, double b, unsigned long long mx, double* partial, AdmmState* st, double* ta,
-                            double* tb, unsigned long long* tm) {
-    __shared__ double ra[kB / 32], rb[kB / 32];
-    __shared__ unsigned long long rm[kB / 32];
-    __shared__ int last;
+// Fixed-order block sums of two doubles and a maximum; the last block (ticket) adds the block
+// partials, all its threads strided over them and then the same fixed tree, and returns true in
+// its thread 0 with the grid totals.
+__device__ __forceinline__ void block_tree(double& a, double& b, unsigned long long& mx, double* ra, double* rb,
+                                           unsigned long long* rm) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -85,29 +83,42 @@ __device__ bool reduce_last(double a, double b, unsigned long long mx, double* p
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double sa = 0, sb = 0;
-        unsigned long long sm = 0;
+        a = 0;
+        b = 0;
+        mx = 0;
         for (int w = 0; w < kB / 32; ++w) {
-            sa += ra[w];
-            sb += rb[w];
-            sm = umax64(sm, rm[w]);
+            a += ra[w];
+            b += rb[w];
+            mx = umax64(mx, rm[w]);
         }
-        partial[3 * blockIdx.x] = sa;
-        partial[3 * blockIdx.x + 1] = sb;
-        partial[3 * blockIdx.x + 2] = __longlong_as_double(static_cast<long long>(sm));
+    }
+}
+
+__device__ bool reduce_last(double a, double b, unsigned long long mx, double* partial, AdmmState* st, double* ta,
+                            double* tb, unsigned long long* tm) {
+    __shared__ double ra[kB / 32], rb[kB / 32];
+    __shared__ unsigned long long rm[kB / 32];
+    __shared__ int last;
+    block_tree(a, b, mx, ra, rb, rm);
+    if (threadIdx.x == 0) {
+        partial[3 * blockIdx.x] = a;
+        partial[3 * blockIdx.x + 1] = b;
+        partial[3 * blockIdx.x + 2] = __longlong_as_double(static_cast<long long>(mx));
         __threadfence();
         last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1 ? 1 : 0;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return false;
+    if (!last) return false;
     __threadfence();
     double sa = 0, sb = 0;
     unsigned long long sm = 0;
-    for (unsigned k = 0; k < gridDim.x; ++k) {
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += kB) {
         sa += __ldcg(partial + 3 * k);
         sb += __ldcg(partial + 3 * k + 1);
         sm = umax64(sm, dbits(__ldcg(partial + 3 * k + 2)));
     }
+    block_tree(sa, sb, sm, ra, rb, rm);  // thread 0 read the first tree's ra/rb/rm before the barrier above
+    if (threadIdx.x != 0) return false;
     st->ticket = 0;
     *ta = sa;
     *tb = sb;
