@@ -1733,27 +1733,36 @@ __device__ __forceinline__ double lanczos_start(int r) {
     return 0.5 + static_cast<double>(mix_index(static_cast<unsigned>(r) * 2654435761u + 12345u) >> 8) * (1.0 / 16777216.0);
 }
 
-// Block sum of one double in a fixed order; the last block (ticket) returns true with the grid
-// total in *total (thread 0 only).
-__device__ bool lanczos_reduce(double x, double* partial, LanczosState* st, double* total) {
-    __shared__ double red[kBlock / 32];
-    __shared__ int last;
+// Block sum of one double in a fixed order; the last block (ticket) adds the block partials with
+// all its threads (strided, then the same tree) and returns true in its thread 0 with the grid
+// total in *total.
+__device__ __forceinline__ double lanczos_block_sum(double x, double* red) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += shfl_xor(x, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double b = 0;
+    double b = 0;
+    if (threadIdx.x == 0)
         for (int w = 0; w < kBlock / 32; ++w) b += red[w];
+    return b;  // thread 0
+}
+
+__device__ bool lanczos_reduce(double x, double* partial, LanczosState* st, double* total) {
+    __shared__ double red[kBlock / 32];
+    __shared__ int last;
+    const double b = lanczos_block_sum(x, red);
+    if (threadIdx.x == 0) {
         partial[blockIdx.x] = b;
         __threadfence();
         last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1 ? 1 : 0;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return false;
+    if (!last) return false;
     __threadfence();
     double t = 0;
-    for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(partial + k);
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += kBlock) t += __ldcg(partial + k);
+    t = lanczos_block_sum(t, red);  // thread 0 read red before the barrier above
+    if (threadIdx.x != 0) return false;
     st->ticket = 0;
     *total = t;
     return true;
