@@ -10,8 +10,10 @@ Follows 02-software/solver/src/qp_admm.cpp:
     finite), alpha = rz / den, x += alpha d, r -= alpha kd, pre = r / M, beta = dot(r, pre) / rz,
     d = pre + beta d;
   * dot (qp_admm.cpp:23) accumulates in long double, norm (qp_admm.cpp:22) is max |.|.
-Parity unpinned: the reference exposes this inner solve only inside its ADMM loop, so there are
-no golden vectors for it; the GPU solve is compared with this restatement.
+solve_qp_admm_restated restates the whole ADMM loop around it (qp_admm.cpp:136-280, below the
+first rho adaptation and polish); it reproduces the reference's solve_qp_admm primal bit for bit
+(tests/golden/reference_admm.npz, generated from the reference itself), which pins the inner
+solve restatement too.
 """
 import numpy as np
 
@@ -104,3 +106,113 @@ class AdmmSystemOracle:
             d = pre + beta * d
             inner += 1
         return x, inner, float(np.max(np.abs(r))) if len(r) else 0.0
+
+
+def _csr_from_rows(rows, n_cols):
+    """CsrMatrix(n, rows) of the reference (sparse_matrix.hpp:10-17): per row, columns merged in a
+    std::map (ascending, duplicates summed in input order), zeros dropped."""
+    rowptr, col, val = [0], [], []
+    for r in rows:
+        merged = {}
+        for j, v in r:
+            merged[j] = merged.get(j, 0.0) + v
+        for j in sorted(merged):
+            if merged[j] != 0:
+                col.append(j)
+                val.append(merged[j])
+        rowptr.append(len(col))
+    return np.array(rowptr, np.int32), np.array(col, np.int32), np.array(val, np.float64)
+
+
+def _clip(x, lo, up):
+    # std::max(lo, std::min(up, x)) elementwise
+    t = np.where(x < up, x, up)
+    return np.where(lo < t, t, lo)
+
+
+def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
+                           iteration_limit, scaling=True, inner=None):
+    """The reference's solve_qp_admm (qp_admm.cpp:136-280) for a minimisation with inequality rows,
+    up to an iteration limit below its first rho adaptation (100) and polish (250), where no
+    check before the limit verifies: returns the primal after `iteration_limit` ADMM iterations
+    (the reference's result.primal, x times the variable units).
+
+    inner(system, rhs, x0, accuracy, max_inner) -> x replaces the restated inner CG when given
+    (system: the scaled H and A as CSR triples, rho, sigma); it is how a GPU inner solve is run
+    inside the restated loop."""
+    assert iteration_limit < 100
+    m = len(a_rowptr) - 1
+    # hessian(q) (qp_admm.cpp:24-29): lower-triangle terms mirrored, merged per row
+    hrows = [[] for _ in range(n)]
+    for i, j, v in zip(hrow, hcol, hval):
+        hrows[i].append((j, v))
+        if i != j:
+            hrows[j].append((i, v))
+    hrp, hci, hva = _csr_from_rows(hrows, n)
+    hva = hva.copy()
+    variable = np.ones(n)
+    diagonal = np.zeros(n)
+    for i in range(n):
+        for k in range(hrp[i], hrp[i + 1]):
+            if hci[k] == i:
+                diagonal[i] = hva[k]
+    if scaling:
+        for j in range(n):
+            if diagonal[j] > 0:
+                variable[j] = 1 / np.sqrt(max(1e-16, diagonal[j]))
+    for i in range(n):
+        for k in range(hrp[i], hrp[i + 1]):
+            hva[k] *= variable[i] * variable[hci[k]]
+    rows = []
+    lo_all, up_all = [], []
+    row_scale = np.ones(m + n)
+    for i in range(m):
+        r = [(int(a_col[k]), float(a_val[k])) for k in range(a_rowptr[i], a_rowptr[i + 1])]
+        maximum = 0.0
+        r2 = []
+        for j, v in r:
+            v = v * variable[j]
+            maximum = max(maximum, abs(v))
+            r2.append((j, v))
+        if scaling and maximum > 0:
+            row_scale[i] = 1 / maximum
+        rows.append([(j, v * row_scale[i]) for j, v in r2])
+        lo_all.append(row_lower[i] * row_scale[i])
+        up_all.append(row_upper[i] * row_scale[i])
+    for j in range(n):
+        rows.append([(j, 1.0)])
+        lo_all.append(lower[j] / variable[j])
+        up_all.append(upper[j] / variable[j])
+    c = np.array(cost, dtype=np.float64) * (1.0 * variable)
+    cost_scale = 1 / max(1.0, float(np.max(np.abs(c)))) if scaling else 1.0
+    hva = hva * cost_scale
+    c = c * cost_scale
+    arp, aci, ava = _csr_from_rows(rows, n)
+    lo_all = np.array(lo_all)
+    up_all = np.array(up_all)
+    constraints = m + n
+    sys_ = AdmmSystemOracle((hrp, hci, hva), (arp, aci, ava), n)
+    rho = np.where(lo_all == up_all, 0.1 * 100, 0.1 * 1)
+    sigma = 1e-8
+    sys_.set_rho(rho, sigma)
+    x = _clip(np.zeros(n), lo_all[m:], up_all[m:])
+    z = _clip(csr_matvec(arp, aci, ava, x), lo_all, up_all)
+    y = np.zeros(constraints)
+    at = sys_.at
+    for iteration in range(iteration_limit):
+        yz = rho * z - y
+        rhs = csr_matvec(*at, yz)
+        rhs = rhs + (sigma * x - c)
+        accuracy = min(1e-7, .05 / (iteration + 1) ** 1.6) * (1 + float(np.max(np.abs(rhs))))
+        max_inner = min(4000, 2 * n + 20)
+        if inner is None:
+            nxt, _, _ = sys_.solve(rhs, x, accuracy, max_inner)
+        else:
+            nxt = inner(((hrp, hci, hva), (arp, aci, ava), rho, sigma), rhs, x, accuracy, max_inner)
+        ax = csr_matvec(arp, aci, ava, nxt)
+        relaxed = 1.6 * ax - .6 * z
+        nz = _clip(relaxed + y / rho, lo_all, up_all)
+        y = y + rho * (relaxed - nz)
+        z = nz
+        x = 1.6 * nxt - .6 * x
+    return x * variable

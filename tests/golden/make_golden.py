@@ -9,7 +9,9 @@ checker on each case below, and writes
     tests/golden/reference_cases.json   statuses, iterations, objectives, residuals, x digests
     tests/golden/reference_x.npz        primal vectors of the cases with n <= 2000
 The cases are the reference's known answers for this path (its tests and published harness)
-plus planted instances of the synthetic families.  QPLIB instances are read from the
+plus planted instances of the synthetic families.  tests/golden/reference_admm.npz holds the
+reference's ADMM (solve_qp_admm) after a few iterations on small constrained QPs (--only admm
+regenerates just that file).  QPLIB instances are read from the
 reference's datasets folder by the reference's own reader; only scalar results and the input
 file's SHA-256 are stored.
 """
@@ -90,12 +92,68 @@ def run_case(name, p, opts, maximize=False, offset=0.0):
     return rec, x
 
 
+def admm_case(seed, n, m, equality_rows):
+    """A constrained QP for the reference's ADMM: lower-triangle Hessian (diagonal U[2,4] plus 3n/2
+    off-diagonal terms U[-0.5,0.5]), bounds [-1, 1], m rows of 4 normal entries with bounds
+    [-U[0.1,0.5], U[0.1,0.5]] (the first `equality_rows` of them equalities at 0.1)."""
+    rng = np.random.default_rng(seed)
+    hrow, hcol, hval = [], [], []
+    for i in range(n):
+        hrow.append(i)
+        hcol.append(i)
+        hval.append(float(rng.uniform(2, 4)))
+    for _ in range(3 * n // 2):
+        i, j = sorted(rng.choice(n, 2, replace=False).tolist())[::-1]
+        hrow.append(i)
+        hcol.append(j)
+        hval.append(float(rng.uniform(-0.5, 0.5)))
+    rowptr, col, val = [0], [], []
+    for _ in range(m):
+        cs = np.sort(rng.choice(n, 4, replace=False))
+        col += cs.tolist()
+        val += rng.normal(size=4).tolist()
+        rowptr.append(len(col))
+    row_lower = -rng.uniform(0.1, 0.5, m)
+    row_upper = rng.uniform(0.1, 0.5, m)
+    row_lower[:equality_rows] = 0.1
+    row_upper[:equality_rows] = 0.1
+    return {'n': n, 'hrow': np.array(hrow, np.int64), 'hcol': np.array(hcol, np.int64), 'hval': np.array(hval),
+            'cost': rng.normal(size=n), 'lower': -np.ones(n), 'upper': np.ones(n),
+            'a_rowptr': np.array(rowptr, np.int32), 'a_col': np.array(col, np.int32), 'a_val': np.array(val),
+            'row_lower': row_lower, 'row_upper': row_upper}
+
+
+def make_admm_golden():
+    """The reference's solve_qp_admm (src/qp_admm.cpp:118-280) after a few ADMM iterations (below its
+    first rho adaptation and polish) on small constrained QPs: tests/golden/reference_admm.npz."""
+    out = {}
+    for name, (seed, n, m, eq, its, scaling) in {'admm_a': (7, 40, 25, 0, 20, True),
+                                                  'admm_b': (8, 120, 60, 10, 12, True),
+                                                  'admm_c': (9, 80, 50, 5, 8, False)}.items():
+        p = admm_case(seed, n, m, eq)
+        status, x, st = O.ref_solve_qp_admm(p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                            p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
+                                            tol=1e-12, iteration_limit=its, scaling=scaling)
+        assert status == 'iteration_limit' and int(st['iterations']) == its, (name, status, st)
+        for k, v in p.items():
+            out[f'{name}.{k}'] = np.asarray(v)
+        out[f'{name}.iterations'] = np.array(its)
+        out[f'{name}.scaling'] = np.array(1 if scaling else 0)
+        out[f'{name}.x'] = x
+        print(name, status, its, float(np.max(np.abs(x))), flush=True)
+    np.savez_compressed(OUT / 'reference_admm.npz', **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference/02-software/solver')
+    ap.add_argument('--only', choices=['admm'], default=None, help='regenerate only that fixture')
     a = ap.parse_args()
     if not O.build_reference(a.reference):
         raise SystemExit('cannot build oracle/_ref from ' + a.reference)
+    make_admm_golden()
+    if a.only == 'admm':
+        return
     records, vectors = [], {}
     for name, inst, opts, gen in cases():
         rec, x = run_case(name, inst, opts)

@@ -50,3 +50,27 @@ def test_restated_system_and_cg():
     assert np.allclose(x, np.linalg.solve(k, rhs), rtol=1e-8, atol=1e-8)
     x0, inner0, _ = o.solve(rhs, np.ones(n), 1e-10, 0)
     assert inner0 == 0 and np.array_equal(x0, np.ones(n))
+
+
+def _golden_admm():
+    from pathlib import Path
+    data = np.load(Path(__file__).resolve().parent / 'golden' / 'reference_admm.npz')
+    names = sorted({k.split('.')[0] for k in data.files})
+    return [(name, {k.split('.', 1)[1]: data[k] for k in data.files if k.startswith(name + '.')}) for name in names]
+
+
+def test_restated_admm_loop_matches_reference_golden():
+    """The restated ADMM loop (scaling, x-update by the restated inner CG, relaxed z/y updates)
+    reproduces the reference's solve_qp_admm primal after a few iterations (fixture made by
+    tests/golden/make_golden.py from the reference itself): bit for bit where numpy's long double
+    is the x87 80-bit type the reference's dot products use, else to 1e-12."""
+    from oracle.admm_pcg import solve_qp_admm_restated
+    exact = np.finfo(np.longdouble).nmant == 63
+    for name, p in _golden_admm():
+        x = solve_qp_admm_restated(int(p['n']), p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                   p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
+                                   int(p['iterations']), scaling=bool(p['scaling']))
+        if exact:
+            assert np.array_equal(x, p['x']), name
+        else:
+            assert np.max(np.abs(x - p['x'])) <= 1e-12, name

@@ -83,3 +83,32 @@ def test_admm_rejects_bad_input():
     with pytest.raises(ValueError):
         gpu.set_rho(np.zeros(20), 1e-8)
     gpu.close()
+
+
+def test_gpu_inner_solve_inside_the_reference_admm_loop():
+    """The restated ADMM loop of the reference (oracle/admm_pcg.py, pinned bit for bit to
+    solve_qp_admm by tests/test_admm_oracle.py) with its x-update solved on the GPU reaches the
+    reference's primal after the fixture's iterations to 1e-5 (each inner solve stops at the
+    reference's accuracy, about 1e-7 relative, and rounds differently)."""
+    from pathlib import Path
+    from oracle.admm_pcg import solve_qp_admm_restated
+    data = np.load(Path(__file__).resolve().parent / 'golden' / 'reference_admm.npz')
+    names = sorted({k.split('.')[0] for k in data.files})
+    for name in names:
+        p = {k.split('.', 1)[1]: data[k] for k in data.files if k.startswith(name + '.')}
+        n = int(p['n'])
+        cache = {}
+
+        def inner(system, rhs, x0, accuracy, max_inner):
+            h, a, rho, sigma = system
+            if 's' not in cache:
+                cache['s'] = AdmmSystem(*h, *a, n)
+                cache['s'].set_rho(rho, sigma)
+            x, _, _ = cache['s'].solve(rhs, x0, accuracy, max_inner)
+            return x
+
+        x = solve_qp_admm_restated(n, p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                   p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
+                                   int(p['iterations']), scaling=bool(p['scaling']), inner=inner)
+        cache['s'].close()
+        assert np.max(np.abs(x - p['x'])) <= 1e-5, (name, float(np.max(np.abs(x - p['x']))))
