@@ -15,6 +15,10 @@ in FP64.  A step is one complete solve of that instance.
           instance; algorithmic bytes per launch nnz*(4+4) + 4(n+1) + 7*4n
   cpu_baseline  the FP64 reference FISTA (CPU oracle port, all host cores) on one full solve
 
+Other workloads (--workload): grid, graph10k, tridiagonal (the reference's published family),
+batch (4,096 uneven instances in one launch), serve (Poisson arrivals into the continuous-batching
+request loop) and admm (the constrained-QP ADMM inner solve, CG iterations/s).
+
 --impl reference times the reference algorithm's CPU implementation (the oracle port of
 src/accelerated_qp.cpp, OpenMP on all host cores) on the same workload and metric.
 Multi-GPU (--gpus N under torchrun): independent replicas, one per GPU (no data exchange).
