@@ -85,6 +85,7 @@ PROTOTYPES = {
     'bqp_admm_set_rho': (c_int, [c_void_p, _F64P, c_double]),
     'bqp_admm_apply': (c_int, [c_void_p, _F64P, _F64P]),
     'bqp_admm_solve': (c_int, [c_void_p, _F64P, _F64P, c_double, c_int64, _I64P, _F64P]),
+    'bqp_admm_iterate': (c_int, [c_void_p, _F64P, _F64P, _F64P, _F64P, _F64P, _F64P, c_int64, c_int64, _I64P]),
     'bqp_admm_last_error': (c_char_p, []),
     'bqp_admm_destroy': (None, [c_void_p]),
     'bqp_box_last_error': (c_char_p, [c_void_p]),

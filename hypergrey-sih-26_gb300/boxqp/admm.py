@@ -8,6 +8,7 @@ runs that inner solve there as one graph launch:
     s = AdmmSystem(h_rowptr, h_col, h_val, a_rowptr, a_col, a_val, n)
     s.set_rho(rho, sigma)                      # also forms the preconditioner
     x, inner, resid = s.solve(rhs, x0, accuracy, max_inner)
+    x, z, y, inner = s.iterate(c, lo, up, x, z, y, first_iteration, iterations)   # whole ADMM steps
 """
 import numpy as np
 
@@ -66,6 +67,21 @@ class AdmmSystem:
         self._check(lib().bqp_admm_solve(self._s, ptr(rhs, N.c_double), ptr(x, N.c_double), float(accuracy),
                                          int(max_inner), N.ctypes.byref(inner), N.ctypes.byref(resid)))
         return x, inner.value, resid.value
+
+    def iterate(self, c, lo, up, x, z, y, first_iteration, iterations):
+        """`iterations` ADMM iterations of the reference's loop on the device (bqp_admm_iterate);
+        returns (x, z, y, inner iterations in total)."""
+        c, lo, up = _f64(c), _f64(lo), _f64(up)
+        x = np.array(x, dtype=np.float64, copy=True)
+        z = np.array(z, dtype=np.float64, copy=True)
+        y = np.array(y, dtype=np.float64, copy=True)
+        if c.shape != (self.n,) or x.shape != (self.n,) or any(v.shape != (self.m,) for v in (lo, up, z, y)):
+            raise ValueError('c and x need n entries; lo, up, z and y one per row of A')
+        total = N.c_int64(0)
+        self._check(lib().bqp_admm_iterate(self._s, ptr(c, N.c_double), ptr(lo, N.c_double), ptr(up, N.c_double),
+                                           ptr(x, N.c_double), ptr(z, N.c_double), ptr(y, N.c_double),
+                                           int(first_iteration), int(iterations), N.ctypes.byref(total)))
+        return x, z, y, total.value
 
     def close(self):
         if getattr(self, '_s', None):

@@ -40,6 +40,7 @@ struct AdmmState {
     unsigned long long rmax;  // max |r| as the bit pattern of a non-negative double
     long long max_inner;
     long long inner;
+    long long inner_sum;      // inner iterations over the ADMM iterations of one bqp_admm_iterate call
     unsigned ticket;
     int stop;                 // a non-positive or non-finite d'K d ended the loop
 };
@@ -251,6 +252,72 @@ __global__ void __launch_bounds__(kB) admm_precond_kernel(Sys s, double* __restr
     }
 }
 
+// ---- the ADMM iteration around the inner solve (qp_admm.cpp:255-279) --------------------------
+// rhs = A'(rho z - y) + (sigma x - c); the inner accuracy min(1e-7, .05 / (it+1)^1.6) (1 + max|rhs|)
+// and the inner iteration cap go to the state the inner solve's set-up reads; x0 of the inner
+// solve = x.
+__global__ void __launch_bounds__(kB) admm_rhs_kernel(Sys s, const double* __restrict__ z, const double* __restrict__ y,
+                                                      const double* __restrict__ xa, const double* __restrict__ c,
+                                                      double* __restrict__ rhs, double* __restrict__ x0, double* partial,
+                                                      AdmmState* st, double iteration_factor) {
+    const int sl = threadIdx.x % kLanes;
+    unsigned long long mx = 0;
+    for (int base = blockIdx.x * kRows; base < s.n; base += gridDim.x * kRows) {
+        const int j = base + static_cast<int>(threadIdx.x) / kLanes;
+        double acc = 0;
+        if (j < s.n) {
+            const int ks = __ldg(s.trp + j), ke = __ldg(s.trp + j + 1);
+            for (int k = ks + sl; k < ke; k += kLanes) {
+                const int i = __ldg(s.tci + k);
+                const double yz = __dsub_rn(__dmul_rn(s.rho[i], z[i]), y[i]);  // the reference's yz[i]
+                acc = fma(__ldg(s.tva + k), yz, acc);
+            }
+        }
+#pragma unroll
+        for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (j < s.n && sl == 0) {
+            const double v = __dadd_rn(acc, __dsub_rn(__dmul_rn(s.sigma, xa[j]), c[j]));
+            rhs[j] = v;
+            x0[j] = xa[j];
+            mx = umax64(mx, dbits(fabs(v)));
+        }
+    }
+    double ta, tb;
+    unsigned long long tm;
+    if (!reduce_last(0.0, 0.0, mx, partial, st, &ta, &tb, &tm)) return;
+    const double rmax = __longlong_as_double(static_cast<long long>(tm));
+    st->accuracy = __dmul_rn(iteration_factor, __dadd_rn(1.0, rmax));
+    st->max_inner = s.n * 2LL + 20 < 4000 ? s.n * 2LL + 20 : 4000;
+    st->stop = 0;  // a breakdown of the previous inner solve does not carry over
+}
+
+// ax = A next; relaxed = 1.6 ax - .6 z; z+ = clip(relaxed + y / rho, lo, up); y += rho (relaxed - z+)
+__global__ void __launch_bounds__(kB) admm_zy_kernel(Sys s, const double* __restrict__ next, double* __restrict__ z,
+                                                     double* __restrict__ y, const double* __restrict__ lo,
+                                                     const double* __restrict__ up, AdmmState* st) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->inner_sum += st->inner;
+    const int sl = threadIdx.x % kLanes;
+    for (int base = blockIdx.x * kRows; base < s.m; base += gridDim.x * kRows) {
+        const int i = base + static_cast<int>(threadIdx.x) / kLanes;
+        const double ax = csr_row(s.arp, s.aci, s.ava, next, i, s.m, sl);
+        if (i < s.m && sl == 0) {
+            const double zi = z[i], yi = y[i], ri = s.rho[i];
+            const double relaxed = __dsub_rn(__dmul_rn(1.6, ax), __dmul_rn(.6, zi));
+            const double w = __dadd_rn(relaxed, __ddiv_rn(yi, ri));
+            const double t = w < up[i] ? w : up[i];  // std::max(lo, std::min(up, w))
+            const double nz = lo[i] < t ? t : lo[i];
+            y[i] = __dadd_rn(yi, __dmul_rn(ri, __dsub_rn(relaxed, nz)));
+            z[i] = nz;
+        }
+    }
+}
+
+// x = 1.6 next - .6 x
+__global__ void __launch_bounds__(kB) admm_x_kernel(int n, const double* __restrict__ next, double* __restrict__ xa) {
+    for (int j = blockIdx.x * kB + threadIdx.x; j < n; j += gridDim.x * kB)
+        xa[j] = __dsub_rn(__dmul_rn(1.6, next[j]), __dmul_rn(.6, xa[j]));
+}
+
 int grid_for(int rows, int per_block) {
     int g = (rows + per_block - 1) / per_block;
     return std::max(1, std::min(g, kMaxBlocks));
@@ -270,6 +337,9 @@ struct bqp_admm {
     double* partial = nullptr;
     AdmmState* st = nullptr;
     AdmmState* h_st = nullptr;
+    // ADMM state of bqp_admm_iterate (allocated on first use): x, the cost, z, y and the
+    // constraint bounds (one per row of A)
+    double *xa = nullptr, *c = nullptr, *z = nullptr, *y = nullptr, *lo = nullptr, *up = nullptr;
     double sigma = 0;
     bool rho_set = false;
     cudaGraph_t graph = nullptr, apply_graph = nullptr;
@@ -367,7 +437,8 @@ struct bqp_admm {
                         static_cast<void*>(tva), static_cast<void*>(rho), static_cast<void*>(t), static_cast<void*>(precond),
                         static_cast<void*>(rhs), static_cast<void*>(x), static_cast<void*>(r), static_cast<void*>(pre),
                         static_cast<void*>(d), static_cast<void*>(kd), static_cast<void*>(v), static_cast<void*>(partial),
-                        static_cast<void*>(st)})
+                        static_cast<void*>(st), static_cast<void*>(xa), static_cast<void*>(c), static_cast<void*>(z),
+                        static_cast<void*>(y), static_cast<void*>(lo), static_cast<void*>(up)})
             if (p) cudaFree(p);
         if (h_st) cudaFreeHost(h_st);
         if (stream) cudaStreamDestroy(stream);
@@ -525,6 +596,63 @@ int bqp_admm_solve(bqp_admm* s, const double* rhs, double* x, double accuracy, i
     }
     if (inner_out) *inner_out = s->h_st->inner;
     if (residual_out) std::memcpy(residual_out, &s->h_st->rmax, sizeof(double));
+    return BQP_OK;
+}
+
+int bqp_admm_iterate(bqp_admm* s, const double* c, const double* lo, const double* up, double* x, double* z, double* y,
+                     int64_t first_iteration, int64_t iterations, int64_t* inner_total) {
+    if (!s || !c || !x || (s->m && (!lo || !up || !z || !y)) || first_iteration < 0 || iterations < 0)
+        return BQP_ERR_INVALID;
+    if (!s->rho_set) return BQP_ERR_NOT_READY;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    const size_t N = static_cast<size_t>(s->n), M = static_cast<size_t>(std::max<int64_t>(s->m, 1));
+    cudaError_t e = cudaSuccess;
+    if (!s->xa) {
+        if ((e = cudaMalloc(&s->xa, sizeof(double) * N)) || (e = cudaMalloc(&s->c, sizeof(double) * N)) ||
+            (e = cudaMalloc(&s->z, sizeof(double) * M)) || (e = cudaMalloc(&s->y, sizeof(double) * M)) ||
+            (e = cudaMalloc(&s->lo, sizeof(double) * M)) || (e = cudaMalloc(&s->up, sizeof(double) * M))) {
+            s->ok(e, "allocate ADMM state");
+            if (prev >= 0) cudaSetDevice(prev);
+            g_admm_error = s->error;
+            return BQP_ERR_NO_MEMORY;
+        }
+    }
+    const size_t mb = sizeof(double) * static_cast<size_t>(s->m);
+    cudaMemcpyAsync(s->xa, x, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->c, c, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream);
+    if (mb) {
+        cudaMemcpyAsync(s->z, z, mb, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->y, y, mb, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->lo, lo, mb, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->up, up, mb, cudaMemcpyHostToDevice, s->stream);
+    }
+    cudaMemsetAsync(s->st, 0, sizeof(AdmmState), s->stream);
+    const Sys sy = s->sys();
+    const int gn = grid_for(static_cast<int>(s->n), kRows), gm = grid_for(static_cast<int>(s->m), kRows);
+    const int gv = grid_for(static_cast<int>(s->n), kB);
+    for (int64_t k = 0; k < iterations; ++k) {
+        const double it = static_cast<double>(first_iteration + k + 1);
+        const double factor = std::min(1e-7, .05 / std::pow(it, 1.6));
+        admm_rhs_kernel<<<gn, kB, 0, s->stream>>>(sy, s->z, s->y, s->xa, s->c, s->rhs, s->x, s->partial, s->st, factor);
+        cudaGraphLaunch(s->exec, s->stream);
+        admm_zy_kernel<<<gm, kB, 0, s->stream>>>(sy, s->x, s->z, s->y, s->lo, s->up, s->st);
+        admm_x_kernel<<<gv, kB, 0, s->stream>>>(static_cast<int>(s->n), s->x, s->xa);
+    }
+    cudaMemcpyAsync(x, s->xa, sizeof(double) * N, cudaMemcpyDeviceToHost, s->stream);
+    if (mb) {
+        cudaMemcpyAsync(z, s->z, mb, cudaMemcpyDeviceToHost, s->stream);
+        cudaMemcpyAsync(y, s->y, mb, cudaMemcpyDeviceToHost, s->stream);
+    }
+    cudaMemcpyAsync(s->h_st, s->st, sizeof(AdmmState), cudaMemcpyDeviceToHost, s->stream);
+    const bool good = s->ok(cudaStreamSynchronize(s->stream), "iterate") && s->ok(cudaGetLastError(), "ADMM kernels");
+    if (prev >= 0) cudaSetDevice(prev);
+    if (!good) {
+        g_admm_error = s->error;
+        return BQP_ERR_CUDA;
+    }
+    if (inner_total) *inner_total = s->h_st->inner_sum;
     return BQP_OK;
 }
 

@@ -204,6 +204,17 @@ int         bqp_admm_set_rho(bqp_admm* s, const double* rho, double sigma);
 int         bqp_admm_apply(bqp_admm* s, const double* v, double* out);
 int         bqp_admm_solve(bqp_admm* s, const double* rhs, double* x, double accuracy, int64_t max_inner,
                            int64_t* inner_out, double* residual_out);
+/* Runs `iterations` iterations of the reference's ADMM loop (qp_admm.cpp:255-279) on the device
+ * for the scaled problem the caller formed (qp_admm.cpp:136-161): A holds every constraint row,
+ * bound rows included; c (n) is the scaled cost, lo/up (one per row of A) the constraint bounds;
+ * x (n), z and y (one per row of A) are the state, read and written back.  Each iteration builds
+ * rhs = A'(rho z - y) + sigma x - c, solves K next = rhs from x as bqp_admm_solve does, with the
+ * accuracy min(1e-7, .05 / (it + 1)^1.6) (1 + max|rhs|) and at most min(4000, 2n + 20) inner
+ * iterations (it = first_iteration + the step), then z, y and x = 1.6 next - .6 x.  The ADMM
+ * checks, rho adaptation and polish stay with the caller.                                    */
+int         bqp_admm_iterate(bqp_admm* s, const double* c, const double* lo, const double* up, double* x,
+                             double* z, double* y, int64_t first_iteration, int64_t iterations,
+                             int64_t* inner_total);
 const char* bqp_admm_last_error(void);
 void        bqp_admm_destroy(bqp_admm* s);
 

@@ -130,17 +130,11 @@ def _clip(x, lo, up):
     return np.where(lo < t, t, lo)
 
 
-def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
-                           iteration_limit, scaling=True, inner=None):
-    """The reference's solve_qp_admm (qp_admm.cpp:136-280) for a minimisation with inequality rows,
-    up to an iteration limit below its first rho adaptation (100) and polish (250), where no
-    check before the limit verifies: returns the primal after `iteration_limit` ADMM iterations
-    (the reference's result.primal, x times the variable units).
-
-    inner(system, rhs, x0, accuracy, max_inner) -> x replaces the restated inner CG when given
-    (system: the scaled H and A as CSR triples, rho, sigma); it is how a GPU inner solve is run
-    inside the restated loop."""
-    assert iteration_limit < 100
+def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
+                  scaling=True):
+    """The reference's set-up of solve_qp_admm (qp_admm.cpp:136-161) for a minimisation: variable
+    units, row scales and the cost scale; A with the bound rows appended; the initial x and z and
+    rho (0.1, x100 on equality rows), sigma 1e-8.  Returns a dict of the scaled problem."""
     m = len(a_rowptr) - 1
     # hessian(q) (qp_admm.cpp:24-29): lower-triangle terms mirrored, merged per row
     hrows = [[] for _ in range(n)]
@@ -190,14 +184,31 @@ def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_
     arp, aci, ava = _csr_from_rows(rows, n)
     lo_all = np.array(lo_all)
     up_all = np.array(up_all)
-    constraints = m + n
-    sys_ = AdmmSystemOracle((hrp, hci, hva), (arp, aci, ava), n)
     rho = np.where(lo_all == up_all, 0.1 * 100, 0.1 * 1)
-    sigma = 1e-8
-    sys_.set_rho(rho, sigma)
     x = _clip(np.zeros(n), lo_all[m:], up_all[m:])
     z = _clip(csr_matvec(arp, aci, ava, x), lo_all, up_all)
-    y = np.zeros(constraints)
+    return {'h': (hrp, hci, hva), 'a': (arp, aci, ava), 'c': c, 'lo': lo_all, 'up': up_all, 'rho': rho,
+            'sigma': 1e-8, 'variable': variable, 'x': x, 'z': z, 'y': np.zeros(m + n)}
+
+
+def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
+                           iteration_limit, scaling=True, inner=None):
+    """The reference's solve_qp_admm (qp_admm.cpp:136-280) for a minimisation with inequality rows,
+    up to an iteration limit below its first rho adaptation (100) and polish (250), where no
+    check before the limit verifies: returns the primal after `iteration_limit` ADMM iterations
+    (the reference's result.primal, x times the variable units).
+
+    inner(system, rhs, x0, accuracy, max_inner) -> x replaces the restated inner CG when given
+    (system: the scaled H and A as CSR triples, rho, sigma); it is how a GPU inner solve is run
+    inside the restated loop."""
+    assert iteration_limit < 100
+    sp = scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
+                       scaling)
+    (hrp, hci, hva), (arp, aci, ava) = sp['h'], sp['a']
+    c, lo_all, up_all, rho, sigma = sp['c'], sp['lo'], sp['up'], sp['rho'], sp['sigma']
+    sys_ = AdmmSystemOracle((hrp, hci, hva), (arp, aci, ava), n)
+    sys_.set_rho(rho, sigma)
+    x, z, y = sp['x'], sp['z'], sp['y']
     at = sys_.at
     for iteration in range(iteration_limit):
         yz = rho * z - y
@@ -215,4 +226,4 @@ def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_
         y = y + rho * (relaxed - nz)
         z = nz
         x = 1.6 * nxt - .6 * x
-    return x * variable
+    return x * sp['variable']

@@ -112,3 +112,28 @@ def test_gpu_inner_solve_inside_the_reference_admm_loop():
                                    int(p['iterations']), scaling=bool(p['scaling']), inner=inner)
         cache['s'].close()
         assert np.max(np.abs(x - p['x'])) <= 1e-5, (name, float(np.max(np.abs(x - p['x']))))
+
+
+def test_device_admm_iterations_reach_the_reference_primal():
+    """bqp_admm_iterate runs whole ADMM iterations of the reference's loop on the device (rhs, inner
+    solve, relaxed z/y and x updates) from the reference's scaled set-up (restated by
+    oracle/admm_pcg.py): the primal after the fixture's iterations matches the reference's
+    solve_qp_admm to 1e-5, and iterations split over two calls give the same bits as one call."""
+    from pathlib import Path
+    from oracle.admm_pcg import scale_qp_admm
+    data = np.load(Path(__file__).resolve().parent / 'golden' / 'reference_admm.npz')
+    for name in sorted({k.split('.')[0] for k in data.files}):
+        p = {k.split('.', 1)[1]: data[k] for k in data.files if k.startswith(name + '.')}
+        n, its = int(p['n']), int(p['iterations'])
+        sp = scale_qp_admm(n, p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'],
+                           p['a_col'], p['a_val'], p['row_lower'], p['row_upper'], bool(p['scaling']))
+        s = AdmmSystem(*sp['h'], *sp['a'], n)
+        s.set_rho(sp['rho'], sp['sigma'])
+        x, z, y, inner = s.iterate(sp['c'], sp['lo'], sp['up'], sp['x'], sp['z'], sp['y'], 0, its)
+        assert inner > 0
+        assert np.max(np.abs(x * sp['variable'] - p['x'])) <= 1e-5, name
+        k = its // 2
+        x1, z1, y1, _ = s.iterate(sp['c'], sp['lo'], sp['up'], sp['x'], sp['z'], sp['y'], 0, k)
+        x2, z2, y2, _ = s.iterate(sp['c'], sp['lo'], sp['up'], x1, z1, y1, k, its - k)
+        assert np.array_equal(x2, x) and np.array_equal(z2, z) and np.array_equal(y2, y), name
+        s.close()
