@@ -129,7 +129,9 @@ def make_admm_golden():
     out = {}
     for name, (seed, n, m, eq, its, scaling) in {'admm_a': (7, 40, 25, 0, 20, True),
                                                   'admm_b': (8, 120, 60, 10, 12, True),
-                                                  'admm_c': (9, 80, 50, 5, 8, False)}.items():
+                                                  'admm_c': (9, 80, 50, 5, 8, False),
+                                                  'admm_d': (10, 300, 150, 30, 15, True),
+                                                  'admm_e': (11, 200, 120, 0, 30, True)}.items():
         p = admm_case(seed, n, m, eq)
         status, x, st = O.ref_solve_qp_admm(p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
                                             p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
