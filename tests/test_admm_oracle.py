@@ -74,3 +74,17 @@ def test_restated_admm_loop_matches_reference_golden():
             assert np.array_equal(x, p['x']), name
         else:
             assert np.max(np.abs(x - p['x'])) <= 1e-12, name
+
+
+def test_restated_cg_stops_on_breakdown():
+    """A zero system (H = 0, A = 0, sigma = 0) breaks down at once: d'K d is not positive, the
+    reference leaves the CG loop before any update (qp_admm.cpp:264)."""
+    n = 5
+    h = (np.zeros(n + 1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    a = (np.zeros(3, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    o = AdmmSystemOracle(h, a, n)
+    with np.errstate(divide='ignore', invalid='ignore'):
+        o.set_rho(np.array([0.1, 0.1]), 0.0)
+        x0 = np.arange(n, dtype=float)
+        x, inner, resid = o.solve(np.ones(n), x0, 1e-9, 50)
+    assert inner == 0 and np.array_equal(x, x0) and resid == 1.0

@@ -137,3 +137,17 @@ def test_device_admm_iterations_reach_the_reference_primal():
         x2, z2, y2, _ = s.iterate(sp['c'], sp['lo'], sp['up'], x1, z1, y1, k, its - k)
         assert np.array_equal(x2, x) and np.array_equal(z2, z) and np.array_equal(y2, y), name
         s.close()
+
+
+def test_gpu_cg_stops_on_breakdown():
+    """The device loop leaves at a non-positive d'K d as the reference does: x unchanged, no
+    iteration counted, max|r| of the start returned."""
+    n = 5
+    h = (np.zeros(n + 1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    a = (np.zeros(3, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    s = AdmmSystem(*h, *a, n)
+    s.set_rho(np.array([0.1, 0.1]), 0.0)
+    x0 = np.arange(n, dtype=float)
+    x, inner, resid = s.solve(np.ones(n), x0, 1e-9, 50)
+    assert inner == 0 and np.array_equal(x, x0) and resid == 1.0
+    s.close()
