@@ -146,15 +146,42 @@ def make_admm_golden():
     np.savez_compressed(OUT / 'reference_admm.npz', **out)
 
 
+OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),
+              ('grid32_open', {'preset': 'grid', 'seed': 4, 'n': 1024, 'open_bounds': 2}, dict(tol=1e-7))]
+
+
+def update_open_cases():
+    """One-sided boxes (infinite lower or upper bounds on a share of the variables) on planted
+    instances, run by the reference and merged into reference_cases.json / reference_x.npz."""
+    sys.path.insert(0, str(OUT.parent))
+    from golden_cases import inputs
+    d = json.loads((OUT / 'reference_cases.json').read_text())
+    xs = dict(np.load(OUT / 'reference_x.npz'))
+    for name, gen, opts in OPEN_CASES:
+        p, inst = inputs({'generator': gen})
+        rec, x = run_case(name, p, opts)
+        rec['generator'] = gen
+        rec['fstar'] = None
+        d['cases'] = [c for c in d['cases'] if c['name'] != name] + [rec]
+        xs[name] = x
+        print(name, rec['status'], rec['iterations'], rec['objective'], flush=True)
+    (OUT / 'reference_cases.json').write_text(json.dumps(d, indent=1) + '\n')
+    np.savez_compressed(OUT / 'reference_x.npz', **xs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference/02-software/solver')
-    ap.add_argument('--only', choices=['admm'], default=None, help='regenerate only that fixture')
+    ap.add_argument('--only', choices=['admm', 'open'], default=None,
+                    help='regenerate only the ADMM fixture, or only the one-sided-box cases in place')
     a = ap.parse_args()
     if not O.build_reference(a.reference):
         raise SystemExit('cannot build oracle/_ref from ' + a.reference)
     make_admm_golden()
     if a.only == 'admm':
+        return
+    if a.only == 'open':
+        update_open_cases()
         return
     records, vectors = [], {}
     for name, inst, opts, gen in cases():

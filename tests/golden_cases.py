@@ -16,6 +16,13 @@ def inputs(rec):
                          lower_triplets=True)
     p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
          'lower': inst['lower'], 'upper': inst['upper']}
+    if g.get('open_bounds'):
+        # one-sided boxes: no lower bound where j % k == 0, no upper bound where j % k == 1
+        k = int(g['open_bounds'])
+        j = np.arange(len(p['lower']))
+        p['lower'] = np.where(j % k == 0, -np.inf, p['lower'])
+        p['upper'] = np.where(j % k == 1, np.inf, p['upper'])
+        inst = dict(inst, lower=p['lower'], upper=p['upper'])
     return p, inst
 
 

@@ -42,7 +42,7 @@ def test_fixture_covers_reference_known_answers(golden):
     assert d['convex'] == {'v2_psd_300': 1, 'v2_indefinite_300': 0}
 
 
-@pytest.mark.parametrize('idx', range(24))
+@pytest.mark.parametrize('idx', range(28))
 def test_oracle_matches_reference(golden, idx):
     d, xs = golden
     if idx >= len(d['cases']):
