@@ -147,12 +147,14 @@ def make_admm_golden():
 
 
 OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),
-              ('grid32_open', {'preset': 'grid', 'seed': 4, 'n': 1024, 'open_bounds': 2}, dict(tol=1e-7))]
+              ('grid32_open', {'preset': 'grid', 'seed': 4, 'n': 1024, 'open_bounds': 2}, dict(tol=1e-7)),
+              ('graph2k_fixed', {'preset': 'graph10k', 'seed': 301, 'n': 2000, 'fixed_every': 5}, dict(tol=1e-6))]
 
 
 def update_open_cases():
-    """One-sided boxes (infinite lower or upper bounds on a share of the variables) on planted
-    instances, run by the reference and merged into reference_cases.json / reference_x.npz."""
+    """One-sided boxes (infinite lower or upper bounds on a share of the variables) and fixed
+    variables (l = u) on planted instances, run by the reference and merged into
+    reference_cases.json / reference_x.npz."""
     sys.path.insert(0, str(OUT.parent))
     from golden_cases import inputs
     d = json.loads((OUT / 'reference_cases.json').read_text())

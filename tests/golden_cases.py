@@ -23,6 +23,13 @@ def inputs(rec):
         p['lower'] = np.where(j % k == 0, -np.inf, p['lower'])
         p['upper'] = np.where(j % k == 1, np.inf, p['upper'])
         inst = dict(inst, lower=p['lower'], upper=p['upper'])
+    if g.get('fixed_every'):
+        # fixed variables: l = u = the planted optimum where j % k == 0 (the optimum is unchanged)
+        k = int(g['fixed_every'])
+        fix = np.arange(len(p['lower'])) % k == 0
+        p['lower'] = np.where(fix, inst['xstar'], p['lower'])
+        p['upper'] = np.where(fix, inst['xstar'], p['upper'])
+        inst = dict(inst, lower=p['lower'], upper=p['upper'])
     return p, inst
 
 

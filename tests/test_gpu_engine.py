@@ -44,7 +44,7 @@ def active_set_ok(inst, x, margin=1e-6):
 
 @pytest.mark.parametrize('name', ['graph2k_s100', 'graph2k_s103', 'graph2k_tol1e-8', 'graph2k_limit60',
                                   'graph2k_limit0', 'tridiagonal_1000', 'grid32_tol1e-08', 'batch_i0',
-                                  'graph10k_s0', 'graph2k_open', 'grid32_open'])
+                                  'graph10k_s0', 'graph2k_open', 'grid32_open', 'graph2k_fixed'])
 def test_exact_mode_reproduces_reference_bits(engine, golden, name):
     d, xs = golden
     rec = next(c for c in d['cases'] if c['name'] == name)
@@ -359,11 +359,12 @@ def test_pinned_host_arrays_give_the_same_bits(engine):
     assert np.array_equal(x2, xs)
 
 
-@pytest.mark.parametrize('name', ['graph2k_open', 'grid32_open'])
+@pytest.mark.parametrize('name', ['graph2k_open', 'grid32_open', 'graph2k_fixed'])
 @pytest.mark.parametrize('precision', ['mixed', 'fp64'])
 def test_one_sided_boxes(engine, golden, name, precision):
-    """Infinite lower or upper bounds on a share of the variables: the FP64 and mixed engines verify
-    at the case's tolerance (oracle checker) and reach the reference's objective."""
+    """Infinite lower or upper bounds on a share of the variables, or fixed variables (l = u): the
+    FP64 and mixed engines return a point inside the box that verifies at the case's tolerance
+    (oracle checker) and reaches the reference's objective."""
     d, _ = golden
     rec = next(c for c in d['cases'] if c['name'] == name)
     p, inst = inputs(rec)
@@ -372,4 +373,5 @@ def test_one_sided_boxes(engine, golden, name, precision):
     chk = O.check(*args(p), x, tol=rec['tol'])
     assert chk['verified']
     assert np.all(np.isfinite(x))
+    assert np.all(x >= p['lower']) and np.all(x <= p['upper'])
     assert st.objective == pytest.approx(rec['objective'], rel=1e-6)
