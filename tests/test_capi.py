@@ -234,3 +234,57 @@ def test_level_a_plugin_links_into_the_reference():
     out = subprocess.run([str(exe), '1000', 'cuda', '1', '30'], capture_output=True, text=True, timeout=120,
                          env={'CUDA_VISIBLE_DEVICES': '', 'PATH': '/usr/bin:/bin'})
     assert out.returncode == 2 and 'No CUDA device available' in out.stderr
+
+
+def test_csr_builder_from_several_threads_at_once():
+    """Callers on several threads share the host worker pool (their tasks queue and the workers
+    help each in turn); each gets exactly the single-caller result."""
+    import threading
+    rng = np.random.default_rng(11)
+    n = 2500
+    jobs = []
+    for t in range(4):
+        k = 400000 + 50000 * t
+        r = rng.integers(0, n, k)
+        c = rng.integers(0, n, k)
+        jobs.append((np.maximum(r, c), np.minimum(r, c), rng.standard_normal(k)))
+    expected = [boxqp.csr_from_lower(n, *j, 1.0) for j in jobs]
+    results = [None] * len(jobs)
+
+    def run(i):
+        for _ in range(3):
+            results[i] = boxqp.csr_from_lower(n, *jobs[i], 1.0)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(len(jobs))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for got, want in zip(results, expected):
+        for x, y in zip(got, want):
+            assert np.array_equal(x, y)
+
+
+def test_gpu_entry_points_fail_loudly_without_a_gpu():
+    """No CPU fallback: with no device visible, page-locking and the ADMM system report a CUDA
+    error instead of running anything on the host."""
+    import subprocess
+    import sys
+    code = ('import sys; sys.path[:0]=[{!r},{!r}]\n'
+            'import numpy as np, boxqp\n'
+            'from boxqp.admm import AdmmSystem\n'
+            'a = np.zeros(1000)\n'
+            'try:\n'
+            '    with boxqp.pinned(a):\n'
+            '        print("PINNED")\n'
+            'except boxqp.EngineError as e:\n'
+            '    print("PIN-ERROR", e)\n'
+            'h = (np.array([0, 1], np.int32), np.array([0], np.int32), np.array([2.0]))\n'
+            'try:\n'
+            '    AdmmSystem(*h, np.array([0], np.int32), np.zeros(0, np.int32), np.zeros(0), 1)\n'
+            '    print("ADMM-CREATED")\n'
+            'except ValueError as e:\n'
+            '    print("ADMM-ERROR", e)\n').format(str(ROOT), str(ROOT / 'hypergrey-sih-26_gb300'))
+    out = subprocess.run([sys.executable, '-c', code], capture_output=True, text=True, timeout=120,
+                         env={'CUDA_VISIBLE_DEVICES': '', 'PATH': '/usr/bin:/bin'})
+    assert 'PIN-ERROR' in out.stdout and 'ADMM-ERROR' in out.stdout, out.stdout + out.stderr
