@@ -148,13 +148,15 @@ def make_admm_golden():
 
 OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),
               ('grid32_open', {'preset': 'grid', 'seed': 4, 'n': 1024, 'open_bounds': 2}, dict(tol=1e-7)),
-              ('graph2k_fixed', {'preset': 'graph10k', 'seed': 301, 'n': 2000, 'fixed_every': 5}, dict(tol=1e-6))]
+              ('graph2k_fixed', {'preset': 'graph10k', 'seed': 301, 'n': 2000, 'fixed_every': 5}, dict(tol=1e-6)),
+              ('graph2k_zero_rows', {'preset': 'graph10k', 'seed': 302, 'n': 2000, 'zero_rows_every': 7},
+               dict(tol=1e-6))]
 
 
 def update_open_cases():
-    """One-sided boxes (infinite lower or upper bounds on a share of the variables) and fixed
-    variables (l = u) on planted instances, run by the reference and merged into
-    reference_cases.json / reference_x.npz."""
+    """One-sided boxes (infinite lower or upper bounds on a share of the variables), fixed
+    variables (l = u), variables with no Hessian entries, and a one-variable problem, run by the
+    reference and merged into reference_cases.json / reference_x.npz."""
     sys.path.insert(0, str(OUT.parent))
     from golden_cases import inputs
     d = json.loads((OUT / 'reference_cases.json').read_text())
@@ -167,6 +169,14 @@ def update_open_cases():
         d['cases'] = [c for c in d['cases'] if c['name'] != name] + [rec]
         xs[name] = x
         print(name, rec['status'], rec['iterations'], rec['objective'], flush=True)
+    # one variable: min x^2 - 3x on [0, 1] (the unconstrained minimiser 1.5 is clipped to 1)
+    single = {'hrow': np.array([0], np.int64), 'hcol': np.array([0], np.int64), 'hval': np.array([2.0]),
+              'cost': np.array([-3.0]), 'lower': np.array([0.0]), 'upper': np.array([1.0])}
+    rec, x = run_case('single_var', single, dict(tol=1e-9))
+    rec['problem'] = {k: np.asarray(v).tolist() for k, v in single.items()}
+    d['cases'] = [c for c in d['cases'] if c['name'] != 'single_var'] + [rec]
+    xs['single_var'] = x
+    print('single_var', rec['status'], rec['iterations'], rec['objective'], x, flush=True)
     (OUT / 'reference_cases.json').write_text(json.dumps(d, indent=1) + '\n')
     np.savez_compressed(OUT / 'reference_x.npz', **xs)
 

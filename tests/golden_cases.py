@@ -23,6 +23,14 @@ def inputs(rec):
         p['lower'] = np.where(j % k == 0, -np.inf, p['lower'])
         p['upper'] = np.where(j % k == 1, np.inf, p['upper'])
         inst = dict(inst, lower=p['lower'], upper=p['upper'])
+    if g.get('zero_rows_every'):
+        # Hessian rows and columns of every k-th variable removed: those variables are linear only
+        k = int(g['zero_rows_every'])
+        keep = (p['hrow'] % k != 0) & (p['hcol'] % k != 0)
+        p['hrow'], p['hcol'], p['hval'] = p['hrow'][keep], p['hcol'][keep], p['hval'][keep]
+        csr = boxqp.csr_from_lower(len(p['cost']), p['hrow'], p['hcol'], p['hval'], 1.0)
+        inst = dict(inst, rowptr=csr[0], col=csr[1], val=csr[2], hrow=p['hrow'], hcol=p['hcol'], hval=p['hval'],
+                    nnz=len(csr[1]))
     if g.get('fixed_every'):
         # fixed variables: l = u = the planted optimum where j % k == 0 (the optimum is unchanged)
         k = int(g['fixed_every'])

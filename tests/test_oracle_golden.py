@@ -42,6 +42,24 @@ def test_fixture_covers_reference_known_answers(golden):
     assert d['convex'] == {'v2_psd_300': 1, 'v2_indefinite_300': 0}
 
 
+def test_edge_case_fixtures_have_their_analytic_answers(golden):
+    """One variable (min x^2 - 3x on [0, 1]: x = 1, objective -2) and variables with no Hessian
+    entries (linear only: at the lower bound where the cost is positive, at the upper where it is
+    negative) in the reference's own answers."""
+    d, xs = golden
+    by = {c['name']: c for c in d['cases']}
+    assert by['single_var']['status'] == 'optimal'
+    assert xs['single_var'].tolist() == [1.0] and by['single_var']['objective'] == pytest.approx(-2.0, abs=1e-12)
+    rec = by['graph2k_zero_rows']
+    p, _ = inputs(rec)
+    x = xs['graph2k_zero_rows']
+    linear = np.arange(len(x)) % rec['generator']['zero_rows_every'] == 0
+    assert not np.isin(np.flatnonzero(linear), np.concatenate([p['hrow'], p['hcol']])).any()
+    assert rec['status'] == 'optimal'
+    assert np.array_equal(x[linear & (p['cost'] > 0)], p['lower'][linear & (p['cost'] > 0)])
+    assert np.array_equal(x[linear & (p['cost'] < 0)], p['upper'][linear & (p['cost'] < 0)])
+
+
 @pytest.mark.parametrize('idx', range(28))
 def test_oracle_matches_reference(golden, idx):
     d, xs = golden
