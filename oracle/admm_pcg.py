@@ -10,10 +10,10 @@ Follows 02-software/solver/src/qp_admm.cpp:
     finite), alpha = rz / den, x += alpha d, r -= alpha kd, pre = r / M, beta = dot(r, pre) / rz,
     d = pre + beta d;
   * dot (qp_admm.cpp:23) accumulates in long double, norm (qp_admm.cpp:22) is max |.|.
-solve_qp_admm_restated restates the whole ADMM loop around it (qp_admm.cpp:136-280, below the
-first rho adaptation and polish); it reproduces the reference's solve_qp_admm primal bit for bit
-(tests/golden/reference_admm.npz, generated from the reference itself), which pins the inner
-solve restatement too.
+solve_qp_admm_restated restates the whole ADMM loop around it (qp_admm.cpp:136-280, with the rho
+adaptation every 100 iterations, below the first polish at iteration 250); it reproduces the
+reference's solve_qp_admm primal bit for bit (tests/golden/reference_admm.npz, generated from the
+reference itself), which pins the inner solve restatement too.
 """
 import numpy as np
 
@@ -191,17 +191,40 @@ def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_va
             'sigma': 1e-8, 'variable': variable, 'x': x, 'z': z, 'y': np.zeros(m + n)}
 
 
+def adapt_rho(sp, system, x, z, y, rho_base):
+    """The reference's rho adaptation (qp_admm.cpp:265-271), run at every 100th iteration: scaled
+    primal residual max|Ax - z| / (1 + max(|Ax|, |z|)) and dual residual max|Hx + c + A'y| /
+    (1 + max(|c|, |Hx|, |A'y|)) (max norms); the candidate rho_base sqrt(primal / dual), both
+    floored at 1e-16 and the result clamped to [1e-6, 1e6], replaces rho_base only when it leaves
+    [rho_base / 5, 5 rho_base].  Returns the (possibly unchanged) rho_base."""
+    ax = csr_matvec(*sp['a'], x)
+    hx = csr_matvec(*sp['h'], x)
+    aty = csr_matvec(*system.at, y)
+
+    def norm(v):
+        return float(np.max(np.abs(v))) if len(v) else 0.0
+
+    primal = norm(ax - z)
+    dual = norm(hx + sp['c'] + aty)
+    primal /= 1 + max(norm(ax), norm(z))
+    dual /= 1 + max(norm(sp['c']), max(norm(hx), norm(aty)))
+    nxt = max(1e-6, min(1e6, rho_base * np.sqrt(max(1e-16, primal) / max(1e-16, dual))))
+    return nxt if (nxt > 5 * rho_base or nxt < rho_base / 5) else rho_base
+
+
 def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
-                           iteration_limit, scaling=True, inner=None):
+                           iteration_limit, scaling=True, inner=None, info=None):
     """The reference's solve_qp_admm (qp_admm.cpp:136-280) for a minimisation with inequality rows,
-    up to an iteration limit below its first rho adaptation (100) and polish (250), where no
-    check before the limit verifies: returns the primal after `iteration_limit` ADMM iterations
-    (the reference's result.primal, x times the variable units).
+    up to an iteration limit below its first polish (250), where no check before the limit
+    verifies: returns the primal after `iteration_limit` ADMM iterations (the reference's
+    result.primal, x times the variable units).  The rho adaptation runs at iterations 100 and 200
+    (adapt_rho); a changed rho_base re-forms rho and the preconditioner (the reference's setup()).
 
     inner(system, rhs, x0, accuracy, max_inner) -> x replaces the restated inner CG when given
     (system: the scaled H and A as CSR triples, rho, sigma); it is how a GPU inner solve is run
-    inside the restated loop."""
-    assert iteration_limit < 100
+    inside the restated loop.  info, a dict, receives 'rho_base': the rho_base after each
+    adaptation."""
+    assert iteration_limit < 250
     sp = scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
                        scaling)
     (hrp, hci, hva), (arp, aci, ava) = sp['h'], sp['a']
@@ -210,7 +233,16 @@ def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_
     sys_.set_rho(rho, sigma)
     x, z, y = sp['x'], sp['z'], sp['y']
     at = sys_.at
+    rho_base = 0.1
     for iteration in range(iteration_limit):
+        if iteration and iteration % 100 == 0:
+            nxt = adapt_rho(sp, sys_, x, z, y, rho_base)
+            if info is not None:
+                info.setdefault('rho_base', []).append(nxt)
+            if nxt != rho_base:
+                rho_base = nxt
+                rho = np.where(lo_all == up_all, rho_base * 100, rho_base * 1)
+                sys_.set_rho(rho, sigma)
         yz = rho * z - y
         rhs = csr_matvec(*at, yz)
         rhs = rhs + (sigma * x - c)

@@ -10,8 +10,9 @@ checker on each case below, and writes
     tests/golden/reference_x.npz        primal vectors of the cases with n <= 2000
 The cases are the reference's known answers for this path (its tests and published harness)
 plus planted instances of the synthetic families.  tests/golden/reference_admm.npz holds the
-reference's ADMM (solve_qp_admm) after a few iterations on small constrained QPs (--only admm
-regenerates just that file).  QPLIB instances are read from the
+reference's ADMM (solve_qp_admm) after a few iterations on small constrained QPs and
+reference_admm_adapt.npz after 120-230 iterations, across its rho adaptation (--only admm
+regenerates just those two files).  QPLIB instances are read from the
 reference's datasets folder by the reference's own reader; only scalar results and the input
 file's SHA-256 are stored.
 """
@@ -125,7 +126,8 @@ def admm_case(seed, n, m, equality_rows):
 
 def make_admm_golden():
     """The reference's solve_qp_admm (src/qp_admm.cpp:118-280) after a few ADMM iterations (below its
-    first rho adaptation and polish) on small constrained QPs: tests/golden/reference_admm.npz."""
+    first rho adaptation and polish) on small constrained QPs: tests/golden/reference_admm.npz;
+    and after 120-230 iterations (across the rho adaptation): reference_admm_adapt.npz."""
     out = {}
     for name, (seed, n, m, eq, its, scaling) in {'admm_a': (7, 40, 25, 0, 20, True),
                                                   'admm_b': (8, 120, 60, 10, 12, True),
@@ -144,6 +146,24 @@ def make_admm_golden():
         out[f'{name}.x'] = x
         print(name, status, its, float(np.max(np.abs(x))), flush=True)
     np.savez_compressed(OUT / 'reference_admm.npz', **out)
+    # longer runs that cross the rho adaptation at iterations 100 and 200 (src/qp_admm.cpp:265-271),
+    # still below the first polish (250): tests/golden/reference_admm_adapt.npz
+    out = {}
+    for name, (seed, n, m, eq, its, scaling) in {'admm_f': (12, 60, 40, 0, 150, True),
+                                                  'admm_g': (13, 100, 70, 8, 230, True),
+                                                  'admm_h': (14, 50, 30, 4, 120, False),
+                                                  'admm_i': (15, 150, 90, 0, 210, True)}.items():
+        p = admm_case(seed, n, m, eq)
+        status, x, st = O.ref_solve_qp_admm(p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                            p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
+                                            tol=1e-12, iteration_limit=its, scaling=scaling)
+        assert status == 'iteration_limit' and int(st['iterations']) == its, (name, status, st)
+        out.update({f'{name}.{k}': np.asarray(v) for k, v in p.items()})
+        out[f'{name}.iterations'] = np.array(its)
+        out[f'{name}.scaling'] = np.array(1 if scaling else 0)
+        out[f'{name}.x'] = x
+        print(name, status, its, float(np.max(np.abs(x))), flush=True)
+    np.savez_compressed(OUT / 'reference_admm_adapt.npz', **out)
 
 
 OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),

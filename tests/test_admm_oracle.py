@@ -52,9 +52,9 @@ def test_restated_system_and_cg():
     assert inner0 == 0 and np.array_equal(x0, np.ones(n))
 
 
-def _golden_admm():
+def _golden_admm(file='reference_admm.npz'):
     from pathlib import Path
-    data = np.load(Path(__file__).resolve().parent / 'golden' / 'reference_admm.npz')
+    data = np.load(Path(__file__).resolve().parent / 'golden' / file)
     names = sorted({k.split('.')[0] for k in data.files})
     return [(name, {k.split('.', 1)[1]: data[k] for k in data.files if k.startswith(name + '.')}) for name in names]
 
@@ -74,6 +74,42 @@ def test_restated_admm_loop_matches_reference_golden():
             assert np.array_equal(x, p['x']), name
         else:
             assert np.max(np.abs(x - p['x'])) <= 1e-12, name
+
+
+def test_restated_admm_loop_with_rho_adaptation_matches_reference_golden():
+    """120-230 iterations, across the reference's rho adaptation at iterations 100 and 200
+    (qp_admm.cpp:265-271: residual-balanced rho_base, a new rho and preconditioner when it moves
+    by more than 5x): the restated loop reproduces solve_qp_admm's primal as above, and the
+    adaptation changes rho_base at least once in every case."""
+    from oracle.admm_pcg import solve_qp_admm_restated
+    exact = np.finfo(np.longdouble).nmant == 63
+    for name, p in _golden_admm('reference_admm_adapt.npz'):
+        info = {}
+        x = solve_qp_admm_restated(int(p['n']), p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                   p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'],
+                                   int(p['iterations']), scaling=bool(p['scaling']), info=info)
+        assert info['rho_base'][0] != 0.1, name
+        if exact:
+            assert np.array_equal(x, p['x']), name
+        else:
+            assert np.max(np.abs(x - p['x'])) <= 1e-12, name
+
+
+def test_restated_rho_adaptation_rule():
+    """adapt_rho keeps rho_base while the balanced candidate stays within a factor 5 and clamps it
+    to [1e-6, 1e6]: a case with Ax = z (no primal residual) drives it to the floor."""
+    from oracle.admm_pcg import AdmmSystemOracle, adapt_rho
+    n = 3
+    h = (np.array([0, 1, 2, 3], np.int32), np.array([0, 1, 2], np.int32), np.array([1.0, 1.0, 1.0]))
+    a = (np.array([0, 1, 2, 3], np.int32), np.array([0, 1, 2], np.int32), np.array([1.0, 1.0, 1.0]))
+    system = AdmmSystemOracle(h, a, n)
+    x = np.array([0.5, -0.25, 0.125])
+    sp = {'a': a, 'h': h, 'c': np.array([1.0, 0.0, -1.0])}
+    # primal 0 -> sqrt(1e-16 / dual) * rho_base is far below rho_base / 5
+    assert adapt_rho(sp, system, x, x.copy(), np.zeros(n), 0.1) == max(1e-6, 0.1 * np.sqrt(1e-16 / (1.5 / 2.0)))
+    # primal and dual residuals balanced: rho_base stays
+    z = x + np.array([1.5, 0.0, 0.0])
+    assert adapt_rho(sp, system, x, z, np.zeros(n), 0.1) == 0.1
 
 
 def test_restated_cg_stops_on_breakdown():
