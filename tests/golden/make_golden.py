@@ -175,8 +175,9 @@ OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'o
 
 def update_open_cases():
     """One-sided boxes (infinite lower or upper bounds on a share of the variables), fixed
-    variables (l = u), variables with no Hessian entries, and a one-variable problem, run by the
-    reference and merged into reference_cases.json / reference_x.npz."""
+    variables (l = u), variables with no Hessian entries, a one-variable problem and the planted
+    KKT box cases of the reference's scripts (planted_kkt_cases), run by the reference and merged
+    into reference_cases.json / reference_x.npz."""
     sys.path.insert(0, str(OUT.parent))
     from golden_cases import inputs
     d = json.loads((OUT / 'reference_cases.json').read_text())
@@ -197,8 +198,100 @@ def update_open_cases():
     d['cases'] = [c for c in d['cases'] if c['name'] != 'single_var'] + [rec]
     xs['single_var'] = x
     print('single_var', rec['status'], rec['iterations'], rec['objective'], x, flush=True)
+    for rec, x in planted_kkt_cases():
+        d['cases'] = [c for c in d['cases'] if c['name'] != rec['name']] + [rec]
+        xs[rec['name']] = x
     (OUT / 'reference_cases.json').write_text(json.dumps(d, indent=1) + '\n')
     np.savez_compressed(OUT / 'reference_x.npz', **xs)
+
+
+CHECK_KEYS = ('objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+              'relative_gap', 'verified')
+
+
+def check_cases():
+    """Candidates that probe the checker's edges (after the adversarial tests of the reference's
+    independent certificate, scripts/test_qp_certificate.py:17-49, restated for a box QP): each is
+    (name, problem, candidate x, maximize, offset, tol)."""
+    inf = float('inf')
+    nan = float('nan')
+
+    def prob(terms, c, lo, up):
+        return {'hrow': [t[0] for t in terms], 'hcol': [t[1] for t in terms], 'hval': [t[2] for t in terms],
+                'cost': c, 'lower': lo, 'upper': up}
+    diag2 = prob([(0, 0, 2.0), (1, 1, 2.0)], [-1.0, -1.0], [-1.0, -1.0], [1.0, 1.0])
+    concave = prob([(0, 0, -2.0), (1, 1, -2.0)], [2.0, 2.0], [-5.0, -5.0], [5.0, 5.0])
+    coupled = prob([(0, 0, 2.0), (1, 0, 1.0), (1, 1, 2.0)], [1.0, 1.0], [-inf, -inf], [inf, inf])
+    return [
+        # tiny curvature, huge box: the projected gradient is small, the separable dual bound is not
+        ('tiny_curvature_huge_box', prob([(0, 0, 1e-16), (1, 1, 1.0)], [0.0, 0.0], [-1e12, -1.0], [1e12, 1.0]),
+         [1e8, 0.0], False, 0.0, 1e-7),
+        ('diagonal_optimum', diag2, [0.5, 0.5], False, 0.0, 1e-7),
+        ('out_of_box', diag2, [2.0, 0.0], False, 0.0, 1e-7),
+        ('non_finite', diag2, [nan, 0.0], False, 0.0, 1e-7),
+        ('infinite_candidate', diag2, [inf, 0.0], False, 0.0, 1e-7),
+        # maximisation with an offset: the bound is reported in the minimisation sense
+        ('maximize_optimum', concave, [1.0, 1.0], True, 3.0, 1e-7),
+        ('maximize_nonstationary', concave, [0.5, 1.5], True, 3.0, 1e-7),
+        # coupled Hessian, free variables: tangent bound toward an infinite bound
+        ('coupled_free_near', coupled, [-1 / 3 + 1e-3, -1 / 3], False, 0.0, 1e-7),
+        ('coupled_free_optimum', coupled, [-1 / 3, -1 / 3], False, 0.0, 1e-7),
+        # a variable without curvature (no positive diagonal): verified by stationarity alone
+        ('linear_variable', prob([(1, 1, 1.0)], [1.0, -1.0], [0.0, 0.0], [1.0, 1.0]), [0.0, 1.0], False, 0.0, 1e-7),
+        ('one_sided_bounds', prob([(0, 0, 1.0), (1, 1, 1.0)], [1.0, -3.0], [0.0, -inf], [inf, 2.0]), [0.0, 2.0],
+         False, 0.0, 1e-7),
+        ('fixed_variable', prob([(0, 0, 1.0), (1, 0, 0.5), (1, 1, 1.0)], [0.0, -1.0], [0.25, -2.0], [0.25, 2.0]),
+         [0.25, 0.875], False, 0.0, 1e-7),
+    ]
+
+
+def make_check_golden():
+    """The reference's check_qp_solution (src/qp_admm.cpp:63-117) on check_cases():
+    tests/golden/reference_checks.json (non-finite numbers as the strings 'nan', 'inf', '-inf')."""
+    def enc(v):
+        return v if np.isfinite(v) else ('nan' if np.isnan(v) else ('inf' if v > 0 else '-inf'))
+    out = []
+    for name, p, x, maximize, offset, tol in check_cases():
+        st = O.ref_check(p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], np.array(x), tol=tol,
+                         maximize=maximize, offset=offset)
+        out.append({'name': name, 'problem': {k: [enc(v) for v in vs] for k, vs in p.items()},
+                    'x': [enc(v) for v in x], 'maximize': maximize, 'offset': offset, 'tol': tol,
+                    'result': {k: enc(st[k]) for k in CHECK_KEYS}})
+        print(name, {k: st[k] for k in CHECK_KEYS}, flush=True)
+    (OUT / 'reference_checks.json').write_text(json.dumps(out, indent=1) + '\n')
+
+
+def planted_kkt_cases():
+    """The box cases 0-14 of the reference's planted KKT tests (scripts/test_qp.py:30-56): n = 5,
+    H = R'R + I with R uniform in [-1, 1], x* uniform in [-1, 1], c = -H x*, box [-3, 3] (x* is
+    interior, so the expected objective is c'x* + x*'H x*/2), drawn from one random.Random(26121)
+    stream in the order the script draws them.  The script writes each as a QPLIB file for the
+    reference's CLI, which sends a box QP to solve_accelerated_box with the default options
+    (tolerance 1e-7); here the same lower-triangle terms go to it directly.  Each record keeps
+    the script's expected objective."""
+    import random
+    rng = random.Random(26121)
+    out = []
+    for case in range(15):
+        n = 5
+        r = [[rng.uniform(-1, 1) for _ in range(n)] for _ in range(n)]
+        h = [[sum(r[k][i] * r[k][j] for k in range(n)) + (1 if i == j else 0) for j in range(n)] for i in range(n)]
+        optimum = [rng.uniform(-1, 1) for _ in range(n)]
+        c = [-sum(h[i][j] * optimum[j] for j in range(n)) for i in range(n)]
+        expected = sum(c[i] * optimum[i] + .5 * sum(h[i][j] * optimum[i] * optimum[j] for j in range(n))
+                       for i in range(n))
+        terms = [(i, j, h[i][j]) for i in range(n) for j in range(i + 1) if h[i][j] != 0]
+        prob = {'hrow': np.array([t[0] for t in terms], np.int64), 'hcol': np.array([t[1] for t in terms], np.int64),
+                'hval': np.array([t[2] for t in terms]), 'cost': np.array(c), 'lower': np.full(n, -3.0),
+                'upper': np.full(n, 3.0)}
+        name = f'kkt5_{case:02d}'
+        rec, x = run_case(name, prob, dict(tol=1e-7))
+        rec['problem'] = {k: np.asarray(v).tolist() for k, v in prob.items()}
+        rec['expected_objective'] = expected
+        rec['planted_x'] = optimum
+        out.append((rec, x))
+        print(name, rec['status'], rec['iterations'], rec['objective'], expected, flush=True)
+    return out
 
 
 def main():
@@ -210,6 +303,7 @@ def main():
     if not O.build_reference(a.reference):
         raise SystemExit('cannot build oracle/_ref from ' + a.reference)
     make_admm_golden()
+    make_check_golden()
     if a.only == 'admm':
         return
     if a.only == 'open':

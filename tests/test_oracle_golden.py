@@ -5,6 +5,7 @@ the oracle must reproduce its statuses and iteration counts exactly and its prim
 for bit (both round every product and sum separately, in the same order).
 """
 import hashlib
+import json
 import math
 import os
 import platform
@@ -60,12 +61,38 @@ def test_edge_case_fixtures_have_their_analytic_answers(golden):
     assert np.array_equal(x[linear & (p['cost'] < 0)], p['upper'][linear & (p['cost'] < 0)])
 
 
-@pytest.mark.parametrize('idx', range(28))
-def test_oracle_matches_reference(golden, idx):
+CASE_NAMES = [c['name'] for c in json.loads((Path(__file__).resolve().parent / 'golden' /
+                                              'reference_cases.json').read_text())['cases']]
+
+
+def test_planted_kkt_cases_of_the_reference_scripts(golden):
+    """The 15 box cases of the reference's planted KKT tests (scripts/test_qp.py:30-56, n = 5, dense
+    PSD Hessian R'R + I, interior planted optimum): the reference's answers pass that script's own
+    criteria (status optimal, objective within 1e-6 relative of the planted one, projected-gradient
+    residual <= 2e-7, x inside [-3, 3])."""
     d, xs = golden
-    if idx >= len(d['cases']):
-        pytest.skip('fewer cases')
-    rec = d['cases'][idx]
+    recs = [c for c in d['cases'] if c['name'].startswith('kkt5_')]
+    assert len(recs) == 15
+    for rec in recs:
+        p, _ = inputs(rec)
+        x = xs[rec['name']]
+        n = len(x)
+        h = np.zeros((n, n))
+        h[p['hrow'], p['hcol']] = p['hval']
+        h = h + np.tril(h, -1).T
+        expected = rec['expected_objective']
+        assert rec['status'] == 'optimal'
+        assert abs(rec['objective'] - expected) / (1 + abs(expected)) <= 1e-6
+        g = h @ x + p['cost']
+        assert np.max(np.abs(x - np.clip(x - g, -3, 3)) / (1 + np.abs(x))) <= 2e-7
+        assert np.all((x >= -3) & (x <= 3))
+        assert np.max(np.abs(x - np.array(rec['planted_x']))) <= 1e-5
+
+
+@pytest.mark.parametrize('name', CASE_NAMES)
+def test_oracle_matches_reference(golden, name):
+    d, xs = golden
+    rec = next(c for c in d['cases'] if c['name'] == name)
     p, inst = inputs(rec)
     status, x, st = O.solve_box(*args(p), tol=rec['tol'], iteration_limit=rec['iteration_limit'], time_limit=600,
                                 threads=1, maximize=rec['maximize'], offset=rec['offset'])
@@ -133,6 +160,38 @@ def test_oracle_checker_agrees_with_reference_checker():
         b = O.ref_check(*args(p), x, tol=1e-6)
         for k in ('objective', 'primal_residual', 'stationarity_residual', 'dual_bound', 'relative_gap', 'verified'):
             assert a[k] == pytest.approx(b[k], rel=1e-15, abs=1e-300), k
+
+
+def _dec(v):
+    return float(v)
+
+
+def test_oracle_checker_reproduces_reference_edge_cases():
+    """The reference's check_qp_solution on candidates that probe the checker's edges
+    (tests/golden/reference_checks.json: tiny curvature on a huge box, out-of-box, NaN and infinite
+    candidates, maximisation with an offset, a coupled Hessian with infinite bounds, variables
+    without curvature, one-sided and fixed bounds): the oracle's checker returns every residual,
+    bound, gap and verdict the reference returned (bit for bit on x86, where long double is the
+    same 80-bit type; to 1e-15 elsewhere)."""
+    cases = json.loads((Path(__file__).resolve().parent / 'golden' / 'reference_checks.json').read_text())
+    assert len(cases) >= 12
+    for c in cases:
+        p = {k: np.array([_dec(v) for v in vs]) for k, vs in c['problem'].items()}
+        p['hrow'] = p['hrow'].astype(np.int64)
+        p['hcol'] = p['hcol'].astype(np.int64)
+        x = np.array([_dec(v) for v in c['x']])
+        st = O.check(*args(p), x, tol=c['tol'], maximize=c['maximize'], offset=c['offset'])
+        for k, v in c['result'].items():
+            want = _dec(v)
+            if math.isnan(want):
+                assert math.isnan(st[k]), (c['name'], k)
+            elif EXACT_HOST or not math.isfinite(want):
+                assert st[k] == want, (c['name'], k, st[k], want)
+            else:
+                assert st[k] == pytest.approx(want, rel=1e-15, abs=1e-300), (c['name'], k)
+    by = {c['name']: c['result'] for c in cases}
+    assert by['tiny_curvature_huge_box']['verified'] == 0 and by['tiny_curvature_huge_box']['stationarity_residual'] < 1e-7
+    assert by['maximize_optimum']['verified'] == 1 and by['maximize_optimum']['objective'] == 5.0
 
 
 def test_oracle_convexity_matches_reference(golden):
