@@ -3,8 +3,9 @@ from ._native import EngineError, LIB_PATH, Options, PlantedSpec, Stats, STATUS_
 from .api import (BoxIteration, Engine, QpOptions, QpResult, QuadraticProblem, check_convex_hessian,
                   csr_from_lower, cuda_device_name, default_engine, gershgorin, make_cuda_box, options_struct,
                   pinned, planted, planted_spec, problem_from_planted, solve_accelerated_box, splitmix64)
+from .admm import AdmmSystem, LinearRows, solve_qp_admm
 
-__all__ = ['BoxIteration', 'Engine', 'EngineError', 'LIB_PATH', 'Options', 'PlantedSpec', 'QpOptions', 'QpResult',
-           'QuadraticProblem', 'STATUS_NAMES', 'Stats', 'check_convex_hessian', 'csr_from_lower',
+__all__ = ['AdmmSystem', 'BoxIteration', 'Engine', 'EngineError', 'LIB_PATH', 'Options', 'PlantedSpec', 'QpOptions', 'QpResult',
+           'QuadraticProblem', 'LinearRows', 'STATUS_NAMES', 'Stats', 'check_convex_hessian', 'csr_from_lower',
            'cuda_device_name', 'default_engine', 'gershgorin', 'lib', 'make_cuda_box', 'options_struct', 'pinned', 'planted',
-           'planted_spec', 'problem_from_planted', 'solve_accelerated_box', 'splitmix64']
+           'planted_spec', 'problem_from_planted', 'solve_accelerated_box', 'solve_qp_admm', 'splitmix64']

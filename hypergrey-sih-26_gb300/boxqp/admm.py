@@ -1,15 +1,25 @@
-"""Host mirror of the constrained-QP ADMM inner solve on the GPU (C-ABI bqp_admm_*).
+"""Constrained-QP ADMM on the GPU: the device system (C-ABI bqp_admm_*) and the reference's
+solve_qp_admm loop around it.
 
-The reference's ADMM (02-software/solver/src/qp_admm.cpp:120-280) spends its iterations in the
+The reference's ADMM (02-software/solver/src/qp_admm.cpp:118-280) spends its iterations in the
 x-update's linear system K x = rhs, K = H + sigma I + A' diag(rho) A, solved by Jacobi-
 preconditioned CG (qp_admm.cpp:262-273).  AdmmSystem keeps H and A resident on the device and
-runs that inner solve there as one graph launch:
+runs that inner solve there as one graph launch, or whole ADMM iterations:
 
     s = AdmmSystem(h_rowptr, h_col, h_val, a_rowptr, a_col, a_val, n)
     s.set_rho(rho, sigma)                      # also forms the preconditioner
     x, inner, resid = s.solve(rhs, x0, accuracy, max_inner)
     x, z, y, inner = s.iterate(c, lo, up, x, z, y, first_iteration, iterations)   # whole ADMM steps
+
+solve_qp_admm(q, rows, options) is the reference's entry point over it: the scaled set-up
+(admm_setup), 25 iterations per device call, the original-model check of the primal and row
+duals every 25 iterations (check_solution, the reference's check_qp_solution with rows) and the
+rho adaptation every 100 (adapt_rho) on the host between calls.
 """
+import math
+import time
+from dataclasses import dataclass
+
 import numpy as np
 
 from . import _native as N
@@ -93,3 +103,379 @@ class AdmmSystem:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------------
+# the reference's solve_qp_admm around the device iterations
+# ------------------------------------------------------------------------------------------
+@dataclass
+class LinearRows:
+    """Linear rows row_lower <= A x <= row_upper of a QP (the reference's LinearProblem rows,
+    row_lower, row_upper, include/mps.hpp), A as CSR with m rows over the n variables.  Equal
+    bounds make an equality row; infinite ones a one-sided row."""
+    rowptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    lower: np.ndarray
+    upper: np.ndarray
+
+    @property
+    def m(self):
+        return int(np.asarray(self.rowptr).shape[0] - 1)
+
+
+def merge_rows(rowptr, col, val):
+    """CSR of rows given as (column, value) lists, as the reference's CsrMatrix(n, rows) forms it
+    (include/sparse_matrix.hpp:10-17): columns ascending, duplicates summed in input order, zero
+    results dropped."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    val = np.asarray(val, dtype=np.float64)
+    m = rowptr.shape[0] - 1
+    row = np.repeat(np.arange(m, dtype=np.int64), np.diff(rowptr))
+    order = np.lexsort((col, row))  # stable: equal (row, column) keys keep their input order
+    r, c, v = row[order], col[order], val[order]
+    first = np.ones(r.shape[0], dtype=bool)
+    first[1:] = (r[1:] != r[:-1]) | (c[1:] != c[:-1])
+    starts = np.flatnonzero(first)
+    sums = v[starts].copy()
+    sizes = np.diff(np.append(starts, r.shape[0]))
+    for g in np.flatnonzero(sizes > 1):  # duplicates: summed one after another, as a std::map entry
+        acc = 0.0
+        for k in range(starts[g], starts[g] + sizes[g]):
+            acc += v[k]
+        sums[g] = acc
+    keep = sums != 0
+    rr, cc, vv = r[starts][keep], c[starts][keep], sums[keep]
+    out_ptr = np.zeros(m + 1, dtype=np.int32)
+    np.cumsum(np.bincount(rr, minlength=m), out=out_ptr[1:])
+    return out_ptr, cc.astype(np.int32), vv
+
+
+def _row_of(rowptr):
+    return np.repeat(np.arange(len(rowptr) - 1), np.diff(np.asarray(rowptr, dtype=np.int64)))
+
+
+def row_sums(rowptr, terms, exact_rows=64):
+    """Per-row sums of CSR-ordered terms, in the terms' dtype, each row summed from 0 in entry
+    order (as the reference's loops sum them) when no row has more than `exact_rows` entries:
+    one entry position at a time across all rows.  Longer rows: numpy's blocked summation."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    out = np.zeros(rowptr.shape[0] - 1, dtype=terms.dtype)
+    if not len(terms):
+        return out
+    lens = np.diff(rowptr)
+    longest = int(lens.max())
+    if longest <= exact_rows:
+        for k in range(longest):
+            rows_k = np.flatnonzero(lens > k)
+            out[rows_k] += terms[rowptr[rows_k] + k]
+    else:
+        nz = np.flatnonzero(lens > 0)
+        out[nz] = np.add.reduceat(terms, rowptr[nz])
+    return out
+
+
+def csr_multiply(rowptr, col, val, v):
+    """A v (CsrMatrix::multiply, include/sparse_matrix.hpp:26-33: each row's products summed from 0
+    in entry order)."""
+    return row_sums(rowptr, np.asarray(val, dtype=np.float64) * v[np.asarray(col, dtype=np.int64)])
+
+
+def _clip(x, lo, up):
+    # max(lo, min(up, x)), elementwise
+    return np.maximum(lo, np.minimum(up, x))
+
+
+def _norm(v):
+    return float(np.max(np.abs(v))) if len(v) else 0.0
+
+
+def admm_setup(q, rows, scaling=True):
+    """The reference's set-up of solve_qp_admm (qp_admm.cpp:136-158) as arrays: the Hessian in
+    full CSR (sign-normalised for a maximisation), variable units 1/sqrt(H_jj) on a positive
+    diagonal, row scales 1/max|a_ij| of the unit-scaled rows, the bound rows x_j appended to A,
+    the cost scale 1/max(1, |c|), the scaled H, A, c and bounds, the initial x = clip(0) and
+    z = clip(A x), rho (0.1, x100 on rows with equal bounds) and sigma = 1e-8."""
+    from .api import csr_from_lower
+    n, m = q.n, rows.m
+    sign = -1.0 if q.maximize else 1.0
+    hrp, hci, hva = csr_from_lower(n, q.hessian_row, q.hessian_col, q.hessian_val, sign)
+    hrow = _row_of(hrp)
+    on_diag = hci == hrow
+
+    def diagonal_of(values):
+        d = np.zeros(n)
+        d[hrow[on_diag]] = values[on_diag]
+        return d
+
+    variable = np.ones(n)
+    diag0 = diagonal_of(hva)
+    if scaling:
+        pos = diag0 > 0
+        variable[pos] = 1 / np.sqrt(np.maximum(1e-16, diag0[pos]))
+    hva = hva * (variable[hrow] * variable[hci])
+    arp = np.asarray(rows.rowptr, dtype=np.int64)
+    acol = np.asarray(rows.col, dtype=np.int64)
+    aval = np.asarray(rows.val, dtype=np.float64) * variable[acol]
+    arow = _row_of(arp)
+    maximum = np.zeros(m)
+    np.maximum.at(maximum, arow, np.abs(aval))
+    row_scale = np.ones(m + n)
+    if scaling:
+        row_scale[:m] = np.where(maximum > 0, 1 / np.where(maximum > 0, maximum, 1.0), 1.0)
+    aval = aval * row_scale[arow]
+    lo = np.concatenate([np.asarray(rows.lower, dtype=np.float64) * row_scale[:m],
+                         np.asarray(q.lower, dtype=np.float64) / variable])
+    up = np.concatenate([np.asarray(rows.upper, dtype=np.float64) * row_scale[:m],
+                         np.asarray(q.upper, dtype=np.float64) / variable])
+    c = np.asarray(q.cost, dtype=np.float64) * (sign * variable)
+    cost_scale = 1 / max(1.0, _norm(c)) if scaling else 1.0
+    hva = hva * cost_scale
+    c = c * cost_scale
+    a_ptr, a_col, a_val = merge_rows(np.concatenate([arp, arp[-1] + 1 + np.arange(n)]),
+                                     np.concatenate([acol, np.arange(n)]), np.concatenate([aval, np.ones(n)]))
+    x = _clip(np.zeros(n), lo[m:], up[m:])
+    z = _clip(csr_multiply(a_ptr, a_col, a_val, x), lo, up)
+    rho_base = 0.1
+    return {'n': n, 'm': m, 'h': (hrp, hci, hva), 'a': (a_ptr, a_col, a_val), 'c': c, 'lo': lo, 'up': up,
+            'variable': variable, 'row_scale': row_scale, 'cost_scale': cost_scale, 'sign': sign,
+            'rho_base': rho_base, 'rho': np.where(lo == up, rho_base * 100, rho_base * 1), 'sigma': 1e-8,
+            'x': x, 'z': z, 'y': np.zeros(m + n)}
+
+
+def transpose(rowptr, col, val, n):
+    """A' in CSR (rows of A' list the rows of A in increasing order)."""
+    row = _row_of(rowptr)
+    order = np.argsort(np.asarray(col, dtype=np.int64), kind='stable')
+    tp = np.zeros(n + 1, dtype=np.int32)
+    np.cumsum(np.bincount(np.asarray(col, dtype=np.int64), minlength=n), out=tp[1:])
+    return tp, row[order].astype(np.int32), np.asarray(val)[order]
+
+
+def adapt_rho(sp, x, z, y, rho_base, at=None):
+    """The reference's rho adaptation (qp_admm.cpp:265-271): primal residual max|Ax - z| /
+    (1 + max(|Ax|, |z|)), dual residual max|Hx + c + A'y| / (1 + max(|c|, |Hx|, |A'y|)); the
+    candidate rho_base sqrt(primal / dual) (both floored at 1e-16, the result clamped to
+    [1e-6, 1e6]) replaces rho_base only when it leaves [rho_base / 5, 5 rho_base]."""
+    if at is None:
+        at = transpose(*sp['a'], sp['n'])
+    ax = csr_multiply(*sp['a'], x)
+    hx = csr_multiply(*sp['h'], x)
+    aty = csr_multiply(*at, y)
+    primal = _norm(ax - z) / (1 + max(_norm(ax), _norm(z)))
+    dual = _norm(hx + sp['c'] + aty) / (1 + max(_norm(sp['c']), max(_norm(hx), _norm(aty))))
+    nxt = max(1e-6, min(1e6, rho_base * math.sqrt(max(1e-16, primal) / max(1e-16, dual))))
+    return nxt if (nxt > 5 * rho_base or nxt < rho_base / 5) else rho_base
+
+
+def original_violation(q, rows, x):
+    """Largest bound violation of x and of the row activities A x, each scaled by
+    1 + |bound| + |x_j| (variables) or 1 + |bound| + sum_k |a_ik x_k| (rows) (the reference's
+    original_violation(p, x, true), src/mps.cpp:279-303); infinite for a non-finite x or
+    activity.  Activities are summed in long double."""
+    x = np.asarray(x, dtype=np.float64)
+    if not np.all(np.isfinite(x)):
+        return math.inf
+    result = 0.0
+    xl = x.astype(np.longdouble)
+    for bound, lower in ((np.asarray(q.lower, dtype=np.float64), True), (np.asarray(q.upper, dtype=np.float64), False)):
+        fin = np.isfinite(bound)
+        if fin.any():
+            v = (bound[fin] - xl[fin]) if lower else (xl[fin] - bound[fin])
+            result = max(result, float(np.max((v / (1 + np.abs(bound[fin]) + np.abs(xl[fin]))).astype(np.float64))))
+    m = rows.m if rows is not None else 0
+    if m:
+        rp = np.asarray(rows.rowptr, dtype=np.int64)
+        term = np.asarray(rows.val, dtype=np.longdouble) * x[np.asarray(rows.col, dtype=np.int64)]
+        act = row_sums(rp, term)
+        scale = row_sums(rp, np.abs(term))
+        if not np.all(np.isfinite(act)):
+            return math.inf
+        for bound, lower in ((np.asarray(rows.lower, dtype=np.float64), True),
+                             (np.asarray(rows.upper, dtype=np.float64), False)):
+            fin = np.isfinite(bound)
+            if fin.any():
+                v = (bound[fin] - act[fin]) if lower else (act[fin] - bound[fin])
+                result = max(result, float(np.max((v / (1 + np.abs(bound[fin]) + scale[fin])).astype(np.float64))))
+    return result
+
+
+def check_solution(q, rows, x, row_dual, tol):
+    """The reference's check_qp_solution (src/qp_admm.cpp:63-117) of a primal x and row duals on
+    the ORIGINAL problem: objective (long double), scaled primal violation, projected-gradient
+    stationarity of H x + c + A' y, complementarity |y_i (a_i x - target_i)| / (1 + |f|), the
+    tangent dual bound (or the separable one when the Hessian is diagonal with a positive
+    diagonal), the relative gap, and verified = max(primal, stationarity, complementarity) <= tol
+    (and gap <= tol for the separable bound).  Returns a dict of those fields."""
+    sign = -1.0 if q.maximize else 1.0
+    n = q.n
+    m = rows.m if rows is not None else 0
+    out = {'objective': math.nan, 'primal_residual': math.inf, 'stationarity_residual': math.inf,
+           'complementarity_residual': math.inf, 'dual_bound': -math.inf, 'relative_gap': math.inf,
+           'verified': False}
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(row_dual, dtype=np.float64)
+    if x.shape != (n,) or y.shape != (m,) or not np.all(np.isfinite(x)) or not np.all(np.isfinite(y)):
+        return out
+    hr = np.asarray(q.hessian_row, dtype=np.int64)
+    hc = np.asarray(q.hessian_col, dtype=np.int64)
+    hv = np.asarray(q.hessian_val, dtype=np.float64)
+    cost = np.asarray(q.cost, dtype=np.float64)
+    lower = np.asarray(q.lower, dtype=np.float64)
+    upper = np.asarray(q.upper, dtype=np.float64)
+    off = hr != hc
+    # gradient scatter in the reference's order: (row, col), then the mirror of an off-diagonal term
+    idx = np.stack([hr, np.where(off, hc, -1)], axis=1).ravel()
+    contrib = np.stack([sign * hv * x[hc], sign * hv * x[hr]], axis=1).ravel()
+    sel = idx >= 0
+    gradient = np.zeros(n)
+    np.add.at(gradient, idx[sel], contrib[sel])
+    positive_diagonal = not np.any(hv[off] != 0)
+    diagonal = linear = None
+    if positive_diagonal:
+        diagonal = np.zeros(n, dtype=np.longdouble)
+        np.add.at(diagonal, hr[~off], (sign * hv[~off]).astype(np.longdouble))
+        positive_diagonal = bool(np.all(diagonal > 0))
+        if positive_diagonal:
+            linear = (sign * cost).astype(np.longdouble)
+    xl = x.astype(np.longdouble)
+    terms = np.longdouble(0.5) * xl * gradient.astype(np.longdouble) + (sign * cost * x).astype(np.longdouble)
+    value = np.cumsum(np.concatenate([[np.longdouble(sign * q.offset)], terms]))[-1]
+    gradient = gradient + sign * cost
+    out['objective'] = sign * float(value)
+    out['primal_residual'] = original_violation(q, rows, x)
+    complementarity = 0.0
+    bound = value
+    dual_constant = np.longdouble(sign * q.offset)
+    if m:
+        rp = np.asarray(rows.rowptr, dtype=np.int64)
+        col = np.asarray(rows.col, dtype=np.int64)
+        val = np.asarray(rows.val, dtype=np.float64)
+        row = _row_of(rp)
+        np.add.at(gradient, col, val * y[row])
+        if positive_diagonal:
+            np.add.at(linear, col, val.astype(np.longdouble) * y[row])
+        act = row_sums(rp, val.astype(np.longdouble) * x[col])
+        target = np.where(y >= 0, np.asarray(rows.upper, dtype=np.float64), np.asarray(rows.lower, dtype=np.float64))
+        act_rows = np.flatnonzero(y != 0)
+        if len(act_rows):
+            yl = y[act_rows].astype(np.longdouble)
+            dual_constant = np.cumsum(np.concatenate([[dual_constant], -yl * target[act_rows]]))[-1]
+            corr = yl * (act[act_rows] - target[act_rows])
+            bound = np.cumsum(np.concatenate([[bound], corr]))[-1]
+            with np.errstate(invalid='ignore', over='ignore'):
+                res = (np.abs(corr) / (1 + abs(value))).astype(np.float64)
+            res[~np.isfinite(res)] = math.inf
+            complementarity = float(np.max(res))
+    out['complementarity_residual'] = complementarity
+    with np.errstate(invalid='ignore', over='ignore'):
+        res = np.abs(x - _clip(x - gradient, lower, upper)) / (1 + np.abs(x))
+    res[~np.isfinite(gradient) | ~np.isfinite(res)] = math.inf
+    out['stationarity_residual'] = float(np.max(res)) if n else 0.0
+    # tangent affine underestimator over the box
+    g = gradient
+    nzg = g != 0
+    tgt = np.where(g > 0, lower, upper)
+    if np.any(nzg & ~np.isfinite(tgt)):
+        bound = np.longdouble(-np.inf)
+    else:
+        bound = np.cumsum(np.concatenate([[bound], (g[nzg] * (tgt[nzg] - x[nzg])).astype(np.longdouble)]))[-1]
+    if positive_diagonal:
+        mn = np.maximum(lower.astype(np.longdouble), np.minimum(upper.astype(np.longdouble), -linear / diagonal))
+        bound = np.cumsum(np.concatenate([[dual_constant],
+                                          np.longdouble(0.5) * diagonal * mn * mn + linear * mn]))[-1]
+    out['dual_bound'] = float(bound)
+    out['relative_gap'] = float(abs(value - bound) / (1 + abs(value))) if np.isfinite(bound) else math.inf
+    verified = math.isfinite(out['objective']) and max(out['primal_residual'], out['stationarity_residual'],
+                                                       out['complementarity_residual']) <= tol
+    if positive_diagonal:
+        verified = verified and out['relative_gap'] <= tol
+    out['verified'] = bool(verified)
+    return out
+
+
+def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
+    """The reference's solve_qp_admm (qp_admm.cpp:118-280) with its iterations on the GPU.
+
+    Mirrors its option and input checks (ValueError 'Invalid QP options' / 'Continuous QP
+    required'), the statuses unsupported_curvature and infeasible_bounds, the scaled set-up, the
+    check of the original model every 25 iterations and at the limit (optimal once verified,
+    numerical_error on a non-finite objective or stationarity, time_limit), and the rho adaptation
+    every 100 iterations; each 25 iterations run on the device in one bqp_admm_iterate call.
+    Not mirrored: the diagonal-Hessian equality solver tried first (qp_dual_newton.cpp), the
+    KKT polish at iterations 250, 1000 and 5000 (its sparse LU), and the time check inside the
+    inner CG.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
+    as CSR triples; the system needs set_rho, iterate and close)."""
+    from .api import QpOptions, QpResult, check_convex_hessian
+    o = options or QpOptions()
+    if (not math.isfinite(o.time_limit) or o.time_limit < 0 or not math.isfinite(o.tolerance) or o.tolerance <= 0
+            or o.threads < 1):
+        raise ValueError('Invalid QP options')
+    start = time.monotonic()
+    if q.integer is not None and np.any(np.asarray(q.integer)):
+        raise ValueError('Continuous QP required')
+    n, m = q.n, rows.m
+    for name, arr, size in (('cost', q.cost, n), ('lower', q.lower, n), ('upper', q.upper, n),
+                            ('row_lower', rows.lower, m), ('row_upper', rows.upper, m)):
+        if np.asarray(arr).shape != (size,):
+            raise ValueError(f'{name} has the wrong size')
+    result = QpResult(algorithm='scaled_admm_pcg')
+    if not check_convex_hessian(q):
+        result.status = 'unsupported_curvature'
+        return result
+    if np.any(np.asarray(q.lower) > np.asarray(q.upper)) or np.any(np.asarray(rows.lower) > np.asarray(rows.upper)):
+        result.status = 'infeasible_bounds'
+        return result
+    sp = admm_setup(q, rows, o.scaling)
+    at = transpose(*sp['a'], n)
+    if make_system is None:
+        system = AdmmSystem(*sp['h'], *sp['a'], n, device)
+    else:
+        system = make_system(sp['h'], sp['a'], n)
+    try:
+        system.set_rho(sp['rho'], sp['sigma'])
+        x, z, y = sp['x'], sp['z'], sp['y']
+        rho_base = sp['rho_base']
+        dual_scale = sp['row_scale'][:m] / sp['cost_scale']
+        limit = int(o.iteration_limit)
+        inner_total = 0
+        result.status = 'iteration_limit'
+        it = 0
+        while True:
+            result.iterations = it
+            if it % 25 == 0 or it == limit:
+                result.primal = x * sp['variable']
+                result.row_dual = y[:m] * dual_scale
+                chk = check_solution(q, rows, result.primal, result.row_dual, o.tolerance)
+                result.objective = chk['objective']
+                result.primal_residual = chk['primal_residual']
+                result.stationarity_residual = chk['stationarity_residual']
+                result.complementarity_residual = chk['complementarity_residual']
+                result.dual_bound = chk['dual_bound']
+                result.relative_gap = chk['relative_gap']
+                result.optimality_verified = chk['verified']
+                if chk['verified']:
+                    result.status = 'optimal'
+                    break
+                if not math.isfinite(chk['objective']) or not math.isfinite(chk['stationarity_residual']):
+                    result.status = 'numerical_error'
+                    break
+                if time.monotonic() - start >= o.time_limit:
+                    result.status = 'time_limit'
+                    break
+                if it and it % 100 == 0:
+                    nxt = adapt_rho(sp, x, z, y, rho_base, at)
+                    if nxt != rho_base:
+                        rho_base = nxt
+                        system.set_rho(np.where(sp['lo'] == sp['up'], rho_base * 100, rho_base * 1), sp['sigma'])
+            if it == limit:
+                break
+            k = min(25 - it % 25, limit - it)
+            x, z, y, inner = system.iterate(sp['c'], sp['lo'], sp['up'], x, z, y, it, k)
+            inner_total += int(inner)
+            it += k
+        result.engine = {'inner_iterations': inner_total, 'rho_base': rho_base, 'seconds': time.monotonic() - start}
+        return result
+    finally:
+        system.close()

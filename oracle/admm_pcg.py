@@ -232,7 +232,6 @@ def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_
     sys_ = AdmmSystemOracle((hrp, hci, hva), (arp, aci, ava), n)
     sys_.set_rho(rho, sigma)
     x, z, y = sp['x'], sp['z'], sp['y']
-    at = sys_.at
     rho_base = 0.1
     for iteration in range(iteration_limit):
         if iteration and iteration % 100 == 0:
@@ -243,19 +242,34 @@ def solve_qp_admm_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_
                 rho_base = nxt
                 rho = np.where(lo_all == up_all, rho_base * 100, rho_base * 1)
                 sys_.set_rho(rho, sigma)
-        yz = rho * z - y
-        rhs = csr_matvec(*at, yz)
-        rhs = rhs + (sigma * x - c)
-        accuracy = min(1e-7, .05 / (iteration + 1) ** 1.6) * (1 + float(np.max(np.abs(rhs))))
-        max_inner = min(4000, 2 * n + 20)
-        if inner is None:
-            nxt, _, _ = sys_.solve(rhs, x, accuracy, max_inner)
-        else:
-            nxt = inner(((hrp, hci, hva), (arp, aci, ava), rho, sigma), rhs, x, accuracy, max_inner)
-        ax = csr_matvec(arp, aci, ava, nxt)
-        relaxed = 1.6 * ax - .6 * z
-        nz = _clip(relaxed + y / rho, lo_all, up_all)
-        y = y + rho * (relaxed - nz)
-        z = nz
-        x = 1.6 * nxt - .6 * x
+        solve = None
+        if inner is not None:
+            def solve(rhs, x0, accuracy, max_inner, rho=rho):
+                return inner(((hrp, hci, hva), (arp, aci, ava), rho, sigma), rhs, x0, accuracy, max_inner), 0
+        x, z, y, _ = admm_iteration(sys_, c, lo_all, up_all, x, z, y, iteration, solve)
     return x * sp['variable']
+
+
+def admm_iteration(system, c, lo, up, x, z, y, iteration, solve=None):
+    """One iteration of the reference's ADMM loop (qp_admm.cpp:255-279) on the scaled problem, with
+    system's rho and sigma (AdmmSystemOracle after set_rho): rhs = A'(rho z - y) + (sigma x - c),
+    the inner accuracy min(1e-7, 0.05 / (iteration + 1)^1.6) (1 + max|rhs|) and limit
+    min(4000, 2n + 20), the inner PCG from x, then the relaxed (1.6) z and y updates and
+    x = 1.6 next - 0.6 x.  solve(rhs, x0, accuracy, max_inner) -> (next, inner) replaces the
+    restated PCG when given.  Returns (x, z, y, inner iterations)."""
+    rho, sigma = system.rho, system.sigma
+    n = system.n
+    yz = rho * z - y
+    rhs = csr_matvec(*system.at, yz)
+    rhs = rhs + (sigma * x - c)
+    accuracy = min(1e-7, .05 / (iteration + 1) ** 1.6) * (1 + float(np.max(np.abs(rhs))))
+    max_inner = min(4000, 2 * n + 20)
+    if solve is None:
+        nxt, inner, _ = system.solve(rhs, x, accuracy, max_inner)
+    else:
+        nxt, inner = solve(rhs, x, accuracy, max_inner)
+    ax = csr_matvec(*system.a, nxt)
+    relaxed = 1.6 * ax - .6 * z
+    nz = _clip(relaxed + y / rho, lo, up)
+    y = y + rho * (relaxed - nz)
+    return 1.6 * nxt - .6 * x, nz, y, inner

@@ -179,7 +179,11 @@ def ref():
         L.ref_solve_qp_admm.restype = c_int
         L.ref_solve_qp_admm.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int64,
                                         POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, c_double, c_int64,
-                                        c_double, c_int, _F64P, _F64P, c_char_p, c_int]
+                                        c_double, c_int, _F64P, _F64P, _F64P, c_char_p, c_int]
+        L.ref_check_rows.restype = c_int
+        L.ref_check_rows.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double,
+                                     c_int64, POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, _F64P, _F64P,
+                                     c_double, _F64P]
         L.ref_check.restype = c_int
         L.ref_check.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double, _F64P,
                                 c_double, _F64P]
@@ -337,20 +341,45 @@ def ref_solve_qp_admm(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_v
     row_upper = np.ascontiguousarray(row_upper, np.float64)
     n, m = cost.shape[0], a_rowptr.shape[0] - 1
     x = np.zeros(n)
+    row_dual = np.zeros(m)
     stats = np.zeros(8)
     msg = ctypes.create_string_buffer(256)
     rc = ref().ref_solve_qp_admm(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
                                  _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), m,
                                  _p(a_rowptr, c_int32), _p(a_col, c_int32), _p(a_val, c_double),
                                  _p(row_lower, c_double), _p(row_upper, c_double), float(tol), int(iteration_limit),
-                                 float(time_limit), 1 if scaling else 0, _p(x, c_double), _p(stats, c_double), msg, 256)
+                                 float(time_limit), 1 if scaling else 0, _p(x, c_double), _p(row_dual, c_double),
+                                 _p(stats, c_double), msg, 256)
     if rc == 1:
         raise ValueError(msg.value.decode())
     if rc != 0:
         raise RuntimeError(msg.value.decode())
     keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
             'relative_gap', 'verified', 'iterations']
-    return msg.value.decode(), x, dict(zip(keys, stats.tolist()))
+    st = dict(zip(keys, stats.tolist()))
+    st['row_dual'] = row_dual
+    return msg.value.decode(), x, st
+
+
+def ref_check_rows(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper, x, row_dual,
+                   tol=1e-7, maximize=False, offset=0.0):
+    """The reference's check_qp_solution (src/qp_admm.cpp:63-117) on a problem with linear rows."""
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    a_rowptr = np.ascontiguousarray(a_rowptr, np.int32)
+    a_col = np.ascontiguousarray(a_col, np.int32)
+    a_val, row_lower, row_upper, x, row_dual = (np.ascontiguousarray(v, np.float64)
+                                                for v in (a_val, row_lower, row_upper, x, row_dual))
+    stats = np.zeros(8)
+    rc = ref().ref_check_rows(cost.shape[0], hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64), _p(hval, c_double),
+                              _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), int(maximize),
+                              float(offset), a_rowptr.shape[0] - 1, _p(a_rowptr, c_int32), _p(a_col, c_int32),
+                              _p(a_val, c_double), _p(row_lower, c_double), _p(row_upper, c_double),
+                              _p(x, c_double), _p(row_dual, c_double), float(tol), _p(stats, c_double))
+    if rc != 0:
+        raise RuntimeError('reference checker failed')
+    keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+            'relative_gap', 'verified']
+    return dict(zip(keys, stats.tolist()))
 
 
 def ref_check(hrow, hcol, hval, cost, lower, upper, x, tol=1e-7, maximize=False, offset=0.0):

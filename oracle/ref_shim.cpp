@@ -98,7 +98,7 @@ int ref_solve_qp_admm(int64_t n, int64_t nh, const int64_t* hrow, const int64_t*
                       const double* cost, const double* lower, const double* upper, int64_t m,
                       const int32_t* a_rowptr, const int32_t* a_col, const double* a_val, const double* row_lower,
                       const double* row_upper, double tol, int64_t iteration_limit, double time_limit, int scaling,
-                      double* x_out, double* stats, char* status_out, int status_cap) {
+                      double* x_out, double* row_dual_out, double* stats, char* status_out, int status_cap) {
     try {
         auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, 0, 0.0);
         auto& p = q.linear;
@@ -117,6 +117,9 @@ int ref_solve_qp_admm(int64_t n, int64_t nh, const int64_t* hrow, const int64_t*
         auto r = sovereign::solve_qp_admm(q, o);
         fill_stats(r, stats);
         for (std::size_t j = 0; j < r.primal.size() && j < static_cast<std::size_t>(n); ++j) x_out[j] = r.primal[j];
+        if (row_dual_out)
+            for (std::size_t i = 0; i < r.row_dual.size() && i < static_cast<std::size_t>(m); ++i)
+                row_dual_out[i] = r.row_dual[i];
         put_message(status_out, static_cast<std::size_t>(status_cap), r.status);
         return 0;
     } catch (const std::invalid_argument& e) {
@@ -124,6 +127,33 @@ int ref_solve_qp_admm(int64_t n, int64_t nh, const int64_t* hrow, const int64_t*
         return 1;
     } catch (const std::exception& e) {
         put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
+        return 2;
+    }
+}
+
+// Runs the reference checker on a caller-supplied primal and row duals of a problem with linear
+// rows (A in CSR, row_lower <= A x <= row_upper).
+int ref_check_rows(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol, const double* hval,
+                   const double* cost, const double* lower, const double* upper, int maximize, double offset,
+                   int64_t m, const int32_t* a_rowptr, const int32_t* a_col, const double* a_val,
+                   const double* row_lower, const double* row_upper, const double* x, const double* row_dual,
+                   double tol, double* stats) {
+    try {
+        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, maximize, offset);
+        auto& p = q.linear;
+        p.rows.resize(static_cast<std::size_t>(m));
+        for (int64_t i = 0; i < m; ++i)
+            for (int32_t k = a_rowptr[i]; k < a_rowptr[i + 1]; ++k)
+                p.rows[static_cast<std::size_t>(i)].push_back({static_cast<std::size_t>(a_col[k]), a_val[k]});
+        p.row_lower.assign(row_lower, row_lower + m);
+        p.row_upper.assign(row_upper, row_upper + m);
+        sovereign::QpResult r;
+        r.primal.assign(x, x + n);
+        r.row_dual.assign(row_dual, row_dual + m);
+        sovereign::check_qp_solution(q, r, tol);
+        fill_stats(r, stats);
+        return 0;
+    } catch (...) {
         return 2;
     }
 }

@@ -164,6 +164,41 @@ def make_admm_golden():
         out[f'{name}.x'] = x
         print(name, status, its, float(np.max(np.abs(x))), flush=True)
     np.savez_compressed(OUT / 'reference_admm_adapt.npz', **out)
+    make_admm_solve_golden()
+
+
+ADMM_SOLVE_CASES = {'solve_20': (20, 60, 40, 0, 1e-6), 'solve_21': (21, 100, 70, 8, 1e-6),
+                    'solve_22': (22, 50, 30, 4, 1e-5), 'solve_23': (23, 150, 90, 0, 1e-5),
+                    'solve_26': (26, 50, 30, 4, 1e-4), 'solve_29': (29, 100, 70, 8, 1e-6)}
+
+
+def make_admm_solve_golden():
+    """The reference's whole solve_qp_admm (src/qp_admm.cpp:118-280, scaled, default limits) on
+    constrained QPs that it verifies before its first polish: status, iterations, primal, row
+    duals and the checker's fields; and its check_qp_solution on candidates around each answer
+    (the answer, a perturbed primal, zero row duals): tests/golden/reference_admm_solve.npz."""
+    out = {}
+    for name, (seed, n, m, eq, tol) in ADMM_SOLVE_CASES.items():
+        p = admm_case(seed, n, m, eq)
+        a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'],
+             p['a_val'], p['row_lower'], p['row_upper'])
+        status, x, st = O.ref_solve_qp_admm(*a, tol=tol, iteration_limit=200000, time_limit=600.0, scaling=True)
+        assert status == 'optimal' and st['iterations'] < 250, (name, status, st)
+        out.update({f'{name}.{k}': np.asarray(v) for k, v in p.items()})
+        out[f'{name}.tol'] = np.array(tol)
+        out[f'{name}.iterations'] = np.array(int(st['iterations']))
+        out[f'{name}.x'] = x
+        out[f'{name}.row_dual'] = st['row_dual']
+        out[f'{name}.stats'] = np.array([st[k] for k in CHECK_KEYS])
+        rng = np.random.default_rng(seed)
+        cands = [(x, st['row_dual']), (x + 1e-3 * rng.standard_normal(n), st['row_dual']), (x, np.zeros(m))]
+        for k, (cx, cy) in enumerate(cands):
+            chk = O.ref_check_rows(*a, cx, cy, tol=tol)
+            out[f'{name}.cand{k}_x'] = cx
+            out[f'{name}.cand{k}_y'] = cy
+            out[f'{name}.cand{k}_stats'] = np.array([chk[k2] for k2 in CHECK_KEYS])
+        print(name, status, int(st['iterations']), st['objective'], flush=True)
+    np.savez_compressed(OUT / 'reference_admm_solve.npz', **out)
 
 
 OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),

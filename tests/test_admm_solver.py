@@ -1,0 +1,197 @@
+"""The reference's solve_qp_admm loop around the device iterations (boxqp/admm.py), without a GPU.
+
+The host side of solve_qp_admm (the scaled set-up, the original-model check with row duals, the
+rho adaptation, the 25-iteration cadence and the statuses) is checked against the reference
+itself: its set-up against the restatement pinned in tests/test_admm_oracle.py, its checker
+against the reference's check_qp_solution on constrained candidates, and the whole loop, driven
+by the restated iterations (oracle/admm_pcg.py) in place of the device, against the reference's
+own solve_qp_admm answers (tests/golden/reference_admm_solve.npz, made by
+tests/golden/make_golden.py from the reference built in oracle/_ref).
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import boxqp
+from boxqp.admm import LinearRows, admm_setup, check_solution, merge_rows, solve_qp_admm
+from oracle.admm_pcg import AdmmSystemOracle, admm_iteration, scale_qp_admm
+
+GOLDEN = Path(__file__).resolve().parent / 'golden'
+KEYS = ('objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+        'relative_gap', 'verified')
+EXACT = np.finfo(np.longdouble).nmant == 63  # x87 80-bit long double, the reference's on x86
+
+
+def _cases(file):
+    data = np.load(GOLDEN / file)
+    names = sorted({k.split('.')[0] for k in data.files})
+    return [(name, {k.split('.', 1)[1]: data[k] for k in data.files if k.startswith(name + '.')}) for name in names]
+
+
+def _problem(p):
+    q = boxqp.QuadraticProblem(cost=p['cost'], lower=p['lower'], upper=p['upper'], hessian_row=p['hrow'],
+                               hessian_col=p['hcol'], hessian_val=p['hval'])
+    rows = LinearRows(p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'])
+    return q, rows
+
+
+class RestatedSystem:
+    """The restated ADMM iterations (oracle/admm_pcg.py, bit for bit the reference's) behind the
+    device system's interface."""
+
+    def __init__(self, h, a, n):
+        self.o = AdmmSystemOracle(h, a, n)
+        self.rho_changes = 0
+
+    def set_rho(self, rho, sigma):
+        self.rho_changes += 1
+        self.o.set_rho(rho, sigma)
+
+    def iterate(self, c, lo, up, x, z, y, first, count):
+        total = 0
+        for k in range(count):
+            x, z, y, inner = admm_iteration(self.o, c, lo, up, x, z, y, first + k)
+            total += inner
+        return x, z, y, total
+
+    def close(self):
+        pass
+
+
+def _same(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b))
+
+
+def test_setup_equals_the_restated_setup():
+    """admm_setup (vectorised) forms the scaled problem of qp_admm.cpp:136-158 with the same bits as
+    the loop-by-loop restatement pinned to the reference."""
+    for file in ('reference_admm.npz', 'reference_admm_adapt.npz', 'reference_admm_solve.npz'):
+        for name, p in _cases(file):
+            scaling = bool(p['scaling']) if 'scaling' in p else True
+            q, rows = _problem(p)
+            sp = admm_setup(q, rows, scaling)
+            ref = scale_qp_admm(int(p['n']), p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
+                                p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'], scaling)
+            for k in ('c', 'lo', 'up', 'variable', 'x', 'z', 'y', 'rho'):
+                assert _same(sp[k], ref[k]), (name, k)
+            for k in ('h', 'a'):
+                for u, v in zip(sp[k], ref[k]):
+                    assert _same(u, v), (name, k)
+            assert sp['sigma'] == ref['sigma']
+
+
+def test_merge_rows_follows_csrmatrix():
+    """Rows with unsorted and repeated columns: ascending columns, repeats summed in input order,
+    zero sums dropped (CsrMatrix(n, rows), include/sparse_matrix.hpp:10-17)."""
+    rowptr = np.array([0, 4, 4, 7])
+    col = np.array([3, 1, 3, 0, 2, 2, 5])
+    val = np.array([0.1, 2.0, 0.2, -1.0, 1.5, -1.5, 4.0])
+    rp, c, v = merge_rows(rowptr, col, val)
+    assert rp.tolist() == [0, 3, 3, 4]
+    assert c.tolist() == [0, 1, 3, 5]
+    assert v.tolist() == [-1.0, 2.0, 0.1 + 0.2, 4.0]
+
+
+def test_checker_matches_the_reference_on_box_edge_cases():
+    """check_solution with no rows returns the reference's check_qp_solution fields on the box
+    candidates of tests/golden/reference_checks.json."""
+    for c in json.loads((GOLDEN / 'reference_checks.json').read_text()):
+        p = {k: np.array([float(v) for v in vs]) for k, vs in c['problem'].items()}
+        q = boxqp.QuadraticProblem(cost=p['cost'], lower=p['lower'], upper=p['upper'],
+                                   hessian_row=p['hrow'].astype(np.int64), hessian_col=p['hcol'].astype(np.int64),
+                                   hessian_val=p['hval'], maximize=c['maximize'], offset=c['offset'])
+        rows = LinearRows(np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), np.zeros(0))
+        got = check_solution(q, rows, np.array([float(v) for v in c['x']]), np.zeros(0), c['tol'])
+        for k in KEYS:
+            want = float(c['result'][k])
+            have = float(got[k])
+            if math.isnan(want):
+                assert math.isnan(have), (c['name'], k)
+            elif EXACT or not math.isfinite(want):
+                assert have == want, (c['name'], k, have, want)
+            else:
+                assert have == pytest.approx(want, rel=1e-15, abs=1e-300), (c['name'], k)
+
+
+def test_checker_matches_the_reference_with_rows():
+    """With linear rows and row duals (the reference's answer, a perturbed primal, zero duals) the
+    residuals, complementarity, bound, gap and verdict equal the reference's check_qp_solution."""
+    for name, p in _cases('reference_admm_solve.npz'):
+        q, rows = _problem(p)
+        tol = float(p['tol'])
+        for k in range(3):
+            got = check_solution(q, rows, p[f'cand{k}_x'], p[f'cand{k}_y'], tol)
+            want = dict(zip(KEYS, p[f'cand{k}_stats'].tolist()))
+            for key in KEYS:
+                if EXACT:
+                    assert float(got[key]) == want[key], (name, k, key, got[key], want[key])
+                else:
+                    assert float(got[key]) == pytest.approx(want[key], rel=1e-14, abs=1e-300), (name, k, key)
+        assert bool(dict(zip(KEYS, p['cand0_stats'].tolist()))['verified'])
+
+
+def test_solve_qp_admm_reproduces_the_reference_answers():
+    """The host loop driven by the restated iterations returns the reference's status, iteration
+    count, primal, row duals and checker fields (the whole solve_qp_admm, including a rho
+    adaptation for the cases that pass iteration 100)."""
+    adapted = 0
+    for name, p in _cases('reference_admm_solve.npz'):
+        q, rows = _problem(p)
+        made = []
+
+        def make(h, a, n):
+            made.append(RestatedSystem(h, a, n))
+            return made[-1]
+
+        r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=float(p['tol'])), make_system=make)
+        assert r.status == 'optimal' and r.optimality_verified, (name, r.status)
+        assert r.iterations == int(p['iterations']), (name, r.iterations, int(p['iterations']))
+        assert r.algorithm == 'scaled_admm_pcg'
+        if EXACT:
+            assert _same(r.primal, p['x']) and _same(r.row_dual, p['row_dual']), name
+        else:
+            assert np.max(np.abs(r.primal - p['x'])) <= 1e-10, name
+        want = dict(zip(KEYS, p['stats'].tolist()))
+        assert r.objective == pytest.approx(want['objective'], rel=1e-13), name
+        adapted += made[0].rho_changes > 1
+    assert adapted >= 1
+
+
+def test_solve_qp_admm_statuses_and_option_checks():
+    """Invalid options and integer variables raise as the reference does; lower > upper gives
+    infeasible_bounds, a non-convex Hessian unsupported_curvature, an iteration limit of 0 the
+    status iteration_limit with the checked starting point."""
+    name, p = _cases('reference_admm_solve.npz')[0]
+    q, rows = _problem(p)
+
+    def make(h, a, n):
+        return RestatedSystem(h, a, n)
+
+    for bad in (dict(tolerance=0.0), dict(tolerance=math.nan), dict(time_limit=-1.0), dict(threads=0)):
+        with pytest.raises(ValueError, match='Invalid QP options'):
+            solve_qp_admm(q, rows, boxqp.QpOptions(**bad), make_system=make)
+    qi = boxqp.QuadraticProblem(cost=q.cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
+                                hessian_col=q.hessian_col, hessian_val=q.hessian_val,
+                                integer=np.arange(q.n) == 0)
+    with pytest.raises(ValueError, match='Continuous QP required'):
+        solve_qp_admm(qi, rows, make_system=make)
+    lo = np.array(q.lower, dtype=float)
+    lo[3] = 2.0
+    qb = boxqp.QuadraticProblem(cost=q.cost, lower=lo, upper=q.upper, hessian_row=q.hessian_row,
+                                hessian_col=q.hessian_col, hessian_val=q.hessian_val)
+    assert solve_qp_admm(qb, rows, make_system=make).status == 'infeasible_bounds'
+    rl = np.array(rows.lower, dtype=float)
+    rl[0] = rows.upper[0] + 1
+    rb = LinearRows(rows.rowptr, rows.col, rows.val, rl, rows.upper)
+    assert solve_qp_admm(q, rb, make_system=make).status == 'infeasible_bounds'
+    hv = np.array(q.hessian_val, dtype=float)
+    hv[q.hessian_row == q.hessian_col] *= -1
+    qn = boxqp.QuadraticProblem(cost=q.cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
+                                hessian_col=q.hessian_col, hessian_val=hv)
+    assert solve_qp_admm(qn, rows, make_system=make).status == 'unsupported_curvature'
+    r = solve_qp_admm(q, rows, boxqp.QpOptions(iteration_limit=0), make_system=make)
+    assert r.status == 'iteration_limit' and r.iterations == 0 and not r.optimality_verified
+    assert np.all(r.primal == 0) and np.all(r.row_dual == 0)
