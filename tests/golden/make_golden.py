@@ -167,6 +167,39 @@ def make_admm_golden():
     make_admm_solve_golden()
 
 
+def admm_rows_case(seed, n=40, m=30):
+    """A constrained QP whose rows exercise the reference's row handling: columns out of order,
+    repeated columns (summed), a pair that cancels to zero (dropped), an empty row, rows with an
+    infinite lower or upper bound, and three equality rows; Hessian and box as admm_case."""
+    p = admm_case(seed, n, 0, 0)
+    rng = np.random.default_rng(seed + 1000)
+    rowptr, col, val = [0], [], []
+    for i in range(m):
+        if i == 5:
+            rowptr.append(len(col))  # empty row
+            continue
+        cs = rng.choice(n, int(rng.integers(3, 6)), replace=False).tolist()
+        vs = rng.normal(size=len(cs)).tolist()
+        if i % 4 == 1:  # a repeated column
+            cs.append(cs[0])
+            vs.append(float(rng.normal()))
+        if i == 7:  # a repeated column that cancels
+            cs += [cs[1]]
+            vs += [-vs[1]]
+        col += cs
+        val += vs
+        rowptr.append(len(col))
+    lo = -rng.uniform(0.1, 0.5, m)
+    up = rng.uniform(0.1, 0.5, m)
+    lo[1::6] = -np.inf
+    up[2::6] = np.inf
+    lo[3:6], up[3:6] = 0.05, 0.05
+    lo[5], up[5] = -1.0, 1.0  # the empty row
+    p.update({'a_rowptr': np.array(rowptr, np.int32), 'a_col': np.array(col, np.int32), 'a_val': np.array(val),
+              'row_lower': lo, 'row_upper': up})
+    return p
+
+
 ADMM_SOLVE_CASES = {'solve_20': (20, 60, 40, 0, 1e-6), 'solve_21': (21, 100, 70, 8, 1e-6),
                     'solve_22': (22, 50, 30, 4, 1e-5), 'solve_23': (23, 150, 90, 0, 1e-5),
                     'solve_26': (26, 50, 30, 4, 1e-4), 'solve_29': (29, 100, 70, 8, 1e-6)}
@@ -199,6 +232,25 @@ def make_admm_solve_golden():
             out[f'{name}.cand{k}_stats'] = np.array([chk[k2] for k2 in CHECK_KEYS])
         print(name, status, int(st['iterations']), st['objective'], flush=True)
     np.savez_compressed(OUT / 'reference_admm_solve.npz', **out)
+    # row handling: the reference's primal after 20 iterations and its whole solve
+    out = {}
+    for name, seed in (('rows_a', 40), ('rows_b', 41)):
+        p = admm_rows_case(seed)
+        a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'],
+             p['a_val'], p['row_lower'], p['row_upper'])
+        out.update({f'{name}.{k}': np.asarray(v) for k, v in p.items()})
+        status, x, st = O.ref_solve_qp_admm(*a, tol=1e-12, iteration_limit=20, time_limit=600.0)
+        assert status == 'iteration_limit', (name, status)
+        out[f'{name}.x20'] = x
+        out[f'{name}.y20'] = st['row_dual']
+        status, x, st = O.ref_solve_qp_admm(*a, tol=1e-5, iteration_limit=200000, time_limit=600.0)
+        out[f'{name}.status'] = np.array(status)
+        out[f'{name}.iterations'] = np.array(int(st['iterations']))
+        out[f'{name}.x'] = x
+        out[f'{name}.row_dual'] = st['row_dual']
+        out[f'{name}.stats'] = np.array([st[k] for k in CHECK_KEYS])
+        print(name, status, int(st['iterations']), st['objective'], flush=True)
+    np.savez_compressed(OUT / 'reference_admm_rows.npz', **out)
 
 
 OPEN_CASES = [('graph2k_open', {'preset': 'graph10k', 'seed': 300, 'n': 2000, 'open_bounds': 3}, dict(tol=1e-6)),

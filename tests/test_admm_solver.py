@@ -68,7 +68,8 @@ def _same(a, b):
 def test_setup_equals_the_restated_setup():
     """admm_setup (vectorised) forms the scaled problem of qp_admm.cpp:136-158 with the same bits as
     the loop-by-loop restatement pinned to the reference."""
-    for file in ('reference_admm.npz', 'reference_admm_adapt.npz', 'reference_admm_solve.npz'):
+    for file in ('reference_admm.npz', 'reference_admm_adapt.npz', 'reference_admm_solve.npz',
+                 'reference_admm_rows.npz'):
         for name, p in _cases(file):
             scaling = bool(p['scaling']) if 'scaling' in p else True
             q, rows = _problem(p)
@@ -158,6 +159,28 @@ def test_solve_qp_admm_reproduces_the_reference_answers():
         assert r.objective == pytest.approx(want['objective'], rel=1e-13), name
         adapted += made[0].rho_changes > 1
     assert adapted >= 1
+
+
+def test_solve_qp_admm_row_handling_matches_the_reference():
+    """Rows with columns out of order, repeated columns, a repeat that cancels, an empty row,
+    one-sided rows (an infinite lower or upper bound) and equality rows: after 20 iterations
+    (tolerance 1e-12, nothing verifies) and over the whole solve at 1e-5 the loop returns the
+    reference's primal and row duals (bit for bit where long double is the reference's type)."""
+    for name, p in _cases('reference_admm_rows.npz'):
+        q, rows = _problem(p)
+
+        def make(h, a, n):
+            return RestatedSystem(h, a, n)
+
+        r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-12, iteration_limit=20), make_system=make)
+        assert r.status == 'iteration_limit' and r.iterations == 20
+        assert _same(r.primal, p['x20']) and _same(r.row_dual, p['y20']), name
+        r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-5), make_system=make)
+        assert r.status == str(p['status']) and r.iterations == int(p['iterations']), (name, r.status, r.iterations)
+        if EXACT:
+            assert _same(r.primal, p['x']) and _same(r.row_dual, p['row_dual']), name
+        else:
+            assert np.max(np.abs(r.primal - p['x'])) <= 1e-10, name
 
 
 def test_solve_qp_admm_statuses_and_option_checks():
