@@ -80,6 +80,27 @@ class _Tokens:
 
 def read_qplib(text, max_columns=100000):
     """Parses QPLIB text; returns (QuadraticProblem, rows) where rows > 0 means linear constraints."""
+    q, m, _ = _parse(text, max_columns)
+    return q, m
+
+
+def read_qplib_rows(text, max_columns=100000):
+    """Parses QPLIB text with its linear constraints; returns (QuadraticProblem, LinearRows), the
+    rows in CSR with each row's entries in file order (the reference appends them to its row
+    vectors as it reads them, src/qp.cpp:88-94) and the row bounds; LinearRows with no rows for
+    a box or unconstrained model."""
+    from .admm import LinearRows
+    q, m, (ri, rj, rv, row_lower, row_upper) = _parse(text, max_columns)
+    ri = np.asarray(ri, dtype=np.int64)
+    order = np.argsort(ri, kind='stable')
+    rowptr = np.zeros(m + 1, dtype=np.int32)
+    if m:
+        np.cumsum(np.bincount(ri, minlength=m), out=rowptr[1:])
+    return q, LinearRows(rowptr, np.asarray(rj, dtype=np.int32)[order], np.asarray(rv, dtype=np.float64)[order],
+                         np.asarray(row_lower, dtype=np.float64), np.asarray(row_upper, dtype=np.float64))
+
+
+def _parse(text, max_columns):
     r = _Tokens(text)
     r.token()  # name
     typ, sense = r.token(), r.token()
@@ -95,7 +116,7 @@ def read_qplib(text, max_columns=100000):
     hrow, hcol, hval, seen = [], [], [], set()
     for _ in range(nz):
         i, j, v = r.index(n), r.index(n), r.number()
-        if i < j or (i, j) in seen:
+        if i < j or (i, j) in seen or not math.isfinite(v):
             raise ValueError('Invalid QPLIB Hessian entry')
         seen.add((i, j))
         hrow.append(i)
@@ -103,20 +124,25 @@ def read_qplib(text, max_columns=100000):
         hval.append(v if i == j else 0.5 * v)
     cost = r.vector(n)
     offset = r.number()
+    ri, rj, rv = [], [], []
+    row_lower = row_upper = np.zeros(0)
     if m:
         cnt = r.count()
         entries = set()
         for _ in range(cnt):
             i, j, v = r.index(m), r.index(n), r.number()
-            if (i, j) in entries:
+            if (i, j) in entries or not math.isfinite(v):
                 raise ValueError('Invalid QPLIB matrix entry')
             entries.add((i, j))
+            ri.append(i)
+            rj.append(j)
+            rv.append(v)
     infinity = r.number()
     if infinity <= 0:
         raise ValueError('Invalid infinity marker')
     if m:
-        r.vector(m, infinity)
-        r.vector(m, infinity)
+        row_lower = r.vector(m, infinity)
+        row_upper = r.vector(m, infinity)
     if typ[2] != 'N':
         lower, upper = r.vector(n, infinity), r.vector(n, infinity)
     else:
@@ -149,7 +175,7 @@ def read_qplib(text, max_columns=100000):
     q = QuadraticProblem(cost=cost, lower=lower, upper=upper, hessian_row=np.asarray(hrow, np.int64),
                          hessian_col=np.asarray(hcol, np.int64), hessian_val=np.asarray(hval, np.float64),
                          offset=offset, maximize=sense == 'maximize', rows=m)
-    return q, m
+    return q, m, (ri, rj, rv, row_lower, row_upper)
 
 
 def write_qplib(path, q: QuadraticProblem, name='GENERATED'):

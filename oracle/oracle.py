@@ -195,6 +195,10 @@ def ref():
         L.ref_qplib_sizes.argtypes = [c_void_p, _I64P, _I64P, _I64P, POINTER(c_int), _F64P]
         L.ref_qplib_copy.restype = None
         L.ref_qplib_copy.argtypes = [c_void_p, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P]
+        L.ref_qplib_rows.restype = None
+        L.ref_qplib_rows.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P]
+        L.ref_qplib_row_entries.restype = c_int64
+        L.ref_qplib_row_entries.argtypes = [c_void_p]
         L.ref_qplib_close.restype = None
         L.ref_qplib_close.argtypes = [c_void_p]
         _ref = L
@@ -418,7 +422,13 @@ def ref_read_qplib(path):
         cost, lo, up = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
         ref().ref_qplib_copy(h, _p(hr, c_int64), _p(hc, c_int64), _p(hv, c_double), _p(cost, c_double),
                              _p(lo, c_double), _p(up, c_double))
+        k = ref().ref_qplib_row_entries(h)
+        rp, rc, rv = np.zeros(m.value + 1, np.int32), np.zeros(max(k, 1), np.int32), np.zeros(max(k, 1))
+        rl, ru = np.zeros(m.value), np.zeros(m.value)
+        ref().ref_qplib_rows(h, _p(rp, c_int32), _p(rc, c_int32), _p(rv, c_double), _p(rl, c_double),
+                             _p(ru, c_double))
         return {'n': n.value, 'rows': m.value, 'maximize': bool(mx.value), 'offset': off.value, 'hrow': hr,
-                'hcol': hc, 'hval': hv, 'cost': cost, 'lower': lo, 'upper': up}
+                'hcol': hc, 'hval': hv, 'cost': cost, 'lower': lo, 'upper': up, 'a_rowptr': rp, 'a_col': rc[:k],
+                'a_val': rv[:k], 'row_lower': rl, 'row_upper': ru}
     finally:
         ref().ref_qplib_close(h)

@@ -223,6 +223,31 @@ void ref_qplib_copy(void* handle, int64_t* hrow, int64_t* hcol, double* hval, do
     }
 }
 
+// The rows of a model read by ref_qplib_open: CSR in the reader's order (row by row, each row's
+// entries as the file listed them) and the row bounds.
+void ref_qplib_rows(void* handle, int32_t* rowptr, int32_t* col, double* val, double* row_lower, double* row_upper) {
+    auto* h = static_cast<QplibHandle*>(handle);
+    const auto& p = h->q.linear;
+    int32_t k = 0;
+    rowptr[0] = 0;
+    for (std::size_t i = 0; i < p.rows.size(); ++i) {
+        for (const auto& e : p.rows[i]) {
+            col[k] = static_cast<int32_t>(e.first);
+            val[k] = e.second;
+            ++k;
+        }
+        rowptr[i + 1] = k;
+        row_lower[i] = p.row_lower[i];
+        row_upper[i] = p.row_upper[i];
+    }
+}
+
+int64_t ref_qplib_row_entries(void* handle) {
+    int64_t k = 0;
+    for (const auto& r : static_cast<QplibHandle*>(handle)->q.linear.rows) k += static_cast<int64_t>(r.size());
+    return k;
+}
+
 void ref_qplib_close(void* handle) { delete static_cast<QplibHandle*>(handle); }
 
 }  // extern "C"

@@ -9,7 +9,7 @@ import pytest
 
 import boxqp
 from boxqp import cli
-from boxqp.qplib import read_qplib, write_qplib
+from boxqp.qplib import read_qplib, read_qplib_rows, write_qplib
 from oracle import oracle as O
 
 
@@ -37,10 +37,58 @@ def test_writer_reader_roundtrip(tmp_path):
     ('x QCB minimize 200000\n', 'oversized'),
     ('x QCB minimize 2 1 1 2 1.0\n', 'Hessian'),
     ('x QCB minimize 2 0 0 0 0', 'Truncated'),
+    ('x QCB minimize 1 1 1 1 1e400\n', 'Hessian'),  # finite as a long double, infinite as a double
+    ('x QCL minimize 1 1 0 0 0 0 1 1 1 1e400\n', 'matrix'),
 ])
 def test_reader_rejects_like_the_reference(text, msg):
     with pytest.raises(ValueError, match=msg):
         read_qplib(text)
+
+
+def constrained_qplib_text(seed=3, n=30, m=12):
+    """A QCL model (linear rows) in QPLIB layout: lower-triangle Hessian, sparse cost, row entries
+    listed in shuffled order, row bounds with the 1e20 infinity marker (one-sided and equality
+    rows), variable bounds."""
+    rng = np.random.default_rng(seed)
+    lines = ['GEN', 'QCL', 'minimize', str(n), str(m)]
+    h = [(j, j, 2.0 + rng.random()) for j in range(n)] + [(j + 1, j, -0.5 * rng.random()) for j in range(n - 1)]
+    lines += [str(len(h))] + [f'{i + 1} {j + 1} {v:.17g}' for i, j, v in h]
+    cost = rng.normal(size=n)
+    lines += ['0', str(n)] + [f'{j + 1} {cost[j]:.17g}' for j in range(n)] + ['0.5']
+    entries = [(i, j, rng.normal()) for i in range(m) for j in sorted(rng.choice(n, 3, replace=False))]
+    entries = [entries[k] for k in rng.permutation(len(entries))]
+    lines += [str(len(entries))] + [f'{i + 1} {j + 1} {v:.17g}' for i, j, v in entries]
+    lines += ['1e20']
+    lo = [-1e20 if i % 4 == 0 else -0.5 for i in range(m)]
+    up = [1e20 if i % 4 == 1 else (-0.5 if i % 4 == 2 else 0.5) for i in range(m)]
+    for vec in (lo, up):
+        lines += ['0', str(m)] + [f'{i + 1} {v:.17g}' for i, v in enumerate(vec)]
+    lines += ['-1', '0', '1', '0']  # variable bounds [-1, 1]
+    lines += ['0', '0', '0', '0', '0', '0', '0', '0']  # start vectors, names
+    return '\n'.join(lines) + '\n'
+
+
+def test_reader_rows_match_the_reference_reader(tmp_path):
+    """read_qplib_rows gives the reference reader's rows (row by row, each in file order), row
+    bounds (the infinity marker mapped to infinity) and the same problem as read_qplib."""
+    if not O.ref_available():
+        pytest.skip('oracle/_ref not built on this host')
+    path = tmp_path / 'c.qplib'
+    path.write_text(constrained_qplib_text())
+    ref = O.ref_read_qplib(path)
+    q, rows = read_qplib_rows(path.read_text())
+    q0, m = read_qplib(path.read_text())
+    assert m == rows.m == ref['rows'] == 12 and q.n == q0.n == ref['n']
+    for k in ('a_rowptr', 'a_col', 'a_val', 'row_lower', 'row_upper'):
+        mine = {'a_rowptr': rows.rowptr, 'a_col': rows.col, 'a_val': rows.val, 'row_lower': rows.lower,
+                'row_upper': rows.upper}[k]
+        assert np.array_equal(mine, ref[k]), k
+    assert np.isinf(rows.lower[0]) and np.isinf(rows.upper[1]) and rows.lower[2] == rows.upper[2] == -0.5
+    for a, b in ((q.hessian_val, ref['hval']), (q.cost, ref['cost']), (q.lower, ref['lower']), (q.upper, ref['upper'])):
+        assert np.array_equal(a, b)
+    assert q.offset == ref['offset'] == 0.5
+    _, none = read_qplib_rows('x QCB minimize 1 1 1 1 2.0 0 0 0 1e20 0 0 1 0 0 0 0 0 0 0\n')
+    assert none.m == 0 and none.rowptr.tolist() == [0]
 
 
 @pytest.mark.skipif(not os.environ.get('BOXQP_REFERENCE_DIR'), reason='set BOXQP_REFERENCE_DIR to the reference solver')
