@@ -131,17 +131,19 @@ def _clip(x, lo, up):
 
 
 def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
-                  scaling=True):
-    """The reference's set-up of solve_qp_admm (qp_admm.cpp:136-161) for a minimisation: variable
-    units, row scales and the cost scale; A with the bound rows appended; the initial x and z and
-    rho (0.1, x100 on equality rows), sigma 1e-8.  Returns a dict of the scaled problem."""
+                  scaling=True, maximize=False):
+    """The reference's set-up of solve_qp_admm (qp_admm.cpp:136-161): variable units, row scales
+    and the cost scale; A with the bound rows appended; the initial x and z and rho (0.1, x100 on
+    equality rows), sigma 1e-8 (a maximisation negates the Hessian and the cost first).  Returns a
+    dict of the scaled problem."""
     m = len(a_rowptr) - 1
-    # hessian(q) (qp_admm.cpp:24-29): lower-triangle terms mirrored, merged per row
+    sign = -1.0 if maximize else 1.0
+    # hessian(q) (qp_admm.cpp:24-29): lower-triangle terms (sign-normalised) mirrored, merged per row
     hrows = [[] for _ in range(n)]
     for i, j, v in zip(hrow, hcol, hval):
-        hrows[i].append((j, v))
+        hrows[i].append((j, sign * v))
         if i != j:
-            hrows[j].append((i, v))
+            hrows[j].append((i, sign * v))
     hrp, hci, hva = _csr_from_rows(hrows, n)
     hva = hva.copy()
     variable = np.ones(n)
@@ -177,7 +179,7 @@ def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_va
         rows.append([(j, 1.0)])
         lo_all.append(lower[j] / variable[j])
         up_all.append(upper[j] / variable[j])
-    c = np.array(cost, dtype=np.float64) * (1.0 * variable)
+    c = np.array(cost, dtype=np.float64) * (sign * variable)
     cost_scale = 1 / max(1.0, float(np.max(np.abs(c)))) if scaling else 1.0
     hva = hva * cost_scale
     c = c * cost_scale

@@ -179,7 +179,7 @@ def ref():
         L.ref_solve_qp_admm.restype = c_int
         L.ref_solve_qp_admm.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int64,
                                         POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, c_double, c_int64,
-                                        c_double, c_int, _F64P, _F64P, _F64P, c_char_p, c_int]
+                                        c_double, c_int, c_int, c_double, _F64P, _F64P, _F64P, c_char_p, c_int]
         L.ref_check_rows.restype = c_int
         L.ref_check_rows.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double,
                                      c_int64, POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, _F64P, _F64P,
@@ -335,7 +335,7 @@ def ref_solve_box(hrow, hcol, hval, cost, lower, upper, tol=1e-7, iteration_limi
 
 
 def ref_solve_qp_admm(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
-                      tol=1e-7, iteration_limit=200000, time_limit=30.0, scaling=True):
+                      tol=1e-7, iteration_limit=200000, time_limit=30.0, scaling=True, maximize=False, offset=0.0):
     """The reference's solve_qp_admm (src/qp_admm.cpp:118-280) on a QP with constraint rows."""
     hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
     a_rowptr = np.ascontiguousarray(a_rowptr, np.int32)
@@ -352,7 +352,8 @@ def ref_solve_qp_admm(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_v
                                  _p(cost, c_double), _p(lower, c_double), _p(upper, c_double), m,
                                  _p(a_rowptr, c_int32), _p(a_col, c_int32), _p(a_val, c_double),
                                  _p(row_lower, c_double), _p(row_upper, c_double), float(tol), int(iteration_limit),
-                                 float(time_limit), 1 if scaling else 0, _p(x, c_double), _p(row_dual, c_double),
+                                 float(time_limit), 1 if scaling else 0, int(maximize), float(offset),
+                                 _p(x, c_double), _p(row_dual, c_double),
                                  _p(stats, c_double), msg, 256)
     if rc == 1:
         raise ValueError(msg.value.decode())

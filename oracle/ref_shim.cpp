@@ -98,9 +98,10 @@ int ref_solve_qp_admm(int64_t n, int64_t nh, const int64_t* hrow, const int64_t*
                       const double* cost, const double* lower, const double* upper, int64_t m,
                       const int32_t* a_rowptr, const int32_t* a_col, const double* a_val, const double* row_lower,
                       const double* row_upper, double tol, int64_t iteration_limit, double time_limit, int scaling,
-                      double* x_out, double* row_dual_out, double* stats, char* status_out, int status_cap) {
+                      int maximize, double offset, double* x_out, double* row_dual_out, double* stats,
+                      char* status_out, int status_cap) {
     try {
-        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, 0, 0.0);
+        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, maximize, offset);
         auto& p = q.linear;
         p.rows.resize(static_cast<std::size_t>(m));
         for (int64_t i = 0; i < m; ++i)

@@ -250,6 +250,23 @@ def make_admm_solve_golden():
         out[f'{name}.row_dual'] = st['row_dual']
         out[f'{name}.stats'] = np.array([st[k] for k in CHECK_KEYS])
         print(name, status, int(st['iterations']), st['objective'], flush=True)
+    # a maximisation (concave objective: the Hessian and cost of admm_case negated) with an offset
+    p = admm_case(24, 60, 40, 4)
+    p['hval'] = -p['hval']
+    p['cost'] = -p['cost']
+    a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'], p['a_val'],
+         p['row_lower'], p['row_upper'])
+    status, x, st = O.ref_solve_qp_admm(*a, tol=1e-5, iteration_limit=200000, time_limit=600.0, maximize=True,
+                                        offset=1.5)
+    out.update({f'max_a.{k}': np.asarray(v) for k, v in p.items()})
+    out['max_a.maximize'] = np.array(1)
+    out['max_a.offset'] = np.array(1.5)
+    out['max_a.status'] = np.array(status)
+    out['max_a.iterations'] = np.array(int(st['iterations']))
+    out['max_a.x'] = x
+    out['max_a.row_dual'] = st['row_dual']
+    out['max_a.stats'] = np.array([st[k] for k in CHECK_KEYS])
+    print('max_a', status, int(st['iterations']), st['objective'], flush=True)
     np.savez_compressed(OUT / 'reference_admm_rows.npz', **out)
 
 

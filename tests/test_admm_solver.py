@@ -33,7 +33,9 @@ def _cases(file):
 
 def _problem(p):
     q = boxqp.QuadraticProblem(cost=p['cost'], lower=p['lower'], upper=p['upper'], hessian_row=p['hrow'],
-                               hessian_col=p['hcol'], hessian_val=p['hval'])
+                               hessian_col=p['hcol'], hessian_val=p['hval'],
+                               maximize=bool(p['maximize']) if 'maximize' in p else False,
+                               offset=float(p['offset']) if 'offset' in p else 0.0)
     rows = LinearRows(p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'])
     return q, rows
 
@@ -75,7 +77,8 @@ def test_setup_equals_the_restated_setup():
             q, rows = _problem(p)
             sp = admm_setup(q, rows, scaling)
             ref = scale_qp_admm(int(p['n']), p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'],
-                                p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'], scaling)
+                                p['a_rowptr'], p['a_col'], p['a_val'], p['row_lower'], p['row_upper'], scaling,
+                                maximize=q.maximize)
             for k in ('c', 'lo', 'up', 'variable', 'x', 'z', 'y', 'rho'):
                 assert _same(sp[k], ref[k]), (name, k)
             for k in ('h', 'a'):
@@ -163,19 +166,22 @@ def test_solve_qp_admm_reproduces_the_reference_answers():
 
 def test_solve_qp_admm_row_handling_matches_the_reference():
     """Rows with columns out of order, repeated columns, a repeat that cancels, an empty row,
-    one-sided rows (an infinite lower or upper bound) and equality rows: after 20 iterations
-    (tolerance 1e-12, nothing verifies) and over the whole solve at 1e-5 the loop returns the
-    reference's primal and row duals (bit for bit where long double is the reference's type)."""
+    one-sided rows (an infinite lower or upper bound) and equality rows, and a maximisation with an
+    offset: after 20 iterations (tolerance 1e-12, nothing verifies) and over the whole solve at
+    1e-5 the loop returns the reference's primal and row duals (bit for bit where long double is
+    the reference's type), and the maximisation its objective in the maximisation sense."""
     for name, p in _cases('reference_admm_rows.npz'):
         q, rows = _problem(p)
 
         def make(h, a, n):
             return RestatedSystem(h, a, n)
 
-        r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-12, iteration_limit=20), make_system=make)
-        assert r.status == 'iteration_limit' and r.iterations == 20
-        assert _same(r.primal, p['x20']) and _same(r.row_dual, p['y20']), name
+        if 'x20' in p:
+            r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-12, iteration_limit=20), make_system=make)
+            assert r.status == 'iteration_limit' and r.iterations == 20
+            assert _same(r.primal, p['x20']) and _same(r.row_dual, p['y20']), name
         r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-5), make_system=make)
+        assert r.objective == pytest.approx(float(p['stats'][0]), rel=1e-13), name
         assert r.status == str(p['status']) and r.iterations == int(p['iterations']), (name, r.status, r.iterations)
         if EXACT:
             assert _same(r.primal, p['x']) and _same(r.row_dual, p['row_dual']), name
