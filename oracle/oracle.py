@@ -180,6 +180,10 @@ def ref():
         L.ref_solve_qp_admm.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int64,
                                         POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, c_double, c_int64,
                                         c_double, c_int, c_int, c_double, _F64P, _F64P, _F64P, c_char_p, c_int]
+        L.ref_solve_diagonal_equalities.restype = c_int
+        L.ref_solve_diagonal_equalities.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P,
+                                                    c_int64, POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P,
+                                                    c_double, c_int64, c_int, _F64P, _F64P, _F64P, c_char_p, c_int]
         L.ref_check_rows.restype = c_int
         L.ref_check_rows.argtypes = [c_int64, c_int64, _I64P, _I64P, _F64P, _F64P, _F64P, _F64P, c_int, c_double,
                                      c_int64, POINTER(c_int32), POINTER(c_int32), _F64P, _F64P, _F64P, _F64P, _F64P,
@@ -357,6 +361,33 @@ def ref_solve_qp_admm(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_v
                                  _p(stats, c_double), msg, 256)
     if rc == 1:
         raise ValueError(msg.value.decode())
+    if rc != 0:
+        raise RuntimeError(msg.value.decode())
+    keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
+            'relative_gap', 'verified', 'iterations']
+    st = dict(zip(keys, stats.tolist()))
+    st['row_dual'] = row_dual
+    return msg.value.decode(), x, st
+
+
+def ref_solve_diagonal_equalities(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower,
+                                  row_upper, tol=1e-7, iteration_limit=200000, scaling=True):
+    """The reference's solve_diagonal_equalities (src/qp_dual_newton.cpp:9-66), the dual Newton
+    solver solve_qp_admm tries first on diagonal Hessians with equality rows; returns (status, x,
+    stats with 'row_dual')."""
+    hrow, hcol, hval, cost, lower, upper = _arrays(hrow, hcol, hval, cost, lower, upper)
+    a_rowptr = np.ascontiguousarray(a_rowptr, np.int32)
+    a_col = np.ascontiguousarray(a_col, np.int32)
+    a_val, row_lower, row_upper = (np.ascontiguousarray(v, np.float64) for v in (a_val, row_lower, row_upper))
+    n, m = cost.shape[0], a_rowptr.shape[0] - 1
+    x, row_dual, stats = np.zeros(n), np.zeros(m), np.zeros(8)
+    msg = ctypes.create_string_buffer(256)
+    rc = ref().ref_solve_diagonal_equalities(n, hrow.shape[0], _p(hrow, c_int64), _p(hcol, c_int64),
+                                             _p(hval, c_double), _p(cost, c_double), _p(lower, c_double),
+                                             _p(upper, c_double), m, _p(a_rowptr, c_int32), _p(a_col, c_int32),
+                                             _p(a_val, c_double), _p(row_lower, c_double), _p(row_upper, c_double),
+                                             float(tol), int(iteration_limit), 1 if scaling else 0, _p(x, c_double),
+                                             _p(row_dual, c_double), _p(stats, c_double), msg, 256)
     if rc != 0:
         raise RuntimeError(msg.value.decode())
     keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',

@@ -17,6 +17,10 @@
 #include <stdexcept>
 #include <string>
 
+namespace sovereign {
+QpResult solve_diagonal_equalities(const QuadraticProblem&, const QpOptions&);
+}
+
 namespace {
 void put_message(char* out, std::size_t cap, const std::string& text) {
     if (!out || !cap) return;
@@ -126,6 +130,42 @@ int ref_solve_qp_admm(int64_t n, int64_t nh, const int64_t* hrow, const int64_t*
     } catch (const std::invalid_argument& e) {
         put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
         return 1;
+    } catch (const std::exception& e) {
+        put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
+        return 2;
+    }
+}
+
+// Runs the reference's diagonal-Hessian equality solver (src/qp_dual_newton.cpp) alone, with the
+// same options solve_qp_admm would pass it except the time limit.
+int ref_solve_diagonal_equalities(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hcol, const double* hval,
+                                  const double* cost, const double* lower, const double* upper, int64_t m,
+                                  const int32_t* a_rowptr, const int32_t* a_col, const double* a_val,
+                                  const double* row_lower, const double* row_upper, double tol, int64_t iteration_limit,
+                                  int scaling, double* x_out, double* row_dual_out, double* stats, char* status_out,
+                                  int status_cap) {
+    try {
+        auto q = make_problem(n, nh, hrow, hcol, hval, cost, lower, upper, 0, 0.0);
+        auto& p = q.linear;
+        p.rows.resize(static_cast<std::size_t>(m));
+        for (int64_t i = 0; i < m; ++i)
+            for (int32_t k = a_rowptr[i]; k < a_rowptr[i + 1]; ++k)
+                p.rows[static_cast<std::size_t>(i)].push_back({static_cast<std::size_t>(a_col[k]), a_val[k]});
+        p.row_lower.assign(row_lower, row_lower + m);
+        p.row_upper.assign(row_upper, row_upper + m);
+        sovereign::QpOptions o;
+        o.tolerance = tol;
+        o.iteration_limit = static_cast<std::size_t>(iteration_limit);
+        o.time_limit = 600;
+        o.threads = 1;
+        o.scaling = scaling != 0;
+        auto r = sovereign::solve_diagonal_equalities(q, o);
+        fill_stats(r, stats);
+        for (std::size_t j = 0; j < r.primal.size() && j < static_cast<std::size_t>(n); ++j) x_out[j] = r.primal[j];
+        for (std::size_t i = 0; i < r.row_dual.size() && i < static_cast<std::size_t>(m); ++i)
+            row_dual_out[i] = r.row_dual[i];
+        put_message(status_out, static_cast<std::size_t>(status_cap), r.status);
+        return 0;
     } catch (const std::exception& e) {
         put_message(status_out, static_cast<std::size_t>(status_cap), e.what());
         return 2;

@@ -200,6 +200,50 @@ def admm_rows_case(seed, n=40, m=30):
     return p
 
 
+def diagonal_equality_case(seed, n=80, m=30):
+    """A QP with a positive diagonal Hessian (U[1, 3]) and m equality rows of 4 normal entries,
+    right-hand sides A x0 for an x0 inside the box [-1, 1]: the structure solve_qp_admm hands to
+    its dual Newton solver first."""
+    rng = np.random.default_rng(seed)
+    rowptr, col, val = [0], [], []
+    for _ in range(m):
+        cs = np.sort(rng.choice(n, 4, replace=False))
+        col += cs.tolist()
+        val += rng.normal(size=4).tolist()
+        rowptr.append(len(col))
+    hval = rng.uniform(1, 3, n)
+    rowptr, col, val = np.array(rowptr, np.int32), np.array(col, np.int32), np.array(val)
+    x0 = rng.uniform(-0.5, 0.5, n)
+    b = np.array([float(np.dot(val[rowptr[i]:rowptr[i + 1]], x0[col[rowptr[i]:rowptr[i + 1]]])) for i in range(m)])
+    return {'n': n, 'hrow': np.arange(n, dtype=np.int64), 'hcol': np.arange(n, dtype=np.int64), 'hval': hval,
+            'cost': 3 * rng.normal(size=n), 'lower': -np.ones(n), 'upper': np.ones(n), 'a_rowptr': rowptr,
+            'a_col': col, 'a_val': val, 'row_lower': b, 'row_upper': b.copy()}
+
+
+def make_dual_newton_golden():
+    """The reference's solve_diagonal_equalities (src/qp_dual_newton.cpp:9-66) on diagonal-Hessian
+    equality QPs: verified solves (scaled and unscaled) and a run stopped after 3 iterations with an
+    unreachable tolerance: tests/golden/reference_dual_newton.npz."""
+    out = {}
+    for name, (seed, tol, limit, scaling) in {'dn_a': (50, 1e-7, 200000, True), 'dn_b': (51, 1e-8, 200000, False),
+                                              'dn_c': (52, 1e-300, 3, True), 'dn_d': (53, 1e-7, 200000, True)}.items():
+        p = diagonal_equality_case(seed)
+        a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'],
+             p['a_val'], p['row_lower'], p['row_upper'])
+        status, x, st = O.ref_solve_diagonal_equalities(*a, tol=tol, iteration_limit=limit, scaling=scaling)
+        out.update({f'{name}.{k}': np.asarray(v) for k, v in p.items()})
+        out[f'{name}.tol'] = np.array(tol)
+        out[f'{name}.limit'] = np.array(limit)
+        out[f'{name}.scaling'] = np.array(1 if scaling else 0)
+        out[f'{name}.status'] = np.array(status)
+        out[f'{name}.iterations'] = np.array(int(st['iterations']))
+        out[f'{name}.x'] = x
+        out[f'{name}.row_dual'] = st['row_dual']
+        out[f'{name}.stats'] = np.array([st[k] for k in CHECK_KEYS])
+        print(name, status, int(st['iterations']), st['objective'], flush=True)
+    np.savez_compressed(OUT / 'reference_dual_newton.npz', **out)
+
+
 ADMM_SOLVE_CASES = {'solve_20': (20, 60, 40, 0, 1e-6), 'solve_21': (21, 100, 70, 8, 1e-6),
                     'solve_22': (22, 50, 30, 4, 1e-5), 'solve_23': (23, 150, 90, 0, 1e-5),
                     'solve_26': (26, 50, 30, 4, 1e-4), 'solve_29': (29, 100, 70, 8, 1e-6)}
@@ -407,6 +451,7 @@ def main():
     if not O.build_reference(a.reference):
         raise SystemExit('cannot build oracle/_ref from ' + a.reference)
     make_admm_golden()
+    make_dual_newton_golden()
     make_check_golden()
     if a.only == 'admm':
         return
