@@ -311,6 +311,18 @@ def make_admm_solve_golden():
     out['max_a.row_dual'] = st['row_dual']
     out['max_a.stats'] = np.array([st[k] for k in CHECK_KEYS])
     print('max_a', status, int(st['iterations']), st['objective'], flush=True)
+    # no linear rows: the ADMM over the bound rows alone
+    p = admm_case(25, 50, 0, 0)
+    a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'], p['a_val'],
+         p['row_lower'], p['row_upper'])
+    status, x, st = O.ref_solve_qp_admm(*a, tol=1e-6, iteration_limit=200000, time_limit=600.0)
+    out.update({f'box_a.{k}': np.asarray(v) for k, v in p.items()})
+    out['box_a.status'] = np.array(status)
+    out['box_a.iterations'] = np.array(int(st['iterations']))
+    out['box_a.x'] = x
+    out['box_a.row_dual'] = st['row_dual']
+    out['box_a.stats'] = np.array([st[k] for k in CHECK_KEYS])
+    print('box_a', status, int(st['iterations']), st['objective'], flush=True)
     np.savez_compressed(OUT / 'reference_admm_rows.npz', **out)
 
 

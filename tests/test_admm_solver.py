@@ -166,8 +166,8 @@ def test_solve_qp_admm_reproduces_the_reference_answers():
 
 def test_solve_qp_admm_row_handling_matches_the_reference():
     """Rows with columns out of order, repeated columns, a repeat that cancels, an empty row,
-    one-sided rows (an infinite lower or upper bound) and equality rows, and a maximisation with an
-    offset: after 20 iterations (tolerance 1e-12, nothing verifies) and over the whole solve at
+    one-sided rows (an infinite lower or upper bound) and equality rows, a maximisation with an
+    offset, and a QP with no linear rows (the ADMM over the bound rows alone): after 20 iterations (tolerance 1e-12, nothing verifies) and over the whole solve at
     1e-5 the loop returns the reference's primal and row duals (bit for bit where long double is
     the reference's type), and the maximisation its objective in the maximisation sense."""
     for name, p in _cases('reference_admm_rows.npz'):
