@@ -224,3 +224,7 @@ def test_solve_qp_admm_statuses_and_option_checks():
     r = solve_qp_admm(q, rows, boxqp.QpOptions(iteration_limit=0), make_system=make)
     assert r.status == 'iteration_limit' and r.iterations == 0 and not r.optimality_verified
     assert np.all(r.primal == 0) and np.all(r.row_dual == 0)
+    # a zero time limit ends the solve at the first check, after the verification and the
+    # non-finite test (qp_admm.cpp:247-249)
+    r = solve_qp_admm(q, rows, boxqp.QpOptions(time_limit=0.0), make_system=make)
+    assert r.status == 'time_limit' and r.iterations == 0
