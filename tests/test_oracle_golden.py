@@ -118,6 +118,30 @@ def test_oracle_multithreaded_equals_single(golden):
     assert s1 == s4 and np.array_equal(x1, x4)
 
 
+def test_tridiagonal_family_known_objectives():
+    """The seeded tridiagonal family of the reference's scale harness (src/scale_benchmark.cpp:
+    LCG seed 26119, H = tridiag(-1, 2.02, -1), box [0, 3], known objective in long double) at the
+    sizes with published known objectives: n = 10,000 (-947.124889445...), 50,000
+    (-4710.360537563), 100,000 (-9446.3140183450014) and 1,000,000 (-94123.887220104109, the
+    benchmark size)."""
+    assert boxqp.planted('tridiagonal', n=10000)['fstar'] == pytest.approx(-947.124889445, abs=1e-9)
+    assert boxqp.planted('tridiagonal', n=50000)['fstar'] == pytest.approx(-4710.360537563, abs=1e-9)
+    assert boxqp.planted('tridiagonal', n=100000)['fstar'] == float('-9446.3140183450014')
+    assert boxqp.planted('tridiagonal', n=1000000)['fstar'] == float('-94123.887220104109')
+
+
+def test_oracle_passes_the_scale_harness_at_50k():
+    """The scale harness's pass criteria (src/scale_benchmark.cpp:21-23) at n = 50,000: status
+    optimal and verified, objective within 1e-8 relative of the known objective, max |x - x*| <
+    1e-4 (the reference's own run took 1700 iterations at 10,000, as here)."""
+    inst = boxqp.planted('tridiagonal', n=50000, lower_triplets=True)
+    status, x, st = O.solve_box(inst['hrow'], inst['hcol'], inst['hval'], inst['c'], inst['lower'], inst['upper'],
+                                tol=1e-7, iteration_limit=20000, threads=4)
+    assert status == 'optimal' and st['verified'] == 1.0
+    assert abs(st['objective'] - inst['fstar']) / (1 + abs(inst['fstar'])) <= 1e-8
+    assert np.max(np.abs(x - inst['xstar'])) < 1e-4
+
+
 def test_planted_optimum_is_verified_by_oracle():
     inst = boxqp.planted('graph10k', seed=5, n=3000, lower_triplets=True)
     p = {'hrow': inst['hrow'], 'hcol': inst['hcol'], 'hval': inst['hval'], 'cost': inst['c'],
