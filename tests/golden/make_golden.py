@@ -421,6 +421,55 @@ def make_check_golden():
     (OUT / 'reference_checks.json').write_text(json.dumps(out, indent=1) + '\n')
 
 
+def _planted_kkt_draws():
+    """The 30 problems of the reference's planted KKT tests (scripts/test_qp.py:30-44), drawn from
+    one random.Random(26121) stream in the script's order: n = 5, H = R'R + I, x* uniform in
+    [-1, 1], and for cases 15-29 three rows a (uniform in [-1, 1]) with duals y in [0.2, 2]
+    active at x* (a x <= b, b = a x*), c = -H x* - A'y; box [-3, 3]."""
+    import random
+    rng = random.Random(26121)
+    out = []
+    for case in range(30):
+        n = 5
+        m = 3 if case >= 15 else 0
+        r = [[rng.uniform(-1, 1) for _ in range(n)] for _ in range(n)]
+        h = [[sum(r[k][i] * r[k][j] for k in range(n)) + (1 if i == j else 0) for j in range(n)] for i in range(n)]
+        optimum = [rng.uniform(-1, 1) for _ in range(n)]
+        a = [[rng.uniform(-1, 1) for _ in range(n)] for _ in range(m)]
+        y = [rng.uniform(.2, 2) for _ in range(m)]
+        b = [sum(v * x for v, x in zip(row, optimum)) for row in a]
+        c = [-sum(h[i][j] * optimum[j] for j in range(n)) - sum(a[k][i] * y[k] for k in range(m)) for i in range(n)]
+        expected = sum(c[i] * optimum[i] + .5 * sum(h[i][j] * optimum[i] * optimum[j] for j in range(n))
+                       for i in range(n))
+        out.append((case, n, h, optimum, a, b, c, expected))
+    return out
+
+
+def make_kkt_rows_golden():
+    """Cases 15-29 of the reference's planted KKT tests (three inequality rows each) through the
+    reference's solve_qp_admm with default options: tests/golden/reference_kkt_rows.json (the
+    problems, the script's expected objectives and the reference's answers)."""
+    recs = []
+    for case, n, h, optimum, a, b, c, expected in _planted_kkt_draws()[15:]:
+        terms = [(i, j, h[i][j]) for i in range(n) for j in range(i + 1) if h[i][j] != 0]
+        m = len(a)
+        rowptr = [n * i for i in range(m + 1)]
+        col = [j for _ in range(m) for j in range(n)]
+        val = [v for row in a for v in row]
+        status, x, st = O.ref_solve_qp_admm(np.array([t[0] for t in terms]), np.array([t[1] for t in terms]),
+                                            np.array([t[2] for t in terms]), np.array(c), np.full(n, -3.0),
+                                            np.full(n, 3.0), np.array(rowptr, np.int32), np.array(col, np.int32),
+                                            np.array(val), np.full(m, -np.inf), np.array(b), tol=1e-7,
+                                            time_limit=600.0)
+        recs.append({'case': case, 'hrow': [t[0] for t in terms], 'hcol': [t[1] for t in terms],
+                     'hval': [t[2] for t in terms], 'cost': c, 'a_rowptr': rowptr, 'a_col': col, 'a_val': val,
+                     'row_upper': b, 'expected_objective': expected, 'planted_x': optimum, 'status': status,
+                     'iterations': int(st['iterations']), 'objective': st['objective'], 'x': x.tolist(),
+                     'row_dual': st['row_dual'].tolist()})
+        print('kkt_rows', case, status, int(st['iterations']), st['objective'], expected, flush=True)
+    (OUT / 'reference_kkt_rows.json').write_text(json.dumps(recs, indent=1) + '\n')
+
+
 def planted_kkt_cases():
     """The box cases 0-14 of the reference's planted KKT tests (scripts/test_qp.py:30-56): n = 5,
     H = R'R + I with R uniform in [-1, 1], x* uniform in [-1, 1], c = -H x*, box [-3, 3] (x* is
@@ -429,17 +478,8 @@ def planted_kkt_cases():
     reference's CLI, which sends a box QP to solve_accelerated_box with the default options
     (tolerance 1e-7); here the same lower-triangle terms go to it directly.  Each record keeps
     the script's expected objective."""
-    import random
-    rng = random.Random(26121)
     out = []
-    for case in range(15):
-        n = 5
-        r = [[rng.uniform(-1, 1) for _ in range(n)] for _ in range(n)]
-        h = [[sum(r[k][i] * r[k][j] for k in range(n)) + (1 if i == j else 0) for j in range(n)] for i in range(n)]
-        optimum = [rng.uniform(-1, 1) for _ in range(n)]
-        c = [-sum(h[i][j] * optimum[j] for j in range(n)) for i in range(n)]
-        expected = sum(c[i] * optimum[i] + .5 * sum(h[i][j] * optimum[i] * optimum[j] for j in range(n))
-                       for i in range(n))
+    for case, n, h, optimum, _, _, c, expected in _planted_kkt_draws()[:15]:
         terms = [(i, j, h[i][j]) for i in range(n) for j in range(i + 1) if h[i][j] != 0]
         prob = {'hrow': np.array([t[0] for t in terms], np.int64), 'hcol': np.array([t[1] for t in terms], np.int64),
                 'hval': np.array([t[2] for t in terms]), 'cost': np.array(c), 'lower': np.full(n, -3.0),
@@ -458,12 +498,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference/02-software/solver')
     ap.add_argument('--only', choices=['admm', 'open'], default=None,
-                    help='regenerate only the ADMM fixture, or only the one-sided-box cases in place')
+                    help='regenerate only the constrained-QP fixtures (ADMM, dual Newton, checker, KKT rows), '
+                         'or those plus the added box cases merged in place')
     a = ap.parse_args()
     if not O.build_reference(a.reference):
         raise SystemExit('cannot build oracle/_ref from ' + a.reference)
     make_admm_golden()
     make_dual_newton_golden()
+    make_kkt_rows_golden()
     make_check_golden()
     if a.only == 'admm':
         return
