@@ -183,6 +183,7 @@ def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_va
     cost_scale = 1 / max(1.0, float(np.max(np.abs(c)))) if scaling else 1.0
     hva = hva * cost_scale
     c = c * cost_scale
+    rows_input = rows
     arp, aci, ava = _csr_from_rows(rows, n)
     lo_all = np.array(lo_all)
     up_all = np.array(up_all)
@@ -190,7 +191,8 @@ def scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_va
     x = _clip(np.zeros(n), lo_all[m:], up_all[m:])
     z = _clip(csr_matvec(arp, aci, ava, x), lo_all, up_all)
     return {'h': (hrp, hci, hva), 'a': (arp, aci, ava), 'c': c, 'lo': lo_all, 'up': up_all, 'rho': rho,
-            'sigma': 1e-8, 'variable': variable, 'x': x, 'z': z, 'y': np.zeros(m + n)}
+            'sigma': 1e-8, 'variable': variable, 'row_scale': row_scale, 'cost_scale': cost_scale, 'x': x, 'z': z,
+            'y': np.zeros(m + n), 'rows_input': rows_input}
 
 
 def adapt_rho(sp, system, x, z, y, rho_base):
@@ -275,3 +277,116 @@ def admm_iteration(system, c, lo, up, x, z, y, iteration, solve=None):
     nz = _clip(relaxed + y / rho, lo, up)
     y = y + rho * (relaxed - nz)
     return 1.6 * nxt - .6 * x, nz, y, inner
+
+
+def solve_qp_admm_full_restated(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower,
+                                row_upper, tol, iteration_limit=200000, scaling=True):
+    """The reference's whole solve_qp_admm (qp_admm.cpp:118-280) for a minimisation whose Hessian is
+    diagonal, rows not all equalities (so its dual Newton pre-solver declines): the checks of the
+    original model every 25 iterations (oracle.dual_newton.check_rows), the rho adaptation every
+    100, and the KKT polish at iterations 250, 1000 and 5000 in its diagonal-Hessian form
+    (qp_admm.cpp:165-205: active rows from |y| > 1e-5 or equal bounds, CG on K D^-1 K' for the
+    row multipliers, x = -(K' lambda + c) / D, accepted when the original model verifies).
+    Returns (status, iterations, primal, row_dual, check fields, polished)."""
+    from oracle.dual_newton import check_rows
+    m = len(a_rowptr) - 1
+    sp = scale_qp_admm(n, hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,
+                       scaling)
+    (hrp, hci, hva), (arp, aci, ava) = sp['h'], sp['a']
+    diag = np.zeros(n)
+    offdiag = False
+    for i in range(n):
+        for k in range(hrp[i], hrp[i + 1]):
+            if hci[k] == i:
+                diag[i] = hva[k]
+            else:
+                offdiag = True
+    assert not offdiag and np.all(diag > 0), 'the restated polish covers positive diagonal Hessians only'
+    orig_rows = [[(int(a_col[k]), float(a_val[k])) for k in range(a_rowptr[i], a_rowptr[i + 1])] for i in range(m)]
+    c, lo_all, up_all, rho, sigma = sp['c'], sp['lo'], sp['up'], sp['rho'], sp['sigma']
+    sys_ = AdmmSystemOracle((hrp, hci, hva), (arp, aci, ava), n)
+    sys_.set_rho(rho, sigma)
+    x, z, y = sp['x'], sp['z'], sp['y']
+    variable, row_scale, cost_scale = sp['variable'], sp['row_scale'], sp['cost_scale']
+    rows_in = sp['rows_input']
+
+    def check(px, py):
+        return check_rows(hrow, hcol, hval, cost, lower, upper, orig_rows, row_lower, row_upper, px, py, tol)
+
+    def polish():
+        active = [i for i in range(m + n) if lo_all[i] == up_all[i] or abs(y[i]) > 1e-5]
+        if n + len(active) > 10000:
+            return None
+        assert active, 'with no active row the reference polishes by its sparse LU, not restated'
+        target = []
+        for i in active:
+            t = lo_all[i] if lo_all[i] == up_all[i] else (up_all[i] if y[i] > 0 else lo_all[i])
+            if not np.isfinite(t):
+                return None
+            target.append(t)
+        k = _csr_from_rows([rows_in[i] for i in active], n)
+        kt = transpose(*k, n)
+        rhs = csr_matvec(*k, c / diag)
+        ds = np.full(len(active), 1e-18)
+        for r, i in enumerate(active):
+            rhs[r] = -rhs[r] - target[r]
+            for j, v in rows_in[i]:
+                ds[r] += v * v / diag[j]
+        residual = rhs.copy()
+        zp = residual / ds
+        direction = zp.copy()
+        lam = np.zeros(len(active))
+        rz = dot(residual, zp)
+        stop = 1e-13 * (1 + float(np.max(np.abs(rhs))))
+        inner = 0
+        while inner < 20000 and float(np.max(np.abs(residual))) > stop:
+            work = csr_matvec(*kt, direction) / diag
+            mv = csr_matvec(*k, work)
+            den = dot(direction, mv)
+            if not (den > 0) or not np.isfinite(den):
+                break
+            alpha = rz / den
+            lam = lam + alpha * direction
+            residual = residual - alpha * mv
+            zp = residual / ds
+            nxt = dot(residual, zp)
+            beta = nxt / rz
+            rz = nxt
+            direction = zp + beta * direction
+            inner += 1
+        work = -(csr_matvec(*kt, lam) + c) / diag
+        px = work * variable
+        py = np.zeros(m)
+        for r, i in enumerate(active):
+            if i < m:
+                py[i] = lam[r] * row_scale[i] / cost_scale
+        chk = check(px, py)
+        return (px, py, chk) if chk['verified'] else None
+
+    rho_base = 0.1
+    status = 'iteration_limit'
+    result = None
+    for iteration in range(iteration_limit + 1):
+        if iteration % 25 == 0 or iteration == iteration_limit:
+            px = x * variable
+            py = y[:m] * (row_scale[:m] / cost_scale)
+            chk = check(px, py)
+            result = (px, py, chk)
+            if chk['verified']:
+                return 'optimal', iteration, px, py, chk, False
+            if not np.isfinite(chk['objective']) or not np.isfinite(chk['stationarity_residual']):
+                return 'numerical_error', iteration, px, py, chk, False
+            if iteration in (250, 1000, 5000):
+                pol = polish()
+                if pol is not None:
+                    return ('optimal', iteration) + pol + (True,)
+            if iteration and iteration % 100 == 0:
+                nxt = adapt_rho(sp, sys_, x, z, y, rho_base)
+                if nxt != rho_base:
+                    rho_base = nxt
+                    rho = np.where(lo_all == up_all, rho_base * 100, rho_base * 1)
+                    sys_.set_rho(rho, sigma)
+        if iteration == iteration_limit:
+            break
+        x, z, y, _ = admm_iteration(sys_, c, lo_all, up_all, x, z, y, iteration)
+    return (status, iteration_limit) + result + (False,)

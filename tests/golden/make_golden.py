@@ -445,6 +445,49 @@ def _planted_kkt_draws():
     return out
 
 
+def diagonal_inequality_case(seed, n=40, m=25, eq=3):
+    """A QP with a positive diagonal Hessian (U[2, 4]) and m rows of 4 normal entries, bounds
+    [-U[0.1, 0.5], U[0.1, 0.5]], the first `eq` equalities at 0.1; box [-1, 1].  Its rows are not all
+    equalities, so solve_qp_admm skips its dual Newton pre-solver and polishes in the
+    diagonal-Hessian form."""
+    rng = np.random.default_rng(seed)
+    rowptr, col, val = [0], [], []
+    for _ in range(m):
+        cs = np.sort(rng.choice(n, 4, replace=False))
+        col += cs.tolist()
+        val += rng.normal(size=4).tolist()
+        rowptr.append(len(col))
+    lo = -rng.uniform(0.1, 0.5, m)
+    up = rng.uniform(0.1, 0.5, m)
+    lo[:eq] = 0.1
+    up[:eq] = 0.1
+    return {'n': n, 'hrow': np.arange(n, dtype=np.int64), 'hcol': np.arange(n, dtype=np.int64),
+            'hval': rng.uniform(2, 4, n), 'cost': 2 * rng.normal(size=n), 'lower': -np.ones(n), 'upper': np.ones(n),
+            'a_rowptr': np.array(rowptr, np.int32), 'a_col': np.array(col, np.int32), 'a_val': np.array(val),
+            'row_lower': lo, 'row_upper': up}
+
+
+def make_polish_golden():
+    """The reference's solve_qp_admm on diagonal-Hessian QPs with inequality rows at tolerances its
+    ADMM does not reach by iteration 250, where its KKT polish (diagonal-Hessian form) verifies:
+    tests/golden/reference_admm_polish.npz."""
+    out = {}
+    for name, (seed, tol) in {'pol_a': (60, 1e-9), 'pol_b': (62, 1e-10), 'pol_c': (65, 1e-9)}.items():
+        p = diagonal_inequality_case(seed)
+        a = (p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'], p['a_col'],
+             p['a_val'], p['row_lower'], p['row_upper'])
+        status, x, st = O.ref_solve_qp_admm(*a, tol=tol, time_limit=600.0)
+        out.update({f'{name}.{k}': np.asarray(v) for k, v in p.items()})
+        out[f'{name}.tol'] = np.array(tol)
+        out[f'{name}.status'] = np.array(status)
+        out[f'{name}.iterations'] = np.array(int(st['iterations']))
+        out[f'{name}.x'] = x
+        out[f'{name}.row_dual'] = st['row_dual']
+        out[f'{name}.stats'] = np.array([st[k] for k in CHECK_KEYS])
+        print(name, status, int(st['iterations']), st['objective'], flush=True)
+    np.savez_compressed(OUT / 'reference_admm_polish.npz', **out)
+
+
 def make_kkt_rows_golden():
     """Cases 15-29 of the reference's planted KKT tests (three inequality rows each) through the
     reference's solve_qp_admm with default options: tests/golden/reference_kkt_rows.json (the
@@ -506,6 +549,7 @@ def main():
     make_admm_golden()
     make_dual_newton_golden()
     make_kkt_rows_golden()
+    make_polish_golden()
     make_check_golden()
     if a.only == 'admm':
         return

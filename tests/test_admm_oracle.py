@@ -124,3 +124,22 @@ def test_restated_cg_stops_on_breakdown():
         x0 = np.arange(n, dtype=float)
         x, inner, resid = o.solve(np.ones(n), x0, 1e-9, 50)
     assert inner == 0 and np.array_equal(x, x0) and resid == 1.0
+
+
+def test_restated_admm_with_kkt_polish_matches_reference_golden():
+    """The whole restated solve_qp_admm (checks every 25 iterations, rho adaptation, and the KKT
+    polish in its diagonal-Hessian form, qp_admm.cpp:165-205) on diagonal-Hessian QPs whose ADMM
+    does not verify by iteration 250: the polish at 250 verifies, and status, iteration count,
+    primal and row duals equal the reference's (tests/golden/reference_admm_polish.npz)."""
+    from oracle.admm_pcg import solve_qp_admm_full_restated
+    exact = np.finfo(np.longdouble).nmant == 63
+    for name, p in _golden_admm('reference_admm_polish.npz'):
+        status, iterations, x, y, chk, polished = solve_qp_admm_full_restated(
+            int(p['n']), p['hrow'], p['hcol'], p['hval'], p['cost'], p['lower'], p['upper'], p['a_rowptr'],
+            p['a_col'], p['a_val'], p['row_lower'], p['row_upper'], float(p['tol']))
+        assert status == str(p['status']) == 'optimal' and iterations == int(p['iterations']) == 250, name
+        assert polished, name
+        if exact:
+            assert np.array_equal(x, p['x']) and np.array_equal(y, p['row_dual']), name
+        else:
+            assert np.max(np.abs(x - p['x'])) <= 1e-12, name
