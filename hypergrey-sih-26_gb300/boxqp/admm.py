@@ -156,12 +156,13 @@ def _row_of(rowptr):
     return np.repeat(np.arange(len(rowptr) - 1), np.diff(np.asarray(rowptr, dtype=np.int64)))
 
 
-def row_sums(rowptr, terms, exact_rows=64):
-    """Per-row sums of CSR-ordered terms, in the terms' dtype, each row summed from 0 in entry
-    order (as the reference's loops sum them) when no row has more than `exact_rows` entries:
-    one entry position at a time across all rows.  Longer rows: numpy's blocked summation."""
+def row_sums(rowptr, terms, exact_rows=64, initial=0.0):
+    """Per-row sums of CSR-ordered terms, in the terms' dtype, each row summed from `initial` in
+    entry order (as the reference's loops sum them) when no row has more than `exact_rows`
+    entries: one entry position at a time across all rows.  Longer rows: numpy's blocked
+    summation."""
     rowptr = np.asarray(rowptr, dtype=np.int64)
-    out = np.zeros(rowptr.shape[0] - 1, dtype=terms.dtype)
+    out = np.full(rowptr.shape[0] - 1, initial, dtype=terms.dtype)
     if not len(terms):
         return out
     lens = np.diff(rowptr)
@@ -172,8 +173,15 @@ def row_sums(rowptr, terms, exact_rows=64):
             out[rows_k] += terms[rowptr[rows_k] + k]
     else:
         nz = np.flatnonzero(lens > 0)
-        out[nz] = np.add.reduceat(terms, rowptr[nz])
+        out[nz] += np.add.reduceat(terms, rowptr[nz])
     return out
+
+
+def dot_ld(a, b):
+    """sum_j a_j b_j accumulated in long double in order (the reference's dot, qp_admm.cpp:23)."""
+    if len(a) == 0:
+        return 0.0
+    return float(np.cumsum(np.asarray(a, dtype=np.longdouble) * np.asarray(b, dtype=np.longdouble))[-1])
 
 
 def csr_multiply(rowptr, col, val, v):
@@ -233,12 +241,16 @@ def admm_setup(q, rows, scaling=True):
     cost_scale = 1 / max(1.0, _norm(c)) if scaling else 1.0
     hva = hva * cost_scale
     c = c * cost_scale
-    a_ptr, a_col, a_val = merge_rows(np.concatenate([arp, arp[-1] + 1 + np.arange(n)]),
-                                     np.concatenate([acol, np.arange(n)]), np.concatenate([aval, np.ones(n)]))
+    rows_input = (np.concatenate([arp, arp[-1] + 1 + np.arange(n)]), np.concatenate([acol, np.arange(n)]),
+                  np.concatenate([aval, np.ones(n)]))
+    a_ptr, a_col, a_val = merge_rows(*rows_input)
     x = _clip(np.zeros(n), lo[m:], up[m:])
     z = _clip(csr_multiply(a_ptr, a_col, a_val, x), lo, up)
     rho_base = 0.1
+    diagonal = diagonal_of(hva)
+    diagonal_hessian = bool(np.all(diagonal > 0) and np.all(on_diag))
     return {'n': n, 'm': m, 'h': (hrp, hci, hva), 'a': (a_ptr, a_col, a_val), 'c': c, 'lo': lo, 'up': up,
+            'rows_input': rows_input, 'diagonal': diagonal, 'diagonal_hessian': diagonal_hessian,
             'variable': variable, 'row_scale': row_scale, 'cost_scale': cost_scale, 'sign': sign,
             'rho_base': rho_base, 'rho': np.where(lo == up, rho_base * 100, rho_base * 1), 'sigma': 1e-8,
             'x': x, 'z': z, 'y': np.zeros(m + n)}
@@ -395,17 +407,80 @@ def check_solution(q, rows, x, row_dual, tol):
     return out
 
 
+def polish_diagonal(q, rows, sp, y, tol):
+    """The reference's KKT polish in its diagonal-Hessian form (qp_admm.cpp:165-205), run at
+    iterations 250, 1000 and 5000: rows with equal bounds or |y_i| > 1e-5 are taken as active at
+    the bound y points to; the multipliers of K x = target (K the active scaled rows, x eliminated
+    through the diagonal, x = -(K' lambda + c) / D) come from Jacobi-preconditioned CG on
+    K D^-1 K' (a 1e-18 shift on its diagonal, stop at max|r| <= 1e-13 (1 + max|rhs|) or 20,000
+    iterations); the candidate is kept only if the original model verifies.  Returns the check
+    fields with 'primal' and 'row_dual', or None (no candidate, or it did not verify).  Not the
+    form for a Hessian with off-diagonal terms or a zero diagonal, which the reference factors
+    with its sparse LU."""
+    n, m = sp['n'], sp['m']
+    lo, up = sp['lo'], sp['up']
+    active = np.flatnonzero((lo == up) | (np.abs(y) > 1e-5))
+    if n + len(active) > 10000 or not sp['diagonal_hessian'] or not len(active):
+        return None
+    target = np.where(lo[active] == up[active], lo[active], np.where(y[active] > 0, up[active], lo[active]))
+    if not np.all(np.isfinite(target)):
+        return None
+    rp_in, col_in, val_in = sp['rows_input']
+    lens = np.diff(rp_in)[active]
+    sel = np.concatenate([np.arange(rp_in[i], rp_in[i + 1]) for i in active]) if len(active) else np.zeros(0, int)
+    sub_ptr = np.zeros(len(active) + 1, dtype=np.int64)
+    np.cumsum(lens, out=sub_ptr[1:])
+    k = merge_rows(sub_ptr, col_in[sel], val_in[sel])
+    kt = transpose(*k, n)
+    d = sp['diagonal']
+    c = sp['c']
+    rhs = -csr_multiply(*k, c / d) - target
+    ds = row_sums(sub_ptr, val_in[sel] * val_in[sel] / d[col_in[sel]], initial=1e-18)
+    residual = rhs.copy()
+    zp = residual / ds
+    direction = zp.copy()
+    lam = np.zeros(len(active))
+    rz = dot_ld(residual, zp)
+    stop = 1e-13 * (1 + _norm(rhs))
+    inner = 0
+    while inner < 20000 and _norm(residual) > stop:
+        mv = csr_multiply(*k, csr_multiply(*kt, direction) / d)
+        den = dot_ld(direction, mv)
+        if not (den > 0) or not math.isfinite(den):
+            break
+        alpha = rz / den
+        lam = lam + alpha * direction
+        residual = residual - alpha * mv
+        zp = residual / ds
+        nxt = dot_ld(residual, zp)
+        beta = nxt / rz
+        rz = nxt
+        direction = zp + beta * direction
+        inner += 1
+    px = (-(csr_multiply(*kt, lam) + c) / d) * sp['variable']
+    py = np.zeros(m)
+    rows_m = active < m
+    py[active[rows_m]] = lam[rows_m] * sp['row_scale'][active[rows_m]] / sp['cost_scale']
+    chk = check_solution(q, rows, px, py, tol)
+    if not chk['verified']:
+        return None
+    chk['primal'] = px
+    chk['row_dual'] = py
+    return chk
+
+
 def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     """The reference's solve_qp_admm (qp_admm.cpp:118-280) with its iterations on the GPU.
 
     Mirrors its option and input checks (ValueError 'Invalid QP options' / 'Continuous QP
     required'), the statuses unsupported_curvature and infeasible_bounds, the scaled set-up, the
     check of the original model every 25 iterations and at the limit (optimal once verified,
-    numerical_error on a non-finite objective or stationarity, time_limit), and the rho adaptation
-    every 100 iterations; each 25 iterations run on the device in one bqp_admm_iterate call.
-    Not mirrored: the diagonal-Hessian equality solver tried first (qp_dual_newton.cpp), the
-    KKT polish at iterations 250, 1000 and 5000 (its sparse LU), and the time check inside the
-    inner CG.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
+    numerical_error on a non-finite objective or stationarity, time_limit), the KKT polish at
+    iterations 250, 1000 and 5000 in its diagonal-Hessian form (polish_diagonal, on the host) and
+    the rho adaptation every 100 iterations; each 25 iterations run on the device in one
+    bqp_admm_iterate call.  Not mirrored: the diagonal-Hessian equality solver tried first
+    (qp_dual_newton.cpp), the polish's sparse-LU form for other Hessians, and the time checks
+    inside the inner and polish CG loops.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
     as CSR triples; the system needs set_rho, iterate and close)."""
     from .api import QpOptions, QpResult, check_convex_hessian
     o = options or QpOptions()
@@ -464,6 +539,20 @@ def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
                 if time.monotonic() - start >= o.time_limit:
                     result.status = 'time_limit'
                     break
+                if it in (250, 1000, 5000):
+                    pol = polish_diagonal(q, rows, sp, y, o.tolerance)
+                    if pol is not None:
+                        result.status = 'optimal'
+                        result.algorithm = 'scaled_admm_pcg_kkt_polish'
+                        result.primal, result.row_dual = pol['primal'], pol['row_dual']
+                        result.objective = pol['objective']
+                        result.primal_residual = pol['primal_residual']
+                        result.stationarity_residual = pol['stationarity_residual']
+                        result.complementarity_residual = pol['complementarity_residual']
+                        result.dual_bound = pol['dual_bound']
+                        result.relative_gap = pol['relative_gap']
+                        result.optimality_verified = True
+                        break
                 if it and it % 100 == 0:
                     nxt = adapt_rho(sp, x, z, y, rho_base, at)
                     if nxt != rho_base:

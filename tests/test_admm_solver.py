@@ -230,6 +230,23 @@ def test_solve_qp_admm_statuses_and_option_checks():
     assert r.status == 'time_limit' and r.iterations == 0
 
 
+def test_solve_qp_admm_kkt_polish_reproduces_the_reference():
+    """Diagonal-Hessian QPs whose ADMM does not verify by iteration 250: the loop's KKT polish
+    (polish_diagonal) verifies there and returns the reference's primal and row duals
+    (tests/golden/reference_admm_polish.npz; bit for bit where long double is the reference's)."""
+    for name, p in _cases('reference_admm_polish.npz'):
+        q, rows = _problem(p)
+        r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=float(p['tol'])),
+                          make_system=lambda h, a, n: RestatedSystem(h, a, n))
+        assert r.status == 'optimal' and r.iterations == 250 == int(p['iterations']), (name, r.status, r.iterations)
+        assert r.algorithm == 'scaled_admm_pcg_kkt_polish' and r.optimality_verified
+        if EXACT:
+            assert _same(r.primal, p['x']) and _same(r.row_dual, p['row_dual']), name
+        else:
+            assert np.max(np.abs(r.primal - p['x'])) <= 1e-10, name
+        assert r.objective == pytest.approx(float(p['stats'][0]), rel=1e-13), name
+
+
 def test_planted_kkt_tests_of_the_reference_scripts_with_rows():
     """Cases 15-29 of the reference's planted KKT tests (scripts/test_qp.py:30-56: n = 5, dense
     PSD Hessian, three inequality rows active at the planted optimum; tests/golden/
