@@ -469,6 +469,62 @@ def polish_diagonal(q, rows, sp, y, tol):
     return chk
 
 
+def polish_kkt(q, rows, sp, y, tol):
+    """The reference's KKT polish in its general form (qp_admm.cpp:206-230), for Hessians that are
+    not a positive diagonal: rows with equal bounds or |y_i| > 1e-5 are active at the bound that
+    y_i >= 0 points to (the lower one for y_i < 0); the regularised KKT system
+    [[H + 1e-9 I, K'], [K, -1e-9 I]] [x; lambda] = [-c; target] is factored once (SuperLU here,
+    the reference's own sparse LU there) and refined 8 times against the unregularised system;
+    the candidate is kept only if the original model verifies.  At most 10,000 unknowns.
+    Returns the check fields with 'primal' and 'row_dual', or None."""
+    import scipy.sparse as sps
+    from scipy.sparse.linalg import splu
+    n, m = sp['n'], sp['m']
+    lo, up = sp['lo'], sp['up']
+    active = np.flatnonzero((lo == up) | (np.abs(y) > 1e-5))
+    na = len(active)
+    if n + na > 10000:
+        return None
+    target = np.where(lo[active] == up[active], lo[active], np.where(y[active] >= 0, up[active], lo[active]))
+    if not np.all(np.isfinite(target)):
+        return None
+    reg = 1e-9
+    hrp, hci, hva = sp['h']
+    arp, aci, ava = sp['a']
+    hrow = _row_of(hrp)
+    lens = np.diff(np.asarray(arp, dtype=np.int64))[active]
+    sel = np.concatenate([np.arange(arp[i], arp[i + 1]) for i in active]) if na else np.zeros(0, dtype=np.int64)
+    krow = np.repeat(np.arange(na), lens)
+    rows_i = np.concatenate([hrow, np.arange(n), n + krow, aci[sel], n + np.arange(na)])
+    cols_i = np.concatenate([hci, np.arange(n), aci[sel], n + krow, n + np.arange(na)])
+    vals = np.concatenate([hva, np.full(n, reg), ava[sel], ava[sel], np.full(na, -reg)])
+    size = n + na
+    mat = sps.coo_matrix((vals, (rows_i, cols_i)), shape=(size, size)).tocsc()
+    shift = np.concatenate([np.full(n, reg), np.full(na, -reg)])
+    rhs = np.concatenate([-sp['c'], target])
+    try:
+        factor = splu(mat)
+    except RuntimeError:  # singular
+        return None
+    solution = np.zeros(size)
+    residual = rhs.copy()
+    for _ in range(8):
+        solution = solution + factor.solve(residual)
+        residual = rhs - mat @ solution + shift * solution
+    if not np.all(np.isfinite(solution)):
+        return None
+    px = solution[:n] * sp['variable']
+    py = np.zeros(m)
+    rows_m = active < m
+    py[active[rows_m]] = solution[n:][rows_m] * sp['row_scale'][active[rows_m]] / sp['cost_scale']
+    chk = check_solution(q, rows, px, py, tol)
+    if not chk['verified']:
+        return None
+    chk['primal'] = px
+    chk['row_dual'] = py
+    return chk
+
+
 def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     """The reference's solve_qp_admm (qp_admm.cpp:118-280) with its iterations on the GPU.
 
@@ -476,11 +532,12 @@ def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     required'), the statuses unsupported_curvature and infeasible_bounds, the scaled set-up, the
     check of the original model every 25 iterations and at the limit (optimal once verified,
     numerical_error on a non-finite objective or stationarity, time_limit), the KKT polish at
-    iterations 250, 1000 and 5000 in its diagonal-Hessian form (polish_diagonal, on the host) and
-    the rho adaptation every 100 iterations; each 25 iterations run on the device in one
+    iterations 250, 1000 and 5000 (on the host, as the reference runs it: polish_diagonal for a
+    positive diagonal Hessian, else polish_kkt, whose factorisation is SuperLU's instead of the
+    reference's own LU, so its candidates agree with the reference's to rounding) and the rho
+    adaptation every 100 iterations; each 25 iterations run on the device in one
     bqp_admm_iterate call.  Not mirrored: the diagonal-Hessian equality solver tried first
-    (qp_dual_newton.cpp), the polish's sparse-LU form for other Hessians, and the time checks
-    inside the inner and polish CG loops.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
+    (qp_dual_newton.cpp) and the time checks inside the inner and polish loops.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
     as CSR triples; the system needs set_rho, iterate and close)."""
     from .api import QpOptions, QpResult, check_convex_hessian
     o = options or QpOptions()
@@ -540,7 +597,10 @@ def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
                     result.status = 'time_limit'
                     break
                 if it in (250, 1000, 5000):
-                    pol = polish_diagonal(q, rows, sp, y, o.tolerance)
+                    if sp['diagonal_hessian'] and np.any((sp['lo'] == sp['up']) | (np.abs(y) > 1e-5)):
+                        pol = polish_diagonal(q, rows, sp, y, o.tolerance)
+                    else:
+                        pol = polish_kkt(q, rows, sp, y, o.tolerance)
                     if pol is not None:
                         result.status = 'optimal'
                         result.algorithm = 'scaled_admm_pcg_kkt_polish'
