@@ -96,6 +96,7 @@ PROTOTYPES = {
     'bqp_csr_from_lower': (c_int, [c_int64, c_int64, _I64P, _I64P, _F64P, c_double, _I32P, _I32P, _F64P, _I64P]),
     'bqp_check_convex': (c_int, [c_int64, c_int64, _I64P, _I64P, _F64P, c_int32]),
     'bqp_gershgorin': (c_double, [c_int64, _I32P, _F64P]),
+    'bqp_dot_ld': (c_double, [c_int64, _F64P, _F64P]),
     'bqp_planted_preset': (c_int, [c_int32, c_uint64, c_int64, c_int64, POINTER(PlantedSpec)]),
     'bqp_planted_create': (c_void_p, [POINTER(PlantedSpec)]),
     'bqp_planted_info': (c_int, [c_void_p, _I64P, _I64P, _I64P, _F64P]),

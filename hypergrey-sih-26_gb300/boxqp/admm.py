@@ -156,32 +156,38 @@ def _row_of(rowptr):
     return np.repeat(np.arange(len(rowptr) - 1), np.diff(np.asarray(rowptr, dtype=np.int64)))
 
 
-def row_sums(rowptr, terms, exact_rows=64, initial=0.0):
-    """Per-row sums of CSR-ordered terms, in the terms' dtype, each row summed from `initial` in
-    entry order (as the reference's loops sum them) when no row has more than `exact_rows`
-    entries: one entry position at a time across all rows.  Longer rows: numpy's blocked
-    summation."""
+def row_sums(rowptr, terms, initial=0.0):
+    """Per-row sums of CSR-ordered terms, in the terms' dtype, each row summed from `initial` one
+    entry after another in entry order, as the reference's loops sum them (np.add.at applies its
+    updates in index order, unbuffered)."""
     rowptr = np.asarray(rowptr, dtype=np.int64)
     out = np.full(rowptr.shape[0] - 1, initial, dtype=terms.dtype)
-    if not len(terms):
-        return out
-    lens = np.diff(rowptr)
-    longest = int(lens.max())
-    if longest <= exact_rows:
-        for k in range(longest):
-            rows_k = np.flatnonzero(lens > k)
-            out[rows_k] += terms[rowptr[rows_k] + k]
-    else:
-        nz = np.flatnonzero(lens > 0)
-        out[nz] += np.add.reduceat(terms, rowptr[nz])
+    if len(terms):
+        np.add.at(out, _row_of(rowptr), terms)
     return out
 
 
 def dot_ld(a, b):
-    """sum_j a_j b_j accumulated in long double in order (the reference's dot, qp_admm.cpp:23)."""
-    if len(a) == 0:
-        return 0.0
-    return float(np.cumsum(np.asarray(a, dtype=np.longdouble) * np.asarray(b, dtype=np.longdouble))[-1])
+    """sum_j a_j b_j accumulated in long double in order (the reference's dot, qp_admm.cpp:23;
+    bqp_dot_ld in the library)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return lib().bqp_dot_ld(a.shape[0], ptr(a, N.c_double), ptr(b, N.c_double))
+
+
+class _Csr:
+    """A CSR matrix for repeated products on the host: scipy's CSR product, which sums each row
+    from 0 in entry order as CsrMatrix::multiply does (include/sparse_matrix.hpp:26-33), with the
+    entries kept in the given order."""
+
+    def __init__(self, rowptr, col, val, n_cols):
+        import scipy.sparse as sps
+        rowptr = np.asarray(rowptr, dtype=np.int64)
+        self.m = sps.csr_matrix((np.asarray(val, dtype=np.float64), np.asarray(col, dtype=np.int64), rowptr),
+                                shape=(rowptr.shape[0] - 1, n_cols))
+
+    def mul(self, v):
+        return self.m @ v
 
 
 def csr_multiply(rowptr, col, val, v):
@@ -430,11 +436,12 @@ def polish_diagonal(q, rows, sp, y, tol):
     sel = np.concatenate([np.arange(rp_in[i], rp_in[i + 1]) for i in active]) if len(active) else np.zeros(0, int)
     sub_ptr = np.zeros(len(active) + 1, dtype=np.int64)
     np.cumsum(lens, out=sub_ptr[1:])
-    k = merge_rows(sub_ptr, col_in[sel], val_in[sel])
-    kt = transpose(*k, n)
+    k_csr = merge_rows(sub_ptr, col_in[sel], val_in[sel])
+    k = _Csr(*k_csr, n)
+    kt = _Csr(*transpose(*k_csr, n), len(active))
     d = sp['diagonal']
     c = sp['c']
-    rhs = -csr_multiply(*k, c / d) - target
+    rhs = -k.mul(c / d) - target
     ds = row_sums(sub_ptr, val_in[sel] * val_in[sel] / d[col_in[sel]], initial=1e-18)
     residual = rhs.copy()
     zp = residual / ds
@@ -444,7 +451,7 @@ def polish_diagonal(q, rows, sp, y, tol):
     stop = 1e-13 * (1 + _norm(rhs))
     inner = 0
     while inner < 20000 and _norm(residual) > stop:
-        mv = csr_multiply(*k, csr_multiply(*kt, direction) / d)
+        mv = k.mul(kt.mul(direction) / d)
         den = dot_ld(direction, mv)
         if not (den > 0) or not math.isfinite(den):
             break
@@ -457,7 +464,7 @@ def polish_diagonal(q, rows, sp, y, tol):
         rz = nxt
         direction = zp + beta * direction
         inner += 1
-    px = (-(csr_multiply(*kt, lam) + c) / d) * sp['variable']
+    px = (-(kt.mul(lam) + c) / d) * sp['variable']
     py = np.zeros(m)
     rows_m = active < m
     py[active[rows_m]] = lam[rows_m] * sp['row_scale'][active[rows_m]] / sp['cost_scale']
@@ -525,19 +532,157 @@ def polish_kkt(q, rows, sp, y, tol):
     return chk
 
 
+def solve_diagonal_equalities(q, rows, options):
+    """The reference's pre-solver for a positive diagonal Hessian with only finite equality rows
+    (src/qp_dual_newton.cpp:9-66), on the host as the reference runs it: whiten the variables by
+    the diagonal, scale rows and magnitude, then Newton steps on the concave dual -- x(y) is the
+    box projection of -(A'y + c), the Newton direction comes from Jacobi-preconditioned CG on the
+    active-set Schur matrix A diag(free) A' (a 1e-12 (1 + max diag) shift), and a backtracking
+    line search (Armijo 1e-4, up to 60 halvings) -- checking the original model at every
+    iteration, at most 500 of them.  Returns a QpResult: 'optimal', 'iteration_limit',
+    'time_limit', 'numerical_stall', 'numerical_scaling_failure' or 'unsupported_structure'
+    (another structure, which solve_qp_admm hands to its ADMM)."""
+    from .api import QpResult
+    start = time.monotonic()
+    result = QpResult(status='unsupported_structure', algorithm='diagonal_qp_dual_newton')
+    n, m = q.n, rows.m
+    sign = -1.0 if q.maximize else 1.0
+    rl = np.asarray(rows.lower, dtype=np.float64)
+    ru = np.asarray(rows.upper, dtype=np.float64)
+    if not m or np.any(rl != ru) or not np.all(np.isfinite(rl)):
+        return result
+    hr = np.asarray(q.hessian_row, dtype=np.int64)
+    hc = np.asarray(q.hessian_col, dtype=np.int64)
+    hv = np.asarray(q.hessian_val, dtype=np.float64)
+    if np.any((hr != hc) & (hv != 0)):
+        return result
+    h = np.zeros(n)
+    np.add.at(h, hr, sign * hv)
+    if not np.all(h > 0) or not np.all(np.isfinite(h)):
+        return result
+    units = 1 / np.sqrt(h)
+    lo = np.asarray(q.lower, dtype=np.float64) / units
+    up = np.asarray(q.upper, dtype=np.float64) / units
+    c = sign * np.asarray(q.cost, dtype=np.float64) * units
+    rp = np.asarray(rows.rowptr, dtype=np.int64)
+    col = np.asarray(rows.col, dtype=np.int64)
+    row = _row_of(rp)
+    val = np.asarray(rows.val, dtype=np.float64) * units[col]
+    maximum = np.zeros(m)
+    np.maximum.at(maximum, row, np.abs(val))
+    row_units = np.where(maximum != 0, 1 / np.where(maximum != 0, maximum, 1.0), 1.0)
+    val = val * row_units[row]
+    b = rl * row_units
+    magnitude = 1.0
+    if options.scaling:
+        magnitude = max(magnitude, _norm(c), _norm(np.maximum(lo, np.minimum(up, 0.0))), _norm(b))
+    units = units * magnitude
+    lo, up, c = lo / magnitude, up / magnitude, c / magnitude
+    b = b / magnitude
+    row_units = row_units * magnitude
+    if (not np.all(np.isfinite(units)) or not np.all(np.isfinite(c)) or np.any(np.isnan(lo)) or np.any(np.isnan(up))
+            or not np.all(np.isfinite(b)) or not np.all(np.isfinite(row_units))):
+        result.status = 'numerical_scaling_failure'
+        return result
+    a_csr = merge_rows(rp, col, val)
+    a = _Csr(*a_csr, n)
+    at = _Csr(*transpose(*a_csr, n), m)
+
+    def evaluate(dual):
+        raw = -(at.mul(dual) + c)
+        free = ((raw >= lo) & (raw <= up)).astype(np.float64)
+        primal = np.maximum(lo, np.minimum(up, raw))
+        g = a.mul(primal) - b
+        terms = np.concatenate([np.longdouble(0.5) * primal.astype(np.longdouble) * primal.astype(np.longdouble)
+                                + (c * primal).astype(np.longdouble),
+                                dual.astype(np.longdouble) * g.astype(np.longdouble)])
+        return np.cumsum(terms)[-1], primal, g, free
+
+    def fill(x, y):
+        result.primal = x * units
+        result.row_dual = y * row_units
+        chk = check_solution(q, rows, result.primal, result.row_dual, options.tolerance)
+        result.objective = chk['objective']
+        result.primal_residual = chk['primal_residual']
+        result.stationarity_residual = chk['stationarity_residual']
+        result.complementarity_residual = chk['complementarity_residual']
+        result.dual_bound = chk['dual_bound']
+        result.relative_gap = chk['relative_gap']
+        result.optimality_verified = chk['verified']
+        return chk['verified']
+
+    y = np.zeros(m)
+    result.status = 'iteration_limit'
+    sq = val * val
+    for iteration in range(min(int(options.iteration_limit), 500)):
+        value, x, gradient, mask = evaluate(y)
+        result.iterations = iteration
+        if fill(x, y):
+            result.status = 'optimal'
+            return result
+        if time.monotonic() - start >= options.time_limit:
+            result.status = 'time_limit'
+            return result
+        diagonal = row_sums(rp, sq * mask[col])
+        regularization = 1e-12 * (1 + _norm(diagonal))
+        diagonal = diagonal + regularization
+        r = gradient.copy()
+        z = r / diagonal
+        direction = z.copy()
+        step = np.zeros(m)
+        rz = dot_ld(r, z)
+        gn = _norm(gradient)
+        accuracy = max(1e-12, min(.01, math.sqrt(gn)) * gn)
+        inner = 0
+        while inner < min(10000, 4 * m + 50) and _norm(r) > accuracy:
+            mv = a.mul(at.mul(direction) * mask) + regularization * direction
+            den = dot_ld(direction, mv)
+            if not (den > 0) or not math.isfinite(den):
+                break
+            alpha = rz / den
+            step = step + alpha * direction
+            r = r - alpha * mv
+            z = r / diagonal
+            nxt = dot_ld(r, z)
+            beta = nxt / rz
+            rz = nxt
+            direction = z + beta * direction
+            if inner % 100 == 0 and time.monotonic() - start >= options.time_limit:
+                break
+            inner += 1
+        slope = dot_ld(gradient, step)
+        if not (slope > 0) or not math.isfinite(slope):
+            step = gradient.copy()
+            slope = dot_ld(gradient, gradient)
+        length = 1.0
+        for _ in range(60):
+            ny = y + length * step
+            nv = evaluate(ny)[0]
+            if (np.isfinite(nv) and nv >= value + np.longdouble(1e-4 * length * slope)
+                    - np.longdouble(1e-13) * (1 + abs(value))):
+                y = ny
+                break
+            length *= .5
+        else:
+            result.status = 'numerical_stall'
+            return result
+    return result
+
+
 def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     """The reference's solve_qp_admm (qp_admm.cpp:118-280) with its iterations on the GPU.
 
     Mirrors its option and input checks (ValueError 'Invalid QP options' / 'Continuous QP
     required'), the statuses unsupported_curvature and infeasible_bounds, the scaled set-up, the
     check of the original model every 25 iterations and at the limit (optimal once verified,
-    numerical_error on a non-finite objective or stationarity, time_limit), the KKT polish at
+    numerical_error on a non-finite objective or stationarity, time_limit), the diagonal-equality
+    pre-solver tried first (solve_diagonal_equalities, on the host as the reference runs it), the
+    KKT polish at
     iterations 250, 1000 and 5000 (on the host, as the reference runs it: polish_diagonal for a
     positive diagonal Hessian, else polish_kkt, whose factorisation is SuperLU's instead of the
     reference's own LU, so its candidates agree with the reference's to rounding) and the rho
     adaptation every 100 iterations; each 25 iterations run on the device in one
-    bqp_admm_iterate call.  Not mirrored: the diagonal-Hessian equality solver tried first
-    (qp_dual_newton.cpp) and the time checks inside the inner and polish loops.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
+    bqp_admm_iterate call.  Not mirrored: the time checks inside the inner and polish loops.  make_system(h, a, n) -> system replaces the device system (h, a: the scaled H and A
     as CSR triples; the system needs set_rho, iterate and close)."""
     from .api import QpOptions, QpResult, check_convex_hessian
     o = options or QpOptions()
@@ -559,6 +704,14 @@ def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     if np.any(np.asarray(q.lower) > np.asarray(q.upper)) or np.any(np.asarray(rows.lower) > np.asarray(rows.upper)):
         result.status = 'infeasible_bounds'
         return result
+    # the pre-solver for diagonal Hessians with equality rows, with part of the time budget
+    # (qp_admm.cpp:128-133)
+    small = n <= 512
+    pre = solve_diagonal_equalities(q, rows, QpOptions(
+        time_limit=min(2.0 if small else 10.0, (.2 if small else .5) * o.time_limit), tolerance=o.tolerance,
+        iteration_limit=o.iteration_limit, threads=o.threads, scaling=o.scaling))
+    if pre.status == 'optimal':
+        return pre
     sp = admm_setup(q, rows, o.scaling)
     at = transpose(*sp['a'], n)
     if make_system is None:

@@ -234,4 +234,10 @@ double bqp_gershgorin(int64_t n, const int32_t* rowptr, const double* val) {
     return lipschitz;
 }
 
+double bqp_dot_ld(int64_t n, const double* a, const double* b) {
+    long double s = 0;
+    for (int64_t j = 0; j < n; ++j) s += static_cast<long double>(a[j]) * b[j];
+    return static_cast<double>(s);
+}
+
 }  // extern "C"

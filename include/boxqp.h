@@ -269,6 +269,9 @@ int bqp_check_convex(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* 
                      const double* hval, int32_t maximize);
 /* Gershgorin bound max_i sum_k |Q_ik| of a full CSR.                                         */
 double bqp_gershgorin(int64_t n, const int32_t* rowptr, const double* val);
+/* sum_j a_j b_j accumulated in long double, in order (the reference's dot, src/qp_admm.cpp:23
+ * and src/qp_dual_newton.cpp:35): the host side of the constrained-QP loop's CG steps.       */
+double bqp_dot_ld(int64_t n, const double* a, const double* b);
 
 /* ---- planted instance generator (synthetic workloads) ------------------------------------
  * Families: 0 random-graph weighted Laplacian + diagonal, 1 five-point grid Laplacian + shift,

@@ -10,13 +10,15 @@ tests/golden/make_golden.py from the reference built in oracle/_ref).
 """
 import json
 import math
+import os
 from pathlib import Path
 
 import numpy as np
 import pytest
 
 import boxqp
-from boxqp.admm import LinearRows, admm_setup, check_solution, merge_rows, solve_qp_admm
+from boxqp.admm import (LinearRows, admm_setup, check_solution, merge_rows, solve_diagonal_equalities,
+                        solve_qp_admm)
 from oracle.admm_pcg import AdmmSystemOracle, admm_iteration, scale_qp_admm
 
 GOLDEN = Path(__file__).resolve().parent / 'golden'
@@ -286,3 +288,43 @@ def test_planted_kkt_tests_of_the_reference_scripts_with_rows():
             assert r.algorithm == 'scaled_admm_pcg_kkt_polish', rec['case']
             assert r.objective == pytest.approx(rec['objective'], rel=1e-12, abs=1e-12), rec['case']
             assert np.max(np.abs(r.primal - np.array(rec['x']))) <= 1e-9, rec['case']
+
+
+def test_diagonal_equality_presolver_reproduces_the_reference():
+    """Positive diagonal Hessian, only equality rows: solve_qp_admm returns its pre-solver's answer
+    (solve_diagonal_equalities, the reference's dual Newton) with the reference's status,
+    iteration count, primal and row duals (tests/golden/reference_dual_newton.npz), scaled and
+    unscaled; a run capped at 3 iterations with an unreachable tolerance stops where the
+    reference's does."""
+    for name, p in _cases('reference_dual_newton.npz'):
+        q, rows = _problem(p)
+        tol, limit = float(p['tol']), int(p['limit'])
+        o = boxqp.QpOptions(tolerance=tol, iteration_limit=limit, scaling=bool(p['scaling']), time_limit=600.0)
+        if str(p['status']) == 'optimal':
+            r = solve_qp_admm(q, rows, o, make_system=lambda h, a, n: pytest.fail('the ADMM must not run'))
+            assert r.algorithm == 'diagonal_qp_dual_newton', name
+        else:
+            r = solve_diagonal_equalities(q, rows, o)
+        assert r.status == str(p['status']) and r.iterations == int(p['iterations']), (name, r.status, r.iterations)
+        if EXACT:
+            assert _same(r.primal, p['x']) and _same(r.row_dual, p['row_dual']), name
+        else:
+            assert np.max(np.abs(r.primal - p['x'])) <= 1e-10, name
+    # other structures are declined at once
+    name, p = _cases('reference_admm_solve.npz')[0]
+    q, rows = _problem(p)
+    assert solve_diagonal_equalities(q, rows, boxqp.QpOptions()).status == 'unsupported_structure'
+
+
+@pytest.mark.skipif(not os.environ.get('BOXQP_REFERENCE_DIR'), reason='set BOXQP_REFERENCE_DIR to the reference solver')
+def test_solve_qp_admm_on_qplib_9002():
+    """QPLIB 9002 (2,890 variables, diagonal Hessian, 1,649 equality rows), read by
+    read_qplib_rows: the pre-solver answers within its 10 s share of the default time limit with
+    the reference's status, iteration count (180), primal and row duals; no ADMM runs."""
+    from boxqp.qplib import read_qplib_rows
+    path = Path(os.environ['BOXQP_REFERENCE_DIR']) / 'datasets' / 'qplib' / '9002.qplib'
+    q, rows = read_qplib_rows(path.read_text())
+    r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-7),
+                      make_system=lambda h, a, n: pytest.fail('the ADMM must not run'))
+    assert r.status == 'optimal' and r.algorithm == 'diagonal_qp_dual_newton' and r.iterations == 180
+    assert r.objective == pytest.approx(5698097498.5664835, rel=1e-15)
