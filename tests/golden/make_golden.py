@@ -405,6 +405,28 @@ def check_cases():
     ]
 
 
+def convexity_cases():
+    """Hessians (lower-triangle triplets) at the edges of the reference's convexity gate
+    (src/qp_admm.cpp:30-62): (name, n, terms, maximize)."""
+    rng = np.random.default_rng(77)
+    n = 30
+    r = rng.normal(size=(8, n))
+    gram = r.T @ r  # rank 8: PSD, singular, not diagonally dominant
+    low = [(i, j, float(gram[i, j])) for i in range(n) for j in range(i + 1) if gram[i, j] != 0]
+    shifted = [(i, j, v - (1e-3 if i == j else 0.0)) for i, j, v in low]  # slightly indefinite
+    return [
+        ('dominant', 3, [(0, 0, 2.0), (1, 0, -1.0), (1, 1, 2.0), (2, 1, -1.0), (2, 2, 2.0)], False),
+        ('zero_diagonal_coupled', 2, [(0, 0, 0.0), (1, 0, 0.5), (1, 1, 1.0)], False),
+        ('zero_row', 3, [(1, 1, 1.0), (2, 2, 1.0)], False),
+        ('negative_diagonal', 2, [(0, 0, -1.0), (1, 1, 1.0)], False),
+        ('concave_maximised', 2, [(0, 0, -2.0), (1, 0, 0.5), (1, 1, -2.0)], True),
+        ('convex_maximised', 2, [(0, 0, 2.0), (1, 1, 2.0)], True),
+        ('psd_singular_gram', n, low, False),
+        ('indefinite_gram_shift', n, shifted, False),
+        ('repeated_diagonal_terms', 2, [(0, 0, 1.0), (0, 0, 1.0), (1, 0, -1.9), (1, 1, 2.0)], False),
+    ]
+
+
 def make_check_golden():
     """The reference's check_qp_solution (src/qp_admm.cpp:63-117) on check_cases():
     tests/golden/reference_checks.json (non-finite numbers as the strings 'nan', 'inf', '-inf')."""
@@ -419,6 +441,16 @@ def make_check_golden():
                     'result': {k: enc(st[k]) for k in CHECK_KEYS}})
         print(name, {k: st[k] for k in CHECK_KEYS}, flush=True)
     (OUT / 'reference_checks.json').write_text(json.dumps(out, indent=1) + '\n')
+    conv = []
+    for name, n, terms, maximize in convexity_cases():
+        hr = np.array([t[0] for t in terms], np.int64)
+        hc = np.array([t[1] for t in terms], np.int64)
+        hv = np.array([t[2] for t in terms])
+        verdict = O.ref_check_convex(n, hr, hc, hv, maximize=maximize)
+        conv.append({'name': name, 'n': n, 'hrow': hr.tolist(), 'hcol': hc.tolist(), 'hval': hv.tolist(),
+                     'maximize': maximize, 'convex': int(verdict)})
+        print('convex', name, verdict, flush=True)
+    (OUT / 'reference_convexity.json').write_text(json.dumps(conv, indent=1) + '\n')
 
 
 def _planted_kkt_draws():

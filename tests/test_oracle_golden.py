@@ -218,6 +218,22 @@ def test_oracle_checker_reproduces_reference_edge_cases():
     assert by['maximize_optimum']['verified'] == 1 and by['maximize_optimum']['objective'] == 5.0
 
 
+def test_convexity_gate_matches_the_reference_on_edge_cases():
+    """The reference's check_convex_hessian verdicts (tests/golden/reference_convexity.json) on a
+    diagonally dominant matrix, a zero diagonal with a coupling, an empty row, a negative
+    diagonal, concave and convex maximisations, a singular PSD Gram matrix (its LDL' path), the
+    same shifted slightly indefinite, and repeated diagonal terms: the oracle's and the product's
+    gate (bqp_check_convex) give the same verdict on each."""
+    cases = json.loads((Path(__file__).resolve().parent / 'golden' / 'reference_convexity.json').read_text())
+    assert {c['convex'] for c in cases} == {0, 1}
+    for c in cases:
+        hr, hc, hv = np.array(c['hrow'], np.int64), np.array(c['hcol'], np.int64), np.array(c['hval'])
+        assert O.check_convex(c['n'], hr, hc, hv, maximize=c['maximize']) == c['convex'], c['name']
+        q = boxqp.QuadraticProblem(cost=np.zeros(c['n']), lower=np.zeros(c['n']), upper=np.ones(c['n']),
+                                   hessian_row=hr, hessian_col=hc, hessian_val=hv, maximize=c['maximize'])
+        assert boxqp.check_convex_hessian(q) == bool(c['convex']), c['name']
+
+
 def test_oracle_convexity_matches_reference(golden):
     d, _ = golden
     p, _ = inputs(next(c for c in d['cases'] if c['name'] == 'v2_psd_300'))
