@@ -669,6 +669,30 @@ def solve_diagonal_equalities(q, rows, options):
     return result
 
 
+def validate_linear_problem(q, rows):
+    """validate_linear_problem (src/mps.cpp:47-60) for a QP with linear rows: sizes and a finite
+    offset, finite costs, no NaN bound, no lower bound of +inf or upper bound of -inf (variables
+    and rows), and row entries with a column below n and a finite value.  ValueError with the
+    reference's messages."""
+    n, m = q.n, rows.m
+    cost = np.asarray(q.cost, dtype=np.float64)
+    lower = np.asarray(q.lower, dtype=np.float64)
+    upper = np.asarray(q.upper, dtype=np.float64)
+    rl = np.asarray(rows.lower, dtype=np.float64)
+    ru = np.asarray(rows.upper, dtype=np.float64)
+    if (not n or lower.shape != (n,) or upper.shape != (n,) or rl.shape != (m,) or ru.shape != (m,)
+            or not math.isfinite(q.offset)):
+        raise ValueError('Invalid linear problem dimensions or offset')
+    if (not np.all(np.isfinite(cost)) or np.any(np.isnan(lower)) or np.any(np.isnan(upper))
+            or np.any(lower == np.inf) or np.any(upper == -np.inf)):
+        raise ValueError('Invalid variable coefficient or bound')
+    if np.any(np.isnan(rl)) or np.any(np.isnan(ru)) or np.any(rl == np.inf) or np.any(ru == -np.inf):
+        raise ValueError('Invalid row bound')
+    col = np.asarray(rows.col)
+    if np.any((col < 0) | (col >= n)) or not np.all(np.isfinite(np.asarray(rows.val, dtype=np.float64))):
+        raise ValueError('Invalid sparse row entry')
+
+
 def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
     """The reference's solve_qp_admm (qp_admm.cpp:118-280) with its iterations on the GPU.
 
@@ -690,13 +714,10 @@ def solve_qp_admm(q, rows, options=None, device=0, make_system=None):
             or o.threads < 1):
         raise ValueError('Invalid QP options')
     start = time.monotonic()
+    validate_linear_problem(q, rows)
     if q.integer is not None and np.any(np.asarray(q.integer)):
         raise ValueError('Continuous QP required')
     n, m = q.n, rows.m
-    for name, arr, size in (('cost', q.cost, n), ('lower', q.lower, n), ('upper', q.upper, n),
-                            ('row_lower', rows.lower, m), ('row_upper', rows.upper, m)):
-        if np.asarray(arr).shape != (size,):
-            raise ValueError(f'{name} has the wrong size')
     result = QpResult(algorithm='scaled_admm_pcg')
     if not check_convex_hessian(q):
         result.status = 'unsupported_curvature'

@@ -204,6 +204,24 @@ def test_solve_qp_admm_statuses_and_option_checks():
     for bad in (dict(tolerance=0.0), dict(tolerance=math.nan), dict(time_limit=-1.0), dict(threads=0)):
         with pytest.raises(ValueError, match='Invalid QP options'):
             solve_qp_admm(q, rows, boxqp.QpOptions(**bad), make_system=make)
+    # validate_linear_problem (src/mps.cpp:47-60)
+    bad_cost = np.array(q.cost, dtype=float)
+    bad_cost[2] = np.nan
+    qc = boxqp.QuadraticProblem(cost=bad_cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
+                                hessian_col=q.hessian_col, hessian_val=q.hessian_val)
+    with pytest.raises(ValueError, match='Invalid variable coefficient or bound'):
+        solve_qp_admm(qc, rows, make_system=make)
+    qo = boxqp.QuadraticProblem(cost=q.cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
+                                hessian_col=q.hessian_col, hessian_val=q.hessian_val, offset=math.inf)
+    with pytest.raises(ValueError, match='dimensions or offset'):
+        solve_qp_admm(qo, rows, make_system=make)
+    rb = LinearRows(rows.rowptr, rows.col, rows.val, np.full(rows.m, np.inf), rows.upper)
+    with pytest.raises(ValueError, match='Invalid row bound'):
+        solve_qp_admm(q, rb, make_system=make)
+    bad_col = np.array(rows.col)
+    bad_col[0] = q.n
+    with pytest.raises(ValueError, match='Invalid sparse row entry'):
+        solve_qp_admm(q, LinearRows(rows.rowptr, bad_col, rows.val, rows.lower, rows.upper), make_system=make)
     qi = boxqp.QuadraticProblem(cost=q.cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
                                 hessian_col=q.hessian_col, hessian_val=q.hessian_val,
                                 integer=np.arange(q.n) == 0)
