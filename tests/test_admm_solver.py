@@ -346,3 +346,26 @@ def test_solve_qp_admm_on_qplib_9002():
                       make_system=lambda h, a, n: pytest.fail('the ADMM must not run'))
     assert r.status == 'optimal' and r.algorithm == 'diagonal_qp_dual_newton' and r.iterations == 180
     assert r.objective == pytest.approx(5698097498.5664835, rel=1e-15)
+
+
+def test_qplib_model_with_rows_end_to_end():
+    """A QCL model in QPLIB text (rows listed out of order, one-sided and equality rows): read by
+    read_qplib_rows and solved by the loop (restated iterations in place of the device), it gets
+    the reference's answer -- the reference's own reader and solve_qp_admm on the same file."""
+    from oracle import oracle as O
+    from test_qplib_cli import constrained_qplib_text
+    from boxqp.qplib import read_qplib_rows
+    if not O.ref_available():
+        pytest.skip('oracle/_ref not built on this host')
+    text = constrained_qplib_text(seed=11)
+    q, rows = read_qplib_rows(text)
+    r = solve_qp_admm(q, rows, boxqp.QpOptions(tolerance=1e-6), make_system=lambda h, a, n: RestatedSystem(h, a, n))
+    status, x, st = O.ref_solve_qp_admm(q.hessian_row, q.hessian_col, q.hessian_val, q.cost, q.lower, q.upper,
+                                        rows.rowptr, rows.col, rows.val, rows.lower, rows.upper, tol=1e-6,
+                                        offset=q.offset)
+    assert r.status == status and r.iterations == int(st['iterations']), (r.status, r.iterations, status, st)
+    if r.algorithm == 'scaled_admm_pcg_kkt_polish':
+        assert np.max(np.abs(r.primal - x)) <= 1e-9
+    elif EXACT:
+        assert _same(r.primal, x) and _same(r.row_dual, st['row_dual'])
+    assert r.objective == pytest.approx(st['objective'], rel=1e-12)
