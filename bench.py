@@ -101,39 +101,70 @@ class ClockSampler:
                 'reasons': sorted(reasons), 'samples': len(sm)}
 
 
-def make_workload(name, rank):
-    import boxqp
-    if name == 'graph1m':
-        inst = boxqp.planted('graph1m', seed=1 + rank, lower_triplets=True)
-        desc = ('planted random-graph Laplacian box QP, n=1,000,000, 7 edges/vertex, bounds [-1,1], '
-                '25/25/50 planted pattern')
-    elif name == 'grid':
-        inst = boxqp.planted('grid', seed=2 + rank, lower_triplets=True)
-        desc = '1024x1024 5-point grid Laplacian + 1e-3 I, random bounds, 20/20/60 planted pattern'
-    elif name == 'graph10k':
-        inst = boxqp.planted('graph10k', seed=rank, lower_triplets=True)
-        desc = 'planted random-graph Laplacian box QP, n=10,000, 5 edges/vertex, bounds [0,1]'
-    elif name == 'tridiagonal':
-        inst = boxqp.planted('tridiagonal', n=1000000, lower_triplets=True)
-        desc = ("the reference's published scale family (src/scale_benchmark.cpp:13-19): tridiagonal 2.02/-1, "
-                'n=1,000,000, bounds [0,3], tolerance 1e-7, iteration limit 20000')
-    else:
+WORKLOADS = {
+    'graph1m': dict(preset='graph1m', seed=1, n=0,
+                    desc='planted random-graph Laplacian box QP, n=1,000,000, 7 edges/vertex, bounds [-1,1], '
+                         '25/25/50 planted pattern'),
+    'grid': dict(preset='grid', seed=2, n=0,
+                 desc='1024x1024 5-point grid Laplacian + 1e-3 I, random bounds, 20/20/60 planted pattern'),
+    'graph10k': dict(preset='graph10k', seed=0, n=0,
+                     desc='planted random-graph Laplacian box QP, n=10,000, 5 edges/vertex, bounds [0,1]'),
+    'tridiagonal': dict(preset='tridiagonal', seed=1, n=1000000,
+                        desc="the reference's published scale family (src/scale_benchmark.cpp:13-19): tridiagonal "
+                             '2.02/-1, n=1,000,000, bounds [0,3], tolerance 1e-7, iteration limit 20000'),
+}
+
+
+def make_workload(name, rank, oracle_side=False):
+    """The workload's planted instance (seed shifted by the rank).  oracle_side: generated by the
+    generator linked into the oracle library, so the reference arm never loads the engine library
+    (the arrays are the same bits)."""
+    if name not in WORKLOADS:
         raise SystemExit(f'unknown workload {name}')
-    return inst, desc
+    w = WORKLOADS[name]
+    seed = w['seed'] + (rank if name != 'tridiagonal' else 0)
+    if oracle_side:
+        from oracle import oracle as O
+        inst = O.planted(w['preset'], seed=seed, n=w['n'], lower_triplets=True)
+    else:
+        import boxqp
+        inst = boxqp.planted(w['preset'], seed=seed, n=w['n'], lower_triplets=True)
+    return inst, w['desc']
 
 
 def oracle_args(inst):
     return inst['hrow'], inst['hcol'], inst['hval'], inst['c'], inst['lower'], inst['upper']
 
 
-def cpu_reference_solve(inst, tol, time_limit=60.0):
-    """One FP64 reference-FISTA solve on all host cores (oracle port); returns (seconds, info)."""
+def cpu_reference_solve(inst, tol, time_limit=120.0, prefer_reference=True):
+    """One FP64 CPU solve on all host cores: the reference's own solve_accelerated_box(q, opt,
+    false) (oracle/_ref, built from its sources on this host) when available, else the oracle
+    port of it.  Returns (seconds of the solve call, info)."""
     from oracle import oracle as O
     threads = O.max_threads()
+    if prefer_reference and O.ref_available():
+        status, x, st = O.ref_solve_box(*oracle_args(inst), tol=tol, threads=threads, time_limit=time_limit)
+        return st['seconds'], {'status': status, 'iterations': int(st['iterations']), 'threads': threads,
+                               'kind': 'reference',
+                               'engine': 'the reference build (oracle/_ref: src/accelerated_qp.cpp and its library, '
+                                         'compiled from the reference sources on this host, -O3 -fopenmp)'}
     t0 = time.perf_counter()
     status, x, st = O.solve_box(*oracle_args(inst), tol=tol, threads=threads, time_limit=time_limit)
     dt = time.perf_counter() - t0
-    return dt, {'status': status, 'iterations': int(st['iterations']), 'threads': threads}
+    return dt, {'status': status, 'iterations': int(st['iterations']), 'threads': threads, 'kind': 'port',
+                'engine': 'the CPU oracle port of src/accelerated_qp.cpp (oracle/boxqp_oracle.c, OpenMP)'}
+
+
+def oracle_check(inst, x, tol):
+    """The oracle's check_qp_solution (restated, pinned to the reference) of a primal on the host,
+    plus the active-set comparison with the planted optimum."""
+    from oracle import oracle as O
+    chk = O.check(*oracle_args(inst), x, tol=tol)
+    fstar = inst['fstar']
+    return {'verified': bool(chk['verified']), 'stationarity': chk['stationarity_residual'],
+            'primal_residual': chk['primal_residual'],
+            'objective_rel_err': abs(chk['objective'] - fstar) / (1 + abs(fstar)),
+            'active_set_mismatches': O.active_set_mismatches(x, inst)}
 
 
 def dist_setup(args):
@@ -173,26 +204,33 @@ def allreduce_sum(pg, value):
 
 
 def run_reference(args, world, rank, pg):
-    """The reference arm: the reference algorithm on the host cores (rank 0 only)."""
+    """The reference arm: the reference's own CPU solve_accelerated_box on the host cores (rank 0
+    only), on the same instance, tolerance and metric.  The instance comes from the oracle
+    library's copy of the generator: nothing of the engine is loaded in this process.  Each step
+    is one full solve; the run is bounded to about a minute of solves (at least one), and `steps`
+    reports how many were timed."""
     if rank != 0:
         return
-    inst, desc = make_workload(args.workload, 0)
-    for _ in range(args.warmup):
+    inst, desc = make_workload(args.workload, 0, oracle_side=True)
+    for _ in range(min(args.warmup, 1)):
         cpu_reference_solve(inst, args.tol)
     times, info = [], {}
-    for _ in range(args.steps):
+    budget = 60.0
+    while len(times) < args.steps and (not times or sum(times) < budget):
         dt, info = cpu_reference_solve(inst, args.tol)
         times.append(dt)
     total = sum(times)
-    value = args.steps / total
+    value = len(times) / total
     line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'solves/s', 'n_gpus': args.gpus,
-            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * total / args.steps,
+            'steps': len(times), 'warmup': min(args.warmup, 1), 'ms_per_step': 1e3 * total / len(times),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
             'config': {'workload': desc, 'n': inst['n'], 'nnz': inst['nnz'], 'tolerance': args.tol,
-                       'engine': 'reference FISTA (src/accelerated_qp.cpp), CPU oracle port, OpenMP'},
-            'cpu_baseline': {'value': value, 'unit': 'solves/s', 'cores': info.get('threads'), 'kind': 'port',
-                             'sample': f'{args.steps} full FP64 solves of the workload at KKT<={args.tol:g} '
-                                       f'({info.get("iterations")} iterations each)'},
+                       'engine': info.get('engine')},
+            'cpu_baseline': {'value': value, 'unit': 'solves/s', 'cores': info.get('threads'), 'kind': info.get('kind'),
+                             'sample': f'{len(times)} full FP64 solves of the workload at KKT<={args.tol:g} '
+                                       f'({info.get("iterations")} iterations each, status {info.get("status")}), '
+                                       f'timed around the solve_accelerated_box call; at most {args.steps} solves '
+                                       f'or about {budget:g} s'},
             'e2e': {'value': value, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     gpu = reference_gpu_row(inst, args.tol)
     if gpu:
@@ -261,6 +299,9 @@ def run_ours(args, world, rank, local, pg):
               'checks': int(st.checks), 'kkt_stationarity': st.stationarity_residual,
               'primal_residual': st.primal_residual,
               'objective_rel_err': abs(st.objective - inst['fstar']) / (1 + abs(inst['fstar']))}
+    # the last timed solve's primal checked on the host by the oracle (check_qp_solution restated
+    # and pinned to the reference) and against the planted active set
+    result['oracle_check'] = oracle_check(inst, x, args.tol)
     # ---- roofline of the dominant kernel (step kernel alone, CUDA events) ----------------------
     step_ms, step_bytes = eng.profile_step(ident, 100)
     achieved = step_bytes / (step_ms * 1e-3) / 1e9
@@ -293,7 +334,7 @@ def run_ours(args, world, rank, local, pg):
         eng.release(id64)
         fp64 = {'solves_per_s': reps / (ms64 / 1e3), 'hbm_gbs': s64.bytes / (ms64 / 1e3 / reps) / 1e9,
                 'iterations': int(s64.iterations), 'status': boxqp.STATUS_NAMES[s64.status],
-                'step_kernel_gbs': b64 / (ms64_step * 1e-3) / 1e9}
+                'step_kernel_gbs': b64 / (ms64_step * 1e-3) / 1e9, 'oracle_check': oracle_check(inst, x64, args.tol)}
     # ---- e2e through the public C-ABI with host buffers -----------------------------------------
     e2e = None
     if not args.quick:
@@ -357,8 +398,8 @@ def run_ours(args, world, rank, local, pg):
     cpu = None
     if rank == 0 and world == 1 and not args.quick:
         dt, info = cpu_reference_solve(inst, args.tol)
-        cpu = {'value': 1.0 / dt, 'unit': 'solves/s', 'cores': info['threads'], 'kind': 'port',
-               'sample': f'one full FP64 reference-FISTA solve of the workload at KKT<={args.tol:g} '
+        cpu = {'value': 1.0 / dt, 'unit': 'solves/s', 'cores': info['threads'], 'kind': info['kind'],
+               'sample': f'one full FP64 solve of the workload at KKT<={args.tol:g} by {info["engine"]} '
                          f'({info["iterations"]} iterations, status {info["status"]})'}
     eng.release(ident)
     eng.close()
@@ -657,6 +698,32 @@ def run_admm(args, world, rank, local, pg):
     sysm.close()
 
 
+def run_case(args):
+    """Small runs for kernel profilers (ncu): `--case solve` one solve of the workload (with
+    BOXQP_LAUNCH=stream its kernels run as plain launches, which per-kernel profilers can see;
+    inside the conditional graph they cannot), `--case step` the FISTA step kernel alone, launched
+    1 + --steps times on the uploaded instance.  Prints a line of text, not the bench JSON."""
+    import boxqp
+    inst, _ = make_workload(args.workload, 0)
+    eng = boxqp.Engine(0)
+    try:
+        if args.case == 'solve':
+            o = boxqp.options_struct(args.tol, 60.0, 200000, args.precision)
+            x, st = eng.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+            print({k: v for k, v in st.as_dict().items() if k in ('status_name', 'iterations', 'polish_iterations',
+                                                                 'checks', 'device_seconds', 'bytes')})
+        else:
+            o = boxqp.options_struct(args.tol, 60.0, 0, args.precision)
+            ident = eng.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+            eng.wait(ident)
+            ms, nbytes = eng.profile_step(ident, args.steps)
+            print(f'step kernel: {ms * 1e3:.1f} us per launch, {nbytes / 1e6:.1f} MB algorithmic, '
+                  f'{nbytes / ms / 1e6:.0f} GB/s')
+            eng.release(ident)
+    finally:
+        eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -675,9 +742,15 @@ def main():
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--tol', type=float, default=None, help='KKT tolerance (default 1e-6; 1e-7 for tridiagonal)')
     ap.add_argument('--quick', action='store_true', help='skip e2e, FP64 and CPU legs')
+    ap.add_argument('--case', choices=['solve', 'step'], default=None,
+                    help='profiling run instead of the benchmark: one solve, or the step kernel alone --steps times')
     args = ap.parse_args()
     if args.tol is None:
         args.tol = 1e-7 if args.workload == 'tridiagonal' else 1e-6
+    if args.case:
+        args.steps = 3 if args.steps is None else args.steps
+        run_case(args)
+        return
     if args.steps is None:
         args.steps = 3 if args.workload in ('batch', 'admm') else (10 if args.impl == 'reference' else 100)
     world, rank, local, pg = dist_setup(args)

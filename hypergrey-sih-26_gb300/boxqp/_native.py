@@ -72,6 +72,7 @@ PROTOTYPES = {
     'bqp_release': (c_int, [c_void_p, c_uint64]),
     'bqp_resolve': (c_int, [c_void_p, _U64P, c_int64]),
     'bqp_set_latency_target': (c_int, [c_void_p, c_double]),
+    'bqp_inject_admission_oom': (c_int, [c_void_p, c_int32]),
     'bqp_load': (c_int, [c_void_p, _I64P, _I64P, _I64P, _I64P]),
     'bqp_timer': (c_int, [c_void_p, c_int32, _F64P, _I64P, _I64P]),
     'bqp_profile_step': (c_int, [c_void_p, c_uint64, c_int32, _F64P, _F64P]),

@@ -277,6 +277,10 @@ class Engine:
     def set_latency_target(self, ms):
         self._check(lib().bqp_set_latency_target(self._ctx, float(ms)))
 
+    def inject_admission_oom(self, count=1):
+        """Host-side fault injection: the next `count` admissions fail as out of memory."""
+        self._check(lib().bqp_inject_admission_oom(self._ctx, int(count)))
+
     def load(self):
         q, r, p, b = (N.c_int64(0) for _ in range(4))
         self._check(lib().bqp_load(self._ctx, N.ctypes.byref(q), N.ctypes.byref(r), N.ctypes.byref(p),

@@ -11,6 +11,8 @@
 #include "engine.cuh"
 #include "kernels.cuh"
 
+#include <cuda.h>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -53,32 +55,74 @@ bool ok(cudaError_t e, std::string& why) {
 // ---- scratch of bqp_check_device_noalloc ------------------------------------------------------
 // The verification reduction needs global scratch for its per-block partials, its completion
 // counter and its 8 result values.  bqp_check_device_noalloc takes that scratch from this
-// file-scope device array instead of cudaMalloc: 96 KiB on every device that loads the library,
-// held until the process exits.  At most 1024 blocks of partials fit, which bounds n to
-// kNoAllocMaxRows.  In host code the name of the array is only a host-side stand-in, so the
-// device address is looked up once per device with cudaGetSymbolAddress.
+// file-scope device array instead of cudaMalloc: 96 KiB in every context that loads this
+// module, held until the context ends.  At most 1024 blocks of partials fit, which bounds n to
+// kNoAllocMaxRows.  In host code the name of the array is only a host-side stand-in, so its
+// device address is looked up with cudaGetSymbolAddress, with the device current, once per
+// context: the lookup is cached under the current context's unique id (cuCtxGetId), so a
+// context that is destroyed and recreated (cudaDeviceReset) gets a fresh lookup instead of a
+// stale address.  The same set-up loads the check kernel into the context, so that later
+// calls do not load code (which takes device memory) under lazy module loading.
 constexpr int64_t kNoAllocMaxRows = 4194304;
 constexpr size_t kNoAllocBytes = 96 * 1024;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
+struct NoallocSlot {
+    unsigned long long context_id = 0;  // 0: not set up
+    void* address = nullptr;
+};
 std::mutex g_noalloc_mu;
-void* g_noalloc_address[kMaxDevices] = {};
+NoallocSlot g_noalloc_slot[kMaxDevices];
 
-// Device address of g_noalloc_scratch on the current device (set up on the first call per device).
+// The driver's cuCtxGetCurrent / cuCtxGetId, reached through the runtime (no libcuda link).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+cudaError_t current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!get_current || !get_id) return cudaErrorNotSupported;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+    return get_id(ctx, id) == CUDA_SUCCESS ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// Device address of g_noalloc_scratch in the current context (set up on the first call there).
+// No context current yet: the symbol lookup initializes the runtime's context on this device.
 cudaError_t noalloc_scratch(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long id = 0;
+    const bool have_id = current_context_id(&id) == cudaSuccess;
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_address[dev]) {
+    NoallocSlot& slot = g_noalloc_slot[dev];
+    if (!have_id || slot.context_id != id) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_noalloc_address[dev] = p;
+        e = current_context_id(&id);
+        if (e != cudaSuccess) return e;
+        e = bqp::load_check_standalone();
+        if (e != cudaSuccess) return e;
+        slot.address = p;
+        slot.context_id = id;
     }
-    *out = g_noalloc_address[dev];
+    *out = slot.address;
     return cudaSuccess;
 }
 }  // namespace
@@ -172,8 +216,11 @@ int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, c
                      const double* d_c, const double* d_lower, const double* d_upper, double tolerance, double offset,
                      int32_t diagonal_gate, bqp_stats* stats) {
     if (n <= 0 || n > 2000000000LL || !d_rowptr || !d_x || !d_c || !d_lower || !d_upper || !stats ||
-        !(tolerance > 0) || !std::isfinite(offset))
+        !(tolerance > 0) || !std::isfinite(offset)) {
+        g_box_error = "bqp_check_device: invalid argument (n must be in 1..2e9, the device pointers and stats "
+                      "non-null, the tolerance positive and the offset finite)";
         return BQP_ERR_INVALID;
+    }
     const size_t bytes = bqp::check_scratch_bytes(n) + 8 * sizeof(double);
     void* scratch = nullptr;
     cudaStream_t s = nullptr;
@@ -210,7 +257,8 @@ int bqp_check_device_noalloc(int64_t n, const int32_t* d_rowptr, const int32_t* 
                              double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats) {
     if (n <= 0 || !d_rowptr || !d_x || !d_c || !d_lower || !d_upper || !stats || !(tolerance > 0) ||
         !std::isfinite(offset)) {
-        g_box_error = "invalid argument";
+        g_box_error = "bqp_check_device_noalloc: invalid argument (n must be positive, the device pointers and "
+                      "stats non-null, the tolerance positive and the offset finite)";
         return BQP_ERR_INVALID;
     }
     if (n > kNoAllocMaxRows) {

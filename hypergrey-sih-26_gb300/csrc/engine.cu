@@ -204,6 +204,7 @@ struct Job {
     Layout layout;
     InstDev rec{};            // host image of the device record
     int error = BQP_OK;
+    bool out_of_memory = false;  // the admission's device allocation failed (or was made to fail)
     std::string error_text;
     bqp_stats stats{};
     // upload in progress (engine thread): host -> device copies still to issue, then the
@@ -270,14 +271,14 @@ std::vector<Tile> make_tiles(int64_t n, const int32_t* rowptr, int variant) {
 }
 
 // Algorithmic bytes, fixed accounting: per FISTA iteration nnz (s_v + 4) + 4 (n + 1) + 7 n s_x;
-// per check nnz 12 + 4 (n + 1) + 32 n; per CG iteration nnz 12 + 4 (n + 1) + 128 n.
-double algorithmic_bytes(int64_t n, int64_t nnz, int precision, int64_t iters, int64_t checks, int64_t cg) {
+// per check nnz 12 + 4 (n + 1) + 32 n.  The polish's bytes are counted on the device on the
+// packed Q_FF of each round (polish_bytes: residual pass and CG iterations, kernels.cu).
+double algorithmic_bytes(int64_t n, int64_t nnz, int precision, int64_t iters, int64_t checks, double polish_bytes) {
     const double N = static_cast<double>(n), Z = static_cast<double>(nnz);
     const double sv = precision == PREC_MIXED ? 4.0 : 8.0;
     const double b_iter = Z * (sv + 4) + 4 * (N + 1) + 7 * N * sv;
     const double b_check = Z * 12 + 4 * (N + 1) + 32 * N;
-    const double b_cg = Z * 12 + 4 * (N + 1) + 128 * N;
-    return static_cast<double>(iters) * b_iter + static_cast<double>(checks) * b_check + static_cast<double>(cg) * b_cg;
+    return static_cast<double>(iters) * b_iter + static_cast<double>(checks) * b_check + polish_bytes;
 }
 
 int status_code(int32_t st) {
@@ -325,6 +326,7 @@ public:
         std::lock_guard<std::mutex> g(mu_);
         latency_ms_ = ms;
     }
+    void inject_admission_oom(int count) { inject_oom_.store(count); }
     void set_error(const std::string& e) {
         std::lock_guard<std::mutex> g(err_mu_);
         error_ = e;
@@ -483,6 +485,7 @@ private:
     int64_t n_running_ = 0, peak_resident_ = 0;
     size_t resident_bytes_ = 0;
     double latency_ms_ = 0;
+    std::atomic<int> inject_oom_{0};  // admissions left to fail as out of memory (host-side fault injection)
     double body_ms_ = 0.5;
     double timer_ms_ = 0;
     int64_t timer_kernels_ = 0, timer_launches_ = 0;
@@ -1031,6 +1034,9 @@ void Engine::reset_record(Job& j) {
     R.cg_total = 0;
     R.fista_iters = 0;
     R.checks = 0;
+    R.ff_nnz = 0;
+    R.ff_rows = 0;
+    R.polish_bytes = 0.0;
     R.iterations = 0;
     R.arm_chunk = (j.opt.precision == PREC_MIXED && R.max_iter > 0) ? 1 : 0;
     R.moved[0] = 0;
@@ -1128,7 +1134,23 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     const int prec = j.opt.precision;
     j.layout = make_layout(j.n, j.nnz, static_cast<int64_t>(j.tiles.size()), prec);
     void* slab = nullptr;
-    if (!cuda_ok(cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, ustream_), why, "allocate solve")) return false;
+    // host-side fault injection (bqp_inject_admission_oom): fail as an exhausted pool would,
+    // without any device call
+    for (int left = inject_oom_.load(); left > 0;) {
+        if (inject_oom_.compare_exchange_weak(left, left - 1)) {
+            j.out_of_memory = true;
+            why = "CUDA: allocate solve: out of memory (injected on the host)";
+            return false;
+        }
+    }
+    const cudaError_t alloc = cudaMallocFromPoolAsync(&slab, j.layout.total, pool_, ustream_);
+    if (alloc == cudaErrorMemoryAllocation) {
+        cudaGetLastError();  // not sticky: clear it so later calls do not report it
+        j.out_of_memory = true;
+        why = std::string("CUDA: allocate solve: ") + cudaGetErrorString(alloc);
+        return false;
+    }
+    if (!cuda_ok(alloc, why, "allocate solve")) return false;
     j.slab = slab;
     j.resident = true;
     const Layout& L = j.layout;
@@ -1364,7 +1386,7 @@ void Engine::fail_admission(Job* j, size_t reserved, const std::string& why) {
         j->slab = nullptr;
         j->resident = false;
     }
-    j->error = BQP_ERR_CUDA;
+    j->error = j->out_of_memory ? BQP_ERR_NO_MEMORY : BQP_ERR_CUDA;
     j->error_text = why;
     j->state = JOB_DONE;
     if (j->notify) completed_.push_back(j->id);
@@ -1557,7 +1579,7 @@ void Engine::collect(std::unique_lock<std::mutex>& lk) {
         s.device_end_ns = R.end_ns;
         s.device_seconds = 1e-9 * static_cast<double>(R.end_ns - R.start_ns);
         s.checks = R.checks;
-        s.bytes = algorithmic_bytes(j.n, j.nnz, j.opt.precision, R.fista_iters, R.checks, R.cg_total);
+        s.bytes = algorithmic_bytes(j.n, j.nnz, j.opt.precision, R.fista_iters, R.checks, R.polish_bytes);
         j.t_done = now;
     }
     lk.lock();
@@ -1618,7 +1640,7 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     if (ms_out) *ms_out = ms / launches;
-    if (bytes_out) *bytes_out = algorithmic_bytes(j.n, j.nnz, j.opt.precision, 1, 0, 0);
+    if (bytes_out) *bytes_out = algorithmic_bytes(j.n, j.nnz, j.opt.precision, 1, 0, 0.0);
     return BQP_OK;
 }
 
@@ -2165,6 +2187,12 @@ int bqp_resolve(bqp_ctx* ctx, const uint64_t* ids, int64_t count) {
 int bqp_set_latency_target(bqp_ctx* ctx, double ms) {
     if (!ctx || !(ms >= 0) || !std::isfinite(ms)) return BQP_ERR_INVALID;
     ctx->engine->set_latency_target(ms);
+    return BQP_OK;
+}
+
+int bqp_inject_admission_oom(bqp_ctx* ctx, int32_t count) {
+    if (!ctx || count < 0) return BQP_ERR_INVALID;
+    ctx->engine->inject_admission_oom(count);
     return BQP_OK;
 }
 

@@ -174,7 +174,11 @@ struct __align__(16) InstDev {
     // accounting
     int64_t fista_iters;
     int64_t checks;
+    int64_t ff_nnz;        // polish: entries of the packed Q_FF of the current polish round
+    int64_t ff_rows;       // polish: free rows of the current polish round
+    double polish_bytes;   // polish: algorithmic bytes of the residual passes and CG iterations
 };
+static_assert(sizeof(InstDev) % 16 == 0, "rearm_kernel copies records as 16-byte words");
 
 struct Ctrl {
     int32_t n_inst;        // instance records in use

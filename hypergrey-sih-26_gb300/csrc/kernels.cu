@@ -644,6 +644,8 @@ __device__ void after_check(InstDev& I, const Acc& tot) {
         if ((I.stable_checks >= 1 && stat <= sw) || (step_stable && stat <= step_sw)) {
             I.phase = PH_POLISH_INIT;
             I.cg_it = 0;
+            I.ff_nnz = 0;
+            I.ff_rows = 0;
             return;
         }
     }
@@ -1217,18 +1219,21 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     }
 }
 
+// Returns the tile's packed Q_FF entries.
 template <int LANES>
-__device__ void residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, int32_t* start_of,
-                              float2* rowsum, Acc& a) {
+__device__ int residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, int32_t* start_of,
+                             float2* rowsum, Acc& a) {
     count_kept<LANES>(I, list, n_free, start_of);
     __syncthreads();
-    block_exclusive_scan(start_of, n_free);
+    const int kept = block_exclusive_scan(start_of, n_free);
     residual_rows<LANES>(I, list, n_free, base, start_of, rowsum, a);
+    return kept;
 }
 
-// Residual (with the packing of Q_FF) or CG product over tile rows [rb, ...) of one instance.
+// Residual (with the packing of Q_FF) or CG product over tile rows [rb, ...) of one instance;
+// the residual returns the tile's packed Q_FF entries (0 for the product).
 template <bool RESIDUAL>
-__device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
+__device__ int polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
     // one copy per kernel, shared by every lane count: free-list positions of the packed rows
     // (residual) and row sums handed to the FP64 epilogue
     __shared__ int32_t start_of[RESIDUAL ? kTileRows : 1];
@@ -1237,12 +1242,12 @@ __device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
     if constexpr (RESIDUAL) {
         const int base = __ldg(I.rowptr + rb);
         switch (I.lanes_res) {
-        case 1: residual_tile<1>(I, list, n_free, base, start_of, rowsum, a); break;
-        case 2: residual_tile<2>(I, list, n_free, base, start_of, rowsum, a); break;
-        case 4: residual_tile<4>(I, list, n_free, base, start_of, rowsum, a); break;
-        case 8: residual_tile<8>(I, list, n_free, base, start_of, rowsum, a); break;
-        case 16: residual_tile<16>(I, list, n_free, base, start_of, rowsum, a); break;
-        default: residual_tile<32>(I, list, n_free, base, start_of, rowsum, a); break;
+        case 1: return residual_tile<1>(I, list, n_free, base, start_of, rowsum, a);
+        case 2: return residual_tile<2>(I, list, n_free, base, start_of, rowsum, a);
+        case 4: return residual_tile<4>(I, list, n_free, base, start_of, rowsum, a);
+        case 8: return residual_tile<8>(I, list, n_free, base, start_of, rowsum, a);
+        case 16: return residual_tile<16>(I, list, n_free, base, start_of, rowsum, a);
+        default: return residual_tile<32>(I, list, n_free, base, start_of, rowsum, a);
         }
     } else {
         switch (I.lanes_cg) {
@@ -1254,6 +1259,7 @@ __device__ void polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
         default: matvec_rows<32>(I, list, n_free, rowsum, a); break;
         }
     }
+    return 0;
 }
 
 __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
@@ -1264,11 +1270,23 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
-        polish_rows<true>(I, T.row_begin, I.free_cnt[t - R.x], a);
+        const int n_free = I.free_cnt[t - R.x];
+        const int kept = polish_rows<true>(I, T.row_begin, n_free, a);
+        if (threadIdx.x == 0) {  // Q_FF size of this polish round, for the byte accounting
+            atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_nnz), static_cast<unsigned long long>(kept));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_rows), static_cast<unsigned long long>(n_free));
+        }
         Acc total = block_reduce_ab(a, I.lanes_res, true, true);
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
+                // residual pass: the full CSR (hi/lo values + columns) and row pointers, xp (its
+                // FP32 pairs, gathered) and c; the packed Q_FF written (hi/lo + column) with its
+                // row starts and counts; r, z, p, s, p2 written and 1/diag read on the free rows
+                const double nnz = static_cast<double>(__ldg(I.rowptr + I.n));
+                const double N = static_cast<double>(I.n);
+                const double fz = static_cast<double>(I.ff_nnz), fr = static_cast<double>(I.ff_rows);
+                I.polish_bytes += 12.0 * nnz + 4.0 * (N + 1) + 16.0 * N + 12.0 * fz + 8.0 * fr + 48.0 * fr;
                 I.rz = inst_total.a;
                 I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
                 I.cg_it = 0;
@@ -1300,6 +1318,9 @@ __global__ void __launch_bounds__(kBlock, 5) cg_matvec_kernel(View v) {
                 const bool first = I.cg_it == 0;
                 I.cg_it++;
                 I.cg_total++;
+                // one CG iteration on Q_FF: its packed entries (hi/lo + column), row starts and
+                // counts, and 16 FP64 vector accesses per free row (product and vector step)
+                I.polish_bytes += 12.0 * static_cast<double>(I.ff_nnz) + 136.0 * static_cast<double>(I.ff_rows);
                 bool stop = I.cg_res <= I.cg_tol || I.cg_it > I.cg_max || !isfinite(gamma) || !isfinite(delta);
                 if (!stop) {
                     const double beta = first ? 0.0 : gamma / I.rz;
@@ -1450,6 +1471,8 @@ __device__ void advance_chunks(const View& v, int steps) {
             I.moved[1] == 0) {
             I.phase = PH_POLISH_INIT;
             I.cg_it = 0;
+            I.ff_nnz = 0;
+            I.ff_rows = 0;
             I.stable_checks = 0;
             I.iterations = I.it_next;
         }
@@ -2182,17 +2205,19 @@ void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* co
     src.gate = gate;
     const int grid = check_grid(n);
     // The kernel's dynamic shared memory plus its static reduction buffer exceed the default
-    // 48 KB: opt in once per device (the engine's set-up does the same for its kernels).
-    static std::atomic<bool> opted[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !opted[dev].load()) {
-        cudaFuncSetAttribute(check_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem8);
-        opted[dev].store(true);
-    }
+    // 48 KB: opt in on every call (a cheap host call; a per-device flag would go stale when the
+    // caller resets the device and its context is recreated).
+    cudaFuncSetAttribute(check_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem8);
     auto* scr = static_cast<StandaloneScratch*>(scratch);
     auto* partial = reinterpret_cast<Partial*>(static_cast<char*>(scratch) + 256);
     check_standalone_kernel<<<grid, kBlock, kSmem8, s>>>(src, static_cast<int>(n), tol, offset, partial, scr, result);
+}
+
+cudaError_t load_check_standalone() {
+    cudaError_t e = cudaFuncSetAttribute(check_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem8);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes attr;
+    return cudaFuncGetAttributes(&attr, check_standalone_kernel);
 }
 
 void launch_box_step(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,

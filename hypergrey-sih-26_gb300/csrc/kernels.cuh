@@ -62,6 +62,9 @@ void launch_check_standalone(int64_t n, const int32_t* rowptr, const int32_t* co
                              const double* x, const double* c, const double* l, const double* u,
                              double tol, double offset, int gate, void* scratch, double* result,
                              cudaStream_t s);
+// Loads the standalone check kernel into the current context now (under lazy module loading
+// its first launch would load it) and opts it into its shared-memory size.
+cudaError_t load_check_standalone();
 
 // Plugin-level FISTA step (reference numerics: FP64, division by L, no FMA), ping-pong w.
 void launch_box_step(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val,

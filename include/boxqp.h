@@ -169,6 +169,14 @@ int bqp_set_latency_target(bqp_ctx* ctx, double ms);
 int bqp_load(bqp_ctx* ctx, int64_t* queued, int64_t* running, int64_t* peak_resident,
              int64_t* resident_bytes);
 
+/* Host-side fault injection for tests: the next `count` admissions on this context fail as if
+ * the device allocation of their memory had failed (no device call is made for them).  Such a
+ * solve finishes with BQP_ERR_NO_MEMORY from bqp_wait / bqp_fetch and its message in
+ * bqp_last_error; the context keeps serving the solves after it.  A real allocation failure at
+ * admission is reported the same way.  No counterpart in the reference (its CUDA plugin has no
+ * admission).                                                                                */
+int bqp_inject_admission_oom(bqp_ctx* ctx, int32_t count);
+
 /* ---- measurement -------------------------------------------------------------------------
  * bqp_timer: device time of the engine stream's graph launches and re-arm kernels since the
  * last reset, measured with CUDA events on that stream; `kernels` counts the engine kernels
@@ -235,7 +243,10 @@ const char* bqp_box_last_error(const bqp_box* box);
 /* ---- verification on device data ----------------------------------------------------------
  * The FP64 KKT / objective reduction of the engine as a standalone call on caller-owned
  * DEVICE pointers (full CSR, x, c, l, u), replacing check_qp_solution's host pass
- * (src/qp_admm.cpp:63-117) for a box QP.  Uses device scratch allocated per call.          */
+ * (src/qp_admm.cpp:63-117) for a box QP.  Uses device scratch allocated per call.  It runs on a
+ * stream of its own (non-blocking), which does not wait for work the caller queued on its own
+ * streams: synchronize the stream that wrote the arrays before calling.  BQP_ERR_INVALID comes
+ * with a message from bqp_box_last_error(NULL).                                             */
 int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
                      const double* d_x, const double* d_c, const double* d_lower, const double* d_upper,
                      double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats);
@@ -245,12 +256,18 @@ int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, c
  * callers that cannot allocate device memory: a serving loop in which cudaMalloc/cudaFree would
  * synchronize the device and stall the solves in flight, or a process whose device memory is
  * already reserved by another allocator (a framework's caching pool), where cudaMalloc fails.
- * It allocates nothing: its scratch is a 96 KiB static device array in libboxqp.so that every
- * GPU loading the library holds until exit, which limits n to 4,194,304 rows (larger n returns
- * BQP_ERR_INVALID with a message from bqp_box_last_error(NULL)).  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress) for the current device; make that
- * first call before any stream capture.  All calls share the one array and run on the legacy
- * default stream: calls that overlap on the GPU (from several host threads) race.            */
+ * It allocates nothing: its scratch is a 96 KiB static device array in libboxqp.so, held by
+ * every context that loads the library until the context ends, which limits n to 4,194,304 rows
+ * (larger n returns BQP_ERR_INVALID with a message from bqp_box_last_error(NULL)).
+ * The first call in a context (per device, and again after that context is destroyed and
+ * recreated) sets up: it looks up the array's device address with cudaGetSymbolAddress and
+ * loads the check kernel.  Under lazy module loading (the CUDA default) that set-up is when the
+ * library's device code and the array take their device memory, so make the first call before
+ * another allocator reserves the device's memory, and before any stream capture.
+ * All calls share the one array and run on the legacy default stream: calls that overlap on the
+ * GPU (from several host threads) race.  The legacy stream does not wait for non-blocking
+ * streams (a framework's side streams): synchronize the stream that wrote the arrays before
+ * calling.                                                                                   */
 int bqp_check_device_noalloc(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
                              const double* d_x, const double* d_c, const double* d_lower,
                              const double* d_upper, double tolerance, double offset,

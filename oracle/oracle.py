@@ -1,11 +1,15 @@
 """ctypes access to the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
-Two libraries:
+Libraries:
   oracle/_build/liboracle.so     the plain-C restatement in oracle/boxqp_oracle.c (always
-                                 buildable: gcc + OpenMP on any host)
+                                 buildable: gcc + OpenMP on any host), linked with the synthetic
+                                 instance generator (hypergrey-sih-26_gb300/csrc/planted.cpp, the
+                                 one generator the engine and the oracle share), so a process can
+                                 make the workloads without loading the engine library
   oracle/_ref/libsovereign_ref.so  the reference's own solver sources compiled by
-                                 oracle/ref.mk plus oracle/ref_shim.cpp (only where the
-                                 reference checkout exists)
+                                 oracle/ref.mk plus oracle/ref_shim.cpp, from the copy that
+                                 `make -f oracle/ref.mk stage` puts in oracle/_ref/src where the
+                                 reference checkout exists (the copy travels with the working tree)
   oracle/_build/libref_cuda.so   oracle/ref_cuda_harness.c: the reference's CUDA plugin kernels
                                  (oracle/_ref/cuda_box_sm103a.cubin, built by oracle/ref.mk from
                                  the reference's cuda_box.cu) under the reference's host loop
@@ -14,14 +18,18 @@ module; the engine never does.
 """
 import ctypes
 import subprocess
-from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_uint64, c_void_p
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ORACLE_SRC = HERE / 'boxqp_oracle.c'
+PLANTED_SRC = HERE.parent / 'hypergrey-sih-26_gb300' / 'csrc' / 'planted.cpp'
+BOXQP_H = HERE.parent / 'include' / 'boxqp.h'
 ORACLE_LIB = HERE / '_build' / 'liboracle.so'
+REF_MK = HERE / 'ref.mk'
+REF_QPLIB = HERE / '_ref' / 'qplib'
 REF_LIB = HERE / '_ref' / 'libsovereign_ref.so'
 REF_CUBIN = HERE / '_ref' / 'cuda_box_sm103a.cubin'
 REF_CUDA_SRC = HERE / 'ref_cuda_harness.c'
@@ -43,15 +51,49 @@ class OrcStats(ctypes.Structure):
 _I32P, _I64P, _F64P = POINTER(c_int32), POINTER(c_int64), POINTER(c_double)
 
 
+class PlantedSpec(ctypes.Structure):
+    """bqp_planted_spec of include/boxqp.h (the generator linked into liboracle.so)."""
+    _fields_ = [('family', c_int32), ('edges_per_vertex', c_int32), ('n', c_int64), ('grid_side', c_int32),
+                ('bounds_mode', c_int32), ('seed', c_uint64), ('lower', c_double), ('upper', c_double),
+                ('frac_lower', c_double), ('frac_upper', c_double), ('interior_lo', c_double),
+                ('interior_hi', c_double), ('diag_lo', c_double), ('diag_hi', c_double),
+                ('weight_lo', c_double), ('weight_hi', c_double), ('shift', c_double), ('dual_lo', c_double),
+                ('dual_hi', c_double)]
+
+
+PRESETS = {'graph10k': 0, 'graph1m': 1, 'grid': 2, 'batch': 3, 'serve': 4, 'tridiagonal': 5}
+
+
 def build_oracle(force=False):
-    """Compiles the C restatement (no FMA contraction, OpenMP)."""
-    if force or not ORACLE_LIB.exists() or ORACLE_SRC.stat().st_mtime > ORACLE_LIB.stat().st_mtime:
-        ORACLE_LIB.parent.mkdir(exist_ok=True)
+    """Compiles the C restatement (no FMA contraction, OpenMP) and the instance generator."""
+    srcs = [ORACLE_SRC, PLANTED_SRC, BOXQP_H]
+    if force or not ORACLE_LIB.exists() or any(p.stat().st_mtime > ORACLE_LIB.stat().st_mtime for p in srcs):
+        out = ORACLE_LIB.parent
+        out.mkdir(exist_ok=True)
+        c_obj, cpp_obj = out / 'boxqp_oracle.o', out / 'planted.o'
+        subprocess.run(['gcc', '-O2', '-std=gnu11', '-fopenmp', '-fPIC', '-ffp-contract=off', '-c', str(ORACLE_SRC),
+                        '-o', str(c_obj)], check=True, capture_output=True)
+        subprocess.run(['g++', '-O3', '-std=c++17', '-fPIC', '-ffp-contract=off', '-I', str(BOXQP_H.parent), '-c',
+                        str(PLANTED_SRC), '-o', str(cpp_obj)], check=True, capture_output=True)
         tmp = ORACLE_LIB.with_suffix('.tmp.so')
-        subprocess.run(['gcc', '-O2', '-std=gnu11', '-fopenmp', '-fPIC', '-shared', '-ffp-contract=off',
-                        str(ORACLE_SRC), '-o', str(tmp), '-lm'], check=True, capture_output=True)
+        subprocess.run(['g++', '-shared', '-fopenmp', str(c_obj), str(cpp_obj), '-o', str(tmp), '-lm'], check=True,
+                       capture_output=True)
         tmp.replace(ORACLE_LIB)
     return ORACLE_LIB
+
+
+def _make(*targets):
+    """Runs oracle/ref.mk from the repository root; returns the finished process."""
+    return subprocess.run(['make', '-s', '-j8', '-f', str(REF_MK), *targets], cwd=str(HERE.parent),
+                          capture_output=True, text=True)
+
+
+def stage_reference():
+    """Copies the reference files oracle/ref.mk compiles into oracle/_ref/src (where the
+    reference checkout exists; BOXQP_REFERENCE_DIR overrides its location).  True when a staged
+    copy is present afterwards."""
+    _make('stage')
+    return (HERE / '_ref' / 'src' / 'src' / 'accelerated_qp.cpp').exists()
 
 
 def build_ref_cuda(force=False):
@@ -72,12 +114,11 @@ def build_ref_cuda(force=False):
     return True
 
 
-def build_ref_cubin(ref_dir='/root/reference/02-software/solver'):
-    """Compiles the reference's cuda_box.cu for sm_103a into oracle/_ref (only where the reference
-    checkout exists); True when the module is present afterwards."""
-    if Path(ref_dir).is_dir():
-        subprocess.run(['make', '-s', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}', 'cuda_cubin'], cwd=str(HERE.parent),
-                       capture_output=True, text=True)
+def build_ref_cubin():
+    """Compiles the reference's cuda_box.cu for sm_103a into oracle/_ref (from the staged copy);
+    True when the module is present afterwards."""
+    if stage_reference():
+        _make('cuda_cubin')
     return REF_CUBIN.exists()
 
 
@@ -109,25 +150,24 @@ def ref_cuda_solve(rowptr, col, val, hrow, hcol, hval, cost, lower, upper, tol=1
     return STATUS.get(status.value, str(status.value)), st.as_dict(), x, (float(secs[0]), float(secs[1]))
 
 
-def build_reference(ref_dir='/root/reference/02-software/solver'):
-    """Builds oracle/_ref from the reference's sources when they are present; True on success."""
-    if not Path(ref_dir).is_dir():
+def build_reference():
+    """Builds oracle/_ref/libsovereign_ref.so from the staged reference sources; True on success."""
+    if not stage_reference():
         return REF_LIB.exists()
-    proc = subprocess.run(['make', '-s', '-j8', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}'],
-                          cwd=str(HERE.parent), capture_output=True, text=True)
+    proc = _make('all')
     return proc.returncode == 0 and REF_LIB.exists()
 
 
-def build_level_a(ref_dir='/root/reference/02-software/solver'):
-    """Links the reference's own CLI and scale harness with the GB300 plugin (Level A); returns the
-    path of the scale harness, or None where the reference checkout is absent."""
-    if not Path(ref_dir).is_dir():
+def build_level_a():
+    """Links the reference's own CLI and scale harness with the GB300 plugin (Level A) and with the
+    engine route (the *_engine binaries); returns oracle/_ref, or None without a staged copy of the
+    reference sources."""
+    if not stage_reference():
         return None
-    proc = subprocess.run(['make', '-s', '-j8', '-f', str(HERE / 'ref.mk'), f'REF={ref_dir}', 'level_a'],
-                          cwd=str(HERE.parent), capture_output=True, text=True)
+    proc = _make('level_a')
     if proc.returncode != 0:
         raise RuntimeError(proc.stdout + proc.stderr)
-    return HERE / '_ref' / 'solver_scale_gb300'
+    return HERE / '_ref'
 
 
 _orc = None
@@ -159,8 +199,67 @@ def orc():
         L.orc_max_abs_row_sum.restype = c_double
         L.orc_max_abs_row_sum.argtypes = [c_int64, _I32P, _F64P]
         L.orc_max_threads.restype = c_int
+        L.bqp_planted_preset.restype = c_int
+        L.bqp_planted_preset.argtypes = [c_int32, c_uint64, c_int64, c_int64, POINTER(PlantedSpec)]
+        L.bqp_planted_create.restype = c_void_p
+        L.bqp_planted_create.argtypes = [POINTER(PlantedSpec)]
+        L.bqp_planted_info.restype = c_int
+        L.bqp_planted_info.argtypes = [c_void_p, _I64P, _I64P, _I64P, _F64P]
+        L.bqp_planted_copy.restype = c_int
+        L.bqp_planted_copy.argtypes = [c_void_p, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P, _F64P, _F64P]
+        L.bqp_planted_copy_lower.restype = c_int
+        L.bqp_planted_copy_lower.argtypes = [c_void_p, _I64P, _I64P, _F64P]
+        L.bqp_planted_free.restype = None
+        L.bqp_planted_free.argtypes = [c_void_p]
         _orc = L
     return _orc
+
+
+def planted(preset, seed=1, index=0, n=0, lower_triplets=True):
+    """One planted instance from the generator linked into liboracle.so (the engine's generator,
+    so the arrays equal boxqp.planted's bit for bit); a dict of numpy arrays and scalars."""
+    L = orc()
+    spec = PlantedSpec()
+    if L.bqp_planted_preset(PRESETS[preset] if isinstance(preset, str) else int(preset), int(seed), int(index), int(n),
+                            spec) != 0:
+        raise ValueError(f'bad preset {preset!r}')
+    h = L.bqp_planted_create(spec)
+    if not h:
+        raise ValueError('planted generation failed')
+    try:
+        nn, nnz, nl, fstar = c_int64(0), c_int64(0), c_int64(0), c_double(0)
+        L.bqp_planted_info(h, ctypes.byref(nn), ctypes.byref(nnz), ctypes.byref(nl), ctypes.byref(fstar))
+        n_, z_ = nn.value, nnz.value
+        out = {'n': n_, 'nnz': z_, 'fstar': fstar.value, 'rowptr': np.empty(n_ + 1, np.int32),
+               'col': np.empty(z_, np.int32), 'val': np.empty(z_), 'c': np.empty(n_), 'lower': np.empty(n_),
+               'upper': np.empty(n_), 'xstar': np.empty(n_), 'z': np.empty(n_)}
+        L.bqp_planted_copy(h, _p(out['rowptr'], c_int32), _p(out['col'], c_int32), _p(out['val'], c_double),
+                           _p(out['c'], c_double), _p(out['lower'], c_double), _p(out['upper'], c_double),
+                           _p(out['xstar'], c_double), _p(out['z'], c_double))
+        if lower_triplets:
+            k = nl.value
+            hr, hc, hv = np.empty(k, np.int64), np.empty(k, np.int64), np.empty(k)
+            L.bqp_planted_copy_lower(h, _p(hr, c_int64), _p(hc, c_int64), _p(hv, c_double))
+            out['hrow'], out['hcol'], out['hval'] = hr, hc, hv
+        return out
+    finally:
+        L.bqp_planted_free(h)
+
+
+def active_set_mismatches(x, inst, margin=1e-6, atol=1e-9):
+    """Variables whose bound state in x differs from the planted optimum's, counted where the
+    planted margin exceeds `margin`: a dual |z| > margin puts x* strictly at its bound (x must sit
+    on that bound within atol), and an interior x* farther than `margin` from both bounds must not
+    sit on a bound."""
+    x = np.asarray(x, dtype=np.float64)
+    lo, up, z, xs = (np.asarray(inst[k], dtype=np.float64) for k in ('lower', 'upper', 'z', 'xstar'))
+    at_lo = np.abs(x - lo) <= atol * (1 + np.abs(lo))
+    at_up = np.abs(x - up) <= atol * (1 + np.abs(up))
+    want_lo = z > margin
+    want_up = z < -margin
+    interior = (z == 0) & (xs - lo > margin) & (up - xs > margin)
+    bad = (want_lo & ~at_lo) | (want_up & ~at_up) | (interior & (at_lo | at_up))
+    return int(np.count_nonzero(bad))
 
 
 def ref_available():
@@ -205,6 +304,8 @@ def ref():
         L.ref_qplib_row_entries.argtypes = [c_void_p]
         L.ref_qplib_close.restype = None
         L.ref_qplib_close.argtypes = [c_void_p]
+        L.ref_last_solve_seconds.restype = c_double
+        L.ref_last_solve_seconds.argtypes = []
         _ref = L
     return _ref
 
@@ -335,7 +436,9 @@ def ref_solve_box(hrow, hcol, hval, cost, lower, upper, tol=1e-7, iteration_limi
         raise RuntimeError(msg.value.decode())
     keys = ['objective', 'primal_residual', 'stationarity_residual', 'complementarity_residual', 'dual_bound',
             'relative_gap', 'verified', 'iterations']
-    return msg.value.decode(), x, dict(zip(keys, stats.tolist()))
+    st = dict(zip(keys, stats.tolist()))
+    st['seconds'] = float(ref().ref_last_solve_seconds())  # the solve_accelerated_box call alone
+    return msg.value.decode(), x, st
 
 
 def ref_solve_qp_admm(hrow, hcol, hval, cost, lower, upper, a_rowptr, a_col, a_val, row_lower, row_upper,

@@ -11,6 +11,7 @@
 #include "accelerated_qp.hpp"
 #include "qp.hpp"
 
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
@@ -63,9 +64,15 @@ void fill_stats(const sovereign::QpResult& r, double* stats) {
 struct QplibHandle {
     sovereign::QuadraticProblem q;
 };
+
+// Wall time of the last solve_accelerated_box call of ref_solve_box: the scope the reference's
+// own scale harness times (src/scale_benchmark.cpp:20-21), without the shim's problem set-up.
+thread_local double g_last_solve_seconds = 0;
 }  // namespace
 
 extern "C" {
+
+double ref_last_solve_seconds() { return g_last_solve_seconds; }
 
 // Runs the reference CPU engine.  status_out receives the reference's status string.
 // Returns 0 on success, 1 if the reference threw std::invalid_argument, 2 for any
@@ -81,7 +88,9 @@ int ref_solve_box(int64_t n, int64_t nh, const int64_t* hrow, const int64_t* hco
         o.iteration_limit = static_cast<std::size_t>(iteration_limit);
         o.time_limit = time_limit;
         o.threads = threads;
+        const auto start = std::chrono::steady_clock::now();
         auto r = sovereign::solve_accelerated_box(q, o, false);
+        g_last_solve_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
         fill_stats(r, stats);
         for (std::size_t j = 0; j < r.primal.size() && j < static_cast<std::size_t>(n); ++j) x_out[j] = r.primal[j];
         put_message(status_out, static_cast<std::size_t>(status_cap), r.status);

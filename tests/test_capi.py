@@ -225,15 +225,23 @@ def test_splitmix64_reference_values():
 
 
 def test_level_a_plugin_links_into_the_reference():
-    """The reference's own scale harness, linked with the GB300 plugin in place of its CUDA file,
-    reaches the plugin: without a GPU it reports the reference's message and exit code 2."""
+    """The reference's own scale harness, linked with the GB300 plugin in place of its CUDA file
+    and with the engine route, reaches the GB300 code: without a GPU both report the reference's
+    message and exit code 2, and the engine route's cpu backend still runs the reference's own
+    solver (its harness passes)."""
+    import json
     import subprocess
-    exe = O.build_level_a()
-    if exe is None:
-        pytest.skip('reference checkout not present on this host')
-    out = subprocess.run([str(exe), '1000', 'cuda', '1', '30'], capture_output=True, text=True, timeout=120,
-                         env={'CUDA_VISIBLE_DEVICES': '', 'PATH': '/usr/bin:/bin'})
-    assert out.returncode == 2 and 'No CUDA device available' in out.stderr
+    out_dir = O.build_level_a()
+    if out_dir is None:
+        pytest.skip('the reference sources are not staged on this host')
+    env = {'CUDA_VISIBLE_DEVICES': '', 'PATH': '/usr/bin:/bin'}
+    for name in ('solver_scale_gb300', 'solver_scale_gb300_engine'):
+        out = subprocess.run([str(out_dir / name), '1000', 'cuda', '1', '30'], capture_output=True, text=True,
+                             timeout=120, env=env)
+        assert out.returncode == 2 and 'No CUDA device available' in out.stderr, (name, out.stderr)
+    out = subprocess.run([str(out_dir / 'solver_scale_gb300_engine'), '1000', 'cpu', '1', '30'], capture_output=True,
+                         text=True, timeout=120, env=env)
+    assert out.returncode == 0 and json.loads(out.stdout)['passed'] is True
 
 
 def test_csr_builder_from_several_threads_at_once():

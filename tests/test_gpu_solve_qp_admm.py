@@ -6,9 +6,6 @@ iterations round differently (FMA, double instead of long double inner products)
 takes its own path to the same answer: on the reference's constrained QPs solved at 1e-4 and
 1e-5 it must return a primal and row duals that the reference's checker (restated bit for bit by
 check_solution) verifies at that tolerance, with the reference's objective to 1e-5 relative.
-
-This file is collected last (tests/test_zzz_*), so a run that stops at the first failure has
-already run every other test.
 """
 from pathlib import Path
 
