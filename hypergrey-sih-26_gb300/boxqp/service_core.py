@@ -114,6 +114,11 @@ async def solve_arrays(rowptr, col, val, c, lower, upper, tolerance=1e-6, precis
     except asyncio.TimeoutError:
         return {'engine': 'gb300', 'status': 'time_limit', 'message': 'no result within the time limit',
                 'objective': None, 'primal': []}
+    except EngineError as exc:
+        if exc.code == 4:  # refused at admission: it can never fit under the loop's memory cap
+            raise HttpError(413, 'request exceeds the device-memory cap: ' + str(exc)[:200])
+        return {'engine': 'gb300', 'status': 'engine_error', 'message': str(exc)[:300], 'objective': None,
+                'primal': []}
     except Exception as exc:
         return {'engine': 'gb300', 'status': 'engine_error', 'message': str(exc)[:300], 'objective': None,
                 'primal': []}

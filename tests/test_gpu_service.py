@@ -56,11 +56,13 @@ def test_npz_request_through_the_route_on_the_engine(server):
 
 
 def test_concurrent_requests_share_the_batch(server):
-    insts = [boxqp.planted('graph10k', seed=60 + k, n=30000 + 5000 * k) for k in range(6)]
+    """Six requests at once (FP64 iterations to 1e-8, long enough to overlap): each gets its own
+    verified answer, and the loop held several of them resident together."""
+    insts = [boxqp.planted('graph10k', seed=60 + k, n=100000 + 20000 * k) for k in range(6)]
 
     async def all_of():
-        return await asyncio.gather(*[core.solve_arrays(*arrays(p), tolerance=1e-6, precision='mixed',
-                                                        time_limit=20.0) for p in insts])
+        return await asyncio.gather(*[core.solve_arrays(*arrays(p), tolerance=1e-8, precision='fp64',
+                                                        time_limit=30.0) for p in insts])
     replies = asyncio.run(all_of())
     for p, r in zip(insts, replies):
         assert r['status'] == 'optimal' and r['columns'] == p['n']
