@@ -312,6 +312,22 @@ def run_ours(args, world, rank, local, pg):
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
                 'traffic': traffic, 'peak_kind': peak_kind, 'kernel': f'step_kernel<{args.precision}>',
                 'ms_per_launch': step_ms, 'algorithmic_bytes_per_launch': step_bytes}
+    # second roofline entry: the polish CG of this solve (mixed precision), its product kernel
+    # (the one that dominates the polish) and its vector kernel, on the packed Q_FF
+    roofline_cg = None
+    if args.precision == 'mixed':
+        eng.resolve([ident])
+        eng.wait(ident)
+        try:
+            ms_mv, ms_vec, b_mv, b_vec = eng.profile_cg(ident, 10)
+            roofline_cg = {'bound': 'hbm', 'kernel': 'cg_matvec_kernel', 'achieved': b_mv / (ms_mv * 1e-3) / 1e9,
+                           'peak': peak, 'unit': 'GB/s', 'frac': b_mv / (ms_mv * 1e-3) / 1e9 / peak,
+                           'peak_kind': peak_kind, 'ms_per_launch': ms_mv, 'algorithmic_bytes_per_launch': b_mv,
+                           'vector_kernel': {'kernel': 'cg_vector_kernel', 'ms_per_launch': ms_vec,
+                                             'algorithmic_bytes_per_launch': b_vec,
+                                             'achieved': b_vec / (ms_vec * 1e-3) / 1e9}}
+        except Exception as exc:  # the solve ended without a polish: no CG to time
+            roofline_cg = {'unavailable': str(exc)[:200]}
     eng.resolve([ident])  # restore a valid iterate
     eng.wait(ident)
     x, st = eng.fetch(ident, n)
@@ -421,7 +437,8 @@ def run_ours(args, world, rank, local, pg):
                        'parallelism': f'replicas x{world}'},
             'hbm_gbs': bytes_total / args.steps / (dev_s / args.steps) / 1e9,
             'wall_ms_per_step': 1e3 * wall / args.steps,
-            'solve': result, 'fp64_engine': fp64, 'roofline': roofline, 'cpu_baseline': cpu, 'e2e': e2e,
+            'solve': result, 'fp64_engine': fp64, 'roofline': roofline, 'roofline_cg': roofline_cg,
+            'cpu_baseline': cpu, 'e2e': e2e,
             'gpu_launches': int(kernels), 'graph_launches': int(launches),
             'clocks': clocks.summary()}
     print(json.dumps(line), flush=True)

@@ -76,6 +76,7 @@ PROTOTYPES = {
     'bqp_load': (c_int, [c_void_p, _I64P, _I64P, _I64P, _I64P]),
     'bqp_timer': (c_int, [c_void_p, c_int32, _F64P, _I64P, _I64P]),
     'bqp_profile_step': (c_int, [c_void_p, c_uint64, c_int32, _F64P, _F64P]),
+    'bqp_profile_cg': (c_int, [c_void_p, c_uint64, c_int32, _F64P, _F64P, _F64P, _F64P]),
     'bqp_solve_sync': (c_int, [c_void_p, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P,
                                POINTER(Options), _F64P, POINTER(Stats)]),
     'bqp_box_create': (c_void_p, [c_int, c_int64, c_int64, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P, c_double]),

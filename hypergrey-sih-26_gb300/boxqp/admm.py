@@ -689,6 +689,13 @@ def validate_linear_problem(q, rows):
     if np.any(np.isnan(rl)) or np.any(np.isnan(ru)) or np.any(rl == np.inf) or np.any(ru == -np.inf):
         raise ValueError('Invalid row bound')
     col = np.asarray(rows.col)
+    # the row pointers of the CSR rows (the reference keeps rows as vectors of entries, so a
+    # malformed pointer array is its 'Invalid sparse row entry' too): m + 1 entries from 0 to the
+    # entry count, non-decreasing
+    rowptr = np.asarray(rows.rowptr)
+    if (rowptr.shape != (m + 1,) or rowptr[0] != 0 or rowptr[-1] != col.shape[0]
+            or np.any(np.diff(rowptr.astype(np.int64)) < 0) or np.asarray(rows.val).shape != col.shape):
+        raise ValueError('Invalid sparse row entry')
     if np.any((col < 0) | (col >= n)) or not np.all(np.isfinite(np.asarray(rows.val, dtype=np.float64))):
         raise ValueError('Invalid sparse row entry')
 

@@ -300,6 +300,14 @@ class Engine:
         self._check(lib().bqp_profile_step(self._ctx, ident, int(launches), N.ctypes.byref(ms), N.ctypes.byref(b)))
         return ms.value, b.value
 
+    def profile_cg(self, ident, iterations=10):
+        """Times the polish CG of a finished mixed solve (bqp_profile_cg); returns
+        (ms per product launch, ms per vector launch, bytes per product launch, bytes per vector
+        launch).  The solve's answer is scrambled afterwards: re-run it with resolve()."""
+        vals = [N.c_double(0) for _ in range(4)]
+        self._check(lib().bqp_profile_cg(self._ctx, ident, int(iterations), *[N.ctypes.byref(v) for v in vals]))
+        return tuple(v.value for v in vals)
+
     def solve(self, rowptr, col, val, c, lower, upper, options: Options):
         """Synchronous solve through bqp_solve_sync; returns (x, Stats)."""
         rowptr, col, val = _i32(rowptr), _i32(col), _f64(val)

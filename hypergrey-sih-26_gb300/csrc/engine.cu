@@ -322,6 +322,8 @@ public:
         return BQP_OK;
     }
     int profile_step(uint64_t id, int launches, double* ms, double* bytes);
+    int profile_cg(uint64_t id, int iterations, double* ms_matvec, double* ms_vector, double* bytes_matvec,
+                   double* bytes_vector);
     void set_latency_target(double ms) {
         std::lock_guard<std::mutex> g(mu_);
         latency_ms_ = ms;
@@ -1644,6 +1646,83 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     return BQP_OK;
 }
 
+// Re-runs the polish of a finished mixed-precision solve from its FP32 iterate (snap, residual and
+// packing untimed), then times `iterations` CG iterations, the product kernel and the vector
+// kernel separately, with CUDA events on the engine stream.  The CG tolerance is set below zero so
+// every timed iteration does the whole work.  Bytes per launch: the device's per-iteration CG
+// accounting split between the two kernels, on the round's packed Q_FF (ff_nnz entries, ff_rows
+// free rows): product 12 ff_nnz + 52 ff_rows (Q_FF values and columns, row starts and counts,
+// the free list, u gathered once, u, r, x read and w written per free row), vector 84 ff_rows.
+int Engine::profile_cg(uint64_t id, int iterations, double* ms_matvec, double* ms_vector, double* bytes_matvec,
+                       double* bytes_vector) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = jobs_.find(id);
+    if (it == jobs_.end()) return BQP_ERR_NOT_FOUND;
+    Job& j = *it->second;
+    if (j.state != JOB_DONE || !j.resident || n_running_ != 0 || !queue_.empty() || iterations < 1 ||
+        j.opt.precision != PREC_MIXED)
+        return BQP_ERR_NOT_READY;
+    cudaSetDevice(device_);
+    update_grid();
+    InstDev saved;
+    cudaMemcpy(&saved, &d_inst_[j.slot], sizeof(InstDev), cudaMemcpyDeviceToHost);
+    if (!saved.polish || saved.result_src != 2) return BQP_ERR_NOT_READY;  // the solve did not end in a polish
+    InstDev R = saved;
+    R.status = ST_RUNNING;
+    R.phase = PH_POLISH_INIT;
+    R.cg_it = 0;
+    R.cg_tol = -1.0;
+    R.cg_max = 1LL << 40;
+    R.ff_nnz = 0;
+    R.ff_rows = 0;
+    cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
+    upload_tables();
+    h_ctrl_->n_inst = n_inst_;
+    h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    h_ctrl_->n_cg = 1;
+    cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
+    const View v = view();
+    const int grid = graph_grid_;
+    launch_polish_init(v, grid, stream_);
+    launch_polish_residual(v, grid, stream_);
+    std::vector<cudaEvent_t> ev(static_cast<size_t>(2 * iterations + 1), nullptr);
+    for (auto& e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], stream_);
+    for (int k = 0; k < iterations; ++k) {
+        launch_cg_matvec(v, grid, stream_);
+        cudaEventRecord(ev[2 * k + 1], stream_);
+        launch_cg_vector(v, grid, stream_);
+        cudaEventRecord(ev[2 * k + 2], stream_);
+    }
+    InstDev after;
+    cudaMemcpyAsync(&after, &d_inst_[j.slot], sizeof(InstDev), cudaMemcpyDeviceToHost, stream_);
+    cudaMemcpyAsync(&d_inst_[j.slot], &saved, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    double mv = 0, vec = 0;
+    for (int k = 0; k < iterations && e == cudaSuccess; ++k) {
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]);
+        cudaEventElapsedTime(&b, ev[2 * k + 1], ev[2 * k + 2]);
+        mv += a;
+        vec += b;
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) {
+        set_error(std::string("CUDA: ") + cudaGetErrorString(e));
+        return BQP_ERR_CUDA;
+    }
+    if (after.phase != PH_POLISH_CG || after.cg_it != iterations) {
+        set_error("profile_cg: the CG iterations did not all run");
+        return BQP_ERR_NOT_READY;
+    }
+    const double fz = static_cast<double>(after.ff_nnz), fr = static_cast<double>(after.ff_rows);
+    if (ms_matvec) *ms_matvec = mv / iterations;
+    if (ms_vector) *ms_vector = vec / iterations;
+    if (bytes_matvec) *bytes_matvec = 12.0 * fz + 52.0 * fr;
+    if (bytes_vector) *bytes_vector = 84.0 * fr;
+    return BQP_OK;
+}
+
 void Engine::loop() {
     cudaSetDevice(device_);
     std::unique_lock<std::mutex> lk(mu_);
@@ -2199,6 +2278,12 @@ int bqp_inject_admission_oom(bqp_ctx* ctx, int32_t count) {
 int bqp_timer(bqp_ctx* ctx, int32_t reset, double* device_ms, int64_t* kernels, int64_t* graph_launches) {
     if (!ctx) return BQP_ERR_INVALID;
     return ctx->engine->timer(reset, device_ms, kernels, graph_launches);
+}
+
+int bqp_profile_cg(bqp_ctx* ctx, uint64_t id, int32_t iterations, double* ms_matvec, double* ms_vector,
+                   double* bytes_matvec, double* bytes_vector) {
+    if (!ctx) return BQP_ERR_INVALID;
+    return ctx->engine->profile_cg(id, iterations, ms_matvec, ms_vector, bytes_matvec, bytes_vector);
 }
 
 int bqp_profile_step(bqp_ctx* ctx, uint64_t id, int32_t launches, double* ms_per_launch, double* bytes_per_launch) {

@@ -188,6 +188,14 @@ int bqp_inject_admission_oom(bqp_ctx* ctx, int32_t count);
 int bqp_timer(bqp_ctx* ctx, int32_t reset, double* device_ms, int64_t* kernels, int64_t* graph_launches);
 int bqp_profile_step(bqp_ctx* ctx, uint64_t id, int32_t launches, double* ms_per_launch,
                      double* bytes_per_launch);
+/* bqp_profile_cg: on a finished, still-resident mixed-precision solve that ended in its FP64
+ * polish, re-runs the polish from the solve's FP32 iterate (untimed) and times `iterations` CG
+ * iterations with CUDA events, the product kernel (w = Q_FF u with the fused reduction) and the
+ * vector kernel separately; returns their mean times and algorithmic bytes per launch on the
+ * packed Q_FF (product 12 nnz_FF + 52 n_F, vector 84 n_F).  Same conditions and side effect as
+ * bqp_profile_step.                                                                         */
+int bqp_profile_cg(bqp_ctx* ctx, uint64_t id, int32_t iterations, double* ms_matvec, double* ms_vector,
+                   double* bytes_matvec, double* bytes_vector);
 
 /* ---- synchronous single solve (the CLI path) --------------------------------------------- */
 int bqp_solve_sync(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,

@@ -222,6 +222,14 @@ def test_solve_qp_admm_statuses_and_option_checks():
     bad_col[0] = q.n
     with pytest.raises(ValueError, match='Invalid sparse row entry'):
         solve_qp_admm(q, LinearRows(rows.rowptr, bad_col, rows.val, rows.lower, rows.upper), make_system=make)
+    # malformed row pointers: not starting at 0, decreasing, not ending at the entry count
+    for fix in (lambda r: r + 1, lambda r: np.concatenate([r[:1], r[2:2], r[1:]])[::-1].copy(),
+                lambda r: np.concatenate([r[:-1], r[-1:] - 1])):
+        bad_ptr = fix(np.array(rows.rowptr, dtype=np.int32))
+        if bad_ptr.shape != np.asarray(rows.rowptr).shape:
+            continue
+        with pytest.raises(ValueError, match='Invalid sparse row entry'):
+            solve_qp_admm(q, LinearRows(bad_ptr, rows.col, rows.val, rows.lower, rows.upper), make_system=make)
     qi = boxqp.QuadraticProblem(cost=q.cost, lower=q.lower, upper=q.upper, hessian_row=q.hessian_row,
                                 hessian_col=q.hessian_col, hessian_val=q.hessian_val,
                                 integer=np.arange(q.n) == 0)

@@ -386,3 +386,24 @@ def test_one_sided_boxes(engine, golden, name, precision):
     assert np.all(np.isfinite(x))
     assert np.all(x >= p['lower']) and np.all(x <= p['upper'])
     assert st.objective == pytest.approx(rec['objective'], rel=1e-6)
+
+
+def test_profile_cg_times_the_polish_and_the_solve_reruns_to_the_same_bits(engine):
+    """bqp_profile_cg re-runs the polish of a finished mixed solve and times its CG kernels; the
+    bytes it reports are the packed Q_FF's, and a re-solve afterwards gives the same answer."""
+    inst = boxqp.planted('graph1m', seed=1, n=200000)
+    o = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+    ident = engine.submit(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+    engine.wait(ident)
+    x, st = engine.fetch(ident, inst['n'])
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal' and st.polish_iterations > 0
+    ms_mv, ms_vec, b_mv, b_vec = engine.profile_cg(ident, 5)
+    assert ms_mv > 0 and ms_vec > 0
+    free_rows = b_vec / 84.0
+    assert 0 < free_rows <= inst['n']
+    assert 0 < (b_mv - 52.0 * free_rows) / 12.0 <= inst['nnz']  # packed Q_FF entries
+    engine.resolve([ident])
+    engine.wait(ident)
+    x2, st2 = engine.fetch(ident, inst['n'])
+    assert np.array_equal(x, x2) and st2.iterations == st.iterations
+    engine.release(ident)
