@@ -410,6 +410,7 @@ private:
         v.status_mirror = d_status_;
         v.ranges = d_ranges_;
         v.group_tiles = d_group_tiles_;
+        v.units = d_units_;
         return v;
     }
     bool cuda_ok(cudaError_t e, std::string& why, const char* what) {
@@ -461,10 +462,12 @@ private:
     std::vector<Job*> slot_job_;
     std::vector<int32_t> slot_prec_;      // precision of the solve in each slot
     std::vector<int32_t> h_group_tiles_;  // tile indices ordered by step group
+    std::vector<int32_t> h_units_;        // first tile of each CG work unit
     int32_t group_begin_[kStepGroups + 1] = {};
     uint32_t groups_present_ = 0;         // step groups with tiles
     uint32_t graph_groups_ = 0;           // step groups the graph launches
     int32_t* d_group_tiles_ = nullptr;
+    int32_t* d_units_ = nullptr;
     std::vector<int> free_slots_;
     int n_inst_ = 0;
     bool tables_dirty_ = false;
@@ -578,9 +581,9 @@ void Engine::shutdown() {
     exec_ = nullptr;
     graph_ = nullptr;
     cudaFree(d_inst_); cudaFree(d_ranges_); cudaFree(d_tile_done_); cudaFree(d_status_);
-    cudaFree(d_tiles_); cudaFree(d_partial_); cudaFree(d_ctrl_);
+    cudaFree(d_tiles_); cudaFree(d_partial_); cudaFree(d_ctrl_); cudaFree(d_group_tiles_); cudaFree(d_units_);
     d_inst_ = nullptr; d_ranges_ = nullptr; d_tile_done_ = nullptr; d_status_ = nullptr;
-    d_tiles_ = nullptr; d_partial_ = nullptr; d_ctrl_ = nullptr;
+    d_tiles_ = nullptr; d_partial_ = nullptr; d_ctrl_ = nullptr; d_group_tiles_ = nullptr; d_units_ = nullptr;
     if (h_ctrl_) cudaFreeHost(h_ctrl_);
     if (h_stage_) cudaFreeHost(h_stage_);
     if (h_stage_slots_) cudaFreeHost(h_stage_slots_);
@@ -652,15 +655,19 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
         Tile* tiles = nullptr;
         Partial* partial = nullptr;
         int32_t* group_tiles = nullptr;
+        int32_t* units = nullptr;
         if (!cuda_ok(cudaMalloc(&tiles, sizeof(Tile) * cap), why, "tile table")) return false;
         if (!cuda_ok(cudaMalloc(&partial, sizeof(Partial) * cap), why, "partials")) return false;
         if (!cuda_ok(cudaMalloc(&group_tiles, sizeof(int32_t) * cap), why, "step groups")) return false;
+        if (!cuda_ok(cudaMalloc(&units, sizeof(int32_t) * cap), why, "CG work units")) return false;
         cudaFree(d_tiles_);
         cudaFree(d_partial_);
         cudaFree(d_group_tiles_);
+        cudaFree(d_units_);
         d_tiles_ = tiles;
         d_partial_ = partial;
         d_group_tiles_ = group_tiles;
+        d_units_ = units;
         tile_cap_ = cap;
         tables_dirty_ = true;
         graph_valid_ = false;
@@ -1448,6 +1455,13 @@ void Engine::upload_tables() {
     if (!h_group_tiles_.empty())
         cudaMemcpyAsync(d_group_tiles_, h_group_tiles_.data(), sizeof(int32_t) * h_group_tiles_.size(),
                         cudaMemcpyHostToDevice, stream_);
+    // CG work units: runs of kCgUnit consecutive tiles of one instance, counted from the
+    // instance's first tile (so a unit depends on the instance alone, not on the batch)
+    h_units_.clear();
+    for (int k = 0; k < static_cast<int>(h_tiles_.size()); ++k)
+        if ((k - h_ranges_[h_tiles_[k].inst].x) % kCgUnit == 0) h_units_.push_back(k);
+    if (!h_units_.empty())
+        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int32_t) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
     cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
     // the pageable sources above are copied out before cudaMemcpyAsync returns
     if (groups_present_ & ~graph_groups_) graph_valid_ = false;
@@ -1466,6 +1480,7 @@ bool Engine::run_once(std::string& why) {
     if (latency > 0) cap = std::max(1, static_cast<int>(latency / std::max(body_ms_, 1e-3)));
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    h_ctrl_->n_units = static_cast<int32_t>(h_units_.size());
     std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
     for (int k = 0; k < 3; ++k) {
         h_ctrl_->check_due[k] = 1;  // the first body checks whatever is due; later ones as counted
@@ -1620,6 +1635,7 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     upload_tables();
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    h_ctrl_->n_units = static_cast<int32_t>(h_units_.size());
     std::memcpy(h_ctrl_->group_begin, group_begin_, sizeof(group_begin_));
     for (int k = 0; k < 3; ++k) h_ctrl_->step_due[k] = kMaxInterval;
     cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
@@ -1679,6 +1695,7 @@ int Engine::profile_cg(uint64_t id, int iterations, double* ms_matvec, double* m
     upload_tables();
     h_ctrl_->n_inst = n_inst_;
     h_ctrl_->n_tiles = static_cast<int32_t>(h_tiles_.size());
+    h_ctrl_->n_units = static_cast<int32_t>(h_units_.size());
     h_ctrl_->n_cg = 1;
     cudaMemcpyAsync(d_ctrl_, h_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, stream_);
     const View v = view();

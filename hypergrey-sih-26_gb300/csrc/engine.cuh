@@ -15,6 +15,8 @@ constexpr int kBlock = 256;          // threads per CTA of every tile kernel
 constexpr int kMaxInterval = 32;     // maximum check interval (iterations per chunk)
 constexpr int kTileNnz = 4096;       // target nonzeros per tile
 constexpr int kTileRows = 512;       // maximum rows per tile
+constexpr int kCgUnit = 4;           // tiles per work unit of the polish CG product kernel
+constexpr int kCgGroups = 2;         // row groups per warp whose loads the CG product keeps in flight
 constexpr int kRearmRows = 8192;     // rows per block when re-arming resident solves
 constexpr int64_t kHostPrimal = 131072;  // primals up to this size come back at completion, larger at fetch
 
@@ -183,6 +185,7 @@ static_assert(sizeof(InstDev) % 16 == 0, "rearm_kernel copies records as 16-byte
 struct Ctrl {
     int32_t n_inst;        // instance records in use
     int32_t n_tiles;       // tiles in use
+    int32_t n_units;       // CG work units in use (View::units)
     int32_t bodies;        // loop bodies run in the current launch
     int32_t body_cap;      // stop the device loop after this many bodies
     int32_t running;       // instances still running (written by the control kernel)
@@ -207,6 +210,8 @@ struct View {
     int32_t* status_mirror;  // per-instance status, rewritten by the control kernel every body
     const int2* ranges;      // per-instance tile range [x, y) in the tile table
     const int32_t* group_tiles;  // tile indices ordered by step group (Ctrl::group_begin)
+    const int32_t* units;        // CG work units: the first tile of each run of kCgUnit consecutive
+                                 // tiles of one instance (instance-local tile index a multiple of kCgUnit)
 };
 
 }  // namespace bqp

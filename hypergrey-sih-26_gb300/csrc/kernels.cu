@@ -268,30 +268,35 @@ __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true, bool
     return v;
 }
 
-__device__ Acc reduce_instance_ab(const View& v, int tb, int te) {
+// Reduces the CG partials of an instance in a fixed order: the partials of tiles tb, tb + stride,
+// ... below te (stride 1: every tile; kCgUnit: the first tile of each CG work unit).
+__device__ Acc reduce_instance_ab(const View& v, int tb, int te, int stride = 1) {
     constexpr int kAhead = 8;
+    const int count = (te - tb + stride - 1) / stride;
     Acc acc = acc_identity();
-    int k = tb + static_cast<int>(threadIdx.x);
-    for (; k + (kAhead - 1) * kBlock < te; k += kAhead * kBlock) {
+    int i = static_cast<int>(threadIdx.x);
+    for (; i + (kAhead - 1) * kBlock < count; i += kAhead * kBlock) {
         double a[kAhead], ob[kAhead];
         unsigned long long b[kAhead];
 #pragma unroll
-        for (int i = 0; i < kAhead; ++i) {
-            a[i] = __ldcg(&v.partial[k + i * kBlock].a);
-            ob[i] = __ldcg(&v.partial[k + i * kBlock].obj);
-            b[i] = __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k + i * kBlock].b));
+        for (int m = 0; m < kAhead; ++m) {
+            const Partial* p = &v.partial[tb + (i + m * kBlock) * stride];
+            a[m] = __ldcg(&p->a);
+            ob[m] = __ldcg(&p->obj);
+            b[m] = __ldcg(reinterpret_cast<const unsigned long long*>(&p->b));
         }
 #pragma unroll
-        for (int i = 0; i < kAhead; ++i) {
-            acc.a += a[i];
-            acc.obj += ob[i];
-            acc.b = umax64(acc.b, b[i]);
+        for (int m = 0; m < kAhead; ++m) {
+            acc.a += a[m];
+            acc.obj += ob[m];
+            acc.b = umax64(acc.b, b[m]);
         }
     }
-    for (; k < te; k += kBlock) {
-        acc.a += __ldcg(&v.partial[k].a);
-        acc.obj += __ldcg(&v.partial[k].obj);
-        acc.b = umax64(acc.b, __ldcg(reinterpret_cast<const unsigned long long*>(&v.partial[k].b)));
+    for (; i < count; i += kBlock) {
+        const Partial* p = &v.partial[tb + i * stride];
+        acc.a += __ldcg(&p->a);
+        acc.obj += __ldcg(&p->obj);
+        acc.b = umax64(acc.b, __ldcg(reinterpret_cast<const unsigned long long*>(&p->b)));
     }
     return block_reduce_ab(acc);
 }
@@ -1109,8 +1114,10 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     int32_t* __restrict__ col_ff = I.col_ff;
     float* __restrict__ hi_ff = I.hi_ff;
     float* __restrict__ lo_ff = I.lo_ff;
-    int32_t* __restrict__ cnt_ff = I.cnt_ff;
-    int32_t* __restrict__ start_ff = I.start_ff;
+    // the packed row's entry count and start, at its position in the tile's free list (the CG
+    // product reads them without first loading the row index)
+    int32_t* __restrict__ cnt_ff = I.cnt_ff + (list - I.free_rows);
+    int32_t* __restrict__ start_ff = I.start_ff + (list - I.free_rows);
     double* __restrict__ r_out = I.r;
     double* __restrict__ z_out = I.z;
     double* __restrict__ p_out = I.p;
@@ -1153,8 +1160,8 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
 #pragma unroll
         for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
         if (sl == 0 && r >= 0) {
-            cnt_ff[r] = kept;
-            start_ff[r] = dst;
+            cnt_ff[j] = kept;
+            start_ff[j] = dst;
             rowsum[j] = acc;
         }
     }
@@ -1175,12 +1182,42 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     }
 }
 
-// CG product w = Q_FF u on a tile's free rows (u gathered from its FP32 pairs), accumulating
-// gamma = r.u, delta = w.u and max |r|/(1+|x|) (the single reduction of the Chronopoulos-Gear
-// form of preconditioned CG).
+// CG product w = Q_FF u over one work unit, the free rows of up to kCgUnit consecutive tiles of
+// one instance taken as one list (position p of the unit: tile k with pre[k] <= p < pre[k + 1],
+// row j = p - pre[k] of that tile's free list), u gathered from its FP32 pairs; accumulates
+// gamma = r.u, delta = w.u and max |r|/(1+|x|) (the single reduction of the Chronopoulos-Gear form
+// of preconditioned CG).  LANES lanes per row for the products, kCgGroups row groups of a warp
+// with their loads in flight together, then the FP64 epilogue one row per thread on full warps.
+__device__ __forceinline__ int unit_tile(const int* pre, int nk, int p) {
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < kCgUnit; ++i) k += (i < nk && p >= pre[i]) ? 1 : 0;
+    return k;
+}
+
+// The unit's free-row table in shared memory: pre[k] (prefix of the tiles' free counts, the
+// total at pre[kCgUnit]) and rbeg[k] (the tile's first row, where its free list starts).  The
+// caller's previous readers of the table are past a block barrier.
+__device__ __forceinline__ void unit_table(const View& v, const InstDev& I, int t0, int first_tile, int nk, int* pre,
+                                          int* rbeg) {
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < nk; ++k) {
+            pre[k] = acc;
+            rbeg[k] = v.tiles[t0 + k].row_begin;
+            acc += I.free_cnt[t0 - first_tile + k];
+        }
+        for (int k = nk; k <= kCgUnit; ++k) pre[k] = acc;
+    }
+    __syncthreads();
+}
+
 template <int LANES>
-__device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, int n, float2* rowsum, Acc& a) {
+__device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, int nk, int total, float2* rowsum,
+                            Acc& a) {
     constexpr int R = 32 / LANES;
+    constexpr int W = kBlock / 32;
+    constexpr int U = kCgGroups;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
     const int32_t* __restrict__ col = I.col_ff;
@@ -1192,26 +1229,50 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     const double* __restrict__ u = I.z;
     const double* __restrict__ rr_v = I.r;
     const double* __restrict__ xp = I.xp;
+    const int32_t* __restrict__ list = I.free_rows;
     double* __restrict__ q_out = I.q;      // w
-    for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
-        const int j = g * R + sub;
-        float2 acc = make_float2(0.f, 0.f);
-        int r = -1;
-        if (j < n) {
-            r = list[j];
-            const int ks = start[r], ke = ks + cnt[r];
-#pragma unroll 4
-            for (int k = ks + sl; k < ke; k += LANES) acc = df_add(acc, df_prod2(__ldg(vhi + k), __ldg(vlo + k), p2[__ldg(col + k)]));
+    const int groups = (total + R - 1) / R;
+    for (int g0 = warp; g0 < groups; g0 += W * U) {  // warp-uniform
+        int ks[U], ke[U];
+#pragma unroll
+        for (int m = 0; m < U; ++m) {
+            const int p = (g0 + m * W) * R + sub;
+            ks[m] = 0;
+            ke[m] = 0;
+            if (p < total) {
+                const int k = unit_tile(pre, nk, p);
+                const int at = rbeg[k] + (p - pre[k]);
+                ks[m] = start[at];
+                ke[m] = ks[m] + cnt[at];
+            }
+        }
+        int longest = 0;
+#pragma unroll
+        for (int m = 0; m < U; ++m) longest = max(longest, ke[m] - ks[m]);
+        float2 acc[U];
+#pragma unroll
+        for (int m = 0; m < U; ++m) acc[m] = make_float2(0.f, 0.f);
+        for (int i = sl; i < longest; i += LANES) {
+#pragma unroll
+            for (int m = 0; m < U; ++m) {
+                const int e = ks[m] + i;
+                if (e < ke[m]) acc[m] = df_add(acc[m], df_prod2(__ldg(vhi + e), __ldg(vlo + e), p2[__ldg(col + e)]));
+            }
         }
 #pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
-        if (sl == 0 && r >= 0) rowsum[j] = acc;
+        for (int m = 0; m < U; ++m) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1) acc[m] = df_add(acc[m], shfl_xor(acc[m], o));
+            const int p = (g0 + m * W) * R + sub;
+            if (sl == 0 && p < total) rowsum[p] = acc[m];
+        }
     }
     // the FP64 epilogue, one free row per thread on full warps
     __syncthreads();
-    for (int t = threadIdx.x; t < n; t += kBlock) {
-        const int r = list[t];
-        const double w = df_value(rowsum[t]), ui = u[r], ri = rr_v[r];
+    for (int p = threadIdx.x; p < total; p += kBlock) {
+        const int k = unit_tile(pre, nk, p);
+        const int r = list[rbeg[k] + (p - pre[k])];
+        const double w = df_value(rowsum[p]), ui = u[r], ri = rr_v[r];
         q_out[r] = w;
         a.a = fma(ri, ui, a.a);
         a.obj = fma(w, ui, a.obj);
@@ -1219,7 +1280,6 @@ __device__ void matvec_rows(const InstDev& I, const int32_t* __restrict__ list, 
     }
 }
 
-// Returns the tile's packed Q_FF entries.
 template <int LANES>
 __device__ int residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, int32_t* start_of,
                              float2* rowsum, Acc& a) {
@@ -1230,36 +1290,21 @@ __device__ int residual_tile(const InstDev& I, const int32_t* list, int n_free, 
     return kept;
 }
 
-// Residual (with the packing of Q_FF) or CG product over tile rows [rb, ...) of one instance;
-// the residual returns the tile's packed Q_FF entries (0 for the product).
-template <bool RESIDUAL>
+// Residual (with the packing of Q_FF) over tile rows [rb, ...) of one instance; returns the
+// tile's packed Q_FF entries.
 __device__ int polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
-    // one copy per kernel, shared by every lane count: free-list positions of the packed rows
-    // (residual) and row sums handed to the FP64 epilogue
-    __shared__ int32_t start_of[RESIDUAL ? kTileRows : 1];
-    __shared__ float2 rowsum[kTileRows];
+    __shared__ int32_t start_of[kTileRows];  // free-list positions of the packed rows
+    __shared__ float2 rowsum[kTileRows];     // row sums handed to the FP64 epilogue
     const int32_t* list = I.free_rows + rb;
-    if constexpr (RESIDUAL) {
-        const int base = __ldg(I.rowptr + rb);
-        switch (I.lanes_res) {
-        case 1: return residual_tile<1>(I, list, n_free, base, start_of, rowsum, a);
-        case 2: return residual_tile<2>(I, list, n_free, base, start_of, rowsum, a);
-        case 4: return residual_tile<4>(I, list, n_free, base, start_of, rowsum, a);
-        case 8: return residual_tile<8>(I, list, n_free, base, start_of, rowsum, a);
-        case 16: return residual_tile<16>(I, list, n_free, base, start_of, rowsum, a);
-        default: return residual_tile<32>(I, list, n_free, base, start_of, rowsum, a);
-        }
-    } else {
-        switch (I.lanes_cg) {
-        case 1: matvec_rows<1>(I, list, n_free, rowsum, a); break;
-        case 2: matvec_rows<2>(I, list, n_free, rowsum, a); break;
-        case 4: matvec_rows<4>(I, list, n_free, rowsum, a); break;
-        case 8: matvec_rows<8>(I, list, n_free, rowsum, a); break;
-        case 16: matvec_rows<16>(I, list, n_free, rowsum, a); break;
-        default: matvec_rows<32>(I, list, n_free, rowsum, a); break;
-        }
+    const int base = __ldg(I.rowptr + rb);
+    switch (I.lanes_res) {
+    case 1: return residual_tile<1>(I, list, n_free, base, start_of, rowsum, a);
+    case 2: return residual_tile<2>(I, list, n_free, base, start_of, rowsum, a);
+    case 4: return residual_tile<4>(I, list, n_free, base, start_of, rowsum, a);
+    case 8: return residual_tile<8>(I, list, n_free, base, start_of, rowsum, a);
+    case 16: return residual_tile<16>(I, list, n_free, base, start_of, rowsum, a);
+    default: return residual_tile<32>(I, list, n_free, base, start_of, rowsum, a);
     }
-    return 0;
 }
 
 __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
@@ -1271,7 +1316,7 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         const int n_free = I.free_cnt[t - R.x];
-        const int kept = polish_rows<true>(I, T.row_begin, n_free, a);
+        const int kept = polish_rows(I, T.row_begin, n_free, a);
         if (threadIdx.x == 0) {  // Q_FF size of this polish round, for the byte accounting
             atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_nnz), static_cast<unsigned long long>(kept));
             atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_rows), static_cast<unsigned long long>(n_free));
@@ -1298,18 +1343,33 @@ __global__ void __launch_bounds__(kBlock, 3) polish_residual_kernel(View v) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock, 5) cg_matvec_kernel(View v) {
-    const int nt = v.ctrl->n_tiles;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-        const Tile T = v.tiles[t];
+__global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
+    __shared__ int pre[kCgUnit + 1];
+    __shared__ int rbeg[kCgUnit];
+    __shared__ float2 rowsum[kCgUnit * kTileRows];
+    const int nu = v.ctrl->n_units;
+    for (int un = blockIdx.x; un < nu; un += gridDim.x) {
+        const int t0 = v.units[un];
+        const Tile T = v.tiles[t0];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         const int2 R = v.ranges[T.inst];
+        const int nk = min(kCgUnit, R.y - t0);
+        unit_table(v, I, t0, R.x, nk, pre, rbeg);
+        const int total = pre[kCgUnit];
         Acc a = acc_identity();
-        polish_rows<false>(I, T.row_begin, I.free_cnt[t - R.x], a);
-        Acc total = block_reduce_ab(a, I.lanes_cg, true, true);
-        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
+        switch (I.lanes_cg) {
+        case 1: matvec_unit<1>(I, pre, rbeg, nk, total, rowsum, a); break;
+        case 2: matvec_unit<2>(I, pre, rbeg, nk, total, rowsum, a); break;
+        case 4: matvec_unit<4>(I, pre, rbeg, nk, total, rowsum, a); break;
+        case 8: matvec_unit<8>(I, pre, rbeg, nk, total, rowsum, a); break;
+        case 16: matvec_unit<16>(I, pre, rbeg, nk, total, rowsum, a); break;
+        default: matvec_unit<32>(I, pre, rbeg, nk, total, rowsum, a); break;
+        }
+        Acc tot = block_reduce_ab(a, I.lanes_cg, true, true);
+        const int units_inst = (R.y - R.x + kCgUnit - 1) / kCgUnit;
+        if (publish_and_test_last(v, t0, T.inst, units_inst, tot)) {
+            Acc inst_total = reduce_instance_ab(v, R.x, R.y, kCgUnit);
             if (threadIdx.x == 0) {
                 // Chronopoulos-Gear: gamma_i = r_i.u_i, delta_i = (Q u_i).u_i, beta_i =
                 // gamma_i / gamma_{i-1}, alpha_i = gamma_i / (delta_i - beta_i gamma_i / alpha_{i-1})
