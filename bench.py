@@ -13,14 +13,21 @@ in FP64.  A step is one complete solve of that instance.
           the inputs at submission; e2e.sync: bqp_solve_sync one call at a time)
   roofline  the FISTA step kernel (dominant kernel) timed alone with CUDA events on the same
           instance; algorithmic bytes per launch nnz*(4+4) + 4(n+1) + 7*4n
-  cpu_baseline  the FP64 reference FISTA (CPU oracle port, all host cores) on one full solve
+  roofline_cg  the polish CG product kernel of the same solve (bqp_profile_cg), bytes per launch
+          12 nnz_FF + 52 n_F on the packed free-free block
+  solve.oracle_check  the timed solve's primal checked on the host by the oracle
+          (check_qp_solution restated) and against the planted active set
+  cpu_baseline  one full FP64 solve by the reference's own solve_accelerated_box, built from its
+          sources on this host (all cores; the oracle port where no staged copy exists)
 
 Other workloads (--workload): grid, graph10k, tridiagonal (the reference's published family),
 batch (4,096 uneven instances in one launch), serve (Poisson arrivals into the continuous-batching
 request loop) and admm (the constrained-QP ADMM inner solve, CG iterations/s).
 
---impl reference times the reference algorithm's CPU implementation (the oracle port of
-src/accelerated_qp.cpp, OpenMP on all host cores) on the same workload and metric.
+--impl reference times the reference's own CPU solve_accelerated_box (src/accelerated_qp.cpp,
+OpenMP on all host cores) on the same workload and metric, on an instance made by the oracle
+library's copy of the generator, so that process never loads the engine library.
+--case solve|step: small runs for kernel profilers (one solve; the step kernel alone).
 Multi-GPU (--gpus N under torchrun): independent replicas, one per GPU (no data exchange).
 """
 import argparse
