@@ -65,7 +65,7 @@ struct Layout {
     size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
-    size_t sstep = kNone, lprec = kNone, s = kNone;
+    size_t sstep = kNone, lprec = kNone, s = kNone, gate = kNone;
     size_t total = 0;
 };
 
@@ -122,6 +122,7 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.w64b = take(N * 8);
     }
     L.lprec = take(8);
+    L.gate = take(sizeof(GateResult));
     L.total = o;
     return L;
 }
@@ -204,6 +205,7 @@ struct Job {
     Layout layout;
     InstDev rec{};            // host image of the device record
     int error = BQP_OK;
+    GateResult* gate_host = nullptr;  // page-locked copy of the admission's convexity gate result
     bool out_of_memory = false;  // the admission's device allocation failed (or was made to fail)
     std::string error_text;
     bqp_stats stats{};
@@ -232,6 +234,45 @@ void free_inputs(Job& j) {
     j.own = nullptr;
     j.own_bytes = 0;
     j.rowptr = nullptr; j.col = nullptr; j.val = nullptr; j.c = nullptr; j.l = nullptr; j.u = nullptr;
+}
+
+// check_convex_hessian (src/qp_admm.cpp:30-62) on the host, from a full CSR: diagonal dominance
+// per row, else the sparse LDL^T of bqp_check_convex on the lower triangle.  Used where the
+// device gate cannot decide (a solve finishing before admission, or a Hessian that is not
+// diagonally dominant).
+bool host_gate_convex(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val) {
+    bool dominant = true;
+    for (int64_t i = 0; i < n; ++i) {
+        double d = 0, radius = 0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            if (col[k] == i) d += val[k];
+            else radius += std::abs(val[k]);
+        }
+        if (d < 0 || (d == 0 && radius > 0)) return false;
+        if (d < radius) dominant = false;
+    }
+    if (dominant) return true;
+    std::vector<int64_t> tr, tc;
+    std::vector<double> tv;
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] <= i) {
+                tr.push_back(i);
+                tc.push_back(col[k]);
+                tv.push_back(val[k]);
+            }
+    return bqp_check_convex(n, static_cast<int64_t>(tr.size()), tr.data(), tc.data(), tv.data(), 0) == 1;
+}
+
+// The result record of a solve refused as unsupported_curvature (the reference's QpResult defaults).
+void set_unsupported(bqp_stats& st) {
+    st.status = BQP_STATUS_UNSUPPORTED_CURVATURE;
+    st.verified = 0;
+    st.iterations = 0;
+    st.objective = std::numeric_limits<double>::quiet_NaN();
+    st.primal_residual = st.stationarity_residual = HUGE_VAL;
+    st.complementarity_residual = st.relative_gap = HUGE_VAL;
+    st.dual_bound = -HUGE_VAL;
 }
 
 // Default SpMV structure of the step kernel when the caller's options do not name one
@@ -329,6 +370,25 @@ public:
         latency_ms_ = ms;
     }
     void inject_admission_oom(int count) { inject_oom_.store(count); }
+    // page-locked slots for the gate results of solves between upload and installation (engine
+    // thread); chunks of kGateChunk slots, kept until the engine closes
+    GateResult* acquire_gate_slot() {
+        if (gate_free_.empty()) {
+            GateResult* chunk = nullptr;
+            if (cudaMallocHost(&chunk, sizeof(GateResult) * kGateChunk) != cudaSuccess) return nullptr;
+            gate_chunks_.push_back(chunk);
+            for (int k = 0; k < kGateChunk; ++k) gate_free_.push_back(chunk + k);
+        }
+        GateResult* g = gate_free_.back();
+        gate_free_.pop_back();
+        return g;
+    }
+    void release_gate_slot(Job& j) {
+        if (j.gate_host) gate_free_.push_back(j.gate_host);
+        j.gate_host = nullptr;
+    }
+    bool gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused, std::string& why);
+    void finish_unsupported(Job* j);  // caller holds mu_
     void set_error(const std::string& e) {
         std::lock_guard<std::mutex> g(err_mu_);
         error_ = e;
@@ -490,7 +550,10 @@ private:
     int64_t n_running_ = 0, peak_resident_ = 0;
     size_t resident_bytes_ = 0;
     double latency_ms_ = 0;
-    std::atomic<int> inject_oom_{0};  // admissions left to fail as out of memory (host-side fault injection)
+    std::atomic<int> inject_oom_{0};
+    static constexpr int kGateChunk = 1024;
+    std::vector<GateResult*> gate_chunks_;
+    std::vector<GateResult*> gate_free_;  // admissions left to fail as out of memory (host-side fault injection)
     double body_ms_ = 0.5;
     double timer_ms_ = 0;
     int64_t timer_kernels_ = 0, timer_launches_ = 0;
@@ -588,6 +651,9 @@ void Engine::shutdown() {
     if (h_stage_) cudaFreeHost(h_stage_);
     if (h_stage_slots_) cudaFreeHost(h_stage_slots_);
     if (h_spans_) cudaFreeHost(h_spans_);
+    for (GateResult* c : gate_chunks_) cudaFreeHost(c);
+    gate_chunks_.clear();
+    gate_free_.clear();
     cudaFree(d_stage_);
     cudaFree(d_stage_slots_);
     cudaFree(d_spans_);
@@ -1210,6 +1276,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.sstep = at<float>(slab, L.sstep);
     R.s = at<double>(slab, L.s);
     R.lprec = at<double>(slab, L.lprec);
+    R.gate = at<GateResult>(slab, L.gate);
     // polish lanes per row: about a quarter of the average row length, a power of two
     auto lanes_for = [](double avg) {
         int lanes = 1;
@@ -1273,6 +1340,15 @@ bool Engine::upload_copy(Job& j, size_t budget) {
 bool Engine::upload_finish(Job& j, std::string& why) {
     InstDev& R = j.rec;
     const int prec = j.opt.precision;
+    // the convexity gate and the Gershgorin bound first: the other admission kernels read L from
+    // its result, and the engine thread reads the result back before it installs the solve
+    j.gate_host = acquire_gate_slot();
+    if (!j.gate_host) {
+        why = "host memory for the convexity gate result";
+        return false;
+    }
+    launch_gate(R, j.n, prec == PREC_MIXED ? static_cast<const double*>(j.tmp) : R.val64, ustream_);
+    cudaMemcpyAsync(j.gate_host, R.gate, sizeof(GateResult), cudaMemcpyDeviceToHost, ustream_);
     if (prec == PREC_MIXED) {
         launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(j.tmp), ustream_);
         launch_precondition(R, j.n, static_cast<const double*>(j.tmp), j.opt.scaling != 2, j.power, ustream_);
@@ -1281,7 +1357,7 @@ bool Engine::upload_finish(Job& j, std::string& why) {
         const double* val = R.val64;
         launch_prepare_instance(R, j.n, j.nnz, val, ustream_);
         if (R.lip_device) {
-            cudaMemcpyAsync(R.lprec, &R.L, sizeof(double), cudaMemcpyHostToDevice, ustream_);
+            cudaMemcpyAsync(R.lprec, &R.gate->lip_bits, sizeof(double), cudaMemcpyDeviceToDevice, ustream_);
             launch_power_lipschitz(R, j.n, val, false, j.power, ustream_);
         }
     }
@@ -1358,10 +1434,7 @@ void Engine::upload_waiting() {
         std::string why;
         const bool copied = upload_copy(*j, kUploadChunk);
         bool ok = true;
-        if (copied) {
-            ok = upload_finish(*j, why);
-            free_inputs(*j);
-        }
+        if (copied) ok = upload_finish(*j, why);
         lk.lock();
         if (copied) {
             uploading_ = nullptr;
@@ -1379,16 +1452,62 @@ void Engine::finish_paused_upload(std::unique_lock<std::mutex>& lk) {
     std::string why;
     upload_copy(*j, static_cast<size_t>(-1));
     const bool ok = upload_finish(*j, why);
-    free_inputs(*j);
     lk.lock();
     uploading_ = nullptr;
     if (ok) uploaded_.push_back(j);
     else fail_admission(j, j->layout.total, why);
 }
 
+// Decides the convexity gate of solves uploaded since the last installation, once their upload
+// stream work is done: the device's Gershgorin bound becomes the solve's L (the FISTA step); an
+// indefinite row, or a Hessian that is not diagonally dominant and fails the host LDL^T test on
+// its CSR (kept for this until now), sends the solve to `refused` (unsupported_curvature).  The
+// inputs are released here.  Engine thread, without mu_.
+bool Engine::gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused, std::string& why) {
+    if (!cuda_ok(cudaEventSynchronize(uev_), why, "admission gate")) return false;
+    std::vector<Job*> keep;
+    keep.reserve(batch.size());
+    for (Job* j : batch) {
+        const GateResult g = *j->gate_host;
+        release_gate_slot(*j);
+        bool convex = g.indefinite == 0;
+        if (convex && g.nondominant) convex = host_gate_convex(j->n, j->rowptr, j->col, j->val);
+        free_inputs(*j);
+        if (!convex) {
+            refused.push_back(j);
+            continue;
+        }
+        double L = 0;
+        std::memcpy(&L, &g.lip_bits, sizeof(double));
+        j->lipschitz = L;
+        j->rec.L = L;
+        j->rec.invL = 1.0 / L;
+        j->rec.invLf = static_cast<float>(1.0 / L);
+        keep.push_back(j);
+    }
+    batch.swap(keep);
+    return true;
+}
+
+// A solve refused by the convexity gate after its upload: its memory goes back and it finishes
+// as unsupported_curvature.  Caller holds mu_.
+void Engine::finish_unsupported(Job* j) {
+    resident_bytes_ -= j->layout.total;
+    if (j->resident) {
+        pending_free_.emplace_back(-1, j->slab);
+        j->slab = nullptr;
+        j->resident = false;
+    }
+    set_unsupported(j->stats);
+    j->state = JOB_DONE;
+    if (j->notify) completed_.push_back(j->id);
+    cv_done_.notify_all();
+}
+
 // A solve whose admission failed: its reserved bytes and any slab go back, it finishes with the
 // CUDA error.  Caller holds mu_.
 void Engine::fail_admission(Job* j, size_t reserved, const std::string& why) {
+    release_gate_slot(*j);
     resident_bytes_ -= reserved;
     if (j->resident) {
         pending_free_.emplace_back(-1, j->slab);
@@ -1803,19 +1922,20 @@ void Engine::loop() {
             lk.unlock();
             std::string why;
             const bool ok = upload(*j, why);
-            free_inputs(*j);
             lk.lock();
             if (ok) uploaded_.push_back(j);
             else fail_admission(j, need, why);
         }
         // install what was uploaded here and during the previous launch
         if (!uploaded_.empty()) {
-            std::vector<Job*> batch;
+            std::vector<Job*> batch, refused;
             batch.swap(uploaded_);
             lk.unlock();
             std::string why;
-            const bool ok = install(batch, why);
+            bool ok = gate_uploaded(batch, refused, why);
+            if (ok && !batch.empty()) ok = install(batch, why);
             lk.lock();
+            for (Job* j : refused) finish_unsupported(j);
             for (Job* j : batch) {
                 if (ok) {
                     j->state = JOB_RUNNING;
@@ -1912,17 +2032,18 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
 }
 
 // One pass over the problem, split over host threads by row ranges: the reference's input checks
-// (validate_linear_problem, src/mps.cpp:47-60, plus CSR sanity), the Gershgorin bound
-// (src/accelerated_qp.cpp:25-26), the positive-diagonal gate (src/qp_admm.cpp:72-78) and
-// infeasible bounds.  Every row checks its own pointers before touching its entries.
+// (validate_linear_problem, src/mps.cpp:47-60, plus CSR sanity: every column index is checked
+// before the upload, since the device uses it as a gather address), the positive-diagonal gate
+// (src/qp_admm.cpp:72-78), infeasible bounds and whether any entry is non-zero (a zero Hessian
+// goes to the reference's LP path).  Every row checks its own pointers before touching its
+// entries.  The convexity gate and the Gershgorin bound are computed on the device at admission
+// (convexity_gate_kernel).
 struct Scan {
     int error = 0;  // 1 row pointers, 2 coefficient/bound, 3 Hessian entry
-    double lipschitz = 0;
+    bool nonzero = false;
     bool diagonal = true;
     bool positive = true;
     bool infeasible = false;
-    bool dominant = true;     // every row: Q_ii >= sum_j!=i |Q_ij| (PSD for a symmetric Q)
-    bool indefinite = false;  // a row with Q_ii < 0, or Q_ii = 0 beside off-diagonal entries
 };
 
 // Destination of the host copy taken during the scan (asynchronous submit), or all null.
@@ -1959,7 +2080,7 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
             return s;
         }
         if (l[i] > u[i]) s.infeasible = true;
-        double abs_sum = 0, d = 0, radius = 0;
+        double d = 0;
         for (int64_t k = a; k < b; ++k) {
             const int32_t cc = col[k];
             const double v = val[k];
@@ -1967,19 +2088,11 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
                 s.error = 3;
                 return s;
             }
-            abs_sum += std::abs(v);
-            if (cc == i) {
-                d += v;
-            } else {
-                s.diagonal = false;
-                radius += std::abs(v);
-            }
+            if (v != 0) s.nonzero = true;
+            if (cc == i) d += v;
+            else s.diagonal = false;
         }
         if (!(d > 0)) s.positive = false;
-        // the diagonal-dominance fast path of check_convex_hessian (src/qp_admm.cpp:30-39)
-        if (d < 0 || (d == 0 && radius > 0)) s.indefinite = true;
-        if (d < radius) s.dominant = false;
-        s.lipschitz = std::max(s.lipschitz, abs_sum);
         // rows [copied, i] validated: their nonzeros lie in [rowptr[copied], rowptr[i + 1]] within [0, nnz]
         if (dst.rowptr && (b - rowptr[copied] >= 16384 || i + 1 - copied >= 4096 || i + 1 == r1)) copy_rows(i + 1);
     }
@@ -1990,7 +2103,7 @@ Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* 
                   const double* c, const double* l, const double* u, const InputCopy& dst) {
     // pieces of about 128K nonzeros (by the average row), at least 2048 rows; below 256K
     // nonzeros the calling thread scans alone.  The result does not depend on the pieces: the
-    // first error by row, the largest row sum, and/or of the flags.
+    // first error by row, and/or of the flags.
     const double avg = static_cast<double>(nnz) / static_cast<double>(n) + 1.0;
     const int64_t rows = std::max<int64_t>(2048, static_cast<int64_t>(131072.0 / avg));
     const int64_t pieces = nnz < 262144 ? 1 : (n + rows - 1) / rows;
@@ -2002,12 +2115,10 @@ Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* 
     Scan s;
     for (const Scan& p : part) {
         if (p.error && !s.error) s.error = p.error;
-        s.lipschitz = std::max(s.lipschitz, p.lipschitz);
+        s.nonzero = s.nonzero || p.nonzero;
         s.diagonal = s.diagonal && p.diagonal;
         s.positive = s.positive && p.positive;
         s.infeasible = s.infeasible || p.infeasible;
-        s.dominant = s.dominant && p.dominant;
-        s.indefinite = s.indefinite || p.indefinite;
     }
     return s;
 }
@@ -2053,37 +2164,21 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
         return BQP_ERR_INVALID;
     }
     const double t_scan = host_seconds();
-    // check_convex_hessian comes first, as in solve_accelerated_box (src/accelerated_qp.cpp:19):
-    // diagonal dominance decides in the scan; otherwise the sparse LDL^T of bqp_check_convex on the
-    // lower triangle of the CSR
-    bool convex = !scan.indefinite;
-    if (convex && !scan.dominant) {
-        std::vector<int64_t> tr, tc;
-        std::vector<double> tv;
-        for (int64_t i = 0; i < n; ++i)
-            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
-                if (col[k] <= i) {
-                    tr.push_back(i);
-                    tc.push_back(col[k]);
-                    tv.push_back(val[k]);
-                }
-        convex = bqp_check_convex(n, static_cast<int64_t>(tr.size()), tr.data(), tc.data(), tv.data(), 0) == 1;
-    }
-    if (!convex) {
+    // check_convex_hessian comes first, as in solve_accelerated_box (src/accelerated_qp.cpp:19).
+    // The device decides it at admission (convexity_gate_kernel, with the host LDL^T only where diagonal
+    // dominance fails).  A solve with infeasible bounds finishes here without an admission, so it
+    // takes the gate on the host first: a non-convex Hessian reports unsupported_curvature before
+    // infeasible_bounds, as in the reference.
+    if (scan.infeasible && !bqp::host_gate_convex(n, rowptr, col, val)) {
         j->n = n;
         j->nnz = nnz;
         j->opt = o;
         j->state = bqp::JOB_DONE;
-        j->stats.status = BQP_STATUS_UNSUPPORTED_CURVATURE;
-        j->stats.objective = std::numeric_limits<double>::quiet_NaN();
-        j->stats.primal_residual = j->stats.stationarity_residual = HUGE_VAL;
-        j->stats.complementarity_residual = j->stats.relative_gap = HUGE_VAL;
-        j->stats.dual_bound = -HUGE_VAL;
+        bqp::set_unsupported(j->stats);
         *out = j.release();
         return BQP_OK;
     }
-    const double lipschitz = scan.lipschitz;
-    if (lipschitz == 0) {
+    if (!scan.nonzero) {  // the Gershgorin bound is zero (src/accelerated_qp.cpp:27-28)
         why = "Zero-Hessian models use the CPU LP path";
         return BQP_ERR_UNSUPPORTED;
     }
@@ -2099,7 +2194,6 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     const bool dear_steps = o.precision == BQP_PRECISION_MIXED && nnz >= 8 * n && nnz >= 4000000;
     if (j->opt.check_interval == 0) j->opt.check_interval = dear_steps ? 8 : 25;
     if (j->opt.polish_switch == 0) j->opt.polish_switch = j->opt.check_interval <= 10 ? 0.1 : 3e-2;
-    j->lipschitz = lipschitz;
     if (o.diagonal_gate >= 0) j->diag_gate = o.diagonal_gate ? 1 : 0;
     else j->diag_gate = (scan.diagonal && scan.positive) ? 1 : 0;
     if (scan.infeasible) {

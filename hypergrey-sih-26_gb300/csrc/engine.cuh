@@ -82,6 +82,15 @@ struct __align__(16) Partial {
     int32_t pad;
 };
 
+// The convexity gate of an instance, computed on the device at admission from the uploaded full
+// CSR (convexity_gate_kernel): the fast path of check_convex_hessian (src/qp_admm.cpp:30-39) and the
+// Gershgorin bound of src/accelerated_qp.cpp:25-26.  Flags are 0/1, OR-reduced over the rows.
+struct __align__(16) GateResult {
+    unsigned long long lip_bits;  // max_i sum_k |Q_ik|, row sums in column order, as double bits
+    int32_t indefinite;           // a row with Q_ii < 0, or Q_ii = 0 beside an off-diagonal entry
+    int32_t nondominant;          // a row with Q_ii < sum_{j != i} |Q_ij| (diagonal dominance fails)
+};
+
 struct __align__(16) InstDev {
     // problem
     const int32_t* rowptr;
@@ -133,6 +142,7 @@ struct __align__(16) InstDev {
     int32_t moved[2];      // mixed: a variable entered or left a bound in the chunk's last two steps
     float* sstep;          // mixed, preconditioned: per-row step 1 / (L' Q_ii) (null: scalar 1/L)
     double* lprec;         // L' of the preconditioned mixed engine, or the power estimate of L (device-computed at admission)
+    GateResult* gate;      // the admission's convexity gate and Gershgorin bound (convexity_gate_kernel)
     int32_t lanes_res;     // polish: lanes per row of the residual pass (full rows)
     int32_t lanes_cg;      // polish: lanes per row of the CG products (free-free rows)
     int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)

@@ -1671,6 +1671,11 @@ __global__ void __launch_bounds__(kBlock) rearm_kernel(View v, const InstDev* __
     }
 }
 
+// The Gershgorin bound the gate found (admission kernels that run after it read L from there).
+__device__ __forceinline__ double gate_lipschitz(const InstDev& I) {
+    return __longlong_as_double(static_cast<long long>(I.gate->lip_bits));
+}
+
 // Derives the device-side forms of an uploaded instance: FP64 diagonal (Jacobi preconditioner and
 // the diagonal dual-gap gate) and, for mixed precision, hi/lo FP32 values (val ~= hi + lo), the
 // FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
@@ -1727,7 +1732,7 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
             if (I.precision == PREC_MIXED) {
                 const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
                 // preconditioner scale v_r, kept in s (free until the polish) for the step set-up
-                I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(I.L);
+                I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(gate_lipschitz(I));
                 const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
                 const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
                 const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
@@ -1743,6 +1748,43 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const
             const_cast<float*>(I.vhi)[k] = hi;
             const_cast<float*>(I.vlo)[k] = __double2float_rn(x - static_cast<double>(hi));
         }
+    }
+}
+
+// ---- convexity gate and Gershgorin bound at admission ---------------------------------------------
+// One thread per row, the row's entries in column order (the order of the reference's Gershgorin
+// sum, src/accelerated_qp.cpp:25-26, so L comes out bit for bit): sum |Q_ik|, the diagonal Q_ii
+// (duplicate diagonal entries summed) and the off-diagonal radius sum_{j != i} |Q_ij|; a row with
+// Q_ii < 0, or Q_ii = 0 beside off-diagonal entries, is indefinite, and one with Q_ii < radius
+// breaks diagonal dominance (check_convex_hessian, src/qp_admm.cpp:30-39).  Warp reductions, then
+// one atomic per warp: the maximum as the bit pattern of a non-negative double, the flags as ORs.
+__global__ void __launch_bounds__(kBlock) convexity_gate_kernel(const int32_t* __restrict__ rowptr,
+                                                      const int32_t* __restrict__ col,
+                                                      const double* __restrict__ val, int n, GateResult* out) {
+    unsigned long long best = 0;
+    int indefinite = 0, nondominant = 0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
+        double abs_sum = 0.0, d = 0.0, radius = 0.0;
+        for (int k = ks; k < ke; ++k) {
+            const double v = __ldg(val + k);
+            abs_sum += fabs(v);
+            if (__ldg(col + k) == r) d += v;
+            else radius += fabs(v);
+        }
+        best = umax64(best, dbits(abs_sum));
+        if (d < 0.0 || (d == 0.0 && radius > 0.0)) indefinite = 1;
+        if (d < radius) nondominant = 1;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = umax64(best, shfl_xor(best, o));
+    indefinite = __reduce_or_sync(0xffffffffu, indefinite);
+    nondominant = __reduce_or_sync(0xffffffffu, nondominant);
+    if ((threadIdx.x & 31) == 0) {
+        if (best) atomicMax(&out->lip_bits, best);
+        if (indefinite) atomicOr(&out->indefinite, 1);
+        if (nondominant) atomicOr(&out->nondominant, 1);
     }
 }
 
@@ -1779,7 +1821,7 @@ __global__ void __launch_bounds__(kBlock) precond_step_kernel(InstDev I, int n, 
     const int stride = gridDim.x * blockDim.x;
     const double lp = (scaled || I.lip_device) ? *I.lprec : 0.0;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        double s = (I.lip_device && lp > 0) ? 1.0 / lp : I.invL;
+        double s = (I.lip_device && lp > 0) ? 1.0 / lp : 1.0 / gate_lipschitz(I);
         if (scaled && lp > 0) {
             const double v = precond_v(I, r);
             s = v * v / lp;
@@ -2195,7 +2237,7 @@ void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool 
         else precond_bound_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni, val);
     }
     if (rec.lip_device) {
-        if (!scaled) cudaMemcpyAsync(rec.lprec, &rec.L, sizeof(double), cudaMemcpyHostToDevice, s);
+        if (!scaled) cudaMemcpyAsync(rec.lprec, &rec.gate->lip_bits, sizeof(double), cudaMemcpyDeviceToDevice, s);
         launch_power_lipschitz(rec, n, val, scaled, power_scratch, s);
     }
     precond_step_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n), scaled ? 1 : 0);
@@ -2230,6 +2272,14 @@ void launch_power_lipschitz(const InstDev& rec, int64_t n, const double* val, bo
         lanczos_product_kernel<<<grid, kBlock, 0, s>>>(rec, ni, val, scaled ? 1 : 0, w, vk, z, partial, st, k);
         lanczos_update_kernel<<<grid, kBlock, 0, s>>>(rec, ni, z, vk, vprev, w, partial, st, k);
     }
+}
+
+void launch_gate(const InstDev& rec, int64_t n, const double* val, cudaStream_t s) {
+    cudaMemsetAsync(rec.gate, 0, sizeof(GateResult), s);
+    int64_t grid = (n + kBlock - 1) / kBlock;
+    if (grid > 152 * 8) grid = 152 * 8;
+    if (grid < 1) grid = 1;
+    convexity_gate_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec.rowptr, rec.col, val, static_cast<int>(n), rec.gate);
 }
 
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {

@@ -34,6 +34,9 @@ void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, c
 // Host-driven variants of the control kernels (no conditional handles).
 void launch_gate_plain(const View& v, int steps, cudaStream_t s);
 void launch_control_plain(const View& v, int steps, cudaStream_t s);
+// Admission, first kernel: the convexity gate and Gershgorin bound of the uploaded full CSR
+// (FP64 values `val`) into *rec.gate (cleared first).  The later admission kernels read L there.
+void launch_gate(const InstDev& rec, int64_t n, const double* val, cudaStream_t s);
 // Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
 // The record is passed by value: the instance is installed in its slot later, between graph launches.
 void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
