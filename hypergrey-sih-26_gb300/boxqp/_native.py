@@ -95,6 +95,8 @@ PROTOTYPES = {
                                  c_double, c_double, c_int32, POINTER(Stats)]),
     'bqp_check_device_noalloc': (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_double, c_double, c_int32, POINTER(Stats)]),
+    'bqp_gate_device': (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, POINTER(c_double),
+                                POINTER(c_int32), POINTER(c_int32)]),
     'bqp_csr_from_lower': (c_int, [c_int64, c_int64, _I64P, _I64P, _F64P, c_double, _I32P, _I32P, _F64P, _I64P]),
     'bqp_check_convex': (c_int, [c_int64, c_int64, _I64P, _I64P, _F64P, c_int32]),
     'bqp_gershgorin': (c_double, [c_int64, _I32P, _F64P]),

@@ -93,6 +93,12 @@ def check_options(tolerance, precision, time_limit):
         raise HttpError(422, 'precision must be mixed, fp64 or fp64_exact')
 
 
+def _unsupported(exc):
+    """Reply for a model the box engine does not take (a zero Hessian goes to the reference's CPU
+    LP path, src/accelerated_qp.cpp:27-28)."""
+    return {'engine': 'gb300', 'status': 'unsupported', 'message': str(exc)[:300], 'objective': None, 'primal': []}
+
+
 async def solve_arrays(rowptr, col, val, c, lower, upper, tolerance=1e-6, precision='mixed', time_limit=20.0,
                        return_primal=True):
     """One box QP through the request loop; returns the reply record."""
@@ -108,15 +114,22 @@ async def solve_arrays(rowptr, col, val, c, lower, upper, tolerance=1e-6, precis
     except EngineError as exc:
         if exc.code == 4:  # BQP_ERR_ADMISSION: can never fit under the loop's device-memory cap
             raise HttpError(413, 'request exceeds the device-memory cap: ' + str(exc)[:200])
+        if exc.code == 7:  # BQP_ERR_UNSUPPORTED: a zero Hessian (the reference's CPU LP path)
+            return _unsupported(exc)
         raise
     try:
         r = await asyncio.wait_for(asyncio.wrap_future(fut), timeout=time_limit + 5.0)
     except asyncio.TimeoutError:
         return {'engine': 'gb300', 'status': 'time_limit', 'message': 'no result within the time limit',
                 'objective': None, 'primal': []}
+    except ValueError as exc:  # entries the admission pass on the device rejected
+        return json_safe({'engine': 'gb300', 'status': 'input_rejected', 'message': str(exc), 'objective': None,
+                          'primal': []})
     except EngineError as exc:
         if exc.code == 4:  # refused at admission: it can never fit under the loop's memory cap
             raise HttpError(413, 'request exceeds the device-memory cap: ' + str(exc)[:200])
+        if exc.code == 7:  # a zero Hessian, found by the admission pass
+            return _unsupported(exc)
         return {'engine': 'gb300', 'status': 'engine_error', 'message': str(exc)[:300], 'objective': None,
                 'primal': []}
     except Exception as exc:

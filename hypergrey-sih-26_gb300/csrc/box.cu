@@ -256,6 +256,38 @@ int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, c
     return BQP_OK;
 }
 
+int bqp_gate_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val, double* d_diag,
+                    double* lipschitz, int32_t* indefinite, int32_t* nondominant) {
+    if (n <= 0 || n > 2000000000LL || !d_rowptr || !d_col || !d_val || !lipschitz || !indefinite || !nondominant) {
+        g_box_error = "bqp_gate_device: invalid argument (n must be in 1..2e9, the CSR device pointers and the "
+                      "three results non-null)";
+        return BQP_ERR_INVALID;
+    }
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return BQP_ERR_CUDA;
+    bqp::GateResult* out = nullptr;
+    if (cudaMalloc(&out, sizeof(bqp::GateResult)) != cudaSuccess) {
+        cudaStreamDestroy(s);
+        g_box_error = "bqp_gate_device: device memory for the result";
+        return BQP_ERR_NO_MEMORY;
+    }
+    bqp::GateResult host{};
+    bqp::launch_gate_raw(n, d_rowptr, d_col, d_val, out, d_diag, nullptr, nullptr, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host, out, sizeof(host), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(out);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        g_box_error = std::string("CUDA: ") + cudaGetErrorString(e);
+        return BQP_ERR_CUDA;
+    }
+    std::memcpy(lipschitz, &host.lip_bits, sizeof(double));
+    *indefinite = host.indefinite;
+    *nondominant = host.nondominant;
+    return BQP_OK;
+}
+
 int bqp_check_device_noalloc(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
                              const double* d_x, const double* d_c, const double* d_lower, const double* d_upper,
                              double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats) {

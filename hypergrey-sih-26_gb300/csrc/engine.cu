@@ -193,7 +193,7 @@ struct Job {
     const double* l = nullptr;
     const double* u = nullptr;
     double lipschitz = 0;
-    int diag_gate = 0;
+    int diag_gate = 0;  // -1: decided by the admission gate (a diagonal Hessian with a positive diagonal)
     int variant = 0;
     std::vector<Tile> tiles;  // local tiles (inst field filled at admission)
     int state = JOB_QUEUED;
@@ -388,7 +388,7 @@ public:
         j.gate_host = nullptr;
     }
     bool gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused, std::string& why);
-    void finish_unsupported(Job* j);  // caller holds mu_
+    void finish_refused(Job* j);  // caller holds mu_
     void set_error(const std::string& e) {
         std::lock_guard<std::mutex> g(err_mu_);
         error_ = e;
@@ -492,6 +492,11 @@ private:
     std::vector<Job*> uploaded_;       // uploaded, not yet installed (engine thread only)
     Job* uploading_ = nullptr;         // upload paused when a launch ended (engine thread, mu_)
     static constexpr size_t kUploadChunk = size_t(32) << 20;  // bytes issued between launch tests
+    // Between launches the engine thread uploads queued solves itself only up to this many input
+    // bytes (always at least one solve when the device would otherwise idle); the rest upload
+    // during the next launch, so a stream of large solves overlaps each upload with the
+    // previous solve instead of idling the device for the whole queue's copies.
+    static constexpr size_t kSyncUploadBudget = size_t(64) << 20;
     bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
     double t_launch_done_ = 0;         // host time of that callback (BOXQP_PROFILE: gap to the next launch)
     cudaMemPool_t pool_ = nullptr;
@@ -1287,7 +1292,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.lanes_res = lanes_for(avg_row);
     R.lanes_cg = lanes_for(0.5 * avg_row);
     R.n = static_cast<int32_t>(j.n);
-    R.diag_gate = j.diag_gate;
+    R.diag_gate = j.diag_gate > 0 ? 1 : 0;
     R.precision = prec;
     R.L = j.lipschitz;
     R.invL = 1.0 / j.lipschitz;
@@ -1350,12 +1355,12 @@ bool Engine::upload_finish(Job& j, std::string& why) {
     launch_gate(R, j.n, prec == PREC_MIXED ? static_cast<const double*>(j.tmp) : R.val64, ustream_);
     cudaMemcpyAsync(j.gate_host, R.gate, sizeof(GateResult), cudaMemcpyDeviceToHost, ustream_);
     if (prec == PREC_MIXED) {
-        launch_prepare_instance(R, j.n, j.nnz, static_cast<const double*>(j.tmp), ustream_);
+        launch_prepare_instance(R, j.n, ustream_);
         launch_precondition(R, j.n, static_cast<const double*>(j.tmp), j.opt.scaling != 2, j.power, ustream_);
         cudaFreeAsync(j.tmp, ustream_);
     } else {
         const double* val = R.val64;
-        launch_prepare_instance(R, j.n, j.nnz, val, ustream_);
+        launch_prepare_instance(R, j.n, ustream_);
         if (R.lip_device) {
             cudaMemcpyAsync(R.lprec, &R.gate->lip_bits, sizeof(double), cudaMemcpyDeviceToDevice, ustream_);
             launch_power_lipschitz(R, j.n, val, false, j.power, ustream_);
@@ -1470,6 +1475,15 @@ bool Engine::gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused,
     for (Job* j : batch) {
         const GateResult g = *j->gate_host;
         release_gate_slot(*j);
+        // the order of solve_accelerated_box (src/accelerated_qp.cpp:19-28): check_convex_hessian
+        // rejects invalid entries, then decides convexity; then a zero Hessian is refused
+        if (g.flags & kGateInvalid) {
+            free_inputs(*j);
+            j->error = BQP_ERR_INVALID;
+            j->error_text = "Invalid Hessian";
+            refused.push_back(j);
+            continue;
+        }
         bool convex = g.indefinite == 0;
         if (convex && g.nondominant) convex = host_gate_convex(j->n, j->rowptr, j->col, j->val);
         free_inputs(*j);
@@ -1477,6 +1491,13 @@ bool Engine::gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused,
             refused.push_back(j);
             continue;
         }
+        if (!(g.flags & kGateNonzero)) {  // the Gershgorin bound is zero
+            j->error = BQP_ERR_UNSUPPORTED;
+            j->error_text = "Zero-Hessian models use the CPU LP path";
+            refused.push_back(j);
+            continue;
+        }
+        if (j->diag_gate < 0) j->rec.diag_gate = (g.flags & (kGateOffDiagonal | kGateNonPositive)) ? 0 : 1;
         double L = 0;
         std::memcpy(&L, &g.lip_bits, sizeof(double));
         j->lipschitz = L;
@@ -1489,16 +1510,18 @@ bool Engine::gate_uploaded(std::vector<Job*>& batch, std::vector<Job*>& refused,
     return true;
 }
 
-// A solve refused by the convexity gate after its upload: its memory goes back and it finishes
-// as unsupported_curvature.  Caller holds mu_.
-void Engine::finish_unsupported(Job* j) {
+// A solve refused at the gate after its upload: its memory goes back and it finishes as
+// unsupported_curvature, or with the error the gate found (invalid entries, zero Hessian).
+// Caller holds mu_.
+void Engine::finish_refused(Job* j) {
     resident_bytes_ -= j->layout.total;
     if (j->resident) {
         pending_free_.emplace_back(-1, j->slab);
         j->slab = nullptr;
         j->resident = false;
     }
-    set_unsupported(j->stats);
+    if (j->error != BQP_OK) set_error(j->error_text);
+    else set_unsupported(j->stats);
     j->state = JOB_DONE;
     if (j->notify) completed_.push_back(j->id);
     cv_done_.notify_all();
@@ -1870,6 +1893,7 @@ void Engine::loop() {
         // admission: FIFO while the head fits under the cap; consecutive re-arms of resident
         // solves go together in one upload and one kernel
         bool admitted = false;
+        size_t sync_bytes = 0;  // inputs uploaded by this thread since the last launch
         while (!queue_.empty()) {
             Job* j = queue_.front();
             if (j->resolve) {
@@ -1916,6 +1940,10 @@ void Engine::loop() {
                 }
                 break;
             }
+            const size_t input = static_cast<size_t>(j->nnz) * 12 + static_cast<size_t>(j->n) * 28 + 4;
+            if ((sync_bytes > 0 || n_running_ > 0 || !uploaded_.empty()) && sync_bytes + input > kSyncUploadBudget)
+                break;  // uploads during the next launch (upload_waiting)
+            sync_bytes += input;
             queue_.pop_front();
             j->state = JOB_ADMITTING;
             resident_bytes_ += need;
@@ -1935,7 +1963,7 @@ void Engine::loop() {
             bool ok = gate_uploaded(batch, refused, why);
             if (ok && !batch.empty()) ok = install(batch, why);
             lk.lock();
-            for (Job* j : refused) finish_unsupported(j);
+            for (Job* j : refused) finish_refused(j);
             for (Job* j : batch) {
                 if (ok) {
                     j->state = JOB_RUNNING;
@@ -2038,11 +2066,14 @@ int validate_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_
 // goes to the reference's LP path).  Every row checks its own pointers before touching its
 // entries.  The convexity gate and the Gershgorin bound are computed on the device at admission
 // (convexity_gate_kernel).
+// The submission's host scan reads the rows: row pointers, costs and bounds (validate_linear_problem,
+// src/mps.cpp:47, comes first in solve_accelerated_box).  The Hessian's entries (column range,
+// finite values, a zero Hessian, the diagonal pattern) are checked by the admission pass on the
+// device, which reads them anyway; only a solve that finishes at submission (infeasible bounds)
+// has them checked here (scan_hessian).
 struct Scan {
     int error = 0;  // 1 row pointers, 2 coefficient/bound, 3 Hessian entry
     bool nonzero = false;
-    bool diagonal = true;
-    bool positive = true;
     bool infeasible = false;
 };
 
@@ -2080,19 +2111,6 @@ Scan scan_rows(int64_t r0, int64_t r1, int64_t n, int64_t nnz, const int32_t* ro
             return s;
         }
         if (l[i] > u[i]) s.infeasible = true;
-        double d = 0;
-        for (int64_t k = a; k < b; ++k) {
-            const int32_t cc = col[k];
-            const double v = val[k];
-            if (cc < 0 || cc >= n || !std::isfinite(v)) {
-                s.error = 3;
-                return s;
-            }
-            if (v != 0) s.nonzero = true;
-            if (cc == i) d += v;
-            else s.diagonal = false;
-        }
-        if (!(d > 0)) s.positive = false;
         // rows [copied, i] validated: their nonzeros lie in [rowptr[copied], rowptr[i + 1]] within [0, nnz]
         if (dst.rowptr && (b - rowptr[copied] >= 16384 || i + 1 - copied >= 4096 || i + 1 == r1)) copy_rows(i + 1);
     }
@@ -2115,10 +2133,32 @@ Scan scan_problem(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* 
     Scan s;
     for (const Scan& p : part) {
         if (p.error && !s.error) s.error = p.error;
-        s.nonzero = s.nonzero || p.nonzero;
-        s.diagonal = s.diagonal && p.diagonal;
-        s.positive = s.positive && p.positive;
         s.infeasible = s.infeasible || p.infeasible;
+    }
+    return s;
+}
+
+// The Hessian entries' checks of the admission pass, on the host (rows already validated):
+// error 3 for a column out of range or a value not finite, and whether some value is nonzero.
+Scan scan_hessian(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val) {
+    const int64_t nnz = rowptr[n];
+    const int64_t pieces = nnz < 262144 ? 1 : std::min<int64_t>(n, (nnz + 131071) / 131072);
+    std::vector<Scan> part(static_cast<size_t>(pieces));
+    bqp::WorkerPool::get().run(pieces, [&](int64_t p) {
+        const int64_t r0 = n * p / pieces, r1 = n * (p + 1) / pieces;
+        Scan& s = part[static_cast<size_t>(p)];
+        for (int64_t k = rowptr[r0]; k < rowptr[r1]; ++k) {
+            if (col[k] < 0 || col[k] >= n || !std::isfinite(val[k])) {
+                s.error = 3;
+                return;
+            }
+            if (val[k] != 0) s.nonzero = true;
+        }
+    });
+    Scan s;
+    for (const Scan& p : part) {
+        if (p.error && !s.error) s.error = p.error;
+        s.nonzero = s.nonzero || p.nonzero;
     }
     return s;
 }
@@ -2159,28 +2199,39 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     }
     const Scan scan = scan_problem(n, nnz, rowptr, col, val, c, l, u, dst);
     if (scan.error) {
-        why = scan.error == 1 ? "Invalid CSR row pointers"
-                              : scan.error == 2 ? "Invalid variable coefficient or bound" : "Invalid Hessian";
+        why = scan.error == 1 ? "Invalid CSR row pointers" : "Invalid variable coefficient or bound";
         return BQP_ERR_INVALID;
     }
     const double t_scan = host_seconds();
-    // check_convex_hessian comes first, as in solve_accelerated_box (src/accelerated_qp.cpp:19).
-    // The device decides it at admission (convexity_gate_kernel, with the host LDL^T only where diagonal
-    // dominance fails).  A solve with infeasible bounds finishes here without an admission, so it
-    // takes the gate on the host first: a non-convex Hessian reports unsupported_curvature before
-    // infeasible_bounds, as in the reference.
-    if (scan.infeasible && !bqp::host_gate_convex(n, rowptr, col, val)) {
-        j->n = n;
-        j->nnz = nnz;
-        j->opt = o;
-        j->state = bqp::JOB_DONE;
-        bqp::set_unsupported(j->stats);
-        *out = j.release();
-        return BQP_OK;
-    }
-    if (!scan.nonzero) {  // the Gershgorin bound is zero (src/accelerated_qp.cpp:27-28)
+    if (nnz == 0) {  // the Gershgorin bound is zero (src/accelerated_qp.cpp:27-28)
         why = "Zero-Hessian models use the CPU LP path";
         return BQP_ERR_UNSUPPORTED;
+    }
+    // check_convex_hessian comes first, as in solve_accelerated_box (src/accelerated_qp.cpp:19).
+    // The device decides it at admission (convexity_gate_kernel, with the host LDL^T only where
+    // diagonal dominance fails), with the entries' validity and the zero-Hessian test.  A solve
+    // with infeasible bounds finishes here without an admission, so it takes those on the host:
+    // invalid entries, then a non-convex Hessian (unsupported_curvature), then a zero Hessian come
+    // before infeasible_bounds, as in the reference.
+    if (scan.infeasible) {
+        const Scan hs = scan_hessian(n, rowptr, col, val);
+        if (hs.error) {
+            why = "Invalid Hessian";
+            return BQP_ERR_INVALID;
+        }
+        if (!bqp::host_gate_convex(n, rowptr, col, val)) {
+            j->n = n;
+            j->nnz = nnz;
+            j->opt = o;
+            j->state = bqp::JOB_DONE;
+            bqp::set_unsupported(j->stats);
+            *out = j.release();
+            return BQP_OK;
+        }
+        if (!hs.nonzero) {
+            why = "Zero-Hessian models use the CPU LP path";
+            return BQP_ERR_UNSUPPORTED;
+        }
     }
     j->n = n;
     j->nnz = nnz;
@@ -2194,8 +2245,7 @@ int make_job(int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col, 
     const bool dear_steps = o.precision == BQP_PRECISION_MIXED && nnz >= 8 * n && nnz >= 4000000;
     if (j->opt.check_interval == 0) j->opt.check_interval = dear_steps ? 8 : 25;
     if (j->opt.polish_switch == 0) j->opt.polish_switch = j->opt.check_interval <= 10 ? 0.1 : 3e-2;
-    if (o.diagonal_gate >= 0) j->diag_gate = o.diagonal_gate ? 1 : 0;
-    else j->diag_gate = (scan.diagonal && scan.positive) ? 1 : 0;
+    j->diag_gate = o.diagonal_gate >= 0 ? (o.diagonal_gate ? 1 : 0) : -1;
     if (scan.infeasible) {
         j->state = bqp::JOB_DONE;
         j->stats.status = BQP_STATUS_INFEASIBLE_BOUNDS;

@@ -89,7 +89,14 @@ struct __align__(16) GateResult {
     unsigned long long lip_bits;  // max_i sum_k |Q_ik|, row sums in column order, as double bits
     int32_t indefinite;           // a row with Q_ii < 0, or Q_ii = 0 beside an off-diagonal entry
     int32_t nondominant;          // a row with Q_ii < sum_{j != i} |Q_ij| (diagonal dominance fails)
+    unsigned long long floor_bits;  // during the pass: the largest lower bound of a row sum seen yet
+    int32_t flags;                  // kGate* bits below
+    int32_t pad;
 };
+constexpr int32_t kGateInvalid = 1;      // an entry whose column is out of range or whose value is not finite
+constexpr int32_t kGateNonzero = 2;      // some value is not zero
+constexpr int32_t kGateOffDiagonal = 4;  // some nonzero value lies off the diagonal
+constexpr int32_t kGateNonPositive = 8;  // some row has Q_ii <= 0 (or no diagonal entry)
 
 struct __align__(16) InstDev {
     // problem

@@ -1,0 +1,91 @@
+// FP64 -> FP32 conversions in integer arithmetic on the IEEE 754 bit patterns, for the admission
+// pass over the nonzeros.  GB300 issues FP64 instructions (conversions included) at 1/64 of the
+// FP32 rate, so a per-nonzero F2F or DADD costs about 30 us on 15M nonzeros; these forms keep
+// that pass on the integer and FP32 pipes.  Host and device share them, so the host tests check
+// them against the C library's conversions.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+
+#ifdef __CUDACC__
+#define BQP_HD __host__ __device__ __forceinline__
+#else
+#define BQP_HD inline
+#endif
+
+namespace bqp {
+
+BQP_HD uint64_t bits64(double v) {
+    uint64_t b;
+    memcpy(&b, &v, sizeof b);
+    return b;
+}
+
+// hi = RN32(v) and lo = RN32(v - hi), the FP32 pair with v ~= hi + lo (round to nearest, ties to
+// even, as an FP32 conversion in the default mode).  Exact in integer arithmetic where both parts
+// are normal floats and hi is finite: biased exponent 949..1150 of v (2^-74 <= |v| < 2^128) and
+// hi below the overflow threshold.  Returns false outside that window (zero included): the caller
+// converts with FP64 instructions there.
+//   hi: the 52-bit fraction rounded to 23 bits by adding 2^28 - 1 plus the lowest kept bit and
+//       truncating; a carry moves into the exponent field, as the rounding of the value does.
+//   lo: |v| - |hi| is an integer D (|D| <= 2^28) of units 2^(e-1075) (e the biased exponent of v;
+//       the bit patterns of two doubles of one sign differ by the count of steps between them,
+//       and every step lies in v's binade), so lo = sign(v) sign(D) RN24(|D|) 2^(e-1075).
+BQP_HD bool split_hilo_bits(uint64_t bits, uint32_t& hi, uint32_t& lo) {
+    const uint64_t mag = bits & 0x7fffffffffffffffull;
+    const uint32_t sign = static_cast<uint32_t>(bits >> 32) & 0x80000000u;
+    const int e = static_cast<int>(mag >> 52);
+    if (e < 949 || e > 1150) return false;
+    const uint64_t r = (mag + 0x0fffffffull + ((mag >> 29) & 1ull)) & ~0x1fffffffull;  // |hi| as FP64 bits
+    const uint32_t h = static_cast<uint32_t>(r >> 29) - (896u << 23);                     // rebias 1023 -> 127
+    if ((h & 0x7f800000u) == 0x7f800000u) return false;                                 // rounds to infinity
+    hi = h | sign;
+    const int64_t D = static_cast<int64_t>(mag - r);
+    if (D == 0) {
+        lo = 0;  // v - hi = +0 in round-to-nearest
+        return true;
+    }
+    uint32_t m = static_cast<uint32_t>(D < 0 ? -D : D);
+#ifdef __CUDA_ARCH__
+    const int p = 31 - __clz(m);  // leading bit, p <= 28
+#else
+    const int p = 31 - __builtin_clz(m);
+#endif
+    uint32_t mant;
+    if (p <= 23) {
+        mant = m << (23 - p);
+    } else {
+        const int sh = p - 23;
+        mant = (m + ((1u << (sh - 1)) - 1u) + ((m >> sh) & 1u)) >> sh;  // in [2^23, 2^24]
+    }
+    // biased exponent p + e - 1075 + 127 >= 1; mant = 2^24 carries into the exponent
+    lo = ((static_cast<uint32_t>(p + e - 948) << 23) + (mant - 0x00800000u)) | (sign ^ (D < 0 ? 0x80000000u : 0u));
+    return true;
+}
+
+// FP32 bounds of a magnitude given by its FP64 bits: rd <= |v| <= ru.  Inside the normal FP32
+// range they are the nearest floats below and above (truncation, plus one unit when a dropped
+// bit is set); below it 0 and 2^-126, above it FLT_MAX and infinity.
+BQP_HD void abs_bounds_bits(uint64_t mag, uint32_t& rd, uint32_t& ru) {
+    const int e = static_cast<int>(mag >> 52);
+    if (e >= 897 && e <= 1150) {
+        rd = static_cast<uint32_t>(mag >> 29) - (896u << 23);
+        ru = rd + ((mag & 0x1fffffffull) != 0 ? 1u : 0u);
+    } else if (e < 897) {
+        rd = 0;
+        ru = mag ? 0x00800000u : 0u;
+    } else {
+        rd = 0x7f7fffffu;
+        ru = 0x7f800000u;
+    }
+}
+
+// FP64 bits of a non-negative float that is 0, normal or infinite (the FP32 sums of
+// abs_bounds_bits values are nothing else).
+BQP_HD uint64_t widen_bits(uint32_t f) {
+    if (f == 0) return 0;
+    if (f >= 0x7f800000u) return 0x7ff0000000000000ull;
+    return (static_cast<uint64_t>(f) + (896ull << 23)) << 29;
+}
+
+}  // namespace bqp

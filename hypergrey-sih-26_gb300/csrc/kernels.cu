@@ -19,6 +19,7 @@
 // FP64 epilogues and reductions run on full warps (an FP64 warp instruction costs the same
 // whatever its active lanes).
 #include "kernels.cuh"
+#include "fpbits.h"
 
 #include <atomic>
 #include <cmath>
@@ -1676,115 +1677,194 @@ __device__ __forceinline__ double gate_lipschitz(const InstDev& I) {
     return __longlong_as_double(static_cast<long long>(I.gate->lip_bits));
 }
 
-// Derives the device-side forms of an uploaded instance: FP64 diagonal (Jacobi preconditioner and
-// the diagonal dual-gap gate) and, for mixed precision, hi/lo FP32 values (val ~= hi + lo), the
-// FP32 cost and FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u,
-// so FP32 iterates never leave the FP64 box).
-// A warp takes 32 consecutive rows; in each of LANES passes its groups of LANES lanes search one
-// row each (consecutive entries, so the column loads of a group coalesce) for the diagonal by
-// integer compares alone, and a shuffle hands every row's diagonal to its own lane, so the FP64
-// epilogue (1/d, 1/sqrt(d), FP32 roundings) runs once per 32 rows on full warps.  A row with
-// several diagonal entries (a CSR with duplicates) sums them in column order.
-template <int LANES>
-__global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n, const double* __restrict__ val) {
-    constexpr int R = 32 / LANES;
-    const int lane = threadIdx.x & 31, sub = lane / LANES, sl = lane % LANES;
-    const int warps = gridDim.x * (kBlock / 32);
-    double* diag = const_cast<double*>(I.diag);
-    for (int base = (blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)) * 32; base < n; base += warps * 32) {
-        double mine = 0;
-#pragma unroll
-        for (int pass = 0; pass < LANES; ++pass) {
-            const int r = base + pass * R + sub;
-            int first = 0x7fffffff, count = 0, ks = 0, ke = 0;
-            if (r < n) {
-                ks = __ldg(I.rowptr + r);
-                ke = __ldg(I.rowptr + r + 1);
-                for (int k = ks + sl; k < ke; k += LANES)
-                    if (__ldg(I.col + k) == r) {
-                        first = min(first, k);
-                        ++count;
+// ---- admission pass over the nonzeros: convexity gate, Gershgorin bound, diagonal, hi/lo split -----
+// Per row, the row's entries in column order (the order of the reference's Gershgorin sum,
+// src/accelerated_qp.cpp:25-26, so L comes out bit for bit): sum |Q_ik| in FP64, the diagonal
+// Q_ii (duplicate diagonal entries summed) and the off-diagonal radius sum_{j != i} |Q_ij|; a row
+// with Q_ii < 0, or Q_ii = 0 beside off-diagonal entries, is indefinite, and one with
+// Q_ii < radius breaks diagonal dominance (check_convex_hessian, src/qp_admm.cpp:30-39).  The same
+// pass stores the FP64 diagonal (the Jacobi preconditioner and the diagonal dual-gap gate; a
+// single diagonal entry is stored as given) and, for the mixed engine, the hi/lo FP32 values.
+// FP64 instructions run at 1/64 of the FP32 rate on GB300 and cost the same whatever a warp's
+// active lanes, so the pass keeps them off the nonzeros:
+//   * the split runs in integer arithmetic (split_hilo_bits);
+//   * both sums are bracketed by FP32 sums rounded down and up of the FP32 bounds of |Q_ij|
+//     (abs_bounds_bits).  By induction over the row, RD32(lo + rd) <= RD64(s + |q|) <=
+//     fl64(s + |q|) and the same upward, so the FP64 column-order sum lies in its bracket;
+//   * Q_ii < lo and Q_ii >= hi decide dominance as the FP64 radius would; a row whose diagonal
+//     falls inside the bracket sums its radius in FP64;
+//   * L is the largest FP64 row sum, and only a row whose upper bound reaches the largest lower
+//     bound of any row can hold it: the pass keeps that floor in the result (an atomic maximum,
+//     read back by each warp per group of rows) and sums in FP64 only the rows at or above it.
+//     The row with the largest sum is always among them, so L is the same bits whatever the
+//     order in which the warps run.
+// A warp takes 32 consecutive rows and walks their entries in windows of kGateBuf: it stages a
+// window's values and columns in shared memory with coalesced loads (writing the split as it
+// goes), and each lane then adds the part of its own row inside the window, so every row's sums
+// run in column order whatever its length; the FP64 sums re-read their rows (from L2).
+constexpr int kGateWarps = 4;      // warps per block of the gate kernel
+constexpr int kGateBuf = 512;      // staged entries per warp (6 KB: values and columns)
+
+__global__ void __launch_bounds__(kGateWarps * 32) convexity_gate_kernel(const int32_t* __restrict__ rowptr,
+                                                                          const int32_t* __restrict__ col,
+                                                                          const double* __restrict__ val, int n,
+                                                                          GateResult* out, double* __restrict__ diag,
+                                                                          float* __restrict__ vhi,
+                                                                          float* __restrict__ vlo) {
+    __shared__ uint64_t sval[kGateWarps][kGateBuf];  // the values' bit patterns
+    __shared__ int32_t scol[kGateWarps][kGateBuf];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t* bv = sval[warp];
+    int32_t* bc = scol[warp];
+    const unsigned long long* __restrict__ vbits = reinterpret_cast<const unsigned long long*>(val);
+    unsigned long long best = 0, floor_seen = 0;
+    int indefinite = 0, nondominant = 0, flags = 0;
+    const int groups = (n + 31) / 32;
+    for (int g = blockIdx.x * kGateWarps + warp; g < groups; g += gridDim.x * kGateWarps) {  // warp-uniform
+        const int r = g * 32 + lane;
+        const bool valid = r < n;
+        const int a = valid ? __ldg(rowptr + r) : 0;
+        const int b = valid ? __ldg(rowptr + r + 1) : 0;
+        const int last = min(n - g * 32, 32) - 1;
+        const int kb = __shfl_sync(0xffffffffu, a, 0);
+        const int ke = __shfl_sync(0xffffffffu, b, last);
+        float sum_lo = 0.0f, sum_hi = 0.0f, rad_lo = 0.0f, rad_hi = 0.0f;
+        int nd = 0, kd = 0;  // diagonal entries of the row and the first one's position
+        bool offd = false;   // a nonzero off-diagonal value (check_qp_solution's positive_diagonal)
+        for (int w = kb; w < ke; w += kGateBuf) {
+            const int we = min(ke, w + kGateBuf);
+            for (int k = w + lane; k < we; k += 32) {
+                const uint64_t vb = __ldg(vbits + k);
+                const int32_t c = __ldg(col + k);
+                bv[k - w] = vb;
+                bc[k - w] = c;
+                if (static_cast<uint32_t>(c) >= static_cast<uint32_t>(n) ||
+                    (vb & 0x7ff0000000000000ull) == 0x7ff0000000000000ull)
+                    flags |= kGateInvalid;
+                if (vb << 1) flags |= kGateNonzero;
+                if (vhi) {
+                    uint32_t h, l;
+                    if (!split_hilo_bits(vb, h, l)) {
+                        const double v = __longlong_as_double(static_cast<long long>(vb));
+                        const float hf = __double2float_rn(v);
+                        h = __float_as_uint(hf);
+                        l = __float_as_uint(__double2float_rn(v - static_cast<double>(hf)));
                     }
-            }
-#pragma unroll
-            for (int o = LANES / 2; o > 0; o >>= 1) {
-                first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
-                count += __shfl_xor_sync(0xffffffffu, count, o);
-            }
-            double d = 0;
-            if (r < n && sl == 0 && count > 0) {
-                if (count == 1) {
-                    d = val[first];
-                } else {
-                    for (int k = first; k < ke; ++k)
-                        if (__ldg(I.col + k) == r) d += val[k];
+                    vhi[k] = __uint_as_float(h);
+                    vlo[k] = __uint_as_float(l);
                 }
             }
-            const int g = lane - pass * R;
-            const bool mine_now = g >= 0 && g < R;
-            const double got = shfl_idx(d, (mine_now ? g : 0) * LANES);
-            if (mine_now) mine = got;
-        }
-        const int r = base + lane;
-        if (r < n) {
-            const double d = mine;
-            diag[r] = d;
-            if (I.precision == PREC_MIXED) {
-                const_cast<double*>(I.dinv)[r] = d > 0 ? 1.0 / d : 1.0;
-                // preconditioner scale v_r, kept in s (free until the polish) for the step set-up
-                I.s[r] = d > 0 ? 1.0 / sqrt(d) : 1.0 / sqrt(gate_lipschitz(I));
-                const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
-                const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
-                const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+            __syncwarp();
+            const int ka = max(a, w), kz = valid ? min(b, we) : ka;
+            for (int k = ka - w; k < kz - w; ++k) {
+                const uint64_t mag = bv[k] & 0x7fffffffffffffffull;
+                uint32_t lo, hi;
+                abs_bounds_bits(mag, lo, hi);
+                sum_lo = __fadd_rd(sum_lo, __uint_as_float(lo));
+                sum_hi = __fadd_ru(sum_hi, __uint_as_float(hi));
+                if (bc[k] == r) {
+                    if (nd++ == 0) kd = k + w;
+                } else {
+                    rad_lo = __fadd_rd(rad_lo, __uint_as_float(lo));
+                    rad_hi = __fadd_ru(rad_hi, __uint_as_float(hi));
+                    if (mag) offd = true;
+                }
             }
+            __syncwarp();
         }
-    }
-    if (I.precision == PREC_MIXED) {
-        const int stride = gridDim.x * blockDim.x;
-        const int nnz = I.rowptr[n];
-        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += stride) {
-            const double x = val[k];
-            const float hi = __double2float_rn(x);
-            const_cast<float*>(I.vhi)[k] = hi;
-            const_cast<float*>(I.vlo)[k] = __double2float_rn(x - static_cast<double>(hi));
+        // the floor: the largest lower bound of a row sum, this group's and the others' so far
+        unsigned long long group_floor = valid ? widen_bits(__float_as_uint(sum_lo)) : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) group_floor = umax64(group_floor, shfl_xor(group_floor, o));
+        if (group_floor > floor_seen) {
+            if (lane == 0) atomicMax(&out->floor_bits, group_floor);
+            floor_seen = group_floor;
         }
-    }
-}
-
-// ---- convexity gate and Gershgorin bound at admission ---------------------------------------------
-// One thread per row, the row's entries in column order (the order of the reference's Gershgorin
-// sum, src/accelerated_qp.cpp:25-26, so L comes out bit for bit): sum |Q_ik|, the diagonal Q_ii
-// (duplicate diagonal entries summed) and the off-diagonal radius sum_{j != i} |Q_ij|; a row with
-// Q_ii < 0, or Q_ii = 0 beside off-diagonal entries, is indefinite, and one with Q_ii < radius
-// breaks diagonal dominance (check_convex_hessian, src/qp_admm.cpp:30-39).  Warp reductions, then
-// one atomic per warp: the maximum as the bit pattern of a non-negative double, the flags as ORs.
-__global__ void __launch_bounds__(kBlock) convexity_gate_kernel(const int32_t* __restrict__ rowptr,
-                                                      const int32_t* __restrict__ col,
-                                                      const double* __restrict__ val, int n, GateResult* out) {
-    unsigned long long best = 0;
-    int indefinite = 0, nondominant = 0;
-    const int stride = gridDim.x * blockDim.x;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
-        double abs_sum = 0.0, d = 0.0, radius = 0.0;
-        for (int k = ks; k < ke; ++k) {
-            const double v = __ldg(val + k);
-            abs_sum += fabs(v);
-            if (__ldg(col + k) == r) d += v;
-            else radius += fabs(v);
+        floor_seen = umax64(floor_seen, *reinterpret_cast<volatile unsigned long long*>(&out->floor_bits));
+        if (valid) {
+            // Q_ii: a single diagonal entry as given, duplicates summed in column order from 0
+            double d = 0.0;
+            if (nd == 1) {
+                d = __ldg(val + kd);
+            } else if (nd > 1) {
+                for (int k = kd; k < b; ++k)
+                    if (__ldg(col + k) == r) d += __ldg(val + k);
+            }
+            if (widen_bits(__float_as_uint(sum_hi)) >= floor_seen) {
+                double total = 0.0;
+                for (int k = a; k < b; ++k) total += fabs(__ldg(val + k));
+                best = umax64(best, dbits(total));
+            }
+            const uint64_t db = static_cast<uint64_t>(__double_as_longlong(d));
+            const uint64_t dm = db & 0x7fffffffffffffffull;
+            const bool negative = (db >> 63) && dm;
+            if (negative || (dm == 0 && rad_hi > 0.0f)) indefinite = 1;
+            bool below;  // Q_ii < the FP64 column-order radius
+            if (negative) {
+                below = true;
+            } else if (dm < widen_bits(__float_as_uint(rad_lo))) {
+                below = true;
+            } else if (dm >= widen_bits(__float_as_uint(rad_hi))) {
+                below = false;
+            } else {
+                double radius = 0.0;
+                for (int k = a; k < b; ++k)
+                    if (__ldg(col + k) != r) radius += fabs(__ldg(val + k));
+                below = d < radius;
+            }
+            if (below) nondominant = 1;
+            if (offd) flags |= kGateOffDiagonal;
+            if (negative || dm == 0 || dm > 0x7ff0000000000000ull) flags |= kGateNonPositive;  // !(Q_ii > 0)
+            if (diag) diag[r] = d;
         }
-        best = umax64(best, dbits(abs_sum));
-        if (d < 0.0 || (d == 0.0 && radius > 0.0)) indefinite = 1;
-        if (d < radius) nondominant = 1;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = umax64(best, shfl_xor(best, o));
     indefinite = __reduce_or_sync(0xffffffffu, indefinite);
     nondominant = __reduce_or_sync(0xffffffffu, nondominant);
-    if ((threadIdx.x & 31) == 0) {
+    flags = static_cast<int>(__reduce_or_sync(0xffffffffu, static_cast<unsigned>(flags)));
+    if (lane == 0) {
         if (best) atomicMax(&out->lip_bits, best);
         if (indefinite) atomicOr(&out->indefinite, 1);
         if (nondominant) atomicOr(&out->nondominant, 1);
+        if (flags) atomicOr(&out->flags, flags);
+    }
+}
+
+// Mixed engine, per row after the gate: 1/Q_ii (the polish's Jacobi preconditioner), the
+// preconditioner scale v_r = Q_ii^-1/2 (rows without a positive diagonal L^-1/2), the FP32 cost
+// and the FP32 bounds rounded inward (l32 = smallest float >= l, u32 = largest float <= u, so FP32
+// iterates never leave the FP64 box).  Both scalings only precondition, so for 2^-100 <= Q_ii <
+// 2^100 they come from the correctly rounded FP32 reciprocal and reciprocal square root of
+// RN32(Q_ii) (two FP64 conversions per row instead of an FP64 division and square root); v is
+// kept as that float in sstep (read by the bound of the scaled matrix, then overwritten by the
+// steps) and widened exactly into s (free until the polish).
+__global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n) {
+    const int stride = gridDim.x * blockDim.x;
+    const float inv_sqrt_l = __double2float_rn(1.0 / sqrt(gate_lipschitz(I)));
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const double d = I.diag[r];
+        const uint64_t db = static_cast<uint64_t>(__double_as_longlong(d));
+        const int e = static_cast<int>(db >> 52);  // biased exponent; sign set => outside
+        double dinv;
+        float v;
+        if (e >= 923 && e < 1123) {
+            const float df = __double2float_rn(d);
+            dinv = static_cast<double>(__frcp_rn(df));
+            v = __frsqrt_rn(df);
+        } else if (d > 0) {
+            dinv = 1.0 / d;
+            v = __double2float_rn(1.0 / sqrt(d));
+        } else {
+            dinv = 1.0;
+            v = inv_sqrt_l;
+        }
+        const_cast<double*>(I.dinv)[r] = dinv;
+        I.s[r] = static_cast<double>(v);
+        I.sstep[r] = v;
+        const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
+        const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
+        const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
     }
 }
 
@@ -1792,41 +1872,56 @@ __global__ void __launch_bounds__(kBlock) convexity_gate_kernel(const int32_t* _
 // x with the per-row step v_i^2 / L', v_i = Q_ii^-1/2 (rows without a positive diagonal keep
 // v_i = L^-1/2, L the plain Gershgorin bound) and L' = max_i v_i sum_j |Q_ij| v_j, the Gershgorin
 // bound of V Q V.  The box stays a box, so the projection maps over unchanged.  prepare_kernel
-// leaves v in the s array.
-__device__ __forceinline__ double precond_v(const InstDev& I, int r) { return I.s[r]; }
+// leaves v (an FP32 value) in sstep and, widened, in the s array.
 
+// L' as an upper bound in FP32 arithmetic rounded up: |Q_ij| <= |hi_ij| plus one unit (hi the
+// nearest float), every product and sum rounded up, so the result is at least the exact bound
+// of V Q V for the v the steps use (FP64 per nonzero would cost more than the pass's bytes).
 template <int LANES>
-__global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n, const double* __restrict__ val) {
+__global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, sl = lane % LANES;
     const int groups = gridDim.x * (kBlock / 32) * R;
-    unsigned long long best = 0;
+    const float* __restrict__ vf = I.sstep;
+    uint32_t best = 0;
     for (int base = (blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)) * R; base < n; base += groups) {
         const int r = base + lane / LANES;
-        double sum = 0;
+        float sum = 0.0f;
         if (r < n) {
             const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
-            for (int k = ks + sl; k < ke; k += LANES) sum += fabs(val[k]) * precond_v(I, __ldg(I.col + k));
+            for (int k = ks + sl; k < ke; k += LANES) {
+                const uint32_t hb = __float_as_uint(__ldg(I.vhi + k)) & 0x7fffffffu;
+                const float q = __uint_as_float(hb >= 0x7f800000u ? 0x7f800000u : hb + 1u);
+                const int32_t c = __ldg(I.col + k);  // in range once the gate passes; clamped until then
+                sum = __fmaf_ru(q, __ldg(vf + (static_cast<uint32_t>(c) < static_cast<uint32_t>(n) ? c : 0)), sum);
+            }
         }
-        sum = group_sum<LANES>(sum);
-        if (r < n && sl == 0) best = umax64(best, dbits(sum * precond_v(I, r)));
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) sum = __fadd_ru(sum, __shfl_xor_sync(0xffffffffu, sum, o));
+        if (r < n && sl == 0) best = max(best, __float_as_uint(__fmul_ru(sum, vf[r])));
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) best = umax64(best, shfl_xor(best, o));
-    if ((threadIdx.x & 31) == 0 && best) atomicMax(reinterpret_cast<unsigned long long*>(I.lprec), best);
+    for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (best && best < 0x00800000u) best = 0x00800000u;  // a subnormal bound: 2^-126 above it
+    if ((threadIdx.x & 31) == 0 && best)
+        atomicMax(reinterpret_cast<unsigned long long*>(I.lprec), static_cast<unsigned long long>(widen_bits(best)));
 }
 
-// scaled = 0: the scalar step 1/L in every row (L from lprec under the power estimate).
+// scaled = 0: the scalar step 1/L in every row (L from lprec under the power estimate); scaled:
+// v^2 / L' rounded down in FP32 (v read from sstep before the step replaces it).
 __global__ void __launch_bounds__(kBlock) precond_step_kernel(InstDev I, int n, int scaled) {
     const int stride = gridDim.x * blockDim.x;
     const double lp = (scaled || I.lip_device) ? *I.lprec : 0.0;
+    const float plain = static_cast<float>((I.lip_device && lp > 0) ? 1.0 / lp : 1.0 / gate_lipschitz(I));
+    const bool per_row = scaled && lp > 0;
+    const float inv = per_row ? __frcp_rd(__double2float_ru(lp)) : 0.0f;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-        double s = (I.lip_device && lp > 0) ? 1.0 / lp : 1.0 / gate_lipschitz(I);
-        if (scaled && lp > 0) {
-            const double v = precond_v(I, r);
-            s = v * v / lp;
+        float s = plain;
+        if (per_row) {
+            const float v = I.sstep[r];
+            s = __fmul_rd(__fmul_rd(v, v), inv);
         }
-        I.sstep[r] = static_cast<float>(s);
+        I.sstep[r] = s;
     }
 }
 
@@ -1919,7 +2014,8 @@ __global__ void __launch_bounds__(kBlock) lanczos_product_kernel(InstDev I, int 
         const int ks = __ldg(I.rowptr + r), ke = __ldg(I.rowptr + r + 1);
         double acc = 0;
         for (int q = ks; q < ke; ++q) {
-            const int j = __ldg(I.col + q);
+            int j = __ldg(I.col + q);
+            if (static_cast<uint32_t>(j) >= static_cast<uint32_t>(n)) j = 0;  // until the gate has checked it
             acc += val[q] * (scaled ? v[j] * w[j] : w[j]);
         }
         if (scaled) acc *= v[r];
@@ -2232,9 +2328,9 @@ void launch_precondition(const InstDev& rec, int64_t n, const double* val, bool 
         if (g > 152 * 16) g = 152 * 16;
         if (g < 1) g = 1;
         const int gi = static_cast<int>(g), ni = static_cast<int>(n);
-        if (lanes == 8) precond_bound_kernel<8><<<gi, kBlock, 0, s>>>(rec, ni, val);
-        else if (lanes == 4) precond_bound_kernel<4><<<gi, kBlock, 0, s>>>(rec, ni, val);
-        else precond_bound_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni, val);
+        if (lanes == 8) precond_bound_kernel<8><<<gi, kBlock, 0, s>>>(rec, ni);
+        else if (lanes == 4) precond_bound_kernel<4><<<gi, kBlock, 0, s>>>(rec, ni);
+        else precond_bound_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni);
     }
     if (rec.lip_device) {
         if (!scaled) cudaMemcpyAsync(rec.lprec, &rec.gate->lip_bits, sizeof(double), cudaMemcpyDeviceToDevice, s);
@@ -2274,24 +2370,29 @@ void launch_power_lipschitz(const InstDev& rec, int64_t n, const double* val, bo
     }
 }
 
-void launch_gate(const InstDev& rec, int64_t n, const double* val, cudaStream_t s) {
-    cudaMemsetAsync(rec.gate, 0, sizeof(GateResult), s);
-    int64_t grid = (n + kBlock - 1) / kBlock;
+void launch_gate_raw(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val, GateResult* out,
+                     double* diag, float* vhi, float* vlo, cudaStream_t s) {
+    cudaMemsetAsync(out, 0, sizeof(GateResult), s);
+    const int64_t groups = (n + 31) / 32;
+    int64_t grid = (groups + kGateWarps - 1) / kGateWarps;
     if (grid > 152 * 8) grid = 152 * 8;
     if (grid < 1) grid = 1;
-    convexity_gate_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec.rowptr, rec.col, val, static_cast<int>(n), rec.gate);
+    convexity_gate_kernel<<<static_cast<int>(grid), kGateWarps * 32, 0, s>>>(rowptr, col, val, static_cast<int>(n), out,
+                                                                             diag, vhi, vlo);
 }
 
-void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s) {
-    const int lanes = row_lanes(rec);
-    const int64_t work = n * lanes > nnz ? n * lanes : nnz;
-    int64_t grid = (work + kBlock - 1) / kBlock;
+void launch_gate(const InstDev& rec, int64_t n, const double* val, cudaStream_t s) {
+    const bool split = rec.precision == PREC_MIXED;
+    launch_gate_raw(n, rec.rowptr, rec.col, val, rec.gate, const_cast<double*>(rec.diag),
+                    split ? const_cast<float*>(rec.vhi) : nullptr, split ? const_cast<float*>(rec.vlo) : nullptr, s);
+}
+
+void launch_prepare_instance(const InstDev& rec, int64_t n, cudaStream_t s) {
+    if (rec.precision != PREC_MIXED) return;  // the gate already stored the FP64 engine's diagonal
+    int64_t grid = (n + kBlock - 1) / kBlock;
     if (grid > 152 * 16) grid = 152 * 16;
     if (grid < 1) grid = 1;
-    const int gi = static_cast<int>(grid), ni = static_cast<int>(n);
-    if (lanes == 8) prepare_kernel<8><<<gi, kBlock, 0, s>>>(rec, ni, val);
-    else if (lanes == 4) prepare_kernel<4><<<gi, kBlock, 0, s>>>(rec, ni, val);
-    else prepare_kernel<2><<<gi, kBlock, 0, s>>>(rec, ni, val);
+    prepare_kernel<<<static_cast<int>(grid), kBlock, 0, s>>>(rec, static_cast<int>(n));
 }
 
 int check_grid(int64_t n) {

@@ -35,11 +35,16 @@ void launch_control(const View& v, cudaGraphConditionalHandle loop, int steps, c
 void launch_gate_plain(const View& v, int steps, cudaStream_t s);
 void launch_control_plain(const View& v, int steps, cudaStream_t s);
 // Admission, first kernel: the convexity gate and Gershgorin bound of the uploaded full CSR
-// (FP64 values `val`) into *rec.gate (cleared first).  The later admission kernels read L there.
+// (FP64 values `val`) into *rec.gate (cleared first), the FP64 diagonal into rec.diag and, for the
+// mixed engine, the hi/lo FP32 values into rec.vhi/rec.vlo.  The later admission kernels read L there.
 void launch_gate(const InstDev& rec, int64_t n, const double* val, cudaStream_t s);
-// Admission: diagonal, hi/lo split and FP32 vectors from the uploaded FP64 values.
+// The same pass on raw device pointers (diag, vhi, vlo may be null: not stored).
+void launch_gate_raw(int64_t n, const int32_t* rowptr, const int32_t* col, const double* val, GateResult* out,
+                     double* diag, float* vhi, float* vlo, cudaStream_t s);
+// Admission, mixed engine, after launch_gate on the same stream: 1/diag, preconditioner scales and
+// the FP32 cost and bounds (nothing for the FP64 engines).
 // The record is passed by value: the instance is installed in its slot later, between graph launches.
-void launch_prepare_instance(const InstDev& rec, int64_t n, int64_t nnz, const double* val, cudaStream_t s);
+void launch_prepare_instance(const InstDev& rec, int64_t n, cudaStream_t s);
 // Mixed engine: per-row FISTA steps (diagonally preconditioned when `scaled`, else 1/L), after
 // launch_prepare_instance on the same stream; val = the FP64 values.  With rec.lip_device the
 // power estimate replaces the Gershgorin bound (power_scratch: power_scratch_bytes()).

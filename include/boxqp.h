@@ -135,7 +135,14 @@ int         bqp_host_unregister(void* ptr);
  * row) and queues it.  The engine admits queued solves into the running batch as memory and
  * slots free up, iterates every resident solve in the same launches, and retires each one when
  * its own verification passes.  Returns BQP_ERR_ADMISSION only when the problem can never fit
- * under the context's memory cap.                                                            */
+ * under the context's memory cap.
+ * Checks, in the reference's order (src/accelerated_qp.cpp:14-28): the call itself validates the
+ * row pointers, costs and bounds (BQP_ERR_INVALID at once).  The Hessian's entries are checked by
+ * the device's admission pass, which reads them anyway: a column out of range or a value that is
+ * not finite ends the solve with BQP_ERR_INVALID ("Invalid Hessian"), a non-convex Hessian with
+ * BQP_STATUS_UNSUPPORTED_CURVATURE, a zero Hessian with BQP_ERR_UNSUPPORTED, reported by bqp_wait
+ * and bqp_fetch (nnz = 0 is refused at once).  A problem with infeasible bounds finishes at the
+ * call, with its entries checked on the host.                                                */
 int bqp_submit(bqp_ctx* ctx, int64_t n, int64_t nnz, const int32_t* rowptr, const int32_t* col,
                const double* val, const double* c, const double* lower, const double* upper,
                const bqp_options* options, uint64_t* id);
@@ -258,6 +265,21 @@ const char* bqp_box_last_error(const bqp_box* box);
 int bqp_check_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
                      const double* d_x, const double* d_c, const double* d_lower, const double* d_upper,
                      double tolerance, double offset, int32_t diagonal_gate, bqp_stats* stats);
+
+/* ---- convexity gate on device data ---------------------------------------------------------
+ * The engine's admission pass as a standalone call on caller-owned DEVICE pointers (full
+ * symmetric CSR, columns ascending per row), replacing the fast path of check_convex_hessian
+ * (src/qp_admm.cpp:30-39) and the Gershgorin bound (src/accelerated_qp.cpp:25-26):
+ * *lipschitz = max_i sum_k |Q_ik| summed in column order (bit for bit the reference's L);
+ * *indefinite = 1 when some row has Q_ii < 0, or Q_ii = 0 beside off-diagonal entries (not
+ * convex); *nondominant = 1 when some row has Q_ii < sum_{j != i} |Q_ij| (the FP64 column-order
+ * sum), where check_convex_hessian goes on to its sparse LDL' (bqp_check_convex on the host).
+ * Q_ii sums a row's diagonal entries; d_diag (n doubles on the device, or NULL) receives it.
+ * Device scratch allocated per call, a non-blocking stream of its own: synchronize the stream
+ * that wrote the arrays before calling.  BQP_ERR_INVALID comes with a message from
+ * bqp_box_last_error(NULL).                                                                   */
+int bqp_gate_device(int64_t n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
+                    double* d_diag, double* lipschitz, int32_t* indefinite, int32_t* nondominant);
 
 /* ---- verification without any device allocation -------------------------------------------
  * No counterpart in the reference.  Same computation and arguments as bqp_check_device, for

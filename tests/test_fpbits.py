@@ -1,0 +1,23 @@
+"""The integer FP64 -> FP32 conversions of the admission pass (csrc/fpbits.h), compiled for the
+host and checked against the C library's conversions (hi/lo split bit for bit, directed bounds
+nearest inside the normal range, exact widening)."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+CSRC = ROOT / 'hypergrey-sih-26_gb300' / 'csrc'
+
+
+@pytest.mark.skipif(shutil.which('g++') is None, reason='needs g++')
+def test_fpbits_conversions_match_the_c_library(tmp_path):
+    exe = tmp_path / 'fpbits_check'
+    subprocess.run(['g++', '-O2', '-std=c++17', '-ffp-contract=off', '-I', str(CSRC),
+                    str(ROOT / 'tests' / 'fpbits_check.cpp'), '-o', str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert 'failures 0' in out.stdout
+    n_split = int(out.stdout.split('split ')[1].split()[0])
+    assert n_split > 100000  # the window holds a good share of the random patterns

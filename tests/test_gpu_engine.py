@@ -201,6 +201,186 @@ def test_check_device_matches_oracle_checker():
     assert bool(st.verified) == bool(ref['verified'])
 
 
+def _gate_expected(rowptr, col, val):
+    """Per-row restatement of bqp_gate_device's contract: FP64 sums in column order."""
+    n = rowptr.shape[0] - 1
+    lip, indefinite, nondominant = 0.0, 0, 0
+    diag = np.zeros(n)
+    for r in range(n):
+        a, b = int(rowptr[r]), int(rowptr[r + 1])
+        total, radius, d, nd = 0.0, 0.0, 0.0, 0
+        for k in range(a, b):
+            v = float(val[k])
+            total += abs(v)
+            if col[k] == r:
+                d = v if nd == 0 else (0.0 + d if nd == 1 else d) + v
+                nd += 1
+            else:
+                radius += abs(v)
+        lip = max(lip, total)
+        if d < 0 or (d == 0 and radius > 0):
+            indefinite = 1
+        if d < radius:
+            nondominant = 1
+        diag[r] = d
+    return lip, indefinite, nondominant, diag
+
+
+def _rows_to_csr(rows):
+    rowptr = np.zeros(len(rows) + 1, np.int32)
+    rowptr[1:] = np.cumsum([len(c) for c, _ in rows])
+    col = np.concatenate([np.asarray(c, np.int32) for c, _ in rows])
+    val = np.concatenate([np.asarray(v, np.float64) for _, v in rows])
+    return rowptr, col, val
+
+
+def _gate_rows(rng, n, degree, mode, long_rows=()):
+    """Rows with random off-diagonal values (not FP32-representable, so the FP32 bracket of the
+    radius has width); the diagonal is the FP64 column-order radius itself ('equal': every row
+    falls inside the bracket and sums again in FP64), one unit below it in one row ('below'), or
+    the radius plus a clear margin ('margin')."""
+    rows = []
+    for r in range(n):
+        m = int(long_rows[r]) if r < len(long_rows) else int(rng.integers(1, 2 * degree))
+        cols = np.unique(rng.integers(0, n, m))
+        cols = cols[cols != r]
+        vals = rng.uniform(-1.0, 1.0, cols.shape[0]) * 10.0 ** rng.integers(-3, 3)
+        radius = 0.0
+        for v in vals:
+            radius += abs(float(v))
+        d = radius + (0.5 if mode == 'margin' else 0.0)
+        cols = np.append(cols, r)
+        vals = np.append(vals, d)
+        order = np.argsort(cols, kind='stable')
+        rows.append((cols[order], vals[order]))
+    if mode == 'below':
+        cols, vals = rows[n // 2]
+        k = int(np.nonzero(cols == n // 2)[0][0])
+        vals[k] = np.nextafter(vals[k], 0.0)
+    return rows
+
+
+def test_gate_device_matches_the_row_restatement():
+    """bqp_gate_device (the engine's admission pass on caller arrays): the Gershgorin bound bit for
+    bit against bqp_gershgorin, the dominance and indefiniteness flags and the stored diagonal
+    against a per-row FP64 restatement, on rows whose diagonal equals the FP64 radius (the FP32
+    bracket cannot decide them), one unit below it, with a margin, with negative or zero
+    diagonals, with duplicate diagonal entries, and with rows longer than a staging window."""
+    torch = pytest.importorskip('torch')
+    from ctypes import byref, c_double, c_int32
+    rng = np.random.default_rng(7)
+    cases = {}
+    for mode in ('equal', 'below', 'margin'):
+        cases[mode] = _rows_to_csr(_gate_rows(rng, 3000, 8, mode))
+        cases[mode + '_long'] = _rows_to_csr(_gate_rows(rng, 3000, 8, mode, long_rows=[2500, 900, 30] * 3))
+    rows = _gate_rows(rng, 500, 6, 'margin')
+    c0, v0 = rows[7]
+    v0 = v0.copy()
+    v0[np.nonzero(c0 == 7)[0][0]] = -1.0
+    cases['negative'] = _rows_to_csr(rows[:7] + [(c0, v0)] + rows[8:])
+    rows = _gate_rows(rng, 500, 6, 'margin')
+    c1, v1 = rows[11]
+    v1 = v1.copy()
+    v1[np.nonzero(c1 == 11)[0][0]] = 0.0
+    cases['zero_diagonal'] = _rows_to_csr(rows[:11] + [(c1, v1)] + rows[12:])
+    rows = _gate_rows(rng, 500, 6, 'margin')
+    rows[3] = (np.array([], np.int32), np.array([]))  # an empty row
+    c2, v2 = rows[5]
+    k = int(np.nonzero(c2 == 5)[0][0])
+    rows[5] = (np.insert(c2, k, 5), np.insert(v2, k, [-0.25]))  # two diagonal entries in one row
+    cases['duplicates_empty'] = _rows_to_csr(rows)
+    lib = boxqp.lib()
+    for name, (rowptr, col, val) in cases.items():
+        n = rowptr.shape[0] - 1
+        d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (rowptr, col, val)]
+        diag = torch.zeros(n, dtype=torch.float64, device='cuda')
+        torch.cuda.synchronize()
+        lip, ind, nond = c_double(), c_int32(), c_int32()
+        rc = lib.bqp_gate_device(n, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), diag.data_ptr(),
+                                 byref(lip), byref(ind), byref(nond))
+        assert rc == 0, name
+        want_lip, want_ind, want_nond, want_diag = _gate_expected(rowptr, col, val)
+        assert lip.value == boxqp.gershgorin(rowptr, val) == want_lip, name
+        assert (ind.value, nond.value) == (want_ind, want_nond), name
+        assert np.array_equal(diag.cpu().numpy(), want_diag), name
+    assert _gate_expected(*cases['equal'])[2] == 0 and _gate_expected(*cases['below'])[2] == 1
+    assert _gate_expected(*cases['negative'])[1] == 1 and _gate_expected(*cases['zero_diagonal'])[1] == 1
+
+
+def test_hessian_entries_are_checked_by_the_admission_pass(engine):
+    """The submission scans rows, costs and bounds on the host (errors at once); the Hessian's
+    entries are checked by the device's admission pass, which reports, in the reference's order
+    (src/accelerated_qp.cpp:14-28), an entry out of range or not finite as invalid_argument
+    ('Invalid Hessian'), a non-convex Hessian as unsupported_curvature and a zero Hessian as the
+    CPU LP path's error, through bqp_wait / bqp_fetch; the context keeps serving afterwards."""
+    inst = boxqp.planted('graph10k', seed=4, n=3000)
+    base = [np.array(a, copy=True) for a in (inst['rowptr'], inst['col'], inst['val'], inst['c'],
+                                             inst['lower'], inst['upper'])]
+    o = boxqp.options_struct(1e-6, 60.0, 200000, 'mixed')
+    x_ok, st_ok = engine.solve(*base, o)
+    assert boxqp.STATUS_NAMES[st_ok.status] == 'optimal'
+
+    def variant(**change):
+        a = [np.array(v, copy=True) for v in base]
+        names = ['rowptr', 'col', 'val', 'c', 'lower', 'upper']
+        for k, f in change.items():
+            f(a[names.index(k)])
+        return a
+
+    out_of_range = variant(col=lambda c: c.__setitem__(17, base[0].shape[0] - 1))
+    not_finite = variant(val=lambda v: v.__setitem__(123, np.nan))
+    zero = variant(val=lambda v: v.__setitem__(slice(None), 0.0))
+    for a, exc, match in ((out_of_range, ValueError, 'Invalid Hessian'), (not_finite, ValueError, 'Invalid Hessian'),
+                          (zero, boxqp.EngineError, 'Zero-Hessian')):
+        with pytest.raises(exc, match=match):
+            engine.solve(*a, o)
+        for copy in (True, False):
+            ident = engine.submit(*a, o, copy=copy)
+            with pytest.raises(exc, match=match):
+                engine.wait(ident, 60.0)
+            engine.release(ident)
+    # host checks still come at submission, before the entries
+    bad_cost = variant(c=lambda c: c.__setitem__(3, np.inf), col=lambda c: c.__setitem__(17, -5))
+    with pytest.raises(ValueError, match='coefficient or bound'):
+        engine.submit(*bad_cost, o)
+    # infeasible bounds finish at submission: the entries are checked on the host there
+    infeasible_bad = variant(lower=lambda l: l.__setitem__(0, 5.0), val=lambda v: v.__setitem__(9, np.inf))
+    with pytest.raises(ValueError, match='Invalid Hessian'):
+        engine.submit(*infeasible_bad, o)
+    infeasible_zero = variant(lower=lambda l: l.__setitem__(0, 5.0), val=lambda v: v.__setitem__(slice(None), 0.0))
+    with pytest.raises(boxqp.EngineError, match='Zero-Hessian'):
+        engine.submit(*infeasible_zero, o)
+    x, st = engine.solve(*base, o)
+    assert np.array_equal(x, x_ok) and st.iterations == st_ok.iterations
+
+
+def test_diagonal_hessian_takes_the_separable_bound(engine):
+    """A diagonal Hessian with a positive diagonal (explicit zero off-diagonal entries allowed, as
+    check_qp_solution's positive_diagonal test counts nonzero values only) is recognised by the
+    admission pass: its dual bound is the separable one, tight at the optimum (relative gap
+    ~0), and equal to the oracle checker's."""
+    rng = np.random.default_rng(5)
+    n = 5000
+    d = rng.uniform(0.5, 3.0, n)
+    rows = []
+    for r in range(n):
+        cols, vals = [r], [d[r]]
+        if r % 7 == 0 and r + 1 < n:
+            cols.append(r + 1)
+            vals.append(0.0)  # an explicit zero off the diagonal
+        rows.append((np.array(cols), np.array(vals)))
+    rowptr, col, val = _rows_to_csr(rows)
+    c = rng.standard_normal(n)
+    lo, up = -np.ones(n), np.ones(n)
+    o = boxqp.options_struct(1e-9, 60.0, 200000, 'fp64')
+    x, st = engine.solve(rowptr, col, val, c, lo, up, o)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal'
+    hrow = np.arange(n, dtype=np.int64)
+    ref = O.check(hrow, hrow, d, c, lo, up, x, tol=1e-9)
+    assert st.dual_bound == pytest.approx(ref['dual_bound'], rel=1e-12)
+    assert st.relative_gap <= 1e-9
+
+
 def test_device_name():
     assert 'GB300' in boxqp.cuda_device_name() or len(boxqp.cuda_device_name()) > 0
 
