@@ -63,6 +63,19 @@ BQP_HD bool split_hilo_bits(uint64_t bits, uint32_t& hi, uint32_t& lo) {
     return true;
 }
 
+// RN32(v) (round to nearest, ties to even) in integer arithmetic where the result is a normal
+// finite float: biased exponent 897..1150 of v and no overflow; returns false elsewhere (zero
+// included), where the caller converts with an FP64 instruction.
+BQP_HD bool round_float_bits(uint64_t bits, uint32_t& f) {
+    const uint64_t mag = bits & 0x7fffffffffffffffull;
+    const int e = static_cast<int>(mag >> 52);
+    if (e < 897 || e > 1150) return false;
+    const uint32_t h = static_cast<uint32_t>((mag + 0x0fffffffull + ((mag >> 29) & 1ull)) >> 29) - (896u << 23);
+    if ((h & 0x7f800000u) == 0x7f800000u) return false;
+    f = h | (static_cast<uint32_t>(bits >> 32) & 0x80000000u);
+    return true;
+}
+
 // FP32 bounds of a magnitude given by its FP64 bits: rd <= |v| <= ru.  Inside the normal FP32
 // range they are the nearest floats below and above (truncation, plus one unit when a dropped
 // bit is set); below it 0 and 2^-126, above it FLT_MAX and infinity.

@@ -461,9 +461,21 @@ __device__ __forceinline__ float2 df_prod2(float h, float l, float2 x) {
     return make_float2(p, __fmaf_rn(h, x.y, __fmaf_rn(l, x.x, e)));
 }
 __device__ __forceinline__ double df_value(float2 a) { return static_cast<double>(a.x) + static_cast<double>(a.y); }
+// The FP32 pair of an FP64 value: hi = RN32(x), lo = RN32(x - hi), in integer arithmetic where
+// both are normal floats (split_hilo_bits), with the FP64 conversions elsewhere; the same bits
+// either way.
 __device__ __forceinline__ float2 df_split(double x) {
-    const float h = __double2float_rn(x);
-    return make_float2(h, __double2float_rn(x - static_cast<double>(h)));
+    uint32_t h, l;
+    if (split_hilo_bits(static_cast<uint64_t>(__double_as_longlong(x)), h, l))
+        return make_float2(__uint_as_float(h), __uint_as_float(l));
+    const float hf = __double2float_rn(x);
+    return make_float2(hf, __double2float_rn(x - static_cast<double>(hf)));
+}
+// RN32(x), in integer arithmetic where the result is a normal float (round_float_bits).
+__device__ __forceinline__ float rn_float(double x) {
+    uint32_t f;
+    if (round_float_bits(static_cast<uint64_t>(__double_as_longlong(x)), f)) return __uint_as_float(f);
+    return __double2float_rn(x);
 }
 
 // check_row for the FP32 iterate of the mixed engine: the iterate lies in [l32, u32], a subset of
@@ -958,10 +970,10 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // (an instance's tiling depends on the instance alone, so the list survives changes of the batch).
 // Fixed rows hold r = z = p = 0, so the products of the CG matvec over all columns are exact.
 // CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with 0.1 tol), as the
-// bit pattern of a non-negative float: maxima reduce on the integer pipes, and the FP64 pipe
-// (1/64 of the FP32 rate on this GPU) only converts r and x.
+// bit pattern of a non-negative float: maxima reduce on the integer pipes, and r and x are
+// rounded to FP32 in integer arithmetic (the FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
 __device__ __forceinline__ unsigned long long cg_ratio_bits(double r, double x) {
-    const float ratio = __fdividef(fabsf(static_cast<float>(r)), 1.0f + fabsf(static_cast<float>(x)));
+    const float ratio = __fdividef(fabsf(rn_float(r)), 1.0f + fabsf(rn_float(x)));
     return static_cast<unsigned long long>(__float_as_uint(ratio));
 }
 

@@ -1,7 +1,7 @@
-// Host check of the integer FP64 -> FP32 conversions the admission kernel uses (csrc/fpbits.h)
-// against the C library's conversions: split_hilo_bits against (float)v and (float)(v - hi),
-// abs_bounds_bits against the neighbouring floats, widen_bits against (double)f.  Prints one
-// line "checked N split M bounds K failures F" and exits non-zero on a failure.
+// Host check of the integer FP64 -> FP32 conversions the kernels use (csrc/fpbits.h) against the
+// C library's conversions: split_hilo_bits against (float)v and (float)(v - hi), round_float_bits
+// against (float)v, abs_bounds_bits against the neighbouring floats, widen_bits against
+// (double)f.  Prints "checked split S bounds B round R failures F" and exits non-zero on a failure.
 #include "fpbits.h"
 
 #include <cfloat>
@@ -30,7 +30,7 @@ static double dfrom(uint64_t b) {
     return d;
 }
 
-static long failures = 0, n_split = 0, n_bounds = 0;
+static long failures = 0, n_split = 0, n_bounds = 0, n_round = 0;
 
 static void fail(const char* what, double v) {
     if (failures++ < 20) std::printf("FAIL %s at %.17g (bits %016llx)\n", what, v, (unsigned long long)bqp::bits64(v));
@@ -45,6 +45,11 @@ static void check(double v) {
         const float lf = static_cast<float>(v - static_cast<double>(hf));
         if (h != fbits(hf)) fail("split hi", v);
         if (l != fbits(lf)) fail("split lo", v);
+    }
+    uint32_t f;
+    if (bqp::round_float_bits(bits, f)) {
+        ++n_round;
+        if (f != fbits(static_cast<float>(v))) fail("round", v);
     }
     if (!std::isfinite(v)) return;
     const uint64_t mag = bits & 0x7fffffffffffffffull;
@@ -97,6 +102,6 @@ int main() {
     check(-2.0);
     check(1.0 / 3.0);
     check(3.4028235677973366e38);  // rounds to infinity in FP32
-    std::printf("checked split %ld bounds %ld failures %ld\n", n_split, n_bounds, failures);
+    std::printf("checked split %ld bounds %ld round %ld failures %ld\n", n_split, n_bounds, n_round, failures);
     return failures ? 1 : 0;
 }
