@@ -143,12 +143,13 @@ def oracle_args(inst):
     return inst['hrow'], inst['hcol'], inst['hval'], inst['c'], inst['lower'], inst['upper']
 
 
-def cpu_reference_solve(inst, tol, time_limit=120.0, prefer_reference=True):
-    """One FP64 CPU solve on all host cores: the reference's own solve_accelerated_box(q, opt,
-    false) (oracle/_ref, built from its sources on this host) when available, else the oracle
-    port of it.  Returns (seconds of the solve call, info)."""
+def cpu_reference_solve(inst, tol, time_limit=600.0, prefer_reference=True, threads=0):
+    """One FP64 CPU solve on `threads` host cores (0: all of them, QpOptions::threads): the
+    reference's own solve_accelerated_box(q, opt, false) (oracle/_ref, built from its sources on
+    this host) when available, else the oracle port of it.  Returns (seconds of the solve call,
+    info)."""
     from oracle import oracle as O
-    threads = O.max_threads()
+    threads = threads or O.max_threads()
     if prefer_reference and O.ref_available():
         status, x, st = O.ref_solve_box(*oracle_args(inst), tol=tol, threads=threads, time_limit=time_limit)
         return st['seconds'], {'status': status, 'iterations': int(st['iterations']), 'threads': threads,
@@ -220,11 +221,11 @@ def run_reference(args, world, rank, pg):
         return
     inst, desc = make_workload(args.workload, 0, oracle_side=True)
     for _ in range(min(args.warmup, 1)):
-        cpu_reference_solve(inst, args.tol)
+        cpu_reference_solve(inst, args.tol, threads=args.cpu_threads)
     times, info = [], {}
     budget = 60.0
     while len(times) < args.steps and (not times or sum(times) < budget):
-        dt, info = cpu_reference_solve(inst, args.tol)
+        dt, info = cpu_reference_solve(inst, args.tol, threads=args.cpu_threads)
         times.append(dt)
     total = sum(times)
     value = len(times) / total
@@ -420,7 +421,7 @@ def run_ours(args, world, rank, local, pg):
     # ---- CPU baseline (rank 0, N = 1) -----------------------------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.quick:
-        dt, info = cpu_reference_solve(inst, args.tol)
+        dt, info = cpu_reference_solve(inst, args.tol, threads=args.cpu_threads)
         cpu = {'value': 1.0 / dt, 'unit': 'solves/s', 'cores': info['threads'], 'kind': info['kind'],
                'sample': f'one full FP64 solve of the workload at KKT<={args.tol:g} by {info["engine"]} '
                          f'({info["iterations"]} iterations, status {info["status"]})'}
@@ -775,6 +776,8 @@ def main():
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--tol', type=float, default=None, help='KKT tolerance (default 1e-6; 1e-7 for tridiagonal)')
     ap.add_argument('--quick', action='store_true', help='skip e2e, FP64 and CPU legs')
+    ap.add_argument('--cpu-threads', type=int, default=0,
+                    help='host threads of the reference CPU solve (cpu_baseline and --impl reference; 0: all cores)')
     ap.add_argument('--case', choices=['solve', 'step'], default=None,
                     help='profiling run instead of the benchmark: one solve, or the step kernel alone --steps times')
     args = ap.parse_args()

@@ -491,7 +491,10 @@ private:
     cudaEvent_t uev_ = nullptr;        // end of the latest upload on ustream_
     std::vector<Job*> uploaded_;       // uploaded, not yet installed (engine thread only)
     Job* uploading_ = nullptr;         // upload paused when a launch ended (engine thread, mu_)
-    static constexpr size_t kUploadChunk = size_t(32) << 20;  // bytes issued between launch tests
+    // bytes issued between launch tests: a pageable chunk holds the engine thread while the host
+    // stages it (about 0.05 ms for 8 MB at this host's ~200 GB/s), so the end of a launch is seen
+    // at most that late (32 MB chunks delayed the next launch by up to 0.45 ms)
+    static constexpr size_t kUploadChunk = size_t(8) << 20;
     // Between launches the engine thread uploads queued solves itself only up to this many input
     // bytes (always at least one solve when the device would otherwise idle); the rest upload
     // during the next launch, so a stream of large solves overlaps each upload with the
@@ -499,6 +502,8 @@ private:
     static constexpr size_t kSyncUploadBudget = size_t(64) << 20;
     bool launch_done_ = true;          // the host callback behind the current launch has run (mu_)
     double t_launch_done_ = 0;         // host time of that callback (BOXQP_PROFILE: gap to the next launch)
+    // BOXQP_PROFILE: host times of the steps between two launches (engine thread)
+    double t_synced_ = 0, t_collected_ = 0, t_freed_ = 0, t_gated_ = 0, t_installed_ = 0;
     cudaMemPool_t pool_ = nullptr;
 
     // device tables
@@ -563,6 +568,11 @@ private:
     double timer_ms_ = 0;
     int64_t timer_kernels_ = 0, timer_launches_ = 0;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    // the last re-arm, not waited for: its staging buffers are reused and its device time counted
+    // once it has completed (settle_rearm)
+    cudaEvent_t rev0_ = nullptr, rev1_ = nullptr;
+    bool rearm_pending_ = false;
+    bool settle_rearm(std::string& why);
     // launch mode: conditional graph (default) or host-driven stream launches (BOXQP_LAUNCH=stream;
     // per-kernel profilers cannot see kernels inside conditional graphs)
     bool stream_mode_ = false;
@@ -617,6 +627,8 @@ bool Engine::init(std::string& why) {
         for (auto& e : pev_) cudaEventCreate(&e);
     if (!cuda_ok(cudaEventCreate(&ev0_), why, "event")) return false;
     if (!cuda_ok(cudaEventCreate(&ev1_), why, "event")) return false;
+    if (!cuda_ok(cudaEventCreate(&rev0_), why, "event")) return false;
+    if (!cuda_ok(cudaEventCreate(&rev1_), why, "event")) return false;
     if (!cuda_ok(cudaMalloc(&d_ctrl_, sizeof(Ctrl)), why, "control block")) return false;
     if (!cuda_ok(cudaMemset(d_ctrl_, 0, sizeof(Ctrl)), why, "control block")) return false;
     if (!cuda_ok(cudaMallocHost(&h_ctrl_, sizeof(Ctrl)), why, "pinned control")) return false;
@@ -676,8 +688,12 @@ void Engine::shutdown() {
     }
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    if (rev0_) cudaEventDestroy(rev0_);
+    if (rev1_) cudaEventDestroy(rev1_);
     ev0_ = nullptr;
     ev1_ = nullptr;
+    rev0_ = nullptr;
+    rev1_ = nullptr;
     if (stream_) cudaStreamDestroy(stream_);
     if (capture_) cudaStreamDestroy(capture_);
     if (ustream_) cudaStreamDestroy(ustream_);
@@ -1126,6 +1142,9 @@ void Engine::reset_record(Job& j) {
 // Re-arms resident solves (bqp_resolve): one upload of the staged records and one kernel for the
 // whole batch.  Engine thread only.
 bool Engine::rearm(const std::vector<Job*>& batch, std::string& why) {
+    // the staging buffers are reused (or reallocated): the previous re-arm must have completed
+    // (in steady state it has, long before)
+    if (!settle_rearm(why)) return false;
     const int count = static_cast<int>(batch.size());
     int spans = 0;
     for (const Job* j : batch) spans += static_cast<int>((j->n + kRearmRows - 1) / kRearmRows);
@@ -1153,7 +1172,6 @@ bool Engine::rearm(const std::vector<Job*>& batch, std::string& why) {
         if (!cuda_ok(cudaMalloc(&d_spans_, sizeof(int2) * cap), why, "re-arm staging")) return false;
         span_cap_ = cap;
     }
-    // the staging buffers are reused: the previous re-arm has completed (it was synchronized)
     int s = 0;
     for (int k = 0; k < count; ++k) {
         Job& j = *batch[k];
@@ -1162,17 +1180,25 @@ bool Engine::rearm(const std::vector<Job*>& batch, std::string& why) {
         h_stage_slots_[k] = j.slot;
         for (int64_t r = 0; r < j.n; r += kRearmRows) h_spans_[s++] = int2{k, static_cast<int>(r)};
     }
-    cudaEventRecord(ev0_, stream_);
+    cudaEventRecord(rev0_, stream_);
     cudaMemcpyAsync(d_stage_, h_stage_, sizeof(InstDev) * count, cudaMemcpyHostToDevice, stream_);
     cudaMemcpyAsync(d_stage_slots_, h_stage_slots_, sizeof(int32_t) * count, cudaMemcpyHostToDevice, stream_);
     cudaMemcpyAsync(d_spans_, h_spans_, sizeof(int2) * spans, cudaMemcpyHostToDevice, stream_);
     launch_rearm(view(), d_stage_, d_stage_slots_, d_spans_, spans, stream_);
-    cudaEventRecord(ev1_, stream_);
-    if (!cuda_ok(cudaEventSynchronize(ev1_), why, "re-arm")) return false;
+    cudaEventRecord(rev1_, stream_);
     if (!cuda_ok(cudaGetLastError(), why, "re-arm kernel")) return false;
-    // re-arming resident solves is part of their device time: count it in the timer
+    rearm_pending_ = true;  // the next launch on stream_ runs after it
+    return true;
+}
+
+// Waits for the last re-arm (if any is outstanding) and counts its device time: re-arming
+// resident solves is part of their device time.
+bool Engine::settle_rearm(std::string& why) {
+    if (!rearm_pending_) return true;
+    if (!cuda_ok(cudaEventSynchronize(rev1_), why, "re-arm")) return false;
+    rearm_pending_ = false;
     float ms = 0;
-    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    cudaEventElapsedTime(&ms, rev0_, rev1_);
     std::lock_guard<std::mutex> g(mu_);
     timer_ms_ += ms;
     timer_kernels_ += 1;
@@ -1643,8 +1669,14 @@ bool Engine::run_once(std::string& why) {
     }
     if (host_profile()) {
         std::lock_guard<std::mutex> g(mu_);
-        std::fprintf(stderr, "[boxqp] launch: %d solves running, %.3f ms since the previous launch ended\n", n_running_,
-                     1e3 * (t0 - t_launch_done_));
+        // steps since the previous launch's callback: its stream synchronised, finished solves
+        // collected, frees, the admission gate read back, installation (each -1 when not run)
+        auto since = [&](double t) { return t >= t_launch_done_ ? 1e3 * (t - t_launch_done_) : -1.0; };
+        std::fprintf(stderr,
+                     "[boxqp] launch: %d solves running, %.3f ms since the previous launch ended (synced %.3f, "
+                     "collected %.3f, freed %.3f, gated %.3f, installed %.3f)\n",
+                     n_running_, 1e3 * (t0 - t_launch_done_), since(t_synced_), since(t_collected_), since(t_freed_),
+                     since(t_gated_), since(t_installed_));
     }
     cudaEventRecord(ev1_, stream_);
     cudaMemcpyAsync(h_status_, d_status_, sizeof(int32_t) * std::max(n_inst_, 1), cudaMemcpyDeviceToHost, stream_);
@@ -1663,6 +1695,8 @@ bool Engine::run_once(std::string& why) {
         if (launch_done_ || stop_) break;
     }
     if (!cuda_ok(cudaStreamSynchronize(stream_), why, "engine launch")) return false;
+    if (host_profile()) t_synced_ = host_seconds();
+    if (!settle_rearm(why)) return false;  // completed before the launch: no wait
     const double dt = host_seconds() - t0;
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
@@ -1887,6 +1921,7 @@ void Engine::loop() {
     std::unique_lock<std::mutex> lk(mu_);
     while (!stop_) {
         if (!pending_free_.empty()) process_frees();
+        if (host_profile()) t_freed_ = host_seconds();
         // an upload paused when the last launch ended continues during the next launch; only
         // when there is nothing else to run is it completed here
         if (uploading_ && n_running_ == 0 && uploaded_.empty()) finish_paused_upload(lk);
@@ -1961,7 +1996,9 @@ void Engine::loop() {
             lk.unlock();
             std::string why;
             bool ok = gate_uploaded(batch, refused, why);
+            if (host_profile()) t_gated_ = host_seconds();
             if (ok && !batch.empty()) ok = install(batch, why);
+            if (host_profile()) t_installed_ = host_seconds();
             lk.lock();
             for (Job* j : refused) finish_refused(j);
             for (Job* j : batch) {
@@ -2010,6 +2047,7 @@ void Engine::loop() {
             continue;
         }
         collect(lk);
+        if (host_profile()) t_collected_ = host_seconds();
     }
 }
 
