@@ -1637,7 +1637,9 @@ void Engine::upload_tables() {
 }
 
 bool Engine::run_once(std::string& why) {
+    const double t_enter = host_profile() ? host_seconds() : 0.0;
     upload_tables();
+    const double t_tables = host_profile() ? host_seconds() : 0.0;
     if (!stream_mode_ && !graph_valid_ && !build_graph(why)) return false;
     int cap = std::numeric_limits<int>::max() / 2;
     double latency;
@@ -1668,6 +1670,9 @@ bool Engine::run_once(std::string& why) {
         return false;
     }
     if (host_profile()) {
+        const double t_launched = host_seconds();
+        std::fprintf(stderr, "[boxqp] launch preparation: tables %.3f ms, control %.3f ms, graph launch %.3f ms\n",
+                     1e3 * (t_tables - t_enter), 1e3 * (t0 - t_tables), 1e3 * (t_launched - t0));
         std::lock_guard<std::mutex> g(mu_);
         // steps since the previous launch's callback: its stream synchronised, finished solves
         // collected, frees, the admission gate read back, installation (each -1 when not run)
