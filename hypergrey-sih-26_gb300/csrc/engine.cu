@@ -66,6 +66,7 @@ struct Layout {
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
     size_t sstep = kNone, lprec = kNone, s = kNone, gate = kNone;
+    size_t pc_inv = kNone, pc_e = kNone, pc_tile = kNone;
     size_t total = 0;
 };
 
@@ -116,6 +117,9 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.start_ff = take(N * 4);
         L.sstep = take(N * 4);
         L.s = take(N * 8);
+        L.pc_inv = take(N * 8);
+        L.pc_e = take(N * 8);
+        L.pc_tile = take(static_cast<size_t>(tiles) * 4);
     } else {
         L.x64 = take(N * 8);
         L.w64a = take(N * 8);
@@ -1299,6 +1303,10 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.dinv = at<double>(slab, L.dinv);
     R.free_rows = at<int32_t>(slab, L.free_rows);
     R.free_cnt = at<int32_t>(slab, L.free_cnt);
+    R.pc_inv = at<double>(slab, L.pc_inv);
+    R.pc_e = at<double>(slab, L.pc_e);
+    R.pc_tile = at<int32_t>(slab, L.pc_tile);
+    R.pc_unused = nullptr;
     R.col_ff = at<int32_t>(slab, L.col_ff);
     R.hi_ff = at<float>(slab, L.hi_ff);
     R.lo_ff = at<float>(slab, L.lo_ff);

@@ -134,6 +134,10 @@ struct __align__(16) InstDev {
     float* lo_ff;          //   [rowptr[row_begin], ...): row r at [start_ff[r], + cnt_ff[r])
     int32_t* cnt_ff;
     int32_t* start_ff;
+    double* pc_inv;        // polish preconditioner, per free-list position: 1 / pivot of the chain factorization
+    double* pc_e;          //   and the kept coupling to the next position (0 ends a chain)
+    int32_t* pc_tile;      //   per tile (index within the instance): 1 when the tile has a chain
+    void* pc_unused;       //   (keeps the record a multiple of 16 bytes)
     // geometry (the instance's tile range lives in View::ranges)
     int32_t n;
     int32_t diag_gate;

@@ -1109,7 +1109,7 @@ __device__ int block_exclusive_scan(int32_t* v, int n) {
 
 template <int LANES>
 __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list, int n, int base,
-                              const int32_t* __restrict__ start_of, float2* rowsum, Acc& a) {
+                              const int32_t* __restrict__ start_of, float2* rowsum, float2* coupling, Acc& a) {
     constexpr int R = 32 / LANES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / LANES, sl = lane % LANES;
@@ -1121,9 +1121,6 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     const float* __restrict__ vlo = I.vlo;
     const uint8_t* __restrict__ fixed = I.fixed;
     const float2* __restrict__ xp2 = I.xp2;
-    const double* __restrict__ c = I.c;
-    const double* __restrict__ dinv = I.dinv;
-    const double* __restrict__ xp = I.xp;
     int32_t* __restrict__ col_ff = I.col_ff;
     float* __restrict__ hi_ff = I.hi_ff;
     float* __restrict__ lo_ff = I.lo_ff;
@@ -1131,11 +1128,6 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     // product reads them without first loading the row index)
     int32_t* __restrict__ cnt_ff = I.cnt_ff + (list - I.free_rows);
     int32_t* __restrict__ start_ff = I.start_ff + (list - I.free_rows);
-    double* __restrict__ r_out = I.r;
-    double* __restrict__ z_out = I.z;
-    double* __restrict__ p_out = I.p;
-    double* __restrict__ s_out = I.s;
-    float2* __restrict__ p2_out = I.p2;
     for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
         const int j = g * R + sub;
         int r = -1, ks = 0, len = 0, dst = 0;
@@ -1147,6 +1139,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
         }
         const int wmax = __reduce_max_sync(0xffffffffu, len);
         float2 acc = make_float2(0.f, 0.f);
+        float2 e_next = make_float2(0.f, 0.f);  // Q(r, r + 1), the coupling to the adjacent row
         int kept = 0;
         for (int i = 0; i < wmax; i += LANES) {  // warp-uniform
             const bool valid = i + sl < len;
@@ -1160,6 +1153,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
                 lo = __ldg(vlo + k);
                 acc = df_add(acc, df_prod2(h, lo, xp2[cc]));
                 keep = !fixed[cc];
+                if (cc == r + 1) e_next = make_float2(e_next.x + h, e_next.y + lo);
             }
             const unsigned m = __ballot_sync(0xffffffffu, keep);
             if (keep) {
@@ -1171,20 +1165,67 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
             kept += __popc(m & group);
         }
 #pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1) acc = df_add(acc, shfl_xor(acc, o));
+        for (int o = LANES / 2; o > 0; o >>= 1) {
+            acc = df_add(acc, shfl_xor(acc, o));
+            e_next.x += __shfl_xor_sync(0xffffffffu, e_next.x, o);
+            e_next.y += __shfl_xor_sync(0xffffffffu, e_next.y, o);
+        }
         if (sl == 0 && r >= 0) {
             cnt_ff[j] = kept;
             start_ff[j] = dst;
             rowsum[j] = acc;
+            coupling[j] = e_next;
         }
     }
-    // the FP64 epilogue, one free row per thread (full warps: an FP64 warp instruction costs the
-    // same with 1 or 32 active lanes)
+}
+
+// The residual pass's FP64 epilogue over a tile's free rows (list positions t < n, after a block
+// barrier): r = -(Q xp + c), the preconditioned z = M^-1 r, p = z, s = 0, and the CG reduction's
+// r.z and max |r|/(1+|x|).  M is the polish's preconditioner: the tridiagonal part of Q_FF within
+// the tile, Q(r, r + 1) between free rows adjacent in the list and in Q, kept only where both
+// rows stay strictly diagonally dominant with their couplings (so every pivot of the chain's
+// LDL' factorization is positive and M is positive definite) and cut every kChain list positions
+// (so a tile's chains run on up to 16 threads); a row without kept couplings is a Jacobi row
+// (1/Q_rr).  On the tridiagonal family M is Q_FF within runs of up to kChain free rows, on the
+// grid it couples the free runs of each grid row (line relaxation), on a random graph it is the
+// Jacobi preconditioner.  A tile without chains runs the Jacobi rows alone (pc_tile 0: the vector
+// step's single pass); otherwise each chain is factored and solved in shared memory by one thread
+// (Thomas recurrence: pivots m_0 = Q_00, m_i = Q_ii - e_{i-1}^2 / m_{i-1}), and 1/m and the kept
+// coupling are stored per list position for the vector step.
+constexpr int kChain = 32;
+constexpr int kChainMin = 8;
+
+// Sum of one int per thread over the block (every thread gets the total); block-wide barriers.
+__device__ int block_sum_int(int v) {
+    __shared__ int part[kBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
-    for (int t = threadIdx.x; t < n; t += kBlock) {
-        const int r = list[t];
-        const double rr = -(df_value(rowsum[t]) + c[r]);
-        const double zz = rr * dinv[r];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int total = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) total += part[w];
+    return total;
+}
+
+__device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ list, int n, int tile,
+                                  const float2* rowsum, const float2* coupling, Acc& a) {
+    __shared__ double res[kTileRows];  // r per list position
+    __shared__ double dg[kTileRows];   // Q_rr per list position
+    __shared__ double ec[kTileRows];   // coupling to the next position; then the forward values
+    __shared__ double ek[kTileRows];   // kept coupling
+    __shared__ double zs[kTileRows];   // z of the chain rows
+    const double* __restrict__ c = I.c;
+    const double* __restrict__ dinv = I.dinv;
+    const double* __restrict__ diag = I.diag;
+    const double* __restrict__ xp = I.xp;
+    double* __restrict__ r_out = I.r;
+    double* __restrict__ z_out = I.z;
+    double* __restrict__ p_out = I.p;
+    double* __restrict__ s_out = I.s;
+    float2* __restrict__ p2_out = I.p2;
+    auto row_out = [&](int r, double rr, double zz) {
         a.a = fma(rr, zz, a.a);
         a.b = umax64(a.b, cg_ratio_bits(rr, xp[r]));
         r_out[r] = rr;
@@ -1192,6 +1233,112 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
         p_out[r] = zz;
         s_out[r] = 0.0;
         p2_out[r] = df_split(zz);
+    };
+    bool any = false;
+    for (int t = threadIdx.x; t < n; t += kBlock) {
+        const int r = list[t];
+        res[t] = -(df_value(rowsum[t]) + c[r]);
+        double e = 0.0;
+        if (t + 1 < n && list[t + 1] == r + 1 && (t + 1) % kChain != 0)
+            e = static_cast<double>(coupling[t].x) + coupling[t].y;
+        ec[t] = e;
+        if (e != 0.0) {
+            any = true;
+            dg[t] = diag[r];
+        }
+        if (t > 0 && list[t - 1] == r - 1) dg[t] = diag[r];  // a possible chain row's pivot source
+    }
+    bool chains = __syncthreads_or(any) != 0;
+    if (chains) {
+        bool kept_any = false;
+        for (int t = threadIdx.x; t < n; t += kBlock) {
+            const double e = ec[t];
+            bool keep = false;
+            if (e != 0.0) {
+                const double left = t > 0 ? fabs(ec[t - 1]) : 0.0;
+                keep = left + fabs(e) < dg[t] && fabs(e) + fabs(ec[t + 1]) < dg[t + 1];
+            }
+            ek[t] = keep ? e : 0.0;
+            kept_any |= keep;
+        }
+        chains = __syncthreads_or(kept_any) != 0;
+        if (chains) {
+            // chains pay for their sequential solves only when they are long: a tile keeps them
+            // when its chained rows average kChainMin or more per chain.  Measured on the 1024^2
+            // grid (free runs of about 2.5 rows, 3.7 among chained rows): chains took CG from 24
+            // to 19 iterations but the vector step from 21 to 45 us, 1.90 -> 2.15 ms per solve,
+            // and tiles averaging 4 or more still cost 2.06 ms; on the tridiagonal family (every
+            // variable free, chains at the kChain cap) CG falls from 78 to 8 iterations.
+            int in_chain = 0, heads = 0;
+            for (int t = threadIdx.x; t < n; t += kBlock) {
+                const bool left = t > 0 && ek[t - 1] != 0.0;
+                if (ek[t] != 0.0 || left) ++in_chain;
+                if (ek[t] != 0.0 && !left) ++heads;
+            }
+            const int rows_in_chains = block_sum_int(in_chain);
+            const int n_chains = block_sum_int(heads);
+            chains = rows_in_chains >= kChainMin * n_chains;
+        }
+    }
+    if (threadIdx.x == 0) I.pc_tile[tile] = chains ? 1 : 0;
+    if (!chains) {
+        for (int t = threadIdx.x; t < n; t += kBlock) {
+            const int r = list[t];
+            row_out(r, res[t], res[t] * dinv[r]);
+        }
+        return;
+    }
+    const int q0 = static_cast<int>(list - I.free_rows);  // list position t is q0 + t in pc_inv / pc_e
+    double* __restrict__ pc_inv = I.pc_inv + q0;
+    double* __restrict__ pc_e = I.pc_e + q0;
+    // chains of two or more rows, one thread each, in shared memory; the chains are numbered
+    // densely so that consecutive lanes take them (an FP64 warp instruction costs the same with 1
+    // or 32 active lanes); each chain's arithmetic does not depend on which thread runs it
+    __shared__ int32_t starts[kTileRows / 2];
+    __shared__ int n_starts;
+    if (threadIdx.x == 0) n_starts = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += kBlock)
+        if (ek[t] != 0.0 && (t == 0 || ek[t - 1] == 0.0)) starts[atomicAdd(&n_starts, 1)] = t;
+    __syncthreads();
+    for (int k = threadIdx.x; k < n_starts; k += kBlock) {
+        const int t = starts[k];
+        int end = t;
+        while (ek[end] != 0.0) ++end;  // ek[n - 1] == 0
+        double inv = 1.0 / dg[t];
+        double y = res[t] * inv;
+        pc_inv[t] = inv;
+        pc_e[t] = ek[t];
+        ec[t] = y;
+        for (int i = t + 1; i <= end; ++i) {
+            const double e = ek[i - 1];
+            inv = 1.0 / (dg[i] - e * e * inv);
+            y = (res[i] - e * y) * inv;
+            pc_inv[i] = inv;
+            pc_e[i] = ek[i];
+            ec[i] = y;
+        }
+        double z = ec[end];
+        zs[end] = z;
+        for (int i = end - 1; i >= t; --i) {
+            z = ec[i] - ek[i] * pc_inv[i] * z;
+            zs[i] = z;
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += kBlock) {
+        const int r = list[t];
+        const bool in_chain = ek[t] != 0.0 || (t > 0 && ek[t - 1] != 0.0);
+        double zz;
+        if (in_chain) {
+            zz = zs[t];
+        } else {  // a Jacobi row
+            const double inv = dinv[r];
+            pc_inv[t] = inv;
+            pc_e[t] = 0.0;
+            zz = res[t] * inv;
+        }
+        row_out(r, res[t], zz);
     }
 }
 
@@ -1295,29 +1442,35 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
 
 template <int LANES>
 __device__ int residual_tile(const InstDev& I, const int32_t* list, int n_free, int base, int32_t* start_of,
-                             float2* rowsum, Acc& a) {
+                             float2* rowsum, float2* coupling, Acc& a) {
     count_kept<LANES>(I, list, n_free, start_of);
     __syncthreads();
     const int kept = block_exclusive_scan(start_of, n_free);
-    residual_rows<LANES>(I, list, n_free, base, start_of, rowsum, a);
+    residual_rows<LANES>(I, list, n_free, base, start_of, rowsum, coupling, a);
     return kept;
 }
 
-// Residual (with the packing of Q_FF) over tile rows [rb, ...) of one instance; returns the
-// tile's packed Q_FF entries.
-__device__ int polish_rows(const InstDev& I, int rb, int n_free, Acc& a) {
+// Residual (with the packing of Q_FF) over tile rows [rb, ...) of one instance (its tile index
+// `tile` within the instance); returns the tile's packed Q_FF entries.
+__device__ int polish_rows(const InstDev& I, int rb, int tile, int n_free, Acc& a) {
     __shared__ int32_t start_of[kTileRows];  // free-list positions of the packed rows
     __shared__ float2 rowsum[kTileRows];     // row sums handed to the FP64 epilogue
+    __shared__ float2 coupling[kTileRows];   // Q(r, r + 1) of each free row (hi, lo)
     const int32_t* list = I.free_rows + rb;
     const int base = __ldg(I.rowptr + rb);
+    int kept;
     switch (I.lanes_res) {
-    case 1: return residual_tile<1>(I, list, n_free, base, start_of, rowsum, a);
-    case 2: return residual_tile<2>(I, list, n_free, base, start_of, rowsum, a);
-    case 4: return residual_tile<4>(I, list, n_free, base, start_of, rowsum, a);
-    case 8: return residual_tile<8>(I, list, n_free, base, start_of, rowsum, a);
-    case 16: return residual_tile<16>(I, list, n_free, base, start_of, rowsum, a);
-    default: return residual_tile<32>(I, list, n_free, base, start_of, rowsum, a);
+    case 1: kept = residual_tile<1>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
+    case 2: kept = residual_tile<2>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
+    case 4: kept = residual_tile<4>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
+    case 8: kept = residual_tile<8>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
+    case 16: kept = residual_tile<16>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
+    default: kept = residual_tile<32>(I, list, n_free, base, start_of, rowsum, coupling, a); break;
     }
+    // the FP64 epilogue, one free row (or one chain of rows) per thread on full warps
+    __syncthreads();
+    residual_epilogue(I, list, n_free, tile, rowsum, coupling, a);
+    return kept;
 }
 
 // Four blocks per SM (64 registers, a few spills): 2.307 ms per 1M random-graph solve against
@@ -1331,7 +1484,7 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
         const int2 R = v.ranges[T.inst];
         Acc a = acc_identity();
         const int n_free = I.free_cnt[t - R.x];
-        const int kept = polish_rows(I, T.row_begin, n_free, a);
+        const int kept = polish_rows(I, T.row_begin, t - R.x, n_free, a);
         if (threadIdx.x == 0) {  // Q_FF size of this polish round, for the byte accounting
             atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_nnz), static_cast<unsigned long long>(kept));
             atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_rows), static_cast<unsigned long long>(n_free));
@@ -1432,6 +1585,7 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
         ctrl->kernels += 2;
         cudaGraphSetConditional(h_cg, (ctrl->n_cg > 0 && it < cap) ? 1u : 0u);
     }
+
     const int nt = v.ctrl->n_tiles;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
         const Tile T = v.tiles[t];
@@ -1449,18 +1603,81 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
             double* __restrict__ xp = I.xp;
             double* __restrict__ rr_v = I.r;
             float2* __restrict__ u2 = I.p2;
-            for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                const int r = list[j];
-                const double pn = fma(beta, p[r], u[r]);
-                const double sn = fma(beta, s[r], w[r]);
-                const double rn = fma(-alpha, sn, rr_v[r]);
-                const double un = rn * dinv[r];
-                p[r] = pn;
-                s[r] = sn;
-                xp[r] = fma(alpha, pn, xp[r]);
-                rr_v[r] = rn;
-                u[r] = un;
-                u2[r] = df_split(un);
+            const int tile = t - v.ranges[T.inst].x;
+            if (!I.pc_tile[tile]) {  // Jacobi rows only: u = r / Q_rr
+                for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                    const int r = list[j];
+                    const double pn = fma(beta, p[r], u[r]);
+                    const double sn = fma(beta, s[r], w[r]);
+                    const double rn = fma(-alpha, sn, rr_v[r]);
+                    const double un = rn * dinv[r];
+                    p[r] = pn;
+                    s[r] = sn;
+                    xp[r] = fma(alpha, pn, xp[r]);
+                    rr_v[r] = rn;
+                    u[r] = un;
+                    u2[r] = df_split(un);
+                }
+            } else {
+                // the residual pass's chains (pc_e links a position to the next): the updates
+                // first; then the Jacobi rows in parallel and one thread per chain (the chains
+                // numbered densely, so consecutive lanes share the FP64 warp instructions), in
+                // shared memory; then the stores of u
+                __shared__ double rs[kTileRows];
+                __shared__ double ys[kTileRows];
+                __shared__ double pi[kTileRows];
+                __shared__ double pe[kTileRows];
+                __shared__ int32_t starts[kTileRows / 2];
+                __shared__ int n_starts_s;
+                int* n_starts = &n_starts_s;
+                if (threadIdx.x == 0) n_starts_s = 0;
+                const int q0 = T.row_begin;  // list position j is q0 + j in pc_inv / pc_e
+                const double* __restrict__ pc_inv = I.pc_inv + q0;
+                const double* __restrict__ pc_e = I.pc_e + q0;
+                for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                    const int r = list[j];
+                    const double pn = fma(beta, p[r], u[r]);
+                    const double sn = fma(beta, s[r], w[r]);
+                    const double rn = fma(-alpha, sn, rr_v[r]);
+                    p[r] = pn;
+                    s[r] = sn;
+                    xp[r] = fma(alpha, pn, xp[r]);
+                    rr_v[r] = rn;
+                    rs[j] = rn;
+                    pi[j] = pc_inv[j];
+                    pe[j] = pc_e[j];
+                }
+                __syncthreads();
+                for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                    const bool linked_left = j > 0 && pe[j - 1] != 0.0;
+                    if (pe[j] == 0.0 && !linked_left) ys[j] = rs[j] * pi[j];  // a Jacobi row
+                    else if (!linked_left) starts[atomicAdd(n_starts, 1)] = j;
+                }
+                __syncthreads();
+                const int chains = *n_starts;
+                for (int k = static_cast<int>(threadIdx.x); k < chains; k += kBlock) {
+                    const int j = starts[k];
+                    double y = rs[j] * pi[j];
+                    ys[j] = y;
+                    int end = j;
+                    while (pe[end] != 0.0) {
+                        ++end;
+                        y = (rs[end] - pe[end - 1] * y) * pi[end];
+                        ys[end] = y;
+                    }
+                    double un = y;
+                    for (int i = end - 1; i >= j; --i) {
+                        un = ys[i] - pe[i] * pi[i] * un;
+                        ys[i] = un;
+                    }
+                }
+                __syncthreads();
+                for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                    const int r = list[j];
+                    u[r] = ys[j];
+                    u2[r] = df_split(ys[j]);
+                }
+                __syncthreads();  // the shared arrays are reused by the block's next chain tile
             }
         } else if (I.phase == PH_POLISH_FINISH) {
             const double* __restrict__ l = I.l;
