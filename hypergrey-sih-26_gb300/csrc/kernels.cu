@@ -1185,14 +1185,17 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
 // the tile, Q(r, r + 1) between free rows adjacent in the list and in Q, kept only where both
 // rows stay strictly diagonally dominant with their couplings (so every pivot of the chain's
 // LDL' factorization is positive and M is positive definite) and cut every kChain list positions
-// (so a tile's chains run on up to 16 threads); a row without kept couplings is a Jacobi row
+// (so a tile's long runs split over several threads); a row without kept couplings is a Jacobi row
 // (1/Q_rr).  On the tridiagonal family M is Q_FF within runs of up to kChain free rows, on the
 // grid it couples the free runs of each grid row (line relaxation), on a random graph it is the
 // Jacobi preconditioner.  A tile without chains runs the Jacobi rows alone (pc_tile 0: the vector
 // step's single pass); otherwise each chain is factored and solved in shared memory by one thread
 // (Thomas recurrence: pivots m_0 = Q_00, m_i = Q_ii - e_{i-1}^2 / m_{i-1}), and 1/m and the kept
 // coupling are stored per list position for the vector step.
-constexpr int kChain = 32;
+// Chain cap, measured on the tridiagonal family (every variable free, 1M rows): 16 / 32 / 64 /
+// 128 / 256 / 512 positions: 2.09 / 1.69 / 1.44 / 1.47 / 2.01 / 3.08 ms per solve (15 / 10 / 6 /
+// 4 / 4 / 4 CG iterations): longer chains precondition better but solve sequentially.
+constexpr int kChain = 64;
 constexpr int kChainMin = 8;
 
 // Sum of one int per thread over the block (every thread gets the total); block-wide barriers.
@@ -1268,7 +1271,7 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
             // grid (free runs of about 2.5 rows, 3.7 among chained rows): chains took CG from 24
             // to 19 iterations but the vector step from 21 to 45 us, 1.90 -> 2.15 ms per solve,
             // and tiles averaging 4 or more still cost 2.06 ms; on the tridiagonal family (every
-            // variable free, chains at the kChain cap) CG falls from 78 to 8 iterations.
+            // variable free, chains at the kChain cap) CG falls from 78 to 6 iterations.
             int in_chain = 0, heads = 0;
             for (int t = threadIdx.x; t < n; t += kBlock) {
                 const bool left = t > 0 && ek[t - 1] != 0.0;
