@@ -437,6 +437,39 @@ def test_mixed_mode_with_and_without_preconditioned_steps(engine, preset, n, see
     assert active_set_ok(inst, x)
 
 
+def test_polish_chains_on_the_tridiagonal_family(engine):
+    """The polish's chain preconditioner (Q_FF's tridiagonal part solved along runs of free rows)
+    on the reference's tridiagonal family, every variable free: verified by the oracle at 1e-7, on
+    the planted optimum, in a handful of CG iterations (Jacobi rows alone need about 78)."""
+    inst = boxqp.planted('tridiagonal', seed=3, n=200000, lower_triplets=True)
+    o = boxqp.options_struct(1e-7, 30.0, 20000, 'mixed')
+    x, st = engine.solve(inst['rowptr'], inst['col'], inst['val'], inst['c'], inst['lower'], inst['upper'], o)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+    chk = O.check(*planted_args(inst), x, tol=1e-7)
+    assert chk['verified'] == 1.0, chk
+    assert abs(chk['objective'] - inst['fstar']) / (1 + abs(inst['fstar'])) <= 1e-7
+    assert 0 < st.polish_iterations <= 12, st.polish_iterations
+
+
+def test_polish_chains_drop_couplings_that_break_strict_dominance(engine):
+    """Rows whose diagonal only equals their off-diagonal sum (weakly dominant: 2 = |-1| + |-1|)
+    lose their couplings in the preconditioner, which stays positive definite; the solve still
+    verifies against the oracle."""
+    inst = boxqp.planted('tridiagonal', seed=5, n=20000, lower_triplets=True)
+    rowptr, col, val = inst['rowptr'], inst['col'], inst['val'].copy()
+    hrow, hcol, hval = inst['hrow'], inst['hcol'], inst['hval'].copy()
+    weak = np.arange(inst['n']) % 3 == 1
+    for r in np.nonzero(weak)[0]:
+        k = rowptr[r] + np.nonzero(col[rowptr[r]:rowptr[r + 1]] == r)[0][0]
+        val[k] = 2.0
+    hval[(hrow == hcol) & weak[hrow]] = 2.0
+    o = boxqp.options_struct(1e-7, 30.0, 20000, 'mixed')
+    x, st = engine.solve(rowptr, col, val, inst['c'], inst['lower'], inst['upper'], o)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+    chk = O.check(hrow, hcol, hval, inst['c'], inst['lower'], inst['upper'], x, tol=1e-7)
+    assert chk['verified'] == 1.0, chk
+
+
 def test_nonconvex_hessian_is_reported_before_solving(engine):
     """check_convex_hessian runs first (src/accelerated_qp.cpp:19): an indefinite Q gets
     unsupported_curvature from the C-ABI solve; a PSD but not diagonally dominant Q solves."""
@@ -509,7 +542,8 @@ def test_mixed_precisions_and_structures_in_one_batch_equal_solo(engine):
     for k, (preset, n, prec, variant) in enumerate([('graph10k', 2000, 'mixed', -1), ('grid', 64 * 64, 'mixed', -1),
                                                     ('graph10k', 2500, 'fp64', -1), ('tridiagonal', 3000, 'fp64', 2),
                                                     ('graph10k', 1500, 'fp64_exact', -1), ('graph10k', 1800, 'mixed', 8),
-                                                    ('grid', 48 * 48, 'fp64', 64), ('graph10k', 2200, 'mixed', 0)]):
+                                                    ('grid', 48 * 48, 'fp64', 64), ('graph10k', 2200, 'mixed', 0),
+                                                    ('tridiagonal', 3000, 'mixed', -1)]):
         inst = boxqp.planted(preset, seed=40 + k, n=n)
         o = boxqp.options_struct(1e-7, 60.0, 200000, prec, kernel_variant=variant)
         cases.append((inst, o))
