@@ -288,6 +288,23 @@ int default_variant(int64_t n, int64_t nnz, int precision) {
     return VAR_TILE;
 }
 
+// Tiles per CG work unit of one instance (its `count` tiles at t): enough that its units fit the
+// product kernel's `slots` resident blocks in one round (a second round of units would run on part
+// of the GPU only), within [kCgUnitMin, kCgUnitMax], with no unit above kCgRowsum rows (the row
+// sums' shared buffer; kCgUnitMin tiles always fit).  Depends on the instance alone, so the
+// product's partial sums, and the CG iterates, are the same in a batch as solo.
+int cg_unit_tiles(const Tile* t, int count, int slots) {
+    int k = slots > 0 ? (count + slots - 1) / slots : kCgUnitMin;
+    k = std::min(kCgUnitMax, std::max(kCgUnitMin, k));
+    for (; k > kCgUnitMin; --k) {
+        bool fits = true;
+        for (int u = 0; u < count && fits; u += k)
+            fits = t[std::min(count, u + k) - 1].row_end - t[u].row_begin <= kCgRowsum;
+        if (fits) break;
+    }
+    return k;
+}
+
 // Row tiles of one instance: contiguous rows with about kTileNnz nonzeros and at most
 // kTileRows rows, the row count rounded down to a multiple of 256 (one 32-row group per warp of
 // a block) or else of 32 where that many fit, so that the warps of a block finish a tile together.
@@ -487,6 +504,7 @@ private:
     size_t cap_;
     int sms_ = 152;
     int grid_max_ = 152 * 8;
+    int cg_slots_ = 152 * 4;  // resident blocks of the CG product kernel
     cudaStream_t stream_ = nullptr;
     cudaStream_t capture_ = nullptr;
     cudaStream_t ustream_ = nullptr;   // uploads of new solves, overlapping the running graph
@@ -536,12 +554,12 @@ private:
     std::vector<Job*> slot_job_;
     std::vector<int32_t> slot_prec_;      // precision of the solve in each slot
     std::vector<int32_t> h_group_tiles_;  // tile indices ordered by step group
-    std::vector<int32_t> h_units_;        // first tile of each CG work unit
+    std::vector<int2> h_units_;           // CG work units: first tile, tiles per unit
     int32_t group_begin_[kStepGroups + 1] = {};
     uint32_t groups_present_ = 0;         // step groups with tiles
     uint32_t graph_groups_ = 0;           // step groups the graph launches
     int32_t* d_group_tiles_ = nullptr;
-    int32_t* d_units_ = nullptr;
+    int2* d_units_ = nullptr;
     std::vector<int> free_slots_;
     int n_inst_ = 0;
     bool tables_dirty_ = false;
@@ -607,6 +625,7 @@ bool Engine::init(std::string& why) {
     if (!cuda_ok(cudaSetDevice(device_), why, "set device")) return false;
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_);
     grid_max_ = tile_grid(sms_);
+    cg_slots_ = cg_matvec_slots();
     if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&ustream_, cudaStreamNonBlocking), why, "stream")) return false;
@@ -746,11 +765,11 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
         Tile* tiles = nullptr;
         Partial* partial = nullptr;
         int32_t* group_tiles = nullptr;
-        int32_t* units = nullptr;
+        int2* units = nullptr;
         if (!cuda_ok(cudaMalloc(&tiles, sizeof(Tile) * cap), why, "tile table")) return false;
         if (!cuda_ok(cudaMalloc(&partial, sizeof(Partial) * cap), why, "partials")) return false;
         if (!cuda_ok(cudaMalloc(&group_tiles, sizeof(int32_t) * cap), why, "step groups")) return false;
-        if (!cuda_ok(cudaMalloc(&units, sizeof(int32_t) * cap), why, "CG work units")) return false;
+        if (!cuda_ok(cudaMalloc(&units, sizeof(int2) * cap), why, "CG work units")) return false;
         cudaFree(d_tiles_);
         cudaFree(d_partial_);
         cudaFree(d_group_tiles_);
@@ -1306,7 +1325,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.pc_inv = at<double>(slab, L.pc_inv);
     R.pc_e = at<double>(slab, L.pc_e);
     R.pc_tile = at<int32_t>(slab, L.pc_tile);
-    R.pc_unused = nullptr;
+    R.stat_floor = 0;
     R.col_ff = at<int32_t>(slab, L.col_ff);
     R.hi_ff = at<float>(slab, L.hi_ff);
     R.lo_ff = at<float>(slab, L.lo_ff);
@@ -1633,13 +1652,17 @@ void Engine::upload_tables() {
     if (!h_group_tiles_.empty())
         cudaMemcpyAsync(d_group_tiles_, h_group_tiles_.data(), sizeof(int32_t) * h_group_tiles_.size(),
                         cudaMemcpyHostToDevice, stream_);
-    // CG work units: runs of kCgUnit consecutive tiles of one instance, counted from the
+    // CG work units: runs of cg_unit_tiles consecutive tiles of one instance, counted from the
     // instance's first tile (so a unit depends on the instance alone, not on the batch)
     h_units_.clear();
-    for (int k = 0; k < static_cast<int>(h_tiles_.size()); ++k)
-        if ((k - h_ranges_[h_tiles_[k].inst].x) % kCgUnit == 0) h_units_.push_back(k);
+    for (int i = 0; i < n_inst_; ++i) {
+        const int2 R = h_ranges_[i];
+        if (R.y <= R.x) continue;
+        const int k = cg_unit_tiles(h_tiles_.data() + R.x, R.y - R.x, cg_slots_);
+        for (int t = R.x; t < R.y; t += k) h_units_.push_back(make_int2(t, k));
+    }
     if (!h_units_.empty())
-        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int32_t) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int2) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
     cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
     // the pageable sources above are copied out before cudaMemcpyAsync returns
     if (groups_present_ & ~graph_groups_) graph_valid_ = false;

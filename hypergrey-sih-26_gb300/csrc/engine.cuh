@@ -15,8 +15,11 @@ constexpr int kBlock = 256;          // threads per CTA of every tile kernel
 constexpr int kMaxInterval = 32;     // maximum check interval (iterations per chunk)
 constexpr int kTileNnz = 4096;       // target nonzeros per tile
 constexpr int kTileRows = 512;       // maximum rows per tile
-constexpr int kCgUnit = 4;           // tiles per work unit of the polish CG product kernel
+constexpr int kCgUnitMin = 4;        // tiles per work unit of the polish CG product kernel: at least
+constexpr int kCgUnitMax = 8;        //   this many, and up to this many for large instances (cg_unit_tiles)
+constexpr int kCgRowsum = kCgUnitMin * kTileRows;  // rows per CG work unit at most (its row sums, 16 KB)
 constexpr int kCgGroups = 2;         // row groups per warp whose loads the CG product keeps in flight
+constexpr int kCgUnroll = 2;         // entries per row group and lane (and epilogue rows per thread) per pass of the CG product
 constexpr int kRearmRows = 8192;     // rows per block when re-arming resident solves
 constexpr int64_t kHostPrimal = 131072;  // primals up to this size come back at completion, larger at fetch
 
@@ -137,7 +140,8 @@ struct __align__(16) InstDev {
     double* pc_inv;        // polish preconditioner, per free-list position: 1 / pivot of the chain factorization
     double* pc_e;          //   and the kept coupling to the next position (0 ends a chain)
     int32_t* pc_tile;      //   per tile (index within the instance): 1 when the tile has a chain
-    void* pc_unused;       //   (keeps the record a multiple of 16 bytes)
+    unsigned long long stat_floor;  // within a running check: the largest stationarity ratio (FP64
+                                    // bits) published so far; rows that cannot exceed it skip the division
     // geometry (the instance's tile range lives in View::ranges)
     int32_t n;
     int32_t diag_gate;
@@ -231,8 +235,8 @@ struct View {
     int32_t* status_mirror;  // per-instance status, rewritten by the control kernel every body
     const int2* ranges;      // per-instance tile range [x, y) in the tile table
     const int32_t* group_tiles;  // tile indices ordered by step group (Ctrl::group_begin)
-    const int32_t* units;        // CG work units: the first tile of each run of kCgUnit consecutive
-                                 // tiles of one instance (instance-local tile index a multiple of kCgUnit)
+    const int2* units;           // CG work units: x the first tile of a run of y consecutive tiles of one
+                                 // instance (y fixed per instance, x - its first tile a multiple of y)
 };
 
 }  // namespace bqp

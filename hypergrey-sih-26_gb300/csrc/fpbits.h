@@ -1,8 +1,9 @@
-// FP64 -> FP32 conversions in integer arithmetic on the IEEE 754 bit patterns, for the admission
-// pass over the nonzeros.  GB300 issues FP64 instructions (conversions included) at 1/64 of the
-// FP32 rate, so a per-nonzero F2F or DADD costs about 30 us on 15M nonzeros; these forms keep
-// that pass on the integer and FP32 pipes.  Host and device share them, so the host tests check
-// them against the C library's conversions.
+// FP64 <-> FP32 conversions and FP64 comparisons in integer arithmetic on the IEEE 754 bit
+// patterns, for the admission pass over the nonzeros and the per-row epilogues of the checks and
+// the polish.  GB300 issues FP64 instructions (conversions and comparisons included) at 1/64 of
+// the FP32 rate, so a per-nonzero F2F or DADD costs about 30 us on 15M nonzeros; these forms keep
+// that work on the integer and FP32 pipes.  Host and device share them, so the host tests check
+// them against the C library's conversions and comparisons.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -15,9 +16,17 @@
 
 namespace bqp {
 
+// The bit pattern of v.  On the device it comes out of an opaque move: the compiler folds masks
+// and comparisons of a plain reinterpretation back into FP64 instructions (x & ~sign becomes
+// |x|, materialized by an FP64 add; exponent tests become FP64 compares), which is the work these
+// forms exist to avoid.
 BQP_HD uint64_t bits64(double v) {
     uint64_t b;
+#ifdef __CUDA_ARCH__
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
+#else
     memcpy(&b, &v, sizeof b);
+#endif
     return b;
 }
 
@@ -99,6 +108,69 @@ BQP_HD uint64_t widen_bits(uint32_t f) {
     if (f == 0) return 0;
     if (f >= 0x7f800000u) return 0x7ff0000000000000ull;
     return (static_cast<uint64_t>(f) + (896ull << 23)) << 29;
+}
+
+// FP64 bits of a float of either sign that is zero or normal; false for subnormals, infinities
+// and NaNs, which the caller converts with an FP64 instruction.
+BQP_HD bool widen_signed_bits(uint32_t f, uint64_t& d) {
+    const uint32_t mag = f & 0x7fffffffu;
+    const uint64_t sign = static_cast<uint64_t>(f & 0x80000000u) << 32;
+    if (mag == 0) {
+        d = sign;
+        return true;
+    }
+    if (mag < 0x00800000u || mag >= 0x7f800000u) return false;
+    d = ((static_cast<uint64_t>(mag) + (896ull << 23)) << 29) | sign;
+    return true;
+}
+
+// IEEE 754 comparisons of two doubles given by their bit patterns, in integer arithmetic: false
+// when either is a NaN, and -0 equal to +0, as the FP64 comparison instructions decide.
+constexpr uint64_t kAbsMask64 = 0x7fffffffffffffffull;
+constexpr uint64_t kExpMask64 = 0x7ff0000000000000ull;
+BQP_HD bool nan_bits(uint64_t b) { return (b & kAbsMask64) > kExpMask64; }
+BQP_HD bool finite_bits(uint64_t b) { return (b & kExpMask64) != kExpMask64; }
+// a key whose unsigned order is the numeric order of non-NaN doubles (-0 just below +0)
+BQP_HD uint64_t order_key(uint64_t b) { return (b >> 63) ? ~b : (b | 0x8000000000000000ull); }
+BQP_HD bool less_bits(uint64_t a, uint64_t b) {
+    if (nan_bits(a) || nan_bits(b) || ((a | b) & kAbsMask64) == 0) return false;
+    return order_key(a) < order_key(b);
+}
+BQP_HD bool less_equal_bits(uint64_t a, uint64_t b) {
+    if (nan_bits(a) || nan_bits(b)) return false;
+    return ((a | b) & kAbsMask64) == 0 || order_key(a) <= order_key(b);
+}
+
+BQP_HD float float_of_bits(uint32_t b) {
+    float f;
+    memcpy(&f, &b, sizeof f);
+    return f;
+}
+
+// A lower bound of a * b for non-negative floats: the product rounded down (the host forms the
+// exact product in FP64 and truncates it to FP32, flushing below the normal range to 0).
+BQP_HD float mul_rd_nonneg(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rd(a, b);
+#else
+    uint32_t rd, ru;
+    abs_bounds_bits(bits64(static_cast<double>(a) * static_cast<double>(b)), rd, ru);
+    return float_of_bits(rd);
+#endif
+}
+
+// Whether num / RN64(1 + |x|), rounded to FP64, can exceed m (num and m non-negative doubles,
+// num finite; all three given by their bits).  No when RU32(num) <= RD32(RD32(m) * max(1,
+// RD32(|x|))): then num <= m * RN64(1 + |x|), because max(1, |x|) <= RN64(1 + |x|), and the
+// rounded quotient is at most m.  Integer and FP32 arithmetic only.
+BQP_HD bool ratio_may_exceed(uint64_t num, uint64_t x, uint64_t m) {
+    uint32_t nrd, nru, xrd, xru, mrd, mru;
+    abs_bounds_bits(num, nrd, nru);
+    abs_bounds_bits(x & kAbsMask64, xrd, xru);
+    abs_bounds_bits(m, mrd, mru);
+    const float xf = float_of_bits(xrd);
+    const float den = xf > 1.0f ? xf : 1.0f;
+    return float_of_bits(nru) > mul_rd_nonneg(float_of_bits(mrd), den);
 }
 
 }  // namespace bqp

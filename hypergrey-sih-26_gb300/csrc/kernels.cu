@@ -66,7 +66,7 @@ __device__ __forceinline__ T group_sum(T v) {
 // ---- check / CG accumulators ---------------------------------------------------------------------
 // Sums in plain FP64, maxima of non-negative doubles as unsigned bit patterns.
 __device__ __forceinline__ unsigned long long dbits(double v) {
-    return static_cast<unsigned long long>(__double_as_longlong(v));
+    return static_cast<unsigned long long>(bits64(v));
 }
 __device__ __forceinline__ double bdouble(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a < b ? b : a; }
@@ -128,13 +128,14 @@ __device__ Acc block_reduce(Acc v) {
 }
 
 // The check's reduction: the two FP64 sums it always needs (objective, tangent bound), the
-// separable bound only for the diagonal dual-gap gate (`gate`), and the integer fields; the CG
-// fields (a, b) stay out (FP64 additions run at 1/64 of the FP32 rate here).
-__device__ __forceinline__ Acc combine_check(const Acc& x, const Acc& y, bool gate) {
+// separable bound only for the diagonal dual-gap gate (GATE, a template parameter so that no
+// FP64 addition runs for it otherwise), and the integer fields; the CG fields (a, b) stay out.
+template <bool GATE>
+__device__ __forceinline__ Acc combine_check(const Acc& x, const Acc& y) {
     Acc r = x;
     r.obj = x.obj + y.obj;
     r.bnd = x.bnd + y.bnd;
-    if (gate) r.sep = x.sep + y.sep;
+    if (GATE) r.sep = x.sep + y.sep;
     r.stat = umax64(x.stat, y.stat);
     r.prim = umax64(x.prim, y.prim);
     r.hash = x.hash ^ y.hash;
@@ -142,35 +143,62 @@ __device__ __forceinline__ Acc combine_check(const Acc& x, const Acc& y, bool ga
     r.flags = x.flags | y.flags;
     return r;
 }
-__device__ __forceinline__ Acc shfl_check(const Acc& x, int o, bool gate) {
-    Acc r = x;
-    r.obj = shfl_xor(x.obj, o);
-    r.bnd = shfl_xor(x.bnd, o);
-    if (gate) r.sep = shfl_xor(x.sep, o);
-    r.stat = shfl_xor(x.stat, o);
-    r.prim = shfl_xor(x.prim, o);
-    r.hash = shfl_xor(x.hash, o);
-    r.nact = shfl_xor(x.nact, o);
-    r.flags = shfl_xor(x.flags, o);
-    return r;
-}
-// publishing = true: the caller passes the result to publish_and_test_last, whose barrier orders
-// warp 0's reads of warp_part before the next call's writes; the trailing barrier is skipped.
-__device__ Acc block_reduce_check(Acc v, bool gate, bool publishing = false) {
-    __shared__ Acc warp_part[kBlock / 32];
+// The integer fields over the warp (xor tree, integer pipes).
+__device__ __forceinline__ void warp_ints(Acc& v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = combine_check(v, shfl_check(v, o, gate), gate);
+    for (int o = 16; o > 0; o >>= 1) {
+        v.stat = umax64(v.stat, shfl_xor(v.stat, o));
+        v.prim = umax64(v.prim, shfl_xor(v.prim, o));
+        v.hash ^= shfl_xor(v.hash, o);
+        v.nact += shfl_xor(v.nact, o);
+        v.flags |= shfl_xor(v.flags, o);
+    }
+}
+// Block reduction of the check fields in a fixed order; valid in thread 0.  The FP64 sums go
+// through shared memory: one warp adds each lane's 8 values (thread t: lane t % 32, in order of
+// t), then an xor tree over the warp, so a block takes 12 FP64 additions per sum instead of one
+// per tree level in every warp (GB300 issues an FP64 warp instruction at 1/64 of the FP32 rate).
+// publishing = true: the caller passes the result to publish_and_test_last, whose barrier orders
+// warp 0's reads of the shared arrays before the next call's writes; the trailing barrier is skipped.
+template <bool GATE>
+__device__ Acc block_reduce_check_t(Acc v, bool publishing) {
+    __shared__ double part_obj[kBlock];
+    __shared__ double part_bnd[kBlock];
+    __shared__ double part_sep[GATE ? kBlock : 1];
+    __shared__ Acc warp_int[kBlock / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) warp_part[warp] = v;
+    warp_ints(v);
+    part_obj[threadIdx.x] = v.obj;
+    part_bnd[threadIdx.x] = v.bnd;
+    if (GATE) part_sep[threadIdx.x] = v.sep;
+    if (lane == 0) warp_int[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        Acc w = lane < kBlock / 32 ? warp_part[lane] : acc_identity();
+        double ob = part_obj[lane], bn = part_bnd[lane], sp = GATE ? part_sep[lane] : 0.0;
 #pragma unroll
-        for (int o = (kBlock / 64); o > 0; o >>= 1) w = combine_check(w, shfl_check(w, o, gate), gate);
+        for (int w = 1; w < kBlock / 32; ++w) {
+            ob += part_obj[lane + 32 * w];
+            bn += part_bnd[lane + 32 * w];
+            if (GATE) sp += part_sep[lane + 32 * w];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ob += shfl_xor(ob, o);
+            bn += shfl_xor(bn, o);
+            if (GATE) sp += shfl_xor(sp, o);
+        }
+        Acc w = lane < kBlock / 32 ? warp_int[lane] : acc_identity();
+        warp_ints(w);
         v = w;
+        v.obj = ob;
+        v.bnd = bn;
+        v.sep = GATE ? sp : 0.0;
     }
     if (!publishing) __syncthreads();
     return v;
+}
+__device__ __forceinline__ Acc block_reduce_check(Acc v, bool gate, bool publishing = false) {
+    return gate ? block_reduce_check_t<true>(v, publishing) : block_reduce_check_t<false>(v, publishing);
 }
 
 __device__ __forceinline__ void store_partial(Partial* p, const Acc& v) {
@@ -209,17 +237,21 @@ __device__ bool publish_and_test_last(const View& v, int t, int inst, int ntiles
 
 // Reduces the check partials of tiles [tb, te) in a fixed order; valid in thread 0.  Pairs of
 // partials are loaded before they are combined (same order, two loads in flight).
-__device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
+template <bool GATE>
+__device__ Acc reduce_instance_t(const View& v, int tb, int te) {
     Acc acc = acc_identity();
     int k = tb + static_cast<int>(threadIdx.x);
     for (; k + kBlock < te; k += 2 * kBlock) {
         const Acc p0 = load_partial(&v.partial[k]);
         const Acc p1 = load_partial(&v.partial[k + kBlock]);
-        acc = combine_check(acc, p0, gate);
-        acc = combine_check(acc, p1, gate);
+        acc = combine_check<GATE>(acc, p0);
+        acc = combine_check<GATE>(acc, p1);
     }
-    if (k < te) acc = combine_check(acc, load_partial(&v.partial[k]), gate);
-    return block_reduce_check(acc, gate);
+    if (k < te) acc = combine_check<GATE>(acc, load_partial(&v.partial[k]));
+    return block_reduce_check_t<GATE>(acc, false);
+}
+__device__ Acc reduce_instance(const View& v, int tb, int te, bool gate) {
+    return gate ? reduce_instance_t<true>(v, tb, te) : reduce_instance_t<false>(v, tb, te);
 }
 
 // The CG reductions carry two sums (a, obj) and one maximum (b).
@@ -270,7 +302,7 @@ __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true, bool
 }
 
 // Reduces the CG partials of an instance in a fixed order: the partials of tiles tb, tb + stride,
-// ... below te (stride 1: every tile; kCgUnit: the first tile of each CG work unit).
+// ... below te (stride 1: every tile; the unit size: the first tile of each CG work unit).
 __device__ Acc reduce_instance_ab(const View& v, int tb, int te, int stride = 1) {
     constexpr int kAhead = 8;
     const int count = (te - tb + stride - 1) / stride;
@@ -310,24 +342,44 @@ __device__ __forceinline__ unsigned mix_index(unsigned k) {
     return k ^ (k >> 13);
 }
 
+// One row of check_qp_solution.  The comparisons and finiteness tests run on the bit patterns
+// (integer pipes) and the stationarity ratio is divided in FP64 only where it can raise the
+// running maximum: this thread's, or `floor`, a maximum other tiles of the same check already
+// reached.  The maximum is the one the plain FP64 form gives, bit for bit.
 __device__ __forceinline__ void check_row(Acc& a, double xi, double gq, double ci, double li, double ui, double di,
-                                          int gate, int row, bool at_lower, bool at_upper) {
-    if (!isfinite(xi)) {
+                                          int gate, int row, bool at_lower, bool at_upper,
+                                          unsigned long long floor = 0) {
+    const uint64_t xb = dbits(xi);
+    if (!finite_bits(xb)) {
         a.flags |= 1;
         return;
     }
     a.obj = fma(0.5 * xi, gq, a.obj);
     a.obj = fma(ci, xi, a.obj);
     const double g = gq + ci;
-    double res = fabs(xi - smax(li, smin(ui, xi - g))) / (1.0 + fabs(xi));
-    if (!isfinite(g) || !isfinite(res)) res = kInf;
-    a.stat = umax64(a.stat, dbits(res));
-    // scaled bound violation, only where the bound is violated (iterates are clamped)
-    if (li - xi > 0) a.prim = umax64(a.prim, dbits((li - xi) / (1.0 + fabs(li) + fabs(xi))));
-    if (xi - ui > 0) a.prim = umax64(a.prim, dbits((xi - ui) / (1.0 + fabs(ui) + fabs(xi))));
-    if (g != 0) {
-        double target = g > 0 ? li : ui;
-        if (isfinite(target)) a.bnd += g * (target - xi);
+    const uint64_t gb = dbits(g), lb = dbits(li), ub = dbits(ui);
+    // |xi - smax(li, smin(ui, xi - g))| with smin(a, b) = b < a ? b : a, smax(a, b) = a < b ? b : a
+    const uint64_t tb = dbits(xi - g);
+    const uint64_t mb = less_bits(tb, ub) ? tb : ub;
+    const uint64_t cb = less_bits(lb, mb) ? mb : lb;
+    const double num = fabs(xi - bdouble(cb));
+    const uint64_t nb = dbits(num);
+    unsigned long long res = 0;  // 0: the ratio leaves the maximum as it is
+    if (!finite_bits(gb) || !finite_bits(nb)) {
+        res = dbits(kInf);
+    } else if (ratio_may_exceed(nb, xb, umax64(a.stat, floor))) {
+        const double q = num / (1.0 + fabs(xi));
+        res = finite_bits(dbits(q)) ? dbits(q) : dbits(kInf);
+    }
+    a.stat = umax64(a.stat, res);
+    // scaled bound violation, only where the bound is violated (iterates are clamped):
+    // li - xi > 0 exactly when xi < li, xi - ui > 0 exactly when ui < xi
+    if (less_bits(xb, lb)) a.prim = umax64(a.prim, dbits((li - xi) / (1.0 + fabs(li) + fabs(xi))));
+    if (less_bits(ub, xb)) a.prim = umax64(a.prim, dbits((xi - ui) / (1.0 + fabs(ui) + fabs(xi))));
+    if ((gb & kAbsMask64) != 0) {  // g != 0 (a NaN included)
+        const bool positive = !(gb >> 63) && !nan_bits(gb);
+        double target = positive ? li : ui;
+        if (finite_bits(dbits(target))) a.bnd += g * (target - xi);
         else a.flags |= 2;
     }
     if (gate) {
@@ -460,13 +512,19 @@ __device__ __forceinline__ float2 df_prod2(float h, float l, float2 x) {
     const float e = __fmaf_rn(h, x.x, -p);
     return make_float2(p, __fmaf_rn(h, x.y, __fmaf_rn(l, x.x, e)));
 }
-__device__ __forceinline__ double df_value(float2 a) { return static_cast<double>(a.x) + static_cast<double>(a.y); }
+// hi + lo in FP64; the two widenings run in integer arithmetic where both parts are zero or normal
+__device__ __forceinline__ double df_value(float2 a) {
+    uint64_t h, l;
+    if (widen_signed_bits(__float_as_uint(a.x), h) && widen_signed_bits(__float_as_uint(a.y), l))
+        return __longlong_as_double(static_cast<long long>(h)) + __longlong_as_double(static_cast<long long>(l));
+    return static_cast<double>(a.x) + static_cast<double>(a.y);
+}
 // The FP32 pair of an FP64 value: hi = RN32(x), lo = RN32(x - hi), in integer arithmetic where
 // both are normal floats (split_hilo_bits), with the FP64 conversions elsewhere; the same bits
 // either way.
 __device__ __forceinline__ float2 df_split(double x) {
     uint32_t h, l;
-    if (split_hilo_bits(static_cast<uint64_t>(__double_as_longlong(x)), h, l))
+    if (split_hilo_bits(bits64(x), h, l))
         return make_float2(__uint_as_float(h), __uint_as_float(l));
     const float hf = __double2float_rn(x);
     return make_float2(hf, __double2float_rn(x - static_cast<double>(hf)));
@@ -474,7 +532,7 @@ __device__ __forceinline__ float2 df_split(double x) {
 // RN32(x), in integer arithmetic where the result is a normal float (round_float_bits).
 __device__ __forceinline__ float rn_float(double x) {
     uint32_t f;
-    if (round_float_bits(static_cast<uint64_t>(__double_as_longlong(x)), f)) return __uint_as_float(f);
+    if (round_float_bits(bits64(x), f)) return __uint_as_float(f);
     return __double2float_rn(x);
 }
 
@@ -537,7 +595,7 @@ __device__ __forceinline__ double gate_diag(const CheckSrc& s, int r, double fal
 
 // Check of rows [rb, re): accumulates check_row terms into a.
 template <int MODE>
-__device__ void check_rows(const CheckSrc& s, int variant, int rb, int re, Acc& a) {
+__device__ void check_rows(const CheckSrc& s, int variant, int rb, int re, Acc& a, unsigned long long floor = 0) {
     const int32_t* __restrict__ col = s.col;
     if constexpr (MODE == 0) {
         tile_rows<double>(
@@ -550,7 +608,9 @@ __device__ void check_rows(const CheckSrc& s, int variant, int rb, int re, Acc& 
                     const int ks = __ldg(s.rowptr + r);
                     di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? __ldg(s.val64 + ks) : 0.0);
                 }
-                check_row(a, xi, gq, s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
+                const double li = s.l[r], ui = s.u[r];
+                check_row(a, xi, gq, s.c[r], li, ui, di, s.gate, r, less_equal_bits(dbits(xi), dbits(li)),
+                          less_equal_bits(dbits(ui), dbits(xi)), floor);
             });
     } else if constexpr (MODE == 1) {
         tile_rows<float2>(
@@ -580,7 +640,9 @@ __device__ void check_rows(const CheckSrc& s, int variant, int rb, int re, Acc& 
                     const int ks = __ldg(s.rowptr + r);
                     di = gate_diag(s, r, __ldg(s.rowptr + r + 1) > ks ? static_cast<double>(__ldg(s.vhi + ks)) + __ldg(s.vlo + ks) : 0.0);
                 }
-                check_row(a, xi, df_value(acc), s.c[r], s.l[r], s.u[r], di, s.gate, r, xi <= s.l[r], xi >= s.u[r]);
+                const double li = s.l[r], ui = s.u[r];
+                check_row(a, xi, df_value(acc), s.c[r], li, ui, di, s.gate, r, less_equal_bits(dbits(xi), dbits(li)),
+                          less_equal_bits(dbits(ui), dbits(xi)), floor);
             });
     }
 }
@@ -946,15 +1008,22 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
         const int ph = I.phase;
         if (FAMILY == FAMILY_VERIFY ? ph != PH_POLISH_FINISH : ph != PH_FISTA) continue;
         const CheckSrc s = source_of(I);
+        // the largest stationarity ratio earlier tiles of this check reached
+        const unsigned long long floor = __ldcg(&I.stat_floor);
         Acc a = acc_identity();
-        if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a);
+        if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a, floor);
         else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, T.variant, T.row_begin, T.row_end, a);
-        else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a);
+        else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a, floor);
         Acc total = block_reduce_check(a, s.gate != 0, true);
+        // raised before this tile's partial is published, so before the finalizer resets it
+        if (threadIdx.x == 0 && total.stat > floor) atomicMax(&I.stat_floor, total.stat);
         const int2 R = v.ranges[T.inst];
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance(v, R.x, R.y, s.gate != 0);
-            if (threadIdx.x == 0) after_check(I, inst_total);
+            if (threadIdx.x == 0) {
+                after_check(I, inst_total);
+                I.stat_floor = 0;  // the next check starts from nothing
+            }
             __syncthreads();
         }
     }
@@ -1345,7 +1414,7 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
     }
 }
 
-// CG product w = Q_FF u over one work unit, the free rows of up to kCgUnit consecutive tiles of
+// CG product w = Q_FF u over one work unit, the free rows of up to kCgUnitMax consecutive tiles of
 // one instance taken as one list (position p of the unit: tile k with pre[k] <= p < pre[k + 1],
 // row j = p - pre[k] of that tile's free list), u gathered from its FP32 pairs; accumulates
 // gamma = r.u, delta = w.u and max |r|/(1+|x|) (the single reduction of the Chronopoulos-Gear form
@@ -1354,12 +1423,12 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
 __device__ __forceinline__ int unit_tile(const int* pre, int nk, int p) {
     int k = 0;
 #pragma unroll
-    for (int i = 1; i < kCgUnit; ++i) k += (i < nk && p >= pre[i]) ? 1 : 0;
+    for (int i = 1; i < kCgUnitMax; ++i) k += (i < nk && p >= pre[i]) ? 1 : 0;
     return k;
 }
 
 // The unit's free-row table in shared memory: pre[k] (prefix of the tiles' free counts, the
-// total at pre[kCgUnit]) and rbeg[k] (the tile's first row, where its free list starts).  The
+// total at pre[kCgUnitMax]) and rbeg[k] (the tile's first row, where its free list starts).  The
 // caller's previous readers of the table are past a block barrier.
 __device__ __forceinline__ void unit_table(const View& v, const InstDev& I, int t0, int first_tile, int nk, int* pre,
                                           int* rbeg) {
@@ -1370,7 +1439,7 @@ __device__ __forceinline__ void unit_table(const View& v, const InstDev& I, int 
             rbeg[k] = v.tiles[t0 + k].row_begin;
             acc += I.free_cnt[t0 - first_tile + k];
         }
-        for (int k = nk; k <= kCgUnit; ++k) pre[k] = acc;
+        for (int k = nk; k <= kCgUnitMax; ++k) pre[k] = acc;
     }
     __syncthreads();
 }
@@ -1415,11 +1484,33 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
         float2 acc[U];
 #pragma unroll
         for (int m = 0; m < U; ++m) acc[m] = make_float2(0.f, 0.f);
-        for (int i = sl; i < longest; i += LANES) {
+        // kCgUnroll entries of each row group per lane per pass: every load of the pass (entries,
+        // then gathers) is issued before the first product; the sums keep the per-lane order
+        for (int i = sl; i < longest; i += LANES * kCgUnroll) {
+            int c[U][kCgUnroll];
+            float h[U][kCgUnroll], l[U][kCgUnroll];
+            float2 xv[U][kCgUnroll];
 #pragma unroll
             for (int m = 0; m < U; ++m) {
-                const int e = ks[m] + i;
-                if (e < ke[m]) acc[m] = df_add(acc[m], df_prod2(__ldg(vhi + e), __ldg(vlo + e), p2[__ldg(col + e)]));
+#pragma unroll
+                for (int q = 0; q < kCgUnroll; ++q) {
+                    const int e = ks[m] + i + q * LANES;
+                    const bool in = e < ke[m];
+                    c[m][q] = in ? __ldg(col + e) : -1;
+                    h[m][q] = in ? __ldg(vhi + e) : 0.f;
+                    l[m][q] = in ? __ldg(vlo + e) : 0.f;
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < U; ++m) {
+#pragma unroll
+                for (int q = 0; q < kCgUnroll; ++q) xv[m][q] = c[m][q] >= 0 ? p2[c[m][q]] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int m = 0; m < U; ++m) {
+#pragma unroll
+                for (int q = 0; q < kCgUnroll; ++q)
+                    if (c[m][q] >= 0) acc[m] = df_add(acc[m], df_prod2(h[m][q], l[m][q], xv[m][q]));
             }
         }
 #pragma unroll
@@ -1430,16 +1521,36 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
             if (sl == 0 && p < total) rowsum[p] = acc[m];
         }
     }
-    // the FP64 epilogue, one free row per thread on full warps
+    // the FP64 epilogue, one free row per thread on full warps, kCgUnroll rows per pass with
+    // their loads issued together; each thread adds its rows in ascending order
     __syncthreads();
-    for (int p = threadIdx.x; p < total; p += kBlock) {
-        const int k = unit_tile(pre, nk, p);
-        const int r = list[rbeg[k] + (p - pre[k])];
-        const double w = df_value(rowsum[p]), ui = u[r], ri = rr_v[r];
-        q_out[r] = w;
-        a.a = fma(ri, ui, a.a);
-        a.obj = fma(w, ui, a.obj);
-        a.b = umax64(a.b, cg_ratio_bits(ri, xp[r]));
+    for (int p0 = threadIdx.x; p0 < total; p0 += kBlock * kCgUnroll) {
+        int r[kCgUnroll];
+        double ui[kCgUnroll], ri[kCgUnroll], xi[kCgUnroll];
+#pragma unroll
+        for (int q = 0; q < kCgUnroll; ++q) {
+            const int p = p0 + q * kBlock;
+            r[q] = -1;
+            if (p < total) {
+                const int k = unit_tile(pre, nk, p);
+                r[q] = list[rbeg[k] + (p - pre[k])];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kCgUnroll; ++q) {
+            ui[q] = r[q] >= 0 ? u[r[q]] : 0.0;
+            ri[q] = r[q] >= 0 ? rr_v[r[q]] : 0.0;
+            xi[q] = r[q] >= 0 ? xp[r[q]] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kCgUnroll; ++q) {
+            if (r[q] < 0) continue;
+            const double w = df_value(rowsum[p0 + q * kBlock]);
+            q_out[r[q]] = w;
+            a.a = fma(ri[q], ui[q], a.a);
+            a.obj = fma(w, ui[q], a.obj);
+            a.b = umax64(a.b, cg_ratio_bits(ri[q], xi[q]));
+        }
     }
 }
 
@@ -1515,19 +1626,20 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
 }
 
 __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
-    __shared__ int pre[kCgUnit + 1];
-    __shared__ int rbeg[kCgUnit];
-    __shared__ float2 rowsum[kCgUnit * kTileRows];
+    __shared__ int pre[kCgUnitMax + 1];
+    __shared__ int rbeg[kCgUnitMax];
+    __shared__ float2 rowsum[kCgRowsum];
     const int nu = v.ctrl->n_units;
     for (int un = blockIdx.x; un < nu; un += gridDim.x) {
-        const int t0 = v.units[un];
+        const int2 U = v.units[un];  // first tile, tiles per unit of its instance
+        const int t0 = U.x, unit = U.y;
         const Tile T = v.tiles[t0];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         const int2 R = v.ranges[T.inst];
-        const int nk = min(kCgUnit, R.y - t0);
+        const int nk = min(unit, R.y - t0);
         unit_table(v, I, t0, R.x, nk, pre, rbeg);
-        const int total = pre[kCgUnit];
+        const int total = pre[kCgUnitMax];
         Acc a = acc_identity();
         switch (I.lanes_cg) {
         case 1: matvec_unit<1>(I, pre, rbeg, nk, total, rowsum, a); break;
@@ -1538,9 +1650,9 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         default: matvec_unit<32>(I, pre, rbeg, nk, total, rowsum, a); break;
         }
         Acc tot = block_reduce_ab(a, I.lanes_cg, true, true);
-        const int units_inst = (R.y - R.x + kCgUnit - 1) / kCgUnit;
+        const int units_inst = (R.y - R.x + unit - 1) / unit;
         if (publish_and_test_last(v, t0, T.inst, units_inst, tot)) {
-            Acc inst_total = reduce_instance_ab(v, R.x, R.y, kCgUnit);
+            Acc inst_total = reduce_instance_ab(v, R.x, R.y, unit);
             if (threadIdx.x == 0) {
                 // Chronopoulos-Gear: gamma_i = r_i.u_i, delta_i = (Q u_i).u_i, beta_i =
                 // gamma_i / gamma_{i-1}, alpha_i = gamma_i / (delta_i - beta_i gamma_i / alpha_{i-1})
@@ -2029,7 +2141,7 @@ __global__ void __launch_bounds__(kGateWarps * 32) convexity_gate_kernel(const i
                 for (int k = a; k < b; ++k) total += fabs(__ldg(val + k));
                 best = umax64(best, dbits(total));
             }
-            const uint64_t db = static_cast<uint64_t>(__double_as_longlong(d));
+            const uint64_t db = bits64(d);
             const uint64_t dm = db & 0x7fffffffffffffffull;
             const bool negative = (db >> 63) && dm;
             if (negative || (dm == 0 && rad_hi > 0.0f)) indefinite = 1;
@@ -2078,7 +2190,7 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n) {
     const float inv_sqrt_l = __double2float_rn(1.0 / sqrt(gate_lipschitz(I)));
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         const double d = I.diag[r];
-        const uint64_t db = static_cast<uint64_t>(__double_as_longlong(d));
+        const uint64_t db = bits64(d);
         const int e = static_cast<int>(db >> 52);  // biased exponent; sign set => outside
         double dinv;
         float v;
@@ -2494,6 +2606,8 @@ int tile_grid(int sms) {
         m = w > m ? w : m;
     return m;
 }
+
+int cg_matvec_slots() { return g_waves.matvec; }
 
 void launch_check(const View& v, int grid, cudaStream_t s) {
     check_kernel<FAMILY_MIXED><<<pick(grid, g_waves.check_mixed), kBlock, kSmem8, s>>>(v);

@@ -8,6 +8,8 @@ namespace bqp {
 // Call once before launching.  The `grid` argument of the launchers below is a cap: each
 // kernel launches min(cap, its own full wave) blocks.
 int tile_grid(int sms);
+// resident blocks of the CG product kernel (after tile_grid)
+int cg_matvec_slots();
 // Tile kernels: grid-stride over the tile table (the grid size is fixed at capture).
 void launch_check(const View& v, int grid, cudaStream_t s);
 // Step j of a body: the step kernel of one group (step_group(precision, variant)) over the group's

@@ -1,7 +1,10 @@
-// Host check of the integer FP64 -> FP32 conversions the kernels use (csrc/fpbits.h) against the
-// C library's conversions: split_hilo_bits against (float)v and (float)(v - hi), round_float_bits
-// against (float)v, abs_bounds_bits against the neighbouring floats, widen_bits against
-// (double)f.  Prints "checked split S bounds B round R failures F" and exits non-zero on a failure.
+// Host check of the integer FP64 <-> FP32 conversions and FP64 comparisons the kernels use
+// (csrc/fpbits.h) against the C library: split_hilo_bits against (float)v and (float)(v - hi),
+// round_float_bits against (float)v, abs_bounds_bits against the neighbouring floats, widen_bits
+// and widen_signed_bits against (double)f, less_bits / less_equal_bits against a < b and a <= b,
+// and ratio_may_exceed's "no" against the FP64 quotient num / (1 + |x|) <= m.
+// Prints "checked split S bounds B round R widen W compare C ratio Q (skipped K) failures F" and
+// exits non-zero on a failure.
 #include "fpbits.h"
 
 #include <cfloat>
@@ -30,7 +33,8 @@ static double dfrom(uint64_t b) {
     return d;
 }
 
-static long failures = 0, n_split = 0, n_bounds = 0, n_round = 0;
+static long failures = 0, n_split = 0, n_bounds = 0, n_round = 0, n_widen = 0, n_compare = 0, n_ratio = 0,
+            n_skipped = 0;
 
 static void fail(const char* what, double v) {
     if (failures++ < 20) std::printf("FAIL %s at %.17g (bits %016llx)\n", what, v, (unsigned long long)bqp::bits64(v));
@@ -70,8 +74,77 @@ static void check(double v) {
     }
 }
 
+// widen_signed_bits against the C conversion, for one float pattern
+static void check_widen(uint32_t f) {
+    uint64_t d;
+    const float v = ffrom(f);
+    const uint32_t mag = f & 0x7fffffffu;
+    const bool expect = mag == 0 || (mag >= 0x00800000u && mag < 0x7f800000u);
+    if (bqp::widen_signed_bits(f, d) != expect) {
+        fail("widen_signed accepts", static_cast<double>(v));
+        return;
+    }
+    ++n_widen;
+    if (expect && d != bqp::bits64(static_cast<double>(v))) fail("widen_signed", static_cast<double>(v));
+}
+
+static void check_compare(double a, double b) {
+    ++n_compare;
+    const uint64_t x = bqp::bits64(a), y = bqp::bits64(b);
+    if (bqp::less_bits(x, y) != (a < b)) fail("less", a);
+    if (bqp::less_equal_bits(x, y) != (a <= b)) fail("less_equal", a);
+    if (bqp::finite_bits(x) != static_cast<bool>(std::isfinite(a))) fail("finite", a);
+    if (bqp::nan_bits(x) != static_cast<bool>(std::isnan(a))) fail("nan", a);
+}
+
+// ratio_may_exceed(num, x, m) false must mean RN64(num / RN64(1 + |x|)) <= m
+static void check_ratio(double num, double x, double m) {
+    ++n_ratio;
+    if (bqp::ratio_may_exceed(bqp::bits64(num), bqp::bits64(x), bqp::bits64(m))) return;
+    ++n_skipped;
+    const volatile double den = 1.0 + std::fabs(x);
+    const volatile double q = num / den;
+    if (!(q <= m)) fail("ratio skipped above the maximum", num);
+}
+
 int main() {
     std::mt19937_64 rng(20261204);
+    // signed widening: random patterns over every exponent, and the range edges
+    for (int i = 0; i < 1000000; ++i) check_widen(static_cast<uint32_t>(rng()));
+    for (uint32_t f : {0u, 0x80000000u, 1u, 0x007fffffu, 0x00800000u, 0x80800000u, 0x7f7fffffu, 0xff7fffffu,
+                       0x7f800000u, 0xff800000u, 0x7fc00000u, 0x3f800000u, 0xbf800000u})
+        check_widen(f);
+    // comparisons: special values against each other, random pairs, equal and adjacent pairs
+    const double specials[] = {0.0, -0.0, 1.0, -1.0, INFINITY, -INFINITY, NAN, -NAN, DBL_MIN, -DBL_MIN,
+                               DBL_TRUE_MIN, -DBL_TRUE_MIN, DBL_MAX, -DBL_MAX, 1e-300, -1e300, 3.0, -3.0};
+    for (double a : specials)
+        for (double b : specials) check_compare(a, b);
+    for (int i = 0; i < 1000000; ++i) {
+        const double a = dfrom(rng()), b = (i & 3) == 0 ? a : dfrom(rng());
+        check_compare(a, b);
+        check_compare(a, std::nextafter(a, INFINITY));
+        check_compare(std::nextafter(a, -INFINITY), a);
+        check_compare(-a, b);
+    }
+    // the division filter: quotients near the maximum (within a few ulps either side), tiny and
+    // huge magnitudes, |x| around 1 where max(1, |x|) is loosest
+    std::uniform_real_distribution<double> unit(0.0, 1.0);
+    for (int i = 0; i < 2000000; ++i) {
+        const double x = (i & 1 ? 1.0 : -1.0) * std::ldexp(unit(rng), static_cast<int>(rng() % 80) - 40);
+        const double m = std::ldexp(unit(rng), static_cast<int>(rng() % 200) - 150);
+        const double q0 = m * (1.0 + std::fabs(x));
+        double num = q0;
+        const int steps = static_cast<int>(rng() % 9) - 4;
+        for (int k = 0; k < (steps < 0 ? -steps : steps); ++k) num = std::nextafter(num, steps < 0 ? 0.0 : INFINITY);
+        if (i % 5 == 0) num *= unit(rng);
+        check_ratio(num, x, m);
+        check_ratio(num, x, std::nextafter(m, 0.0));
+    }
+    for (double num : {0.0, DBL_TRUE_MIN, 1e-300, 1e-40, 1.0, 3e38, 1e300}) {
+        for (double x : {0.0, -0.0, 1e-30, 0.5, 1.0, -1.0, 2.0, 1e30, 1e300, -1e300}) {
+            for (double m : {0.0, DBL_TRUE_MIN, 1e-300, 1e-40, 1e-7, 1.0, 3e38, 1e300, static_cast<double>(INFINITY)}) check_ratio(num, x, m);
+        }
+    }
     // random bit patterns over the whole exponent range, both signs
     for (int i = 0; i < 2000000; ++i) {
         const uint64_t e = (i & 1) ? rng() % 2047 : 890 + rng() % 270;  // half of them around the window
@@ -102,6 +175,7 @@ int main() {
     check(-2.0);
     check(1.0 / 3.0);
     check(3.4028235677973366e38);  // rounds to infinity in FP32
-    std::printf("checked split %ld bounds %ld round %ld failures %ld\n", n_split, n_bounds, n_round, failures);
+    std::printf("checked split %ld bounds %ld round %ld widen %ld compare %ld ratio %ld (skipped %ld) failures %ld\n",
+                n_split, n_bounds, n_round, n_widen, n_compare, n_ratio, n_skipped, failures);
     return failures ? 1 : 0;
 }

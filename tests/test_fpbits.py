@@ -1,6 +1,8 @@
-"""The integer FP64 -> FP32 conversions of the admission pass (csrc/fpbits.h), compiled for the
-host and checked against the C library's conversions (hi/lo split bit for bit, directed bounds
-nearest inside the normal range, exact widening)."""
+"""The integer FP64 <-> FP32 conversions and FP64 comparisons of the admission pass and the row
+epilogues (csrc/fpbits.h), compiled for the host and checked against the C library (hi/lo split
+bit for bit, directed bounds nearest inside the normal range, exact widening of either sign, IEEE
+comparisons with NaNs and signed zeros, and the check's division filter never skipping a
+quotient above the running maximum)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -21,3 +23,5 @@ def test_fpbits_conversions_match_the_c_library(tmp_path):
     assert 'failures 0' in out.stdout
     n_split = int(out.stdout.split('split ')[1].split()[0])
     assert n_split > 100000  # the window holds a good share of the random patterns
+    skipped = int(out.stdout.split('skipped ')[1].split(')')[0])
+    assert skipped > 100000  # the filter's "no" is exercised, near the boundary included
