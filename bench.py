@@ -14,7 +14,7 @@ in FP64.  A step is one complete solve of that instance.
   roofline  the FISTA step kernel (dominant kernel) timed alone with CUDA events on the same
           instance; algorithmic bytes per launch nnz*(4+4) + 4(n+1) + 7*4n
   roofline_cg  the polish CG product kernel of the same solve (bqp_profile_cg), bytes per launch
-          12 nnz_FF + 52 n_F on the packed free-free block
+          12 nnz_FF + 48 n_F on the packed free-free block
   solve.oracle_check  the timed solve's primal checked on the host by the oracle
           (check_qp_solution restated) and against the planted active set
   cpu_baseline  one full FP64 solve by the reference's own solve_accelerated_box, built from its

@@ -62,7 +62,7 @@ struct Layout {
     size_t c = kNone, l = kNone, u = kNone, diag = kNone;
     size_t c32 = kNone, l32 = kNone, u32 = kNone, x32 = kNone, w32a = kNone, w32b = kNone;
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
-    size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, fixed = kNone;
+    size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, pos_of = kNone, xf = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
     size_t sstep = kNone, lprec = kNone, s = kNone, gate = kNone;
@@ -107,7 +107,8 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.xp2 = take(N * 8);
         L.p2 = take(N * 8);
         L.dinv = take(N * 8);
-        L.fixed = take(N);
+        L.pos_of = take(N * 4);
+        L.xf = take(N * 8);
         L.free_rows = take(N * 4);
         L.free_cnt = take(static_cast<size_t>(tiles) * 4);
         L.col_ff = take(Z * 4);
@@ -1306,6 +1307,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.u32 = at<float>(slab, L.u32);
     R.diag = at<double>(slab, L.diag);
     R.x64 = at<double>(slab, L.x64);
+    if (L.xf != kNone) R.xf = at<double>(slab, L.xf);  // the same field (mixed engines have no x64)
     R.w64[0] = at<double>(slab, L.w64a);
     R.w64[1] = at<double>(slab, L.w64b);
     R.x32 = at<float>(slab, L.x32);
@@ -1316,7 +1318,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.p = at<double>(slab, L.p);
     R.q = at<double>(slab, L.q);
     R.z = at<double>(slab, L.z);
-    R.fixed = at<uint8_t>(slab, L.fixed);
+    R.pos_of = at<int32_t>(slab, L.pos_of);
     R.xp2 = at<float2>(slab, L.xp2);
     R.p2 = at<float2>(slab, L.p2);
     R.dinv = at<double>(slab, L.dinv);
@@ -1949,8 +1951,11 @@ int Engine::profile_cg(uint64_t id, int iterations, double* ms_matvec, double* m
     const double fz = static_cast<double>(after.ff_nnz), fr = static_cast<double>(after.ff_rows);
     if (ms_matvec) *ms_matvec = mv / iterations;
     if (ms_vector) *ms_vector = vec / iterations;
-    if (bytes_matvec) *bytes_matvec = 12.0 * fz + 52.0 * fr;
-    if (bytes_vector) *bytes_vector = 84.0 * fr;
+    // product: the packed entries (column, hi, lo); per free row its start and count, u, r and x
+    // read, w written, and u's FP32 pair gathered once.  Vector step: p, u, s, w, r, x and the
+    // preconditioner read, p, s, x, r, u and u's pair written.
+    if (bytes_matvec) *bytes_matvec = 12.0 * fz + 48.0 * fr;
+    if (bytes_vector) *bytes_vector = 104.0 * fr;
     return BQP_OK;
 }
 

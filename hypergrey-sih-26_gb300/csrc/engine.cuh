@@ -117,19 +117,25 @@ struct __align__(16) InstDev {
     const double* diag;    // FP64 diagonal of Q
     const double* dinv;    // 1 / diagonal (mixed: Jacobi preconditioner of the polish)
     // iterates
-    double* x64;
+    union {
+        double* x64;       // FP64 engines: the iterate
+        double* xf;        // mixed engine: the polish's x on the free-list positions (below)
+    };
     double* w64[2];
     float* x32;
     float* w32[2];
     double* xp;            // polished point (FP64)
     float2* xp2;           // xp as an FP32 pair (hi, lo) for FP32-only gathers
-    float2* p2;            // CG direction p as an FP32 pair
+    // The polish's CG vectors live on free-list positions: free row j of a tile is position
+    // row_begin + j (each tile's free rows packed at the front of its row range), so the CG
+    // kernels stream them without the row indices, and Q_FF's packed columns are positions.
+    float2* p2;            // CG: u as an FP32 pair (gathered by the product)
     double* r;
     double* p;
-    double* q;
+    double* q;             // CG: w = Q_FF u
     double* s;             // polish: s = Q p (Chronopoulos-Gear CG)
-    double* z;
-    uint8_t* fixed;        // polish: 1 = held at a bound
+    double* z;             // CG: u = M^-1 r
+    int32_t* pos_of;       // polish: a row's free-list position, -1 for a row held at a bound
     int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row
     int32_t* free_cnt;     // polish: free rows per tile (index within the instance's tiles)
     int32_t* col_ff;       // polish: the free-column entries of a tile's free rows, packed row
@@ -137,7 +143,7 @@ struct __align__(16) InstDev {
     float* lo_ff;          //   [rowptr[row_begin], ...): row r at [start_ff[r], + cnt_ff[r])
     int32_t* cnt_ff;
     int32_t* start_ff;
-    double* pc_inv;        // polish preconditioner, per free-list position: 1 / pivot of the chain factorization
+    double* pc_inv;        // polish preconditioner, per free-list position: 1 / pivot of the chain factorization (1 / Q_rr on a Jacobi row)
     double* pc_e;          //   and the kept coupling to the next position (0 ends a chain)
     int32_t* pc_tile;      //   per tile (index within the instance): 1 when the tile has a chain
     unsigned long long stat_floor;  // within a running check: the largest stationarity ratio (FP64

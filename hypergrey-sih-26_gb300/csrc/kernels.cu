@@ -1034,10 +1034,11 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // being the variables the FP32 iterate holds strictly inside its bounds.  Vectors are FP64; the
 // matrix products are formed in FP32 double-float arithmetic from the hi/lo values and the FP32
 // pairs xp2 / p2 kept beside xp / p.
-// polish_init lists each tile's free rows in ascending order at free_rows[row_begin ...] and
-// their count at free_cnt[tile index within the instance]; the CG kernels visit only those rows
-// (an instance's tiling depends on the instance alone, so the list survives changes of the batch).
-// Fixed rows hold r = z = p = 0, so the products of the CG matvec over all columns are exact.
+// polish_init lists each tile's free rows in ascending order at free_rows[row_begin ...], their
+// count at free_cnt[tile index within the instance] and each free row's list position (row_begin
+// + its index) at pos_of[row], -1 for the rows held at a bound; the CG vectors (r, z, p, s, q, p2,
+// xf) live on those positions, and the packed Q_FF's columns are positions too (an instance's
+// tiling depends on the instance alone, so the positions survive changes of the batch).
 // CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with 0.1 tol), as the
 // bit pattern of a non-negative float: maxima reduce on the integer pipes, and r and x are
 // rounded to FP32 in integer arithmetic (the FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
@@ -1065,11 +1066,7 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
         const double* __restrict__ u = I.u;
         double* __restrict__ xp = I.xp;
         float2* __restrict__ xp2 = I.xp2;
-        uint8_t* __restrict__ fixed_out = I.fixed;
-        double* __restrict__ r_out = I.r;
-        double* __restrict__ z_out = I.z;
-        double* __restrict__ p_out = I.p;
-        float2* __restrict__ p2_out = I.p2;
+        int32_t* __restrict__ pos_out = I.pos_of;
         int32_t* __restrict__ list = I.free_rows + T.row_begin;
         int count = 0;
         for (int r0 = T.row_begin; r0 < T.row_end; r0 += kBlock) {
@@ -1083,13 +1080,6 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
                 else { xv = static_cast<double>(xf); is_free = true; }
                 xp[r] = xv;
                 xp2[r] = df_split(xv);
-                fixed_out[r] = is_free ? 0 : 1;
-                if (!is_free) {
-                    r_out[r] = 0.0;
-                    z_out[r] = 0.0;
-                    p_out[r] = 0.0;
-                    p2_out[r] = make_float2(0.f, 0.f);
-                }
             }
             const unsigned m = __ballot_sync(0xffffffffu, is_free);
             if (lane == 0) warp_free[warp] = __popc(m);
@@ -1100,7 +1090,11 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
                 before += w < warp ? warp_free[w] : 0;
                 total += warp_free[w];
             }
-            if (is_free) list[before + __popc(m & ((1u << lane) - 1u))] = r;
+            if (r < T.row_end) {
+                const int j = before + __popc(m & ((1u << lane) - 1u));
+                if (is_free) list[j] = r;
+                pos_out[r] = is_free ? T.row_begin + j : -1;
+            }
             __syncthreads();
             count = total;
         }
@@ -1125,7 +1119,7 @@ __device__ void count_kept(const InstDev& I, const int32_t* __restrict__ list, i
     const int sub = lane / LANES, sl = lane % LANES;
     const int32_t* __restrict__ rowptr = I.rowptr;
     const int32_t* __restrict__ col = I.col;
-    const uint8_t* __restrict__ fixed = I.fixed;
+    const int32_t* __restrict__ pos_of = I.pos_of;
     for (int g = warp; g * R < n; g += kBlock / 32) {  // warp-uniform
         const int j = g * R + sub;
         int cnt = 0;
@@ -1133,7 +1127,7 @@ __device__ void count_kept(const InstDev& I, const int32_t* __restrict__ list, i
             const int r = list[j];
             const int ks = __ldg(rowptr + r), ke = __ldg(rowptr + r + 1);
 #pragma unroll 4
-            for (int k = ks + sl; k < ke; k += LANES) cnt += fixed[__ldg(col + k)] ? 0 : 1;
+            for (int k = ks + sl; k < ke; k += LANES) cnt += pos_of[__ldg(col + k)] >= 0 ? 1 : 0;
         }
 #pragma unroll
         for (int o = LANES / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -1188,7 +1182,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     const int32_t* __restrict__ col = I.col;
     const float* __restrict__ vhi = I.vhi;
     const float* __restrict__ vlo = I.vlo;
-    const uint8_t* __restrict__ fixed = I.fixed;
+    const int32_t* __restrict__ pos_of = I.pos_of;
     const float2* __restrict__ xp2 = I.xp2;
     int32_t* __restrict__ col_ff = I.col_ff;
     float* __restrict__ hi_ff = I.hi_ff;
@@ -1213,7 +1207,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
         for (int i = 0; i < wmax; i += LANES) {  // warp-uniform
             const bool valid = i + sl < len;
             bool keep = false;
-            int cc = 0;
+            int cc = 0, pc = -1;
             float h = 0.f, lo = 0.f;
             if (valid) {
                 const int k = ks + i + sl;
@@ -1221,13 +1215,14 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
                 h = __ldg(vhi + k);
                 lo = __ldg(vlo + k);
                 acc = df_add(acc, df_prod2(h, lo, xp2[cc]));
-                keep = !fixed[cc];
+                pc = pos_of[cc];
+                keep = pc >= 0;
                 if (cc == r + 1) e_next = make_float2(e_next.x + h, e_next.y + lo);
             }
             const unsigned m = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const int pos = dst + kept + __popc(m & group & below);
-                col_ff[pos] = cc;
+                col_ff[pos] = pc;  // the column's free-list position
                 hi_ff[pos] = h;
                 lo_ff[pos] = lo;
             }
@@ -1292,19 +1287,26 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
     const double* __restrict__ dinv = I.dinv;
     const double* __restrict__ diag = I.diag;
     const double* __restrict__ xp = I.xp;
-    double* __restrict__ r_out = I.r;
-    double* __restrict__ z_out = I.z;
-    double* __restrict__ p_out = I.p;
-    double* __restrict__ s_out = I.s;
-    float2* __restrict__ p2_out = I.p2;
-    auto row_out = [&](int r, double rr, double zz) {
+    const int q0 = static_cast<int>(list - I.free_rows);  // list position t is q0 + t
+    double* __restrict__ r_out = I.r + q0;
+    double* __restrict__ z_out = I.z + q0;
+    double* __restrict__ p_out = I.p + q0;
+    double* __restrict__ s_out = I.s + q0;
+    double* __restrict__ xf_out = I.xf + q0;
+    float2* __restrict__ p2_out = I.p2 + q0;
+    double* __restrict__ pc_inv = I.pc_inv + q0;
+    double* __restrict__ pc_e = I.pc_e + q0;
+    // the CG start on list position t (row r): r, z = M^-1 r, p = z, s = 0 and x
+    auto row_out = [&](int t, int r, double rr, double zz) {
+        const double xr = xp[r];
         a.a = fma(rr, zz, a.a);
-        a.b = umax64(a.b, cg_ratio_bits(rr, xp[r]));
-        r_out[r] = rr;
-        z_out[r] = zz;
-        p_out[r] = zz;
-        s_out[r] = 0.0;
-        p2_out[r] = df_split(zz);
+        a.b = umax64(a.b, cg_ratio_bits(rr, xr));
+        r_out[t] = rr;
+        z_out[t] = zz;
+        p_out[t] = zz;
+        s_out[t] = 0.0;
+        p2_out[t] = df_split(zz);
+        xf_out[t] = xr;
     };
     bool any = false;
     for (int t = threadIdx.x; t < n; t += kBlock) {
@@ -1356,13 +1358,12 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
     if (!chains) {
         for (int t = threadIdx.x; t < n; t += kBlock) {
             const int r = list[t];
-            row_out(r, res[t], res[t] * dinv[r]);
+            const double inv = dinv[r];
+            pc_inv[t] = inv;  // the vector step's Jacobi rows read 1 / Q_rr by position
+            row_out(t, r, res[t], res[t] * inv);
         }
         return;
     }
-    const int q0 = static_cast<int>(list - I.free_rows);  // list position t is q0 + t in pc_inv / pc_e
-    double* __restrict__ pc_inv = I.pc_inv + q0;
-    double* __restrict__ pc_e = I.pc_e + q0;
     // chains of two or more rows, one thread each, in shared memory; the chains are numbered
     // densely so that consecutive lanes take them (an FP64 warp instruction costs the same with 1
     // or 32 active lanes); each chain's arithmetic does not depend on which thread runs it
@@ -1410,7 +1411,7 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
             pc_e[t] = 0.0;
             zz = res[t] * inv;
         }
-        row_out(r, res[t], zz);
+        row_out(t, r, res[t], zz);
     }
 }
 
@@ -1460,8 +1461,7 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
     const float2* __restrict__ p2 = I.p2;  // u as FP32 pairs
     const double* __restrict__ u = I.z;
     const double* __restrict__ rr_v = I.r;
-    const double* __restrict__ xp = I.xp;
-    const int32_t* __restrict__ list = I.free_rows;
+    const double* __restrict__ xf = I.xf;
     double* __restrict__ q_out = I.q;      // w
     const int groups = (total + R - 1) / R;
     for (int g0 = warp; g0 < groups; g0 += W * U) {  // warp-uniform
@@ -1525,7 +1525,7 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
     // their loads issued together; each thread adds its rows in ascending order
     __syncthreads();
     for (int p0 = threadIdx.x; p0 < total; p0 += kBlock * kCgUnroll) {
-        int r[kCgUnroll];
+        int r[kCgUnroll];  // list positions
         double ui[kCgUnroll], ri[kCgUnroll], xi[kCgUnroll];
 #pragma unroll
         for (int q = 0; q < kCgUnroll; ++q) {
@@ -1533,14 +1533,14 @@ __device__ void matvec_unit(const InstDev& I, const int* pre, const int* rbeg, i
             r[q] = -1;
             if (p < total) {
                 const int k = unit_tile(pre, nk, p);
-                r[q] = list[rbeg[k] + (p - pre[k])];
+                r[q] = rbeg[k] + (p - pre[k]);
             }
         }
 #pragma unroll
         for (int q = 0; q < kCgUnroll; ++q) {
             ui[q] = r[q] >= 0 ? u[r[q]] : 0.0;
             ri[q] = r[q] >= 0 ? rr_v[r[q]] : 0.0;
-            xi[q] = r[q] >= 0 ? xp[r[q]] : 0.0;
+            xi[q] = r[q] >= 0 ? xf[r[q]] : 0.0;
         }
 #pragma unroll
         for (int q = 0; q < kCgUnroll; ++q) {
@@ -1609,11 +1609,12 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
             if (threadIdx.x == 0) {
                 // residual pass: the full CSR (hi/lo values + columns) and row pointers, xp (its
                 // FP32 pairs, gathered) and c; the packed Q_FF written (hi/lo + column) with its
-                // row starts and counts; r, z, p, s, p2 written and 1/diag read on the free rows
+                // row starts and counts; r, z, p, s, p2, x and the preconditioner's 1/pivot written
+                // and 1/diag read on the free rows
                 const double nnz = static_cast<double>(__ldg(I.rowptr + I.n));
                 const double N = static_cast<double>(I.n);
                 const double fz = static_cast<double>(I.ff_nnz), fr = static_cast<double>(I.ff_rows);
-                I.polish_bytes += 12.0 * nnz + 4.0 * (N + 1) + 16.0 * N + 12.0 * fz + 8.0 * fr + 48.0 * fr;
+                I.polish_bytes += 12.0 * nnz + 4.0 * (N + 1) + 16.0 * N + 12.0 * fz + 8.0 * fr + 64.0 * fr;
                 I.rz = inst_total.a;
                 I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
                 I.cg_it = 0;
@@ -1661,9 +1662,9 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
                 const bool first = I.cg_it == 0;
                 I.cg_it++;
                 I.cg_total++;
-                // one CG iteration on Q_FF: its packed entries (hi/lo + column), row starts and
-                // counts, and 16 FP64 vector accesses per free row (product and vector step)
-                I.polish_bytes += 12.0 * static_cast<double>(I.ff_nnz) + 136.0 * static_cast<double>(I.ff_rows);
+                // one CG iteration on Q_FF: its packed entries (hi/lo + column), and per free
+                // row the product's 48 bytes and the vector step's 104 (bqp_profile_cg)
+                I.polish_bytes += 12.0 * static_cast<double>(I.ff_nnz) + 152.0 * static_cast<double>(I.ff_rows);
                 bool stop = I.cg_res <= I.cg_tol || I.cg_it > I.cg_max || !isfinite(gamma) || !isfinite(delta);
                 if (!stop) {
                     const double beta = first ? 0.0 : gamma / I.rz;
@@ -1687,9 +1688,10 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
     }
 }
 
-// CG vector step on the free rows: p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s,
-// u = D^-1 r (and its FP32 pairs for the next product).  No reduction: the product kernel's
-// finalizer already chose alpha and beta.  Instances that finished CG snap x into the box here.
+// CG vector step on the free-list positions: p = u + beta p, s = w + beta s, x += alpha p,
+// r -= alpha s, u = M^-1 r (and its FP32 pairs for the next product), every vector streamed by
+// position.  No reduction: the product kernel's finalizer already chose alpha and beta.  Instances
+// that finished CG write x back to their free rows, snapped into the box, here.
 // In a graph, block 0 also decides whether the CG loop runs another iteration: while an instance
 // still iterates and fewer than `cap` iterations ran (the product kernel, which completed before
 // this launch, counted finishing instances down).
@@ -1708,30 +1710,29 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
         if (I.status != ST_RUNNING) continue;
         if (I.phase == PH_POLISH_CG) {
             const double alpha = I.alpha, beta = I.beta_cg;
-            const int32_t* __restrict__ list = I.free_rows + T.row_begin;
-            const int n_free = I.free_cnt[t - v.ranges[T.inst].x];
-            const double* __restrict__ dinv = I.dinv;
-            const double* __restrict__ w = I.q;
-            double* __restrict__ u = I.z;
-            double* __restrict__ p = I.p;
-            double* __restrict__ s = I.s;
-            double* __restrict__ xp = I.xp;
-            double* __restrict__ rr_v = I.r;
-            float2* __restrict__ u2 = I.p2;
             const int tile = t - v.ranges[T.inst].x;
+            const int n_free = I.free_cnt[tile];
+            const int q0 = T.row_begin;  // free row j of the tile is list position q0 + j
+            const double* __restrict__ w = I.q + q0;
+            double* __restrict__ u = I.z + q0;
+            double* __restrict__ p = I.p + q0;
+            double* __restrict__ s = I.s + q0;
+            double* __restrict__ xf = I.xf + q0;
+            double* __restrict__ rr_v = I.r + q0;
+            float2* __restrict__ u2 = I.p2 + q0;
+            const double* __restrict__ pc_inv = I.pc_inv + q0;
             if (!I.pc_tile[tile]) {  // Jacobi rows only: u = r / Q_rr
                 for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                    const int r = list[j];
-                    const double pn = fma(beta, p[r], u[r]);
-                    const double sn = fma(beta, s[r], w[r]);
-                    const double rn = fma(-alpha, sn, rr_v[r]);
-                    const double un = rn * dinv[r];
-                    p[r] = pn;
-                    s[r] = sn;
-                    xp[r] = fma(alpha, pn, xp[r]);
-                    rr_v[r] = rn;
-                    u[r] = un;
-                    u2[r] = df_split(un);
+                    const double pn = fma(beta, p[j], u[j]);
+                    const double sn = fma(beta, s[j], w[j]);
+                    const double rn = fma(-alpha, sn, rr_v[j]);
+                    const double un = rn * pc_inv[j];
+                    p[j] = pn;
+                    s[j] = sn;
+                    xf[j] = fma(alpha, pn, xf[j]);
+                    rr_v[j] = rn;
+                    u[j] = un;
+                    u2[j] = df_split(un);
                 }
             } else {
                 // the residual pass's chains (pc_e links a position to the next): the updates
@@ -1746,18 +1747,15 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
                 __shared__ int n_starts_s;
                 int* n_starts = &n_starts_s;
                 if (threadIdx.x == 0) n_starts_s = 0;
-                const int q0 = T.row_begin;  // list position j is q0 + j in pc_inv / pc_e
-                const double* __restrict__ pc_inv = I.pc_inv + q0;
                 const double* __restrict__ pc_e = I.pc_e + q0;
                 for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                    const int r = list[j];
-                    const double pn = fma(beta, p[r], u[r]);
-                    const double sn = fma(beta, s[r], w[r]);
-                    const double rn = fma(-alpha, sn, rr_v[r]);
-                    p[r] = pn;
-                    s[r] = sn;
-                    xp[r] = fma(alpha, pn, xp[r]);
-                    rr_v[r] = rn;
+                    const double pn = fma(beta, p[j], u[j]);
+                    const double sn = fma(beta, s[j], w[j]);
+                    const double rn = fma(-alpha, sn, rr_v[j]);
+                    p[j] = pn;
+                    s[j] = sn;
+                    xf[j] = fma(alpha, pn, xf[j]);
+                    rr_v[j] = rn;
                     rs[j] = rn;
                     pi[j] = pc_inv[j];
                     pe[j] = pc_e[j];
@@ -1788,19 +1786,24 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
                 }
                 __syncthreads();
                 for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                    const int r = list[j];
-                    u[r] = ys[j];
-                    u2[r] = df_split(ys[j]);
+                    u[j] = ys[j];
+                    u2[j] = df_split(ys[j]);
                 }
                 __syncthreads();  // the shared arrays are reused by the block's next chain tile
             }
         } else if (I.phase == PH_POLISH_FINISH) {
+            // x of the free rows back from the list positions, snapped into the box (the rows
+            // held at a bound kept their bound from polish_init); repeating it changes nothing
+            const int n_free = I.free_cnt[t - v.ranges[T.inst].x];
+            const int32_t* __restrict__ list = I.free_rows + T.row_begin;
+            const double* __restrict__ xf = I.xf + T.row_begin;
             const double* __restrict__ l = I.l;
             const double* __restrict__ uu = I.u;
             double* __restrict__ xp = I.xp;
             float2* __restrict__ xp2 = I.xp2;
-            for (int r = T.row_begin + static_cast<int>(threadIdx.x); r < T.row_end; r += kBlock) {
-                const double xv = smax(l[r], smin(uu[r], xp[r]));
+            for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
+                const int r = list[j];
+                const double xv = smax(l[r], smin(uu[r], xf[j]));
                 xp[r] = xv;
                 xp2[r] = df_split(xv);
             }

@@ -199,7 +199,7 @@ int bqp_profile_step(bqp_ctx* ctx, uint64_t id, int32_t launches, double* ms_per
  * polish, re-runs the polish from the solve's FP32 iterate (untimed) and times `iterations` CG
  * iterations with CUDA events, the product kernel (w = Q_FF u with the fused reduction) and the
  * vector kernel separately; returns their mean times and algorithmic bytes per launch on the
- * packed Q_FF (product 12 nnz_FF + 52 n_F, vector 84 n_F).  Same conditions and side effect as
+ * packed Q_FF (product 12 nnz_FF + 48 n_F, vector 104 n_F).  Same conditions and side effect as
  * bqp_profile_step.                                                                         */
 int bqp_profile_cg(bqp_ctx* ctx, uint64_t id, int32_t iterations, double* ms_matvec, double* ms_vector,
                    double* bytes_matvec, double* bytes_vector);
