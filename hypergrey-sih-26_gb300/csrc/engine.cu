@@ -62,7 +62,7 @@ struct Layout {
     size_t c = kNone, l = kNone, u = kNone, diag = kNone;
     size_t c32 = kNone, l32 = kNone, u32 = kNone, x32 = kNone, w32a = kNone, w32b = kNone;
     size_t x64 = kNone, w64a = kNone, w64b = kNone;
-    size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, pos_of = kNone, xf = kNone;
+    size_t xp = kNone, r = kNone, p = kNone, q = kNone, z = kNone, xq = kNone, pos_of = kNone, xf = kNone;
     size_t xp2 = kNone, p2 = kNone, dinv = kNone, free_rows = kNone, free_cnt = kNone;
     size_t col_ff = kNone, hi_ff = kNone, lo_ff = kNone, cnt_ff = kNone, start_ff = kNone;
     size_t sstep = kNone, lprec = kNone, s = kNone, gate = kNone;
@@ -107,6 +107,7 @@ Layout make_layout(int64_t n, int64_t nnz, int64_t tiles, int precision) {
         L.xp2 = take(N * 8);
         L.p2 = take(N * 8);
         L.dinv = take(N * 8);
+        L.xq = take(N * 16);
         L.pos_of = take(N * 4);
         L.xf = take(N * 8);
         L.free_rows = take(N * 4);
@@ -1318,6 +1319,7 @@ bool Engine::upload_begin(Job& j, std::string& why) {
     R.p = at<double>(slab, L.p);
     R.q = at<double>(slab, L.q);
     R.z = at<double>(slab, L.z);
+    R.xq = at<int4>(slab, L.xq);
     R.pos_of = at<int32_t>(slab, L.pos_of);
     R.xp2 = at<float2>(slab, L.xp2);
     R.p2 = at<float2>(slab, L.p2);

@@ -135,7 +135,10 @@ struct __align__(16) InstDev {
     double* q;             // CG: w = Q_FF u
     double* s;             // polish: s = Q p (Chronopoulos-Gear CG)
     double* z;             // CG: u = M^-1 r
-    int32_t* pos_of;       // polish: a row's free-list position, -1 for a row held at a bound
+    int4* xq;              // polish: per row the snapped point's FP32 pair (x, y as bits) and the row's
+                           // free-list position (z; -1 held at a bound): one 16-byte gather per entry
+                           // of the residual pass's products
+    int32_t* pos_of;       // polish: the free-list positions alone (-1 held at a bound), for its count
     int32_t* free_rows;    // polish: free rows of each tile, listed from the tile's first row
     int32_t* free_cnt;     // polish: free rows per tile (index within the instance's tiles)
     int32_t* col_ff;       // polish: the free-column entries of a tile's free rows, packed row
@@ -165,7 +168,7 @@ struct __align__(16) InstDev {
     double* lprec;         // L' of the preconditioned mixed engine, or the power estimate of L (device-computed at admission)
     GateResult* gate;      // the admission's convexity gate and Gershgorin bound (convexity_gate_kernel)
     int32_t lanes_res;     // polish: lanes per row of the residual pass (full rows)
-    int32_t lanes_cg;      // polish: lanes per row of the CG products (free-free rows)
+    int32_t lanes_cg;      // polish: lanes per row of the CG products (free-free rows) and of the mixed checks
     int64_t it0;          // first iteration of the current chunk (beta[k] is iteration it0 + k)
     int64_t it_cur;        // iteration of the body's first step launch; a chunk may span bodies
     int64_t it_next;       // iteration of the next check

@@ -1011,8 +1011,13 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
         // the largest stationarity ratio earlier tiles of this check reached
         const unsigned long long floor = __ldcg(&I.stat_floor);
         Acc a = acc_identity();
-        if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, T.variant, T.row_begin, T.row_end, a, floor);
-        else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, T.variant, T.row_begin, T.row_end, a);
+        // the mixed checks sum double-float products (eight FP32 additions each), so they take
+        // sub-warp rows of a few lanes (the CG product's choice, about two entries per lane)
+        // rather than the step's structure: on the 1M random graph the verification with 2 / 4 /
+        // 8 / 16 lanes or the step's warp-staged rows measured 2.004 / 2.016 / 2.027 / 2.083 /
+        // 2.047 ms per solve
+        if constexpr (FAMILY == FAMILY_VERIFY) check_rows<2>(s, I.lanes_cg, T.row_begin, T.row_end, a, floor);
+        else if constexpr (FAMILY == FAMILY_MIXED) check_rows<1>(s, I.lanes_cg, T.row_begin, T.row_end, a);
         else check_rows<0>(s, T.variant, T.row_begin, T.row_end, a, floor);
         Acc total = block_reduce_check(a, s.gate != 0, true);
         // raised before this tile's partial is published, so before the finalizer resets it
@@ -1036,9 +1041,9 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // pairs xp2 / p2 kept beside xp / p.
 // polish_init lists each tile's free rows in ascending order at free_rows[row_begin ...], their
 // count at free_cnt[tile index within the instance] and each free row's list position (row_begin
-// + its index) at pos_of[row], -1 for the rows held at a bound; the CG vectors (r, z, p, s, q, p2,
-// xf) live on those positions, and the packed Q_FF's columns are positions too (an instance's
-// tiling depends on the instance alone, so the positions survive changes of the batch).
+// + its index) in pos_of[row] and xq[row].z, -1 for the rows held at a bound; the CG vectors (r,
+// z, p, s, q, p2, xf) live on those positions, and the packed Q_FF's columns are positions too (an
+// instance's tiling depends on the instance alone, so the positions survive changes of the batch).
 // CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with 0.1 tol), as the
 // bit pattern of a non-negative float: maxima reduce on the integer pipes, and r and x are
 // rounded to FP32 in integer arithmetic (the FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
@@ -1066,20 +1071,23 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
         const double* __restrict__ u = I.u;
         double* __restrict__ xp = I.xp;
         float2* __restrict__ xp2 = I.xp2;
+        int4* __restrict__ xq = I.xq;
         int32_t* __restrict__ pos_out = I.pos_of;
         int32_t* __restrict__ list = I.free_rows + T.row_begin;
         int count = 0;
         for (int r0 = T.row_begin; r0 < T.row_end; r0 += kBlock) {
             const int r = r0 + static_cast<int>(threadIdx.x);
             bool is_free = false;
+            float2 x2 = make_float2(0.f, 0.f);
             if (r < T.row_end) {
                 const float xf = x32[r];
                 double xv;
                 if (xf <= l32[r]) xv = l[r];
                 else if (xf >= u32[r]) xv = u[r];
                 else { xv = static_cast<double>(xf); is_free = true; }
+                x2 = df_split(xv);
                 xp[r] = xv;
-                xp2[r] = df_split(xv);
+                xp2[r] = x2;
             }
             const unsigned m = __ballot_sync(0xffffffffu, is_free);
             if (lane == 0) warp_free[warp] = __popc(m);
@@ -1093,7 +1101,9 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
             if (r < T.row_end) {
                 const int j = before + __popc(m & ((1u << lane) - 1u));
                 if (is_free) list[j] = r;
-                pos_out[r] = is_free ? T.row_begin + j : -1;
+                const int pos = is_free ? T.row_begin + j : -1;
+                xq[r] = make_int4(__float_as_int(x2.x), __float_as_int(x2.y), pos, 0);
+                pos_out[r] = pos;
             }
             __syncthreads();
             count = total;
@@ -1107,7 +1117,7 @@ __global__ void __launch_bounds__(kBlock) polish_init_kernel(View v) {
 // rows, so a tile's few hundred free rows spread evenly over the block, and the leading lane of
 // each group runs the row's epilogue.  Per row: lane-strided partial sums, then an xor tree.
 
-// Residual pass: r = -(Q xp + c) over the full rows (xp2 holds the snapped point), and the
+// Residual pass: r = -(Q xp + c) over the full rows (xq holds the snapped point's pairs), and the
 // tile's Q_FF entries (free rows, free columns; p is zero on the fixed rows, so the omitted
 // entries contribute nothing to the CG products) packed densely from the start of the tile's
 // extent: a first pass counts each free row's kept entries, a block scan places the rows, and
@@ -1182,8 +1192,7 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
     const int32_t* __restrict__ col = I.col;
     const float* __restrict__ vhi = I.vhi;
     const float* __restrict__ vlo = I.vlo;
-    const int32_t* __restrict__ pos_of = I.pos_of;
-    const float2* __restrict__ xp2 = I.xp2;
+    const int4* __restrict__ xq = I.xq;
     int32_t* __restrict__ col_ff = I.col_ff;
     float* __restrict__ hi_ff = I.hi_ff;
     float* __restrict__ lo_ff = I.lo_ff;
@@ -1214,8 +1223,9 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
                 cc = __ldg(col + k);
                 h = __ldg(vhi + k);
                 lo = __ldg(vlo + k);
-                acc = df_add(acc, df_prod2(h, lo, xp2[cc]));
-                pc = pos_of[cc];
+                const int4 q = xq[cc];  // the column's pair and position in one gather
+                acc = df_add(acc, df_prod2(h, lo, make_float2(__int_as_float(q.x), __int_as_float(q.y))));
+                pc = q.z;
                 keep = pc >= 0;
                 if (cc == r + 1) e_next = make_float2(e_next.x + h, e_next.y + lo);
             }
@@ -1607,14 +1617,14 @@ __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
         if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
             Acc inst_total = reduce_instance_ab(v, R.x, R.y);
             if (threadIdx.x == 0) {
-                // residual pass: the full CSR (hi/lo values + columns) and row pointers, xp (its
-                // FP32 pairs, gathered) and c; the packed Q_FF written (hi/lo + column) with its
-                // row starts and counts; r, z, p, s, p2, x and the preconditioner's 1/pivot written
-                // and 1/diag read on the free rows
+                // residual pass: the full CSR (hi/lo values + columns) and row pointers, xq (the
+                // snapped point's pairs and the positions, gathered) and c; the packed Q_FF
+                // written (hi/lo + column) with its row starts and counts; r, z, p, s, p2, x and
+                // the preconditioner's 1/pivot written and 1/diag read on the free rows
                 const double nnz = static_cast<double>(__ldg(I.rowptr + I.n));
                 const double N = static_cast<double>(I.n);
                 const double fz = static_cast<double>(I.ff_nnz), fr = static_cast<double>(I.ff_rows);
-                I.polish_bytes += 12.0 * nnz + 4.0 * (N + 1) + 16.0 * N + 12.0 * fz + 8.0 * fr + 64.0 * fr;
+                I.polish_bytes += 12.0 * nnz + 4.0 * (N + 1) + 24.0 * N + 12.0 * fz + 8.0 * fr + 64.0 * fr;
                 I.rz = inst_total.a;
                 I.cg_res = static_cast<double>(__uint_as_float(static_cast<unsigned>(inst_total.b)));
                 I.cg_it = 0;
