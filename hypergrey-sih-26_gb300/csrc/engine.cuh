@@ -20,7 +20,7 @@ constexpr int kCgUnitMax = 8;        //   this many, and up to this many for lar
 constexpr int kCgRowsum = kCgUnitMin * kTileRows;  // rows per CG work unit at most (its row sums, 16 KB)
 constexpr int kCgGroups = 2;         // row groups per warp whose loads the CG product keeps in flight
 constexpr int kCgUnroll = 2;         // entries per row group and lane (and epilogue rows per thread) per pass of the CG product
-constexpr int kRearmRows = 8192;     // rows per block when re-arming resident solves
+constexpr int kRearmRows = 1024;     // rows per block when re-arming resident solves (8192: 32 us on 1M rows, latency-bound)
 constexpr int64_t kHostPrimal = 131072;  // primals up to this size come back at completion, larger at fetch
 
 enum Phase : int32_t {

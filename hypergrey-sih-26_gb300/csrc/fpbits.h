@@ -141,6 +141,36 @@ BQP_HD bool less_equal_bits(uint64_t a, uint64_t b) {
     return ((a | b) & kAbsMask64) == 0 || order_key(a) <= order_key(b);
 }
 
+// FP32 conversions of a double in a given rounding direction (dir 0 to nearest even, 1 up, -1
+// down), in integer arithmetic for zeros, infinities and every result that is a normal float or
+// an overflow; false for results in FP32's subnormal range and for NaNs, which the caller
+// converts with an FP64 instruction.  Up and down come from the magnitude's bounds
+// (abs_bounds_bits): RU(x) = ru(|x|) and RD(x) = rd(|x|) for x > 0, -rd(|x|) and -ru(|x|) for x < 0.
+BQP_HD bool round_dir_bits(uint64_t bits, int dir, uint32_t& f) {
+    const uint64_t mag = bits & kAbsMask64;
+    const uint32_t sign = static_cast<uint32_t>(bits >> 32) & 0x80000000u;
+    if (mag == 0 || mag == kExpMask64) {  // zeros and infinities keep their sign
+        f = sign | (mag ? 0x7f800000u : 0u);
+        return true;
+    }
+    const int e = static_cast<int>(mag >> 52);
+    if (e < 897 || mag > kExpMask64) return false;  // a subnormal result, or a NaN
+    if (dir == 0) {
+        if (e > 1150) {  // beyond every float: rounds to infinity
+            f = sign | 0x7f800000u;
+            return true;
+        }
+        if (round_float_bits(bits, f)) return true;
+        f = sign | 0x7f800000u;  // rounds past the largest float
+        return true;
+    }
+    uint32_t rd, ru;
+    abs_bounds_bits(mag, rd, ru);
+    const bool away = (dir > 0) == (sign == 0);  // rounding away from zero
+    f = sign | (away ? ru : rd);
+    return true;
+}
+
 BQP_HD float float_of_bits(uint32_t b) {
     float f;
     memcpy(&f, &b, sizeof f);

@@ -529,11 +529,35 @@ __device__ __forceinline__ float2 df_split(double x) {
     const float hf = __double2float_rn(x);
     return make_float2(hf, __double2float_rn(x - static_cast<double>(hf)));
 }
-// RN32(x), in integer arithmetic where the result is a normal float (round_float_bits).
+// RN32(x), in integer arithmetic where the result is a normal float (round_float_bits); the
+// short form for the per-row epilogues, whose values are rarely zero.
 __device__ __forceinline__ float rn_float(double x) {
     uint32_t f;
     if (round_float_bits(bits64(x), f)) return __uint_as_float(f);
     return __double2float_rn(x);
+}
+// RN32(x), RU32(x) and RD32(x) in integer arithmetic (round_dir_bits), zeros and infinities
+// included; the FP64 conversion instruction only where the result is subnormal (or x a NaN).
+__device__ __forceinline__ float rn_float_all(double x) {
+    uint32_t f;
+    if (round_dir_bits(bits64(x), 0, f)) return __uint_as_float(f);
+    return __double2float_rn(x);
+}
+__device__ __forceinline__ float ru_float(double x) {
+    uint32_t f;
+    if (round_dir_bits(bits64(x), 1, f)) return __uint_as_float(f);
+    return __double2float_ru(x);
+}
+__device__ __forceinline__ float rd_float(double x) {
+    uint32_t f;
+    if (round_dir_bits(bits64(x), -1, f)) return __uint_as_float(f);
+    return __double2float_rd(x);
+}
+// (double)f for a float, in integer arithmetic where f is zero or normal
+__device__ __forceinline__ double widen_float(float f) {
+    uint64_t d;
+    if (widen_signed_bits(__float_as_uint(f), d)) return bdouble(d);
+    return static_cast<double>(f);
 }
 
 // check_row for the FP32 iterate of the mixed engine: the iterate lies in [l32, u32], a subset of
@@ -2092,11 +2116,17 @@ __global__ void __launch_bounds__(kGateWarps * 32) convexity_gate_kernel(const i
         bool offd = false;   // a nonzero off-diagonal value (check_qp_solution's positive_diagonal)
         for (int w = kb; w < ke; w += kGateBuf) {
             const int we = min(ke, w + kGateBuf);
+            // the window's loads first, several per lane in flight; then the entry work from
+            // shared memory
+#pragma unroll 4
             for (int k = w + lane; k < we; k += 32) {
-                const uint64_t vb = __ldg(vbits + k);
-                const int32_t c = __ldg(col + k);
-                bv[k - w] = vb;
-                bc[k - w] = c;
+                bv[k - w] = __ldg(vbits + k);
+                bc[k - w] = __ldg(col + k);
+            }
+            __syncwarp();
+            for (int k = w + lane; k < we; k += 32) {
+                const uint64_t vb = bv[k - w];
+                const int32_t c = bc[k - w];
                 if (static_cast<uint32_t>(c) >= static_cast<uint32_t>(n) ||
                     (vb & 0x7ff0000000000000ull) == 0x7ff0000000000000ull)
                     flags |= kGateInvalid;
@@ -2198,9 +2228,11 @@ __global__ void __launch_bounds__(kGateWarps * 32) convexity_gate_kernel(const i
 // RN32(Q_ii) (two FP64 conversions per row instead of an FP64 division and square root); v is
 // kept as that float in sstep (read by the bound of the scaled matrix, then overwritten by the
 // steps) and widened exactly into s (free until the polish).
+// The conversions run in integer arithmetic (rn_float*, ru_float, rd_float, widen_float: the same
+// bits as the FP64 conversion instructions, which GB300 issues at 1/64 of the FP32 rate), and
+// the rows outside the window take FP64 arithmetic alone.
 __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n) {
     const int stride = gridDim.x * blockDim.x;
-    const float inv_sqrt_l = __double2float_rn(1.0 / sqrt(gate_lipschitz(I)));
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         const double d = I.diag[r];
         const uint64_t db = bits64(d);
@@ -2208,22 +2240,22 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(InstDev I, int n) {
         double dinv;
         float v;
         if (e >= 923 && e < 1123) {
-            const float df = __double2float_rn(d);
-            dinv = static_cast<double>(__frcp_rn(df));
+            const float df = rn_float(d);
+            dinv = widen_float(__frcp_rn(df));
             v = __frsqrt_rn(df);
         } else if (d > 0) {
             dinv = 1.0 / d;
             v = __double2float_rn(1.0 / sqrt(d));
         } else {
             dinv = 1.0;
-            v = inv_sqrt_l;
+            v = __double2float_rn(1.0 / sqrt(gate_lipschitz(I)));
         }
         const_cast<double*>(I.dinv)[r] = dinv;
-        I.s[r] = static_cast<double>(v);
+        I.s[r] = widen_float(v);
         I.sstep[r] = v;
-        const_cast<float*>(I.c32)[r] = __double2float_rn(I.c[r]);
-        const_cast<float*>(I.l32)[r] = __double2float_ru(I.l[r]);
-        const_cast<float*>(I.u32)[r] = __double2float_rd(I.u[r]);
+        const_cast<float*>(I.c32)[r] = rn_float_all(I.c[r]);
+        const_cast<float*>(I.l32)[r] = ru_float(I.l[r]);
+        const_cast<float*>(I.u32)[r] = rd_float(I.u[r]);
     }
 }
 
@@ -2271,9 +2303,11 @@ __global__ void __launch_bounds__(kBlock) precond_bound_kernel(InstDev I, int n)
 __global__ void __launch_bounds__(kBlock) precond_step_kernel(InstDev I, int n, int scaled) {
     const int stride = gridDim.x * blockDim.x;
     const double lp = (scaled || I.lip_device) ? *I.lprec : 0.0;
-    const float plain = static_cast<float>((I.lip_device && lp > 0) ? 1.0 / lp : 1.0 / gate_lipschitz(I));
     const bool per_row = scaled && lp > 0;
-    const float inv = per_row ? __frcp_rd(__double2float_ru(lp)) : 0.0f;
+    // per thread setup: the FP64 division of the scalar step only where it is used
+    const float plain =
+        per_row ? 0.0f : static_cast<float>((I.lip_device && lp > 0) ? 1.0 / lp : 1.0 / gate_lipschitz(I));
+    const float inv = per_row ? __frcp_rd(ru_float(lp)) : 0.0f;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
         float s = plain;
         if (per_row) {

@@ -2,11 +2,13 @@
 // (csrc/fpbits.h) against the C library: split_hilo_bits against (float)v and (float)(v - hi),
 // round_float_bits against (float)v, abs_bounds_bits against the neighbouring floats, widen_bits
 // and widen_signed_bits against (double)f, less_bits / less_equal_bits against a < b and a <= b,
-// and ratio_may_exceed's "no" against the FP64 quotient num / (1 + |x|) <= m.
-// Prints "checked split S bounds B round R widen W compare C ratio Q (skipped K) failures F" and
-// exits non-zero on a failure.
+// ratio_may_exceed's "no" against the FP64 quotient num / (1 + |x|) <= m, and round_dir_bits
+// against the conversion under the C library's rounding modes (compiled with -frounding-math).
+// Prints "checked split S bounds B round R widen W compare C ratio Q (skipped K) directed D
+// failures F" and exits non-zero on a failure.
 #include "fpbits.h"
 
+#include <cfenv>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -34,7 +36,7 @@ static double dfrom(uint64_t b) {
 }
 
 static long failures = 0, n_split = 0, n_bounds = 0, n_round = 0, n_widen = 0, n_compare = 0, n_ratio = 0,
-            n_skipped = 0;
+            n_skipped = 0, n_directed = 0;
 
 static void fail(const char* what, double v) {
     if (failures++ < 20) std::printf("FAIL %s at %.17g (bits %016llx)\n", what, v, (unsigned long long)bqp::bits64(v));
@@ -107,8 +109,44 @@ static void check_ratio(double num, double x, double m) {
     if (!(q <= m)) fail("ratio skipped above the maximum", num);
 }
 
+// round_dir_bits in the three directions against (float)v under the matching rounding mode
+static void check_directed(double v) {
+    static const int modes[3] = {FE_TONEAREST, FE_UPWARD, FE_DOWNWARD};
+    static const int dirs[3] = {0, 1, -1};
+    for (int i = 0; i < 3; ++i) {
+        uint32_t f;
+        if (!bqp::round_dir_bits(bqp::bits64(v), dirs[i], f)) {
+            // only NaNs and results in the subnormal range fall back
+            const double a = std::fabs(v);
+            if (!(std::isnan(v) || (a != 0 && a < FLT_MIN))) fail("directed refused", v);
+            continue;
+        }
+        std::fesetround(modes[i]);
+        volatile double in = v;
+        volatile float out = static_cast<float>(in);
+        std::fesetround(FE_TONEAREST);
+        ++n_directed;
+        if (f != fbits(out)) fail(i == 0 ? "directed RN" : (i == 1 ? "directed RU" : "directed RD"), v);
+    }
+}
+
 int main() {
     std::mt19937_64 rng(20261204);
+    // directed conversions: random patterns over every exponent, the float range's edges, zeros
+    // and infinities of both signs
+    for (int i = 0; i < 1000000; ++i) {
+        const uint64_t e = (i & 1) ? rng() % 2047 : 890 + rng() % 270;
+        check_directed(dfrom((rng() & 0x800fffffffffffffull) | (e << 52)));
+    }
+    for (double v : {0.0, -0.0, static_cast<double>(INFINITY), -static_cast<double>(INFINITY), 1.0, -1.0,
+                     static_cast<double>(FLT_MAX), -static_cast<double>(FLT_MAX), static_cast<double>(FLT_MIN),
+                     -static_cast<double>(FLT_MIN), 1e300, -1e300, 1e-300, -1e-300, 0.1, -0.1})
+        check_directed(v);
+    for (int k = -3; k <= 3; ++k) {
+        check_directed(std::nextafter(static_cast<double>(FLT_MAX), k < 0 ? 0.0 : 1e300) * (1.0 + k * 1e-10));
+        check_directed(-std::nextafter(static_cast<double>(FLT_MAX), k < 0 ? 0.0 : 1e300) * (1.0 + k * 1e-10));
+        check_directed(static_cast<double>(FLT_MIN) * (1.0 + k * 1e-9));
+    }
     // signed widening: random patterns over every exponent, and the range edges
     for (int i = 0; i < 1000000; ++i) check_widen(static_cast<uint32_t>(rng()));
     for (uint32_t f : {0u, 0x80000000u, 1u, 0x007fffffu, 0x00800000u, 0x80800000u, 0x7f7fffffu, 0xff7fffffu,
@@ -175,7 +213,8 @@ int main() {
     check(-2.0);
     check(1.0 / 3.0);
     check(3.4028235677973366e38);  // rounds to infinity in FP32
-    std::printf("checked split %ld bounds %ld round %ld widen %ld compare %ld ratio %ld (skipped %ld) failures %ld\n",
-                n_split, n_bounds, n_round, n_widen, n_compare, n_ratio, n_skipped, failures);
+    std::printf("checked split %ld bounds %ld round %ld widen %ld compare %ld ratio %ld (skipped %ld) directed %ld "
+                "failures %ld\n",
+                n_split, n_bounds, n_round, n_widen, n_compare, n_ratio, n_skipped, n_directed, failures);
     return failures ? 1 : 0;
 }
