@@ -1848,7 +1848,10 @@ int Engine::profile_step(uint64_t id, int launches, double* ms_out, double* byte
     R.it0 = 0;
     R.it_cur = 0;
     R.it_next = 1LL << 40;
-    for (int k = 0; k < kMaxInterval; ++k) R.beta[k] = 0.5;
+    for (int k = 0; k < kMaxInterval; ++k) {
+        R.beta[k] = 0.5;
+        R.beta32[k] = 0.5f;
+    }
     cudaMemcpyAsync(&d_inst_[j.slot], &R, sizeof(InstDev), cudaMemcpyHostToDevice, stream_);
     upload_tables();
     h_ctrl_->n_inst = n_inst_;

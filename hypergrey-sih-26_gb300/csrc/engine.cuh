@@ -184,6 +184,7 @@ struct __align__(16) InstDev {
     double offset;
     double t;              // FISTA t_k
     double beta[kMaxInterval];
+    float beta32[kMaxInterval];  // the same rounded to FP32, for the mixed steps (no per-tile conversion)
     // last check
     double objective;
     double primal_res;

@@ -687,6 +687,7 @@ __device__ void fista_betas(InstDev& I, int64_t count) {
     for (int64_t j = 0; j < count; ++j) {
         double nt = __ddiv_rn(__dadd_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(4.0, t), t)))), 2.0);
         I.beta[j] = __ddiv_rn(__dsub_rn(t, 1.0), nt);
+        I.beta32[j] = static_cast<float>(I.beta[j]);
         t = nt;
     }
     I.t = t;
@@ -820,7 +821,7 @@ __device__ void step_rows_staged(const InstDev& I, int rb, int re, int j, int tr
         const float* __restrict__ c = I.c32;
         const float* __restrict__ l = I.l32;
         const float* __restrict__ u = I.u32;
-        const float beta = static_cast<float>(I.beta[j]);
+        const float beta = I.beta32[j];
         const float* __restrict__ sstep = I.sstep;  // per-row step (preconditioned or 1/L)
         float* buf = warp_buffer<float>();
         bool moved = false;
@@ -881,7 +882,7 @@ __device__ void step_rows_subwarp(const InstDev& I, int rb, int re, int j, int t
     T beta, invL;
     if constexpr (PREC == PREC_MIXED) {
         val = I.vhi; win = I.w32[in]; wout = I.w32[out]; x = I.x32; c = I.c32; l = I.l32; u = I.u32;
-        beta = static_cast<float>(I.beta[j]); invL = I.invLf;
+        beta = I.beta32[j]; invL = I.invLf;
     } else {
         val = I.val64; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
         beta = I.beta[j]; invL = I.invL;
@@ -936,7 +937,7 @@ __device__ void step_tile_block(const InstDev& I, int rb, int re, int j, int tra
     T beta, invL;
     if constexpr (PREC == PREC_MIXED) {
         val = I.vhi + kb; win = I.w32[in]; wout = I.w32[out]; x = I.x32; c = I.c32; l = I.l32; u = I.u32;
-        beta = static_cast<float>(I.beta[j]); invL = I.invLf;
+        beta = I.beta32[j]; invL = I.invLf;
     } else {
         val = I.val64 + kb; win = I.w64[in]; wout = I.w64[out]; x = I.x64; c = I.c; l = I.l; u = I.u;
         beta = I.beta[j]; invL = I.invL;
