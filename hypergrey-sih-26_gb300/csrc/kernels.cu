@@ -1289,11 +1289,13 @@ __device__ void residual_rows(const InstDev& I, const int32_t* __restrict__ list
 // grid it couples the free runs of each grid row (line relaxation), on a random graph it is the
 // Jacobi preconditioner.  A tile without chains runs the Jacobi rows alone (pc_tile 0: the vector
 // step's single pass); otherwise each chain is factored and solved in shared memory by one thread
-// (Thomas recurrence: pivots m_0 = Q_00, m_i = Q_ii - e_{i-1}^2 / m_{i-1}), and 1/m and the kept
-// coupling are stored per list position for the vector step.
-// Chain cap, measured on the tridiagonal family (every variable free, 1M rows): 16 / 32 / 64 /
-// 128 / 256 / 512 positions: 2.09 / 1.69 / 1.44 / 1.47 / 2.01 / 3.08 ms per solve (15 / 10 / 6 /
-// 4 / 4 / 4 CG iterations): longer chains precondition better but solve sequentially.
+// in FP32 (Thomas recurrence: pivots m_0 = Q_00, m_i = Q_ii - e_{i-1}^2 / m_{i-1}), and 1/m and the
+// kept coupling (FP32 values) are stored per list position for the vector step.  FP32 chains took
+// the tridiagonal family from 1.33 to 1.22 ms per solve (residual pass 252 -> 166 us, vector step
+// 65 -> 48 us cold; CG 6 -> 7 iterations).
+// Chain cap, measured on the tridiagonal family (every variable free, 1M rows; FP64 chains):
+// 16 / 32 / 64 / 128 / 256 / 512 positions: 2.09 / 1.69 / 1.44 / 1.47 / 2.01 / 3.08 ms per solve
+// (15 / 10 / 6 / 4 / 4 / 4 CG iterations): longer chains precondition better but solve sequentially.
 constexpr int kChain = 64;
 constexpr int kChainMin = 8;
 
@@ -1400,37 +1402,69 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
         return;
     }
     // chains of two or more rows, one thread each, in shared memory; the chains are numbered
-    // densely so that consecutive lanes take them (an FP64 warp instruction costs the same with 1
-    // or 32 active lanes); each chain's arithmetic does not depend on which thread runs it
+    // densely so that consecutive lanes take them; each chain's arithmetic does not depend on
+    // which thread runs it.  The factorization and the solves run in FP32: M only preconditions
+    // (CG's recurrences and the verification stay FP64), a chain's recurrence is sequential, and
+    // an FP32 step is about a tenth of an FP64 one on this GPU.  The shared arrays of the
+    // dominance test are reused as FP32 arrays (dg: Q_rr and r; ec: forward values and 1/pivot;
+    // zs: z and the kept couplings).
     __shared__ int32_t starts[kTileRows / 2];
     __shared__ int n_starts;
+    float* dgf = reinterpret_cast<float*>(dg);
+    float* rsf = dgf + kTileRows;
+    float* yf = reinterpret_cast<float*>(ec);
+    float* ivf = yf + kTileRows;
+    float* zf = reinterpret_cast<float*>(zs);
+    float* ekf = zf + kTileRows;
+    double dv[kTileRows / kBlock], rv[kTileRows / kBlock];
+#pragma unroll
+    for (int q = 0; q < kTileRows / kBlock; ++q) {
+        const int t = threadIdx.x + q * kBlock;
+        dv[q] = t < n ? dg[t] : 0.0;
+        rv[q] = t < n ? res[t] : 0.0;
+    }
     if (threadIdx.x == 0) n_starts = 0;
-    __syncthreads();
-    for (int t = threadIdx.x; t < n; t += kBlock)
-        if (ek[t] != 0.0 && (t == 0 || ek[t - 1] == 0.0)) starts[atomicAdd(&n_starts, 1)] = t;
+    __syncthreads();  // every FP64 Q_rr read before the FP32 views overwrite it
+#pragma unroll
+    for (int q = 0; q < kTileRows / kBlock; ++q) {
+        const int t = threadIdx.x + q * kBlock;
+        if (t < n) {
+            dgf[t] = rn_float_all(dv[q]);
+            rsf[t] = rn_float_all(rv[q]);
+            ekf[t] = rn_float_all(ek[t]);
+            if (ek[t] != 0.0 && (t == 0 || ek[t - 1] == 0.0)) starts[atomicAdd(&n_starts, 1)] = t;
+        }
+    }
     __syncthreads();
     for (int k = threadIdx.x; k < n_starts; k += kBlock) {
         const int t = starts[k];
         int end = t;
-        while (ek[end] != 0.0) ++end;  // ek[n - 1] == 0
-        double inv = 1.0 / dg[t];
-        double y = res[t] * inv;
-        pc_inv[t] = inv;
-        pc_e[t] = ek[t];
-        ec[t] = y;
+        while (ekf[end] != 0.0f) ++end;  // ek[n - 1] == 0
+        float iv = __frcp_rn(dgf[t]);
+        float y = rsf[t] * iv;
+        ivf[t] = iv;
+        yf[t] = y;
         for (int i = t + 1; i <= end; ++i) {
-            const double e = ek[i - 1];
-            inv = 1.0 / (dg[i] - e * e * inv);
-            y = (res[i] - e * y) * inv;
-            pc_inv[i] = inv;
-            pc_e[i] = ek[i];
-            ec[i] = y;
+            float e = ekf[i - 1];
+            // pivot m_i = Q_ii - e^2 / m_{i-1}; strict dominance keeps it above the row's margin in
+            // exact arithmetic, and where FP32 rounding would eat a margin below 2^-20 Q_ii the
+            // chain is cut here instead (the coupling dropped, the same in the vector step)
+            float m = __fmaf_rn(-e, e * iv, dgf[i]);
+            if (!(m > dgf[i] * 0x1p-20f)) {
+                m = dgf[i];
+                e = 0.0f;
+                ekf[i - 1] = 0.0f;
+            }
+            iv = __frcp_rn(m);
+            y = (rsf[i] - e * y) * iv;
+            ivf[i] = iv;
+            yf[i] = y;
         }
-        double z = ec[end];
-        zs[end] = z;
+        float z = yf[end];
+        zf[end] = z;
         for (int i = end - 1; i >= t; --i) {
-            z = ec[i] - ek[i] * pc_inv[i] * z;
-            zs[i] = z;
+            z = yf[i] - ekf[i] * ivf[i] * z;
+            zf[i] = z;
         }
     }
     __syncthreads();
@@ -1439,7 +1473,9 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
         const bool in_chain = ek[t] != 0.0 || (t > 0 && ek[t - 1] != 0.0);
         double zz;
         if (in_chain) {
-            zz = zs[t];
+            zz = widen_float(zf[t]);
+            pc_inv[t] = widen_float(ivf[t]);
+            pc_e[t] = widen_float(ekf[t]);
         } else {  // a Jacobi row
             const double inv = dinv[r];
             pc_inv[t] = inv;
@@ -1771,13 +1807,16 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
                 }
             } else {
                 // the residual pass's chains (pc_e links a position to the next): the updates
-                // first; then the Jacobi rows in parallel and one thread per chain (the chains
-                // numbered densely, so consecutive lanes share the FP64 warp instructions), in
-                // shared memory; then the stores of u
+                // first; then the Jacobi rows in parallel (FP64) and one thread per chain (the
+                // chains numbered densely; the recurrence in FP32 from the FP32 factors the
+                // residual pass stored), in shared memory; then the stores of u
                 __shared__ double rs[kTileRows];
                 __shared__ double ys[kTileRows];
                 __shared__ double pi[kTileRows];
-                __shared__ double pe[kTileRows];
+                __shared__ float rsf[kTileRows];
+                __shared__ float pif[kTileRows];
+                __shared__ float pef[kTileRows];
+                __shared__ float yf[kTileRows];
                 __shared__ int32_t starts[kTileRows / 2];
                 __shared__ int n_starts_s;
                 int* n_starts = &n_starts_s;
@@ -1787,42 +1826,51 @@ __global__ void __launch_bounds__(kBlock) cg_vector_kernel(View v, cudaGraphCond
                     const double pn = fma(beta, p[j], u[j]);
                     const double sn = fma(beta, s[j], w[j]);
                     const double rn = fma(-alpha, sn, rr_v[j]);
+                    const double iv = pc_inv[j];
                     p[j] = pn;
                     s[j] = sn;
                     xf[j] = fma(alpha, pn, xf[j]);
                     rr_v[j] = rn;
                     rs[j] = rn;
-                    pi[j] = pc_inv[j];
-                    pe[j] = pc_e[j];
+                    pi[j] = iv;
+                    rsf[j] = rn_float_all(rn);
+                    pif[j] = rn_float_all(iv);         // exact on chain rows (stored from FP32)
+                    pef[j] = rn_float_all(pc_e[j]);    // exact: FP32 couplings or 0
                 }
                 __syncthreads();
                 for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                    const bool linked_left = j > 0 && pe[j - 1] != 0.0;
-                    if (pe[j] == 0.0 && !linked_left) ys[j] = rs[j] * pi[j];  // a Jacobi row
+                    const bool linked_left = j > 0 && pef[j - 1] != 0.0f;
+                    if (pef[j] == 0.0f && !linked_left) ys[j] = rs[j] * pi[j];  // a Jacobi row
                     else if (!linked_left) starts[atomicAdd(n_starts, 1)] = j;
                 }
                 __syncthreads();
                 const int chains = *n_starts;
                 for (int k = static_cast<int>(threadIdx.x); k < chains; k += kBlock) {
                     const int j = starts[k];
-                    double y = rs[j] * pi[j];
-                    ys[j] = y;
+                    float y = rsf[j] * pif[j];
+                    yf[j] = y;
                     int end = j;
-                    while (pe[end] != 0.0) {
+                    while (pef[end] != 0.0f) {
                         ++end;
-                        y = (rs[end] - pe[end - 1] * y) * pi[end];
-                        ys[end] = y;
+                        y = (rsf[end] - pef[end - 1] * y) * pif[end];
+                        yf[end] = y;
                     }
-                    double un = y;
+                    float un = y;
                     for (int i = end - 1; i >= j; --i) {
-                        un = ys[i] - pe[i] * pi[i] * un;
-                        ys[i] = un;
+                        un = yf[i] - pef[i] * pif[i] * un;
+                        yf[i] = un;
                     }
                 }
                 __syncthreads();
                 for (int j = static_cast<int>(threadIdx.x); j < n_free; j += kBlock) {
-                    u[j] = ys[j];
-                    u2[j] = df_split(ys[j]);
+                    const bool in_chain = pef[j] != 0.0f || (j > 0 && pef[j - 1] != 0.0f);
+                    if (in_chain) {
+                        u[j] = widen_float(yf[j]);
+                        u2[j] = make_float2(yf[j], 0.0f);
+                    } else {
+                        u[j] = ys[j];
+                        u2[j] = df_split(ys[j]);
+                    }
                 }
                 __syncthreads();  // the shared arrays are reused by the block's next chain tile
             }
