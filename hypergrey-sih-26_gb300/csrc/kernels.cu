@@ -1431,8 +1431,11 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
         if (t < n) {
             dgf[t] = rn_float_all(dv[q]);
             rsf[t] = rn_float_all(rv[q]);
-            ekf[t] = rn_float_all(ek[t]);
-            if (ek[t] != 0.0 && (t == 0 || ek[t - 1] == 0.0)) starts[atomicAdd(&n_starts, 1)] = t;
+            const float e = rn_float_all(ek[t]);
+            ekf[t] = e;
+            // a chain starts where an FP32 coupling follows none (a coupling below FP32's range
+            // ends a chain, as it does in the vector step)
+            if (e != 0.0f && (t == 0 || rn_float_all(ek[t - 1]) == 0.0f)) starts[atomicAdd(&n_starts, 1)] = t;
         }
     }
     __syncthreads();
@@ -1470,7 +1473,8 @@ __device__ void residual_epilogue(const InstDev& I, const int32_t* __restrict__ 
     __syncthreads();
     for (int t = threadIdx.x; t < n; t += kBlock) {
         const int r = list[t];
-        const bool in_chain = ek[t] != 0.0 || (t > 0 && ek[t - 1] != 0.0);
+        // the rows the chain phase wrote
+        const bool in_chain = rn_float_all(ek[t]) != 0.0f || (t > 0 && rn_float_all(ek[t - 1]) != 0.0f);
         double zz;
         if (in_chain) {
             zz = widen_float(zf[t]);

@@ -470,6 +470,30 @@ def test_polish_chains_drop_couplings_that_break_strict_dominance(engine):
     assert chk['verified'] == 1.0, chk
 
 
+def test_polish_chains_with_marginal_pivots_and_tiny_couplings(engine):
+    """The chain preconditioner runs in FP32: couplings below FP32's range (1e-50) end a chain
+    where they stand, and rows dominant in FP64 by only 1e-9 (Q_ii = 2 + 1e-9 beside two couplings
+    of -1, below the pivot guard's 2^-20 margin in FP32) cut or drop their chain; the solve still
+    verifies against the oracle."""
+    inst = boxqp.planted('tridiagonal', seed=6, n=20000, lower_triplets=True)
+    rowptr, col, val = inst['rowptr'], inst['col'], inst['val'].copy()
+    hrow, hcol, hval = inst['hrow'], inst['hcol'], inst['hval'].copy()
+    n = inst['n']
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    tiny = np.arange(n) % 5 == 2  # the coupling of row r to row r + 1
+    lo_end, hi_end = np.minimum(rows, col), np.maximum(rows, col)
+    val[(hi_end == lo_end + 1) & tiny[lo_end]] = -1e-50
+    hval[(hrow == hcol + 1) & tiny[hcol]] = -1e-50
+    marginal = np.arange(n) % 7 == 3
+    val[(rows == col) & marginal[rows]] = 2.0 + 1e-9
+    hval[(hrow == hcol) & marginal[hrow]] = 2.0 + 1e-9
+    o = boxqp.options_struct(1e-7, 30.0, 20000, 'mixed')
+    x, st = engine.solve(rowptr, col, val, inst['c'], inst['lower'], inst['upper'], o)
+    assert boxqp.STATUS_NAMES[st.status] == 'optimal', st.as_dict()
+    chk = O.check(hrow, hcol, hval, inst['c'], inst['lower'], inst['upper'], x, tol=1e-7)
+    assert chk['verified'] == 1.0, chk
+
+
 def test_nonconvex_hessian_is_reported_before_solving(engine):
     """check_convex_hessian runs first (src/accelerated_qp.cpp:19): an indefinite Q gets
     unsupported_curvature from the C-ABI solve; a PSD but not diagonally dominant Q solves."""
