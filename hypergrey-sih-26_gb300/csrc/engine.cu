@@ -628,9 +628,14 @@ bool Engine::init(std::string& why) {
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_);
     grid_max_ = tile_grid(sms_);
     cg_slots_ = cg_matvec_slots();
-    if (!cuda_ok(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), why, "stream")) return false;
+    // the running launch's stream at the highest priority, the uploads and admission kernels of
+    // new solves at the lowest: their blocks take the SMs the launch leaves free (its kernels'
+    // tails and the gaps between them) instead of slowing it down
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (!cuda_ok(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, prio_greatest), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking), why, "stream")) return false;
-    if (!cuda_ok(cudaStreamCreateWithFlags(&ustream_, cudaStreamNonBlocking), why, "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithPriority(&ustream_, cudaStreamNonBlocking, prio_least), why, "stream")) return false;
     if (!cuda_ok(cudaStreamCreateWithFlags(&fstream_, cudaStreamNonBlocking), why, "stream")) return false;
     if (!cuda_ok(cudaEventCreateWithFlags(&uev_, cudaEventDisableTiming), why, "event")) return false;
     cudaMemPoolProps props;
