@@ -518,7 +518,7 @@ private:
     // bytes issued between launch tests: a pageable chunk holds the engine thread while the host
     // stages it (about 0.05 ms for 8 MB at this host's ~200 GB/s), so the end of a launch is seen
     // at most that late (32 MB chunks delayed the next launch by up to 0.45 ms)
-    static constexpr size_t kUploadChunk = size_t(8) << 20;
+    static constexpr size_t kUploadChunk = size_t(4) << 20;
     // Between launches the engine thread uploads queued solves itself only up to this many input
     // bytes (always at least one solve when the device would otherwise idle); the rest upload
     // during the next launch, so a stream of large solves overlaps each upload with the
