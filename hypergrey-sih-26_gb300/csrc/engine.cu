@@ -290,21 +290,30 @@ int default_variant(int64_t n, int64_t nnz, int precision) {
     return VAR_TILE;
 }
 
-// Tiles per CG work unit of one instance (its `count` tiles at t): enough that its units fit the
-// product kernel's `slots` resident blocks in one round (a second round of units would run on part
-// of the GPU only), within [kCgUnitMin, kCgUnitMax], with no unit above kCgRowsum rows (the row
-// sums' shared buffer; kCgUnitMin tiles always fit).  Depends on the instance alone, so the
-// product's partial sums, and the CG iterates, are the same in a batch as solo.
-int cg_unit_tiles(const Tile* t, int count, int slots) {
-    int k = slots > 0 ? (count + slots - 1) / slots : kCgUnitMin;
-    k = std::min(kCgUnitMax, std::max(kCgUnitMin, k));
-    for (; k > kCgUnitMin; --k) {
+// CG work units of one instance (its `count` tiles at t), appended to `out` as {first tile, tiles,
+// index, units}: as many units as the product kernel has resident blocks (`slots`), so that one
+// round runs them on the whole GPU, but units of about kCgUnitMin tiles at least; the tiles are
+// spread evenly (sizes differ by one at most), and no unit goes above kCgRowsum rows (the row
+// sums' shared buffer; units of kCgUnitMin tiles always fit).  Depends on the instance alone, so
+// the product's partial sums, and the CG iterates, are the same in a batch as solo.
+void cg_units(const Tile* t, int count, int first, int slots, std::vector<int4>& out) {
+    const int fewest = (count + kCgUnitMax - 1) / kCgUnitMax;
+    const int most = std::max(1, (count + kCgUnitMin - 1) / kCgUnitMin);
+    int u = std::max(fewest, std::min(std::max(slots, 1), most));
+    for (;; ++u) {
         bool fits = true;
-        for (int u = 0; u < count && fits; u += k)
-            fits = t[std::min(count, u + k) - 1].row_end - t[u].row_begin <= kCgRowsum;
-        if (fits) break;
+        for (int k = 0, b = 0; k < u && fits; ++k) {
+            const int e = b + count / u + (k < count % u ? 1 : 0);
+            fits = t[e - 1].row_end - t[b].row_begin <= kCgRowsum;
+            b = e;
+        }
+        if (fits || u >= count) break;
     }
-    return k;
+    for (int k = 0, b = 0; k < u; ++k) {
+        const int len = count / u + (k < count % u ? 1 : 0);
+        out.push_back(make_int4(first + b, len, k, u));
+        b += len;
+    }
 }
 
 // Row tiles of one instance: contiguous rows with about kTileNnz nonzeros and at most
@@ -556,12 +565,12 @@ private:
     std::vector<Job*> slot_job_;
     std::vector<int32_t> slot_prec_;      // precision of the solve in each slot
     std::vector<int32_t> h_group_tiles_;  // tile indices ordered by step group
-    std::vector<int2> h_units_;           // CG work units: first tile, tiles per unit
+    std::vector<int4> h_units_;           // CG work units: first tile, tiles, index, units of the instance
     int32_t group_begin_[kStepGroups + 1] = {};
     uint32_t groups_present_ = 0;         // step groups with tiles
     uint32_t graph_groups_ = 0;           // step groups the graph launches
     int32_t* d_group_tiles_ = nullptr;
-    int2* d_units_ = nullptr;
+    int4* d_units_ = nullptr;
     std::vector<int> free_slots_;
     int n_inst_ = 0;
     bool tables_dirty_ = false;
@@ -772,11 +781,11 @@ bool Engine::ensure_tables(int need_inst, int need_tiles, std::string& why) {
         Tile* tiles = nullptr;
         Partial* partial = nullptr;
         int32_t* group_tiles = nullptr;
-        int2* units = nullptr;
+        int4* units = nullptr;
         if (!cuda_ok(cudaMalloc(&tiles, sizeof(Tile) * cap), why, "tile table")) return false;
         if (!cuda_ok(cudaMalloc(&partial, sizeof(Partial) * cap), why, "partials")) return false;
         if (!cuda_ok(cudaMalloc(&group_tiles, sizeof(int32_t) * cap), why, "step groups")) return false;
-        if (!cuda_ok(cudaMalloc(&units, sizeof(int2) * cap), why, "CG work units")) return false;
+        if (!cuda_ok(cudaMalloc(&units, sizeof(int4) * cap), why, "CG work units")) return false;
         cudaFree(d_tiles_);
         cudaFree(d_partial_);
         cudaFree(d_group_tiles_);
@@ -1661,17 +1670,15 @@ void Engine::upload_tables() {
     if (!h_group_tiles_.empty())
         cudaMemcpyAsync(d_group_tiles_, h_group_tiles_.data(), sizeof(int32_t) * h_group_tiles_.size(),
                         cudaMemcpyHostToDevice, stream_);
-    // CG work units: runs of cg_unit_tiles consecutive tiles of one instance, counted from the
-    // instance's first tile (so a unit depends on the instance alone, not on the batch)
+    // CG work units: runs of consecutive tiles of one instance (cg_units; a unit depends on the
+    // instance alone, not on the batch)
     h_units_.clear();
     for (int i = 0; i < n_inst_; ++i) {
         const int2 R = h_ranges_[i];
-        if (R.y <= R.x) continue;
-        const int k = cg_unit_tiles(h_tiles_.data() + R.x, R.y - R.x, cg_slots_);
-        for (int t = R.x; t < R.y; t += k) h_units_.push_back(make_int2(t, k));
+        if (R.y > R.x) cg_units(h_tiles_.data() + R.x, R.y - R.x, R.x, cg_slots_, h_units_);
     }
     if (!h_units_.empty())
-        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int2) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
+        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int4) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
     cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
     // the pageable sources above are copied out before cudaMemcpyAsync returns
     if (groups_present_ & ~graph_groups_) graph_valid_ = false;

@@ -15,8 +15,8 @@ constexpr int kBlock = 256;          // threads per CTA of every tile kernel
 constexpr int kMaxInterval = 32;     // maximum check interval (iterations per chunk)
 constexpr int kTileNnz = 4096;       // target nonzeros per tile
 constexpr int kTileRows = 512;       // maximum rows per tile
-constexpr int kCgUnitMin = 4;        // tiles per work unit of the polish CG product kernel: at least
-constexpr int kCgUnitMax = 8;        //   this many, and up to this many for large instances (cg_unit_tiles)
+constexpr int kCgUnitMin = 4;        // tiles per work unit of the polish CG product kernel: about
+constexpr int kCgUnitMax = 8;        //   this many at least, and up to this many for large instances (cg_units)
 constexpr int kCgRowsum = kCgUnitMin * kTileRows;  // rows per CG work unit at most (its row sums, 16 KB)
 constexpr int kCgGroups = 2;         // row groups per warp whose loads the CG product keeps in flight
 constexpr int kCgUnroll = 2;         // entries per row group and lane (and epilogue rows per thread) per pass of the CG product
@@ -245,8 +245,8 @@ struct View {
     int32_t* status_mirror;  // per-instance status, rewritten by the control kernel every body
     const int2* ranges;      // per-instance tile range [x, y) in the tile table
     const int32_t* group_tiles;  // tile indices ordered by step group (Ctrl::group_begin)
-    const int2* units;           // CG work units: x the first tile of a run of y consecutive tiles of one
-                                 // instance (y fixed per instance, x - its first tile a multiple of y)
+    const int4* units;           // CG work units: x the first tile of a run of y consecutive tiles of one
+                                 // instance, z the unit's index within the instance, w its unit count
 };
 
 }  // namespace bqp

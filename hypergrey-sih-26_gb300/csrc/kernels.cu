@@ -302,7 +302,7 @@ __device__ Acc block_reduce_ab(Acc v, int lanes = 1, bool warp_data = true, bool
 }
 
 // Reduces the CG partials of an instance in a fixed order: the partials of tiles tb, tb + stride,
-// ... below te (stride 1: every tile; the unit size: the first tile of each CG work unit).
+// ... below te (stride 1: every tile, or every CG work unit's slot).
 __device__ Acc reduce_instance_ab(const View& v, int tb, int te, int stride = 1) {
     constexpr int kAhead = 8;
     const int count = (te - tb + stride - 1) / stride;
@@ -1707,13 +1707,13 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
     __shared__ float2 rowsum[kCgRowsum];
     const int nu = v.ctrl->n_units;
     for (int un = blockIdx.x; un < nu; un += gridDim.x) {
-        const int2 U = v.units[un];  // first tile, tiles per unit of its instance
-        const int t0 = U.x, unit = U.y;
+        const int4 U = v.units[un];  // first tile, tiles, index and units of its instance
+        const int t0 = U.x;
         const Tile T = v.tiles[t0];
         InstDev& I = v.inst[T.inst];
         if (!polish_phase(I, PH_POLISH_CG)) continue;
         const int2 R = v.ranges[T.inst];
-        const int nk = min(unit, R.y - t0);
+        const int nk = U.y;
         unit_table(v, I, t0, R.x, nk, pre, rbeg);
         const int total = pre[kCgUnitMax];
         Acc a = acc_identity();
@@ -1726,9 +1726,9 @@ __global__ void __launch_bounds__(kBlock, 4) cg_matvec_kernel(View v) {
         default: matvec_unit<32>(I, pre, rbeg, nk, total, rowsum, a); break;
         }
         Acc tot = block_reduce_ab(a, I.lanes_cg, true, true);
-        const int units_inst = (R.y - R.x + unit - 1) / unit;
-        if (publish_and_test_last(v, t0, T.inst, units_inst, tot)) {
-            Acc inst_total = reduce_instance_ab(v, R.x, R.y, unit);
+        // the unit's partial in slot R.x + index: the instance's partials are contiguous
+        if (publish_and_test_last(v, R.x + U.z, T.inst, U.w, tot)) {
+            Acc inst_total = reduce_instance_ab(v, R.x, R.x + U.w);
             if (threadIdx.x == 0) {
                 // Chronopoulos-Gear: gamma_i = r_i.u_i, delta_i = (Q u_i).u_i, beta_i =
                 // gamma_i / gamma_{i-1}, alpha_i = gamma_i / (delta_i - beta_i gamma_i / alpha_{i-1})
