@@ -1664,23 +1664,33 @@ __device__ int polish_rows(const InstDev& I, int rb, int tile, int n_free, Acc& 
 
 // Four blocks per SM (64 registers, a few spills): 2.307 ms per 1M random-graph solve against
 // 2.329 ms at the compiler's three (80 registers); the check kernels measured slower at four.
+// Over the CG product's work units (runs of consecutive tiles of one instance, as many as the
+// resident blocks): one unit per block in one round, the unit's tiles one after the other, one
+// reduction and one publication per unit (the unit's partial in its instance's slot R.x + index).
 __global__ void __launch_bounds__(kBlock, 4) polish_residual_kernel(View v) {
-    const int nt = v.ctrl->n_tiles;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-        const Tile T = v.tiles[t];
-        InstDev& I = v.inst[T.inst];
+    const int nu = v.ctrl->n_units;
+    for (int un = blockIdx.x; un < nu; un += gridDim.x) {
+        const int4 U = v.units[un];  // first tile, tiles, index and units of its instance
+        const Tile T0 = v.tiles[U.x];
+        InstDev& I = v.inst[T0.inst];
         if (!polish_phase(I, PH_POLISH_INIT)) continue;
-        const int2 R = v.ranges[T.inst];
+        const int2 R = v.ranges[T0.inst];
         Acc a = acc_identity();
-        const int n_free = I.free_cnt[t - R.x];
-        const int kept = polish_rows(I, T.row_begin, t - R.x, n_free, a);
+        int kept = 0, n_free_unit = 0;
+        for (int q = 0; q < U.y; ++q) {
+            const int t = U.x + q;
+            if (q > 0) __syncthreads();  // the previous tile's shared arrays have been read
+            const int n_free = I.free_cnt[t - R.x];
+            kept += polish_rows(I, v.tiles[t].row_begin, t - R.x, n_free, a);
+            n_free_unit += n_free;
+        }
         if (threadIdx.x == 0) {  // Q_FF size of this polish round, for the byte accounting
             atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_nnz), static_cast<unsigned long long>(kept));
-            atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_rows), static_cast<unsigned long long>(n_free));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&I.ff_rows), static_cast<unsigned long long>(n_free_unit));
         }
         Acc total = block_reduce_ab(a, I.lanes_res, true, true);
-        if (publish_and_test_last(v, t, T.inst, R.y - R.x, total)) {
-            Acc inst_total = reduce_instance_ab(v, R.x, R.y);
+        if (publish_and_test_last(v, R.x + U.z, T0.inst, U.w, total)) {
+            Acc inst_total = reduce_instance_ab(v, R.x, R.x + U.w);
             if (threadIdx.x == 0) {
                 // residual pass: the full CSR (hi/lo values + columns) and row pointers, xq (the
                 // snapped point's pairs and the positions, gathered) and c; the packed Q_FF
