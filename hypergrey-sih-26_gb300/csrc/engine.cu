@@ -565,6 +565,10 @@ private:
     std::vector<Job*> slot_job_;
     std::vector<int32_t> slot_prec_;      // precision of the solve in each slot
     std::vector<int32_t> h_group_tiles_;  // tile indices ordered by step group
+    // page-locked staging of the tables above: their copies to the device run as DMA behind the
+    // engine stream instead of a pageable copy each (rewritten only after that stream drained)
+    unsigned char* h_table_stage_ = nullptr;
+    size_t table_stage_bytes_ = 0;
     std::vector<int4> h_units_;           // CG work units: first tile, tiles, index, units of the instance
     int32_t group_begin_[kStepGroups + 1] = {};
     uint32_t groups_present_ = 0;         // step groups with tiles
@@ -707,6 +711,9 @@ void Engine::shutdown() {
     if (h_stage_) cudaFreeHost(h_stage_);
     if (h_stage_slots_) cudaFreeHost(h_stage_slots_);
     if (h_spans_) cudaFreeHost(h_spans_);
+    if (h_table_stage_) cudaFreeHost(h_table_stage_);
+    h_table_stage_ = nullptr;
+    table_stage_bytes_ = 0;
     for (GateResult* c : gate_chunks_) cudaFreeHost(c);
     gate_chunks_.clear();
     gate_free_.clear();
@@ -1665,11 +1672,6 @@ void Engine::upload_tables() {
         const int g = step_group(slot_prec_[h_tiles_[k].inst], h_tiles_[k].variant);
         if (g >= 0) h_group_tiles_[static_cast<size_t>(count[g]++)] = k;
     }
-    if (!h_tiles_.empty())
-        cudaMemcpyAsync(d_tiles_, h_tiles_.data(), sizeof(Tile) * h_tiles_.size(), cudaMemcpyHostToDevice, stream_);
-    if (!h_group_tiles_.empty())
-        cudaMemcpyAsync(d_group_tiles_, h_group_tiles_.data(), sizeof(int32_t) * h_group_tiles_.size(),
-                        cudaMemcpyHostToDevice, stream_);
     // CG work units: runs of consecutive tiles of one instance (cg_units; a unit depends on the
     // instance alone, not on the batch)
     h_units_.clear();
@@ -1677,10 +1679,36 @@ void Engine::upload_tables() {
         const int2 R = h_ranges_[i];
         if (R.y > R.x) cg_units(h_tiles_.data() + R.x, R.y - R.x, R.x, cg_slots_, h_units_);
     }
-    if (!h_units_.empty())
-        cudaMemcpyAsync(d_units_, h_units_.data(), sizeof(int4) * h_units_.size(), cudaMemcpyHostToDevice, stream_);
-    cudaMemcpyAsync(d_ranges_, h_ranges_.data(), sizeof(int2) * std::max(n_inst_, 1), cudaMemcpyHostToDevice, stream_);
-    // the pageable sources above are copied out before cudaMemcpyAsync returns
+    // the four tables through one page-locked staging buffer (16-byte aligned parts)
+    const size_t b_tiles = sizeof(Tile) * h_tiles_.size();
+    const size_t b_group = sizeof(int32_t) * h_group_tiles_.size();
+    const size_t b_units = sizeof(int4) * h_units_.size();
+    const size_t b_ranges = sizeof(int2) * static_cast<size_t>(std::max(n_inst_, 1));
+    auto up16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+    const size_t need = up16(b_tiles) + up16(b_group) + up16(b_units) + up16(b_ranges);
+    if (need > table_stage_bytes_) {
+        const size_t cap = std::max(need, 2 * table_stage_bytes_);
+        if (h_table_stage_) cudaFreeHost(h_table_stage_);
+        h_table_stage_ = nullptr;
+        table_stage_bytes_ = 0;
+        if (cudaMallocHost(&h_table_stage_, cap) == cudaSuccess) table_stage_bytes_ = cap;
+    }
+    auto stage = [&](void* dst, const void* src, size_t bytes, size_t& at) {
+        if (bytes == 0) return;
+        if (h_table_stage_) {
+            std::memcpy(h_table_stage_ + at, src, bytes);
+            cudaMemcpyAsync(dst, h_table_stage_ + at, bytes, cudaMemcpyHostToDevice, stream_);
+            at += up16(bytes);
+        } else {
+            cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream_);  // pageable fallback
+        }
+    };
+    size_t at = 0;
+    stage(d_tiles_, h_tiles_.data(), b_tiles, at);
+    stage(d_group_tiles_, h_group_tiles_.data(), b_group, at);
+    stage(d_units_, h_units_.data(), b_units, at);
+    stage(d_ranges_, h_ranges_.data(), b_ranges, at);
+    // the staging buffer is rewritten only by the next call, after the engine stream drained
     if (groups_present_ & ~graph_groups_) graph_valid_ = false;
     tables_dirty_ = false;
 }
