@@ -592,6 +592,13 @@ def run_serve(args, world, rank, local, pg):
     for p in producers:
         p.join()
     server = BoxQPServer(local, mem_cap_bytes=40 << 30, latency_ms=args.latency_ms)
+    # untimed warm-up (with --warmup > 0): every pool instance once, both tolerances, so that the
+    # engine's graphs and kernels for all request sizes exist before the first timed arrival
+    n_warm = pool_size if args.warmup > 0 else 0
+    warm = [server.submit(pool[i]['rowptr'], pool[i]['col'], pool[i]['val'], pool[i]['c'], pool[i]['lower'],
+                          pool[i]['upper'], 1e-4 if i & 1 else 1e-8) for i in range(n_warm)]
+    for fut in warm:
+        fut.result(timeout=300)
     results = []
     lag = []
     barrier(pg)
@@ -627,7 +634,7 @@ def run_serve(args, world, rank, local, pg):
     thr = allreduce_sum(pg, len(done)) / allreduce_max(pg, elapsed)
     if rank != 0:
         return
-    line = {'metric': METRIC, 'value': thr, 'unit': 'solves/s', 'n_gpus': world, 'steps': len(done), 'warmup': 0,
+    line = {'metric': METRIC, 'value': thr, 'unit': 'solves/s', 'n_gpus': world, 'steps': len(done), 'warmup': n_warm,
             'ms_per_step': float(np.median(lat)), 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f32+f64', 'data': 'synthetic',
             'config': {'workload': f'serving stream: Poisson arrivals {rate:g}/s for {duration:g} s, n log-uniform '
