@@ -1069,9 +1069,10 @@ __global__ void __launch_bounds__(kBlock, 3) check_kernel(View v) {
 // + its index) in pos_of[row] and xq[row].z, -1 for the rows held at a bound; the CG vectors (r,
 // z, p, s, q, p2, xf) live on those positions, and the packed Q_FF's columns are positions too (an
 // instance's tiling depends on the instance alone, so the positions survive changes of the batch).
-// CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with 0.1 tol), as the
-// bit pattern of a non-negative float: maxima reduce on the integer pipes, and r and x are
-// rounded to FP32 in integer arithmetic (the FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
+// CG stopping measure |r| / (1 + |x|) of one row, in FP32 (it is compared with half the
+// tolerance), as the bit pattern of a non-negative float: maxima reduce on the integer pipes, and
+// r and x are rounded to FP32 in integer arithmetic (the FP64 pipe runs at 1/64 of the FP32 rate
+// on this GPU).
 __device__ __forceinline__ unsigned long long cg_ratio_bits(double r, double x) {
     const float ratio = __fdividef(fabsf(rn_float(r)), 1.0f + fabsf(rn_float(x)));
     return static_cast<unsigned long long>(__float_as_uint(ratio));
